@@ -1,0 +1,946 @@
+// alfgpu: host orchestration of the sweep and the C ABI (include/alfgpu.h).
+//
+// The sweep follows Prog/main.F90:714-887 step by step; every matrix product,
+// Metropolis block, QR and solve is a kernel on one CUDA stream, with all state
+// (G, the UDV stack, fields, phase, counters) resident on the device.  The
+// launch sequence of a sweep does not depend on the data (the accepted count
+// of a delayed-update block is read by the flush GEMM on the device), so a
+// whole sweep can be captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "gemm.cuh"
+#include "kernels_misc.cuh"
+#include "linalg.cuh"
+#include "update.cuh"
+
+namespace {
+
+struct UDVSet {  // one UDV state for all B = C*F (chain, flavour) pairs
+  zd* U = nullptr;
+  zd* V = nullptr;
+  double* D = nullptr;
+  zd* detU = nullptr;
+};
+
+}  // namespace
+
+struct alfgpu_s {
+  alfgpu_dims d;
+  int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
+  std::vector<int> stab_nt;
+  cudaStream_t st = nullptr;
+  cudaError_t last_cuda = cudaSuccess;
+  bool hop_ok = false, vert_ok = false, fields_ok = false, state_ok = false;
+  // model
+  double *expT = nullptr, *expTinv = nullptr;
+  int* v_site = nullptr;
+  zd *v_g = nullptr, *v_alpha = nullptr, *v_Eexp = nullptr;
+  double* v_E = nullptr;
+  int8_t* v_type = nullptr;
+  int8_t* fields = nullptr;
+  // state
+  zd *G = nullptr, *Gw = nullptr, *T1 = nullptr;
+  zd *S = nullptr, *Sinv = nullptr;
+  UDVSet udvl, udvr;
+  std::vector<UDVSet> udvst;  // index nst-1
+  // stabilisation work
+  zd *TP = nullptr, *Qb = nullptr, *RHS = nullptr, *tau = nullptr, *Vtmp = nullptr, *dphase = nullptr;
+  int *jpvt = nullptr, *perm = nullptr, *iperm = nullptr;
+  double *DUP = nullptr, *vn = nullptr, *cmp = nullptr, *opang = nullptr;
+  QRInfo* info = nullptr;
+  // delayed update
+  int *m = nullptr, *sites = nullptr;
+  zd *W = nullptr, *X = nullptr, *Y = nullptr;
+  // per chain
+  zd* phase = nullptr;
+  long long* cnt = nullptr;
+  double* stat = nullptr;
+  int* err = nullptr;
+  double* draws = nullptr;
+  unsigned long long *rngkey = nullptr, *rngctr = nullptr;
+  std::vector<unsigned long long> h_key, h_ctr;
+  // recording
+  int recording = 0, rec_stab = 0;
+  int8_t* rec_acc = nullptr;
+  zd *rec_ratio = nullptr, *rec_G = nullptr, *rec_Gw = nullptr, *rec_phase = nullptr;
+  FieldTables ft;
+  std::vector<void*> allocs;
+};
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) {                    \
+      h->last_cuda = e_;                        \
+      return ALFGPU_ERROR_CUDA;                 \
+    }                                           \
+  } while (0)
+#define RET(x)                \
+  do {                        \
+    int r_ = (x);             \
+    if (r_) return r_;        \
+  } while (0)
+
+template <typename T>
+static int dalloc(alfgpu_s* h, T** p, size_t count) {
+  void* q = nullptr;
+  CK(cudaMalloc(&q, count * sizeof(T) + 16));
+  CK(cudaMemset(q, 0, count * sizeof(T) + 16));
+  h->allocs.push_back(q);
+  *p = (T*)q;
+  return 0;
+}
+
+static void fill_tables(FieldTables& ft) {
+  const double sq6 = 2.449489742783178098197284074705891391965947480656670128432692567;
+  for (int s = -2; s <= 2; ++s) { ft.phi[0][s + 2] = (double)s; ft.gama[0][s + 2] = 1.0; }
+  const double a = sqrt(2.0 * (3.0 + sq6)), bq = sqrt(2.0 * (3.0 - sq6));
+  ft.phi[1][0] = -a; ft.phi[1][1] = -bq; ft.phi[1][2] = 0.0; ft.phi[1][3] = bq; ft.phi[1][4] = a;
+  ft.gama[1][0] = 1.0 - sq6 / 3.0; ft.gama[1][1] = 1.0 + sq6 / 3.0; ft.gama[1][2] = 1.0;
+  ft.gama[1][3] = 1.0 + sq6 / 3.0; ft.gama[1][4] = 1.0 - sq6 / 3.0;
+  const int8_t fl[5][3] = {{-1, 1, 2}, {1, 2, -2}, {0, 0, 0}, {2, -2, -1}, {-2, -1, 1}};
+  memcpy(ft.flip, fl, sizeof(fl));
+}
+
+static int cluster_size(int N) {
+  if (N >= 256) return 16;
+  if (N >= 128) return 8;
+  if (N >= 64) return 4;
+  if (N >= 32) return 2;
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel launch helpers
+// ---------------------------------------------------------------------------
+static int launch_qr(alfgpu_s* h, zd* A, const double* colscale, int nb) {
+  QRParams q;
+  memset(&q, 0, sizeof(q));
+  const int N = h->N;
+  q.A = A; q.lda = N; q.sA = (long long)N * N; q.N = N;
+  q.tau = h->tau; q.sT = N;
+  q.jpvt = h->jpvt; q.sP = N;
+  q.D = h->DUP; q.sD = N;
+  q.vn = h->vn; q.sV = 2 * N;
+  q.colscale = colscale; q.sCS = N;
+  q.info = h->info;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(h->CL, nb, 1);
+  cfg.blockDim = dim3(QR_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = (size_t)N * sizeof(zd);
+  cfg.stream = h->st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, k_qrp, q));
+  return 0;
+}
+
+static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
+  OrgqrParams q;
+  const int N = h->N;
+  q.A = A; q.lda = N; q.sA = (long long)N * N; q.tau = h->tau; q.sT = N; q.N = N;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(h->CL, nb, 1);
+  cfg.blockDim = dim3(QR_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = (size_t)N * sizeof(zd);
+  cfg.stream = h->st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, k_orgqr, q));
+  return 0;
+}
+
+static int gemm(alfgpu_s* h, const GemmParams& p) {
+  CK(launch_zgemm(p, h->st));
+  return 0;
+}
+
+static GemmParams gsq(alfgpu_s* h, int batch) {  // N x N x N square product, batch strides N*N
+  GemmParams p = gemm_defaults();
+  const int N = h->N;
+  p.m = p.n = p.k = N;
+  p.lda = p.ldb = p.ldc = N;
+  p.sA = p.sB = p.sC = (long long)N * N;
+  p.batch = batch;
+  return p;
+}
+
+static int copy_mats(alfgpu_s* h, zd* dst, const zd* src, size_t count) {
+  CK(cudaMemcpyAsync(dst, src, count * sizeof(zd), cudaMemcpyDeviceToDevice, h->st));
+  return 0;
+}
+
+static int udv_copy(alfgpu_s* h, UDVSet& dst, const UDVSet& src) {
+  const size_t NN = (size_t)h->N * h->N, B = h->B;
+  RET(copy_mats(h, dst.U, src.U, B * NN));
+  RET(copy_mats(h, dst.V, src.V, B * NN));
+  CK(cudaMemcpyAsync(dst.D, src.D, B * h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemcpyAsync(dst.detU, src.detU, B * sizeof(zd), cudaMemcpyDeviceToDevice, h->st));
+  return 0;
+}
+
+static int udv_reset(alfgpu_s* h, UDVSet& s) {
+  const int N = h->N;
+  dim3 grid((unsigned)(((long long)N * N + 255) / 256), h->B);
+  k_udv_reset<<<grid, 256, 0, h->st>>>(s.U, s.V, s.D, s.detU, N);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// Slice scale vectors S / Sinv of slice nt1 from the current fields.
+static int slice_scale(alfgpu_s* h, int nt1) {
+  k_slice_scale<<<h->B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->N, h->F, nt1, h->v_site, h->v_Eexp, h->S,
+                                          h->Sinv);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// decompose_UDV_state (udv_state_mod.F90:466-578) on all B pairs; s.U holds the propagated A.
+static int decompose(alfgpu_s* h, UDVSet& s, int left) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  RET(launch_qr(h, s.U, s.D, B));
+  k_decomp_phase<<<B, 256, 0, h->st>>>(s.U, N, N, h->info, left, h->dphase, s.detU);
+  CK(cudaGetLastError());
+  k_perm0<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->perm, N, N);
+  CK(cudaGetLastError());
+  GemmParams p = gsq(h, B);
+  if (!left) {  // V = R * P^T V   (ZLAPMR forward, ZTRMM L,U,N)
+    p.A = s.U; p.opA = OP_N; p.triA = 1;
+    p.B = s.V; p.opB = OP_N; p.permB = h->perm; p.sPB = N;
+  } else {      // V = (V P) * R^H (ZLAPMT forward, ZTRMM R,U,C)
+    p.A = s.V; p.opA = OP_N; p.permA = h->perm; p.sPA = N;
+    p.B = s.U; p.opB = OP_C; p.triB = 1;
+  }
+  p.C = h->Vtmp;
+  RET(gemm(h, p));
+  RET(copy_mats(h, s.V, h->Vtmp, (size_t)B * NN));
+  CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  RET(launch_orgqr(h, s.U, B));
+  k_scale_col0<<<B, 256, 0, h->st>>>(s.U, N, h->dphase);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// WRAPUR (wrapur_mod.F90:101-124): U <- prod_nt [D_nt expT] U, then decompose (side R)
+static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
+  const int N = h->N, B = h->B;
+  for (int nt = ntau + 1; nt <= ntau1; ++nt) {
+    RET(slice_scale(h, nt));
+    GemmParams p = gsq(h, B);
+    p.A = h->expT; p.realA = 1; p.sA = 0;  // replaced by flavour offsets below
+    p.B = h->udvr.U; p.C = h->T1;
+    p.rs = h->S; p.sRS = N;
+    if (h->F == 1) {
+      RET(gemm(h, p));
+    } else {
+      for (int f = 0; f < h->F; ++f) {  // per flavour: A = expT[f], batch over chains (stride F)
+        GemmParams q = p;
+        q.A = h->expT + (long long)f * N * N;
+        q.B = h->udvr.U + (long long)f * N * N; q.sB = (long long)h->F * N * N;
+        q.C = h->T1 + (long long)f * N * N; q.sC = (long long)h->F * N * N;
+        q.rs = h->S + (long long)f * N; q.sRS = (long long)h->F * N;
+        q.batch = h->C;
+        RET(gemm(h, q));
+      }
+    }
+    RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
+  }
+  return decompose(h, h->udvr, 0);
+}
+
+// WRAPUL (wrapul_mod.F90:108-131): U <- prod_nt [expT conj(D_nt)] U (descending nt), decompose (side L)
+static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
+  const int N = h->N;
+  for (int nt = ntau1; nt >= ntau + 1; --nt) {
+    RET(slice_scale(h, nt));
+    for (int f = 0; f < h->F; ++f) {
+      GemmParams q = gsq(h, h->C);
+      q.A = h->expT + (long long)f * N * N; q.realA = 1; q.sA = 0;
+      q.B = h->udvl.U + (long long)f * N * N; q.sB = (long long)h->F * N * N;
+      q.C = h->T1 + (long long)f * N * N; q.sC = (long long)h->F * N * N;
+      q.ks = h->S + (long long)f * N; q.sKS = (long long)h->F * N; q.ksConj = 1;
+      RET(gemm(h, q));
+    }
+    RET(copy_mats(h, h->udvl.U, h->T1, (size_t)h->B * N * N));
+  }
+  return decompose(h, h->udvl, 1);
+}
+
+// CGR default branch (cgr1_mod.F90:174-447) for all pairs into G; phase pieces into info/dphase.
+static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Gout) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  // RHS = U_R^H U_L
+  {
+    GemmParams p = gsq(h, B);
+    p.A = ur.U; p.opA = OP_C; p.B = ul.U; p.opB = OP_N; p.C = h->RHS;
+    RET(gemm(h, p));
+  }
+  // TPUP = D_R (V_R V_L) D_L + RHS  (D's packed as complex scale vectors in S / Sinv)
+  RET(copy_mats(h, h->TP, h->RHS, (size_t)B * NN));
+  k_real_to_complex2<<<(unsigned)((B * N + 255) / 256), 256, 0, h->st>>>(ur.D, ul.D, h->S, h->Sinv, (long long)B * N);
+  CK(cudaGetLastError());
+  {
+    GemmParams p = gsq(h, B);
+    p.A = ur.V; p.B = ul.V; p.C = h->TP; p.beta = zmk(1.0, 0.0);
+    p.rs = h->S; p.sRS = N;
+    p.cs = h->Sinv; p.sCS = N;
+    RET(gemm(h, p));
+  }
+  zd* QR = h->TP;
+  if (nvar != 1) {
+    dim3 grid((N + 31) / 32, (N + 31) / 32, B);
+    k_transpose<<<grid, dim3(32, 8), 0, h->st>>>(h->TP, N, NN, h->Qb, N, NN, N, 1);
+    CK(cudaGetLastError());
+    QR = h->Qb;
+  }
+  RET(launch_qr(h, QR, nullptr, B));
+  // keep R: copy the factored matrix, form Q in the copy
+  zd* Q = (QR == h->TP) ? h->Qb : h->TP;
+  RET(copy_mats(h, Q, QR, (size_t)B * NN));
+  RET(launch_orgqr(h, Q, B));
+  k_invperm<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->iperm, N, N);
+  CK(cudaGetLastError());
+  k_real_to_complex<<<(B * N + 255) / 256, 256, 0, h->st>>>(h->DUP, h->S, (long long)B * N);
+  CK(cudaGetLastError());
+  if (nvar == 1) {
+    // RHS = Q^H U_R^H, rows divided by DUP
+    GemmParams p = gsq(h, B);
+    p.A = Q; p.opA = OP_C; p.B = ur.U; p.opB = OP_C; p.C = h->RHS;
+    p.rs = h->S; p.sRS = N; p.rsInv = 1;
+    RET(gemm(h, p));
+    // R y = RHS (ZTRSM L,U,N), columns of RHS
+    TrsvParams t;
+    t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
+    t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
+    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    CK(cudaGetLastError());
+    // G = U_L * P RHS (ZLAPMR backward folded into the B load)
+    GemmParams g = gsq(h, B);
+    g.A = ul.U; g.B = h->RHS; g.permB = h->iperm; g.sPB = N; g.C = Gout;
+    RET(gemm(h, g));
+  } else {
+    // RHS = U_L Q, columns divided by DUP
+    GemmParams p = gsq(h, B);
+    p.A = ul.U; p.B = Q; p.C = h->RHS;
+    p.cs = h->S; p.sCS = N; p.csInv = 1;
+    RET(gemm(h, p));
+    // y R^H = RHS (ZTRSM R,U,C): rows of RHS, conjugated, upper solve
+    TrsvParams t;
+    t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
+    t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 1;
+    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    CK(cudaGetLastError());
+    // G = (RHS P) U_R^H (ZLAPMT backward folded into the A load)
+    GemmParams g = gsq(h, B);
+    g.A = h->RHS; g.permA = h->iperm; g.sPA = N; g.B = ur.U; g.opB = OP_C; g.C = Gout;
+    RET(gemm(h, g));
+  }
+  return 0;
+}
+
+
+// One stabilisation: Gw = G (TEST), CGR into G, compare, phases (main.F90:734-753).
+static int stabilise(alfgpu_s* h, int nvar, int compare) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  if (compare) RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
+  RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
+  if (compare) {
+    k_compare<<<B, 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
+    CK(cudaGetLastError());
+  }
+  k_opphase<<<B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->F, h->v_g, h->v_alpha, h->v_type, h->ft, h->opang);
+  CK(cudaGetLastError());
+  StabFinishParams sp;
+  sp.C = h->C; sp.F = h->F; sp.NSUN = h->NSUN; sp.nvar = nvar; sp.compare = compare; sp.init = !compare;
+  sp.detUR = h->udvr.detU; sp.detUL = h->udvl.detU; sp.info = h->info; sp.opang = h->opang; sp.cmp = h->cmp;
+  sp.phase = h->phase; sp.stat = h->stat; sp.err = h->err;
+  sp.rec_phase = nullptr;
+  if (h->recording && compare) {
+    sp.rec_phase = h->rec_phase + (long long)h->rec_stab * h->C;
+    RET(copy_mats(h, h->rec_G + (long long)h->rec_stab * B * NN, h->G, (size_t)B * NN));
+    RET(copy_mats(h, h->rec_Gw + (long long)h->rec_stab * B * NN, h->Gw, (size_t)B * NN));
+    h->rec_stab++;
+  }
+  k_stab_finish<<<(h->C + 127) / 128, 128, 0, h->st>>>(sp);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// Hopping wraps with the slice's deferred vertex scalings (Wrapgr_mod.F90:110-114, 237-241).
+// up:   G <- expT (S G Sinv) expTinv      down: G <- expTinv (Sinv G S) expT
+static int hop(alfgpu_s* h, int up, int with_scale) {
+  const int N = h->N, F = h->F;
+  const long long NN = (long long)N * N;
+  for (int f = 0; f < F; ++f) {
+    const double* E1 = (up ? h->expT : h->expTinv) + f * NN;
+    const double* E2 = (up ? h->expTinv : h->expT) + f * NN;
+    const zd* s1 = up ? h->S : h->Sinv;  // applied next to the first (left) factor
+    const zd* s2 = up ? h->Sinv : h->S;
+    if (up) {
+      // T1 = expT * diag(S) * G
+      GemmParams p = gsq(h, h->C);
+      p.A = E1; p.realA = 1; p.sA = 0;
+      p.B = h->G + f * NN; p.sB = F * NN;
+      p.C = h->T1 + f * NN; p.sC = F * NN;
+      if (with_scale) { p.ks = s1 + (long long)f * N; p.sKS = (long long)F * N; p.ksOnA = 0; }
+      RET(gemm(h, p));
+      // G = T1 * diag(Sinv) * expTinv
+      GemmParams q = gsq(h, h->C);
+      q.A = h->T1 + f * NN; q.sA = F * NN;
+      q.B = E2; q.realB = 1; q.sB = 0;
+      q.C = h->G + f * NN; q.sC = F * NN;
+      if (with_scale) { q.ks = s2 + (long long)f * N; q.sKS = (long long)F * N; q.ksOnA = 1; }
+      RET(gemm(h, q));
+    } else {
+      // T1 = G * diag(S) * expT
+      GemmParams p = gsq(h, h->C);
+      p.A = h->G + f * NN; p.sA = F * NN;
+      p.B = E2; p.realB = 1; p.sB = 0;
+      p.C = h->T1 + f * NN; p.sC = F * NN;
+      if (with_scale) { p.ks = s2 + (long long)f * N; p.sKS = (long long)F * N; p.ksOnA = 1; }
+      RET(gemm(h, p));
+      // G = expTinv * diag(Sinv) * T1
+      GemmParams q = gsq(h, h->C);
+      q.A = E1; q.realA = 1; q.sA = 0;
+      q.B = h->T1 + f * NN; q.sB = F * NN;
+      q.C = h->G + f * NN; q.sC = F * NN;
+      if (with_scale) { q.ks = s1 + (long long)f * N; q.sKS = (long long)F * N; q.ksOnA = 0; }
+      RET(gemm(h, q));
+    }
+  }
+  return 0;
+}
+
+// Metropolis updates of one slice in blocks of kblk visits, each followed by its flush.
+static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const double* draws_dev) {
+  const int N = h->N, F = h->F, M = h->M;
+  const long long NN = (long long)N * N;
+  for (int q0 = 0; q0 < M; q0 += h->kblk) {
+    UpdParams u;
+    memset(&u, 0, sizeof(u));
+    u.N = N; u.F = F; u.M = M; u.L = h->L; u.NSUN = h->NSUN;
+    u.nt1 = nt1; u.dir = dir; u.q0 = q0; u.nq = (M - q0 < h->kblk) ? M - q0 : h->kblk;
+    u.visit_base = visit_base;
+    u.G = h->G; u.sG = F * NN;
+    u.V.site = h->v_site; u.V.g = h->v_g; u.V.alpha = h->v_alpha; u.V.E = h->v_E; u.V.type = h->v_type;
+    u.V.Eexp = h->v_Eexp; u.V.sK = (long long)F * M;
+    u.fields = h->fields;
+    u.draws = draws_dev; u.sDraws = 6ll * M * h->L;
+    u.rngkey = h->rngkey; u.rngctr = h->rngctr;
+    u.phase = h->phase; u.m_out = h->m; u.sites_out = h->sites; u.W_out = h->W; u.cnt = h->cnt;
+    if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
+    u.ft = h->ft;
+    k_update_block<<<h->C, 64, UPD_SMEM_BYTES, h->st>>>(u);
+    CK(cudaGetLastError());
+    k_flush_prep<<<dim3((N + 127) / 128, F, h->C), 128, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->X,
+                                                                     h->Y);
+    CK(cudaGetLastError());
+    // G -= X Y, rank m per chain
+    GemmParams p = gemm_defaults();
+    p.m = N; p.n = N; p.k = UPD_KMAX;
+    p.A = h->X; p.lda = N; p.sA = (long long)N * UPD_KMAX;
+    p.B = h->Y; p.ldb = UPD_KMAX; p.sB = (long long)N * UPD_KMAX;
+    p.C = h->G; p.ldc = N; p.sC = NN;
+    p.alpha = zmk(-1.0, 0.0); p.beta = zmk(1.0, 0.0);
+    p.batch = h->B;
+    // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
+    if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
+    k_expand_m<<<(h->B + 127) / 128, 128, 0, h->st>>>(h->m, h->m + h->C, h->C, F);
+    CK(cudaGetLastError());
+    p.kdyn = h->m + h->C;
+    RET(gemm(h, p));
+  }
+  return 0;
+}
+
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* alfgpu_error_string(int code) {
+  switch (code) {
+    case ALFGPU_ERROR_NONE: return "no error";
+    case ALFGPU_ERROR_GENERIC: return "generic error";
+    case ALFGPU_ERROR_UNSTABLE_MATRIX: return "Precision Green exceeds 10: unstable calculation";
+    case ALFGPU_ERROR_FIELDS: return "invalid field values";
+    case ALFGPU_ERROR_HAMILTONIAN: return "invalid operator tables";
+    case ALFGPU_ERROR_CUDA: return "CUDA runtime error";
+    case ALFGPU_ERROR_ARGUMENT: return "invalid argument";
+    case ALFGPU_ERROR_UNSUPPORTED: return "model feature not supported on the GPU path";
+    case ALFGPU_ERROR_NAN: return "NaN in the Green function";
+    case ALFGPU_ERROR_TIMEOUT: return "device wait timed out";
+    default: return "unknown error";
+  }
+}
+
+int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
+  if (!out || !dims) return ALFGPU_ERROR_ARGUMENT;
+  *out = nullptr;
+  const alfgpu_dims& d = *dims;
+  if (d.ndim < 1 || d.ndim > 4096 || d.n_fl < 1 || d.n_fl > 2 || d.n_sun < 1 || d.n_op < 1 || d.ltrot < 1 ||
+      d.nwrap < 1 || d.n_chains < 1)
+    return ALFGPU_ERROR_ARGUMENT;
+  if (d.precision != ALFGPU_PRECISION_FP64) return ALFGPU_ERROR_UNSUPPORTED;
+  if (d.ltau) return ALFGPU_ERROR_UNSUPPORTED;
+  alfgpu_s* h = new alfgpu_s();
+  h->d = d;
+  h->N = d.ndim; h->F = d.n_fl; h->M = d.n_op; h->L = d.ltrot; h->C = d.n_chains; h->B = d.n_chains * d.n_fl;
+  h->NSUN = d.n_sun;
+  h->Nstm = (d.ltrot % d.nwrap == 0) ? d.ltrot / d.nwrap : d.ltrot / d.nwrap + 1;
+  h->stab_nt.resize(h->Nstm + 1);
+  h->stab_nt[0] = 0;
+  for (int n = 1; n < h->Nstm; ++n) h->stab_nt[n] = d.nwrap * n;
+  h->stab_nt[h->Nstm] = d.ltrot;
+  h->CL = cluster_size(h->N);
+  h->kblk = (d.delay_k > 0 && d.delay_k <= UPD_KMAX) ? d.delay_k : UPD_KMAX;
+  h->dev = d.device;
+  fill_tables(h->ft);
+  auto fail = [&](int code) { alfgpu_destroy(h); return code; };
+  if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
+  if (h->CL > 8) {
+    if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      return fail(ALFGPU_ERROR_CUDA);
+  }
+  if (cudaFuncSetAttribute(k_update_block, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM_BYTES) != cudaSuccess)
+    return fail(ALFGPU_ERROR_CUDA);
+  // shrink the QR cluster until at least one cluster fits on the device
+  while (h->CL > 1) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(h->CL, 1, 1);
+    cfg.blockDim = dim3(QR_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = (size_t)h->N * sizeof(zd);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    cfg.attrs = at; cfg.numAttrs = 1;
+    int n1 = 0, n2 = 0;
+    if (cudaOccupancyMaxActiveClusters(&n1, k_qrp, &cfg) == cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&n2, k_orgqr, &cfg) == cudaSuccess && n1 > 0 && n2 > 0)
+      break;
+    cudaGetLastError();
+    h->CL /= 2;
+  }
+  const size_t N = h->N, NN = N * N, B = h->B, C = h->C, F = h->F, M = h->M, L = h->L;
+  int r = 0;
+  r |= dalloc(h, &h->expT, F * NN); r |= dalloc(h, &h->expTinv, F * NN);
+  r |= dalloc(h, &h->v_site, C * F * M); r |= dalloc(h, &h->v_g, C * F * M); r |= dalloc(h, &h->v_alpha, C * F * M);
+  r |= dalloc(h, &h->v_E, C * F * M); r |= dalloc(h, &h->v_type, C * F * M); r |= dalloc(h, &h->v_Eexp, C * F * M * 5);
+  r |= dalloc(h, &h->fields, C * L * M);
+  r |= dalloc(h, &h->G, B * NN); r |= dalloc(h, &h->Gw, B * NN); r |= dalloc(h, &h->T1, B * NN);
+  r |= dalloc(h, &h->S, B * N); r |= dalloc(h, &h->Sinv, B * N);
+  auto mk_udv = [&](UDVSet& s) {
+    int q = 0;
+    q |= dalloc(h, &s.U, B * NN); q |= dalloc(h, &s.V, B * NN); q |= dalloc(h, &s.D, B * N); q |= dalloc(h, &s.detU, B);
+    return q;
+  };
+  r |= mk_udv(h->udvl); r |= mk_udv(h->udvr);
+  h->udvst.resize(h->Nstm);
+  for (auto& s : h->udvst) r |= mk_udv(s);
+  r |= dalloc(h, &h->TP, B * NN); r |= dalloc(h, &h->Qb, B * NN); r |= dalloc(h, &h->RHS, B * NN);
+  r |= dalloc(h, &h->Vtmp, B * NN);
+  r |= dalloc(h, &h->tau, B * N); r |= dalloc(h, &h->jpvt, B * N); r |= dalloc(h, &h->perm, B * N);
+  r |= dalloc(h, &h->iperm, B * N); r |= dalloc(h, &h->DUP, B * N); r |= dalloc(h, &h->vn, B * 2 * N);
+  r |= dalloc(h, &h->info, B); r |= dalloc(h, &h->dphase, B); r |= dalloc(h, &h->cmp, 2 * B);
+  r |= dalloc(h, &h->opang, B);
+  r |= dalloc(h, &h->m, C + B); r |= dalloc(h, &h->sites, C * UPD_KMAX);
+  r |= dalloc(h, &h->W, C * 2 * UPD_KMAX * UPD_KMAX);
+  r |= dalloc(h, &h->X, C * 2 * N * UPD_KMAX); r |= dalloc(h, &h->Y, C * 2 * N * UPD_KMAX);
+  r |= dalloc(h, &h->phase, C); r |= dalloc(h, &h->cnt, 4 * C); r |= dalloc(h, &h->stat, 8 * C);
+  r |= dalloc(h, &h->err, 1);
+  r |= dalloc(h, &h->draws, C * 6 * M * L);
+  r |= dalloc(h, &h->rngkey, C); r |= dalloc(h, &h->rngctr, C);
+  if (r) return fail(ALFGPU_ERROR_CUDA);
+  h->h_key.assign(C, 0); h->h_ctr.assign(C, 0);
+  for (size_t c = 0; c < C; ++c) { h->h_key[c] = alf_chain_key(0, c); h->h_ctr[c] = M * L; }
+  *out = h;
+  return ALFGPU_ERROR_NONE;
+}
+
+void alfgpu_destroy(alfgpu_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->dev);
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+void* alfgpu_stream(alfgpu_t* h) { return h ? (void*)h->st : nullptr; }
+
+int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv) {
+  if (!h || !expT || !expTinv) return ALFGPU_ERROR_ARGUMENT;
+  const size_t NN = (size_t)h->N * h->N;
+  for (size_t i = 0; i < h->F * NN; ++i)
+    if (!std::isfinite(expT[i]) || !std::isfinite(expTinv[i])) return ALFGPU_ERROR_HAMILTONIAN;
+  CK(cudaMemcpy(h->expT, expT, h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->expTinv, expTinv, h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  h->hop_ok = true;
+  return 0;
+}
+
+int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v) {
+  if (!h || !v || chain < -1 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  const int F = h->F, M = h->M, N = h->N;
+  const size_t K = (size_t)F * M;
+  std::vector<int> site(K);
+  std::vector<zd> g(K), al(K), ee(K * 5);
+  std::vector<double> E(K);
+  std::vector<int8_t> ty(K);
+  for (size_t k = 0; k < K; ++k) {
+    if (v->op_n[k] != 1 || !v->op_diag[k]) return ALFGPU_ERROR_UNSUPPORTED;  // single-site diagonal only
+    if (v->op_type[k] != 1 && v->op_type[k] != 2) return ALFGPU_ERROR_UNSUPPORTED;
+    if (v->op_nz[k] != 1) return ALFGPU_ERROR_UNSUPPORTED;
+    int p = v->op_P[2 * k];
+    if (p < 0 || p >= N) return ALFGPU_ERROR_HAMILTONIAN;
+    site[k] = p;
+    g[k] = zmk(v->op_g[2 * k], v->op_g[2 * k + 1]);
+    al[k] = zmk(v->op_alpha[2 * k], v->op_alpha[2 * k + 1]);
+    E[k] = v->op_E[2 * k];
+    ty[k] = (int8_t)v->op_type[k];
+    for (int s = 0; s < 5; ++s) ee[k * 5 + s] = zmk(v->op_Eexp[(k * 10 + s) * 2], v->op_Eexp[(k * 10 + s) * 2 + 1]);
+    if (!std::isfinite(g[k].x) || !std::isfinite(g[k].y)) return ALFGPU_ERROR_HAMILTONIAN;
+  }
+  // sites of one flavour must be distinct within every block of visits, and equal across flavours
+  for (int n = 0; n < M; ++n)
+    for (int f = 1; f < F; ++f)
+      if (site[(size_t)f * M + n] != site[n]) return ALFGPU_ERROR_UNSUPPORTED;
+  // a delayed-update block needs distinct sites; check the up-pass and down-pass blockings
+  for (int dir = 0; dir < 2; ++dir) {
+    std::vector<int> seen(N, 0);
+    for (int pos = 0; pos < M; ++pos) {
+      if (pos % h->kblk == 0) std::fill(seen.begin(), seen.end(), 0);
+      int s = site[dir == 0 ? pos : M - 1 - pos];
+      if (seen[s]) return ALFGPU_ERROR_UNSUPPORTED;
+      seen[s] = 1;
+    }
+  }
+  int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->C : chain + 1;
+  for (int c = c0; c < c1; ++c) {
+    CK(cudaMemcpy(h->v_site + c * K, site.data(), K * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_g + c * K, g.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_alpha + c * K, al.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_E + c * K, E.data(), K * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_type + c * K, ty.data(), K, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_Eexp + c * K * 5, ee.data(), K * 5 * sizeof(zd), cudaMemcpyHostToDevice));
+  }
+  h->vert_ok = true;
+  return 0;
+}
+
+int alfgpu_set_fields(alfgpu_t* h, int32_t chain, const int8_t* f) {
+  if (!h || !f || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  const size_t ML = (size_t)h->M * h->L;
+  for (size_t i = 0; i < ML; ++i)
+    if (f[i] != 1 && f[i] != -1 && f[i] != 2 && f[i] != -2) return ALFGPU_ERROR_FIELDS;
+  CK(cudaMemcpy(h->fields + chain * ML, f, ML, cudaMemcpyHostToDevice));
+  h->fields_ok = true;
+  return 0;
+}
+
+int alfgpu_set_fields_c128(alfgpu_t* h, int32_t chain, const double* f) {
+  if (!h || !f) return ALFGPU_ERROR_ARGUMENT;
+  const size_t ML = (size_t)h->M * h->L;
+  std::vector<int8_t> b(ML);
+  for (size_t i = 0; i < ML; ++i) {
+    double x = f[2 * i];
+    long v = lround(x);
+    if ((double)v != x || f[2 * i + 1] != 0.0) return ALFGPU_ERROR_FIELDS;
+    b[i] = (int8_t)v;
+  }
+  return alfgpu_set_fields(h, chain, b.data());
+}
+
+int alfgpu_get_fields(alfgpu_t* h, int32_t chain, int8_t* f) {
+  if (!h || !f || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  const size_t ML = (size_t)h->M * h->L;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(f, h->fields + chain * ML, ML, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int alfgpu_set_rng(alfgpu_t* h, int32_t chain, uint64_t seed, uint64_t counter) {
+  if (!h || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  h->h_key[chain] = alf_chain_key(seed, (uint64_t)chain);
+  h->h_ctr[chain] = counter;
+  return 0;
+}
+
+static int check_err(alfgpu_s* h) {
+  int e = 0;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    CK(cudaMemset(h->err, 0, sizeof(int)));
+    if (e & 1) return ALFGPU_ERROR_NAN;
+    if (e & 2) return ALFGPU_ERROR_UNSTABLE_MATRIX;
+    return ALFGPU_ERROR_GENERIC;
+  }
+  return 0;
+}
+
+int alfgpu_init_state(alfgpu_t* h, double* phase_out) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  if (!h->hop_ok || !h->vert_ok || !h->fields_ok) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  RET(udv_reset(h, h->udvl));
+  RET(udv_reset(h, h->udvr));
+  RET(udv_reset(h, h->udvst[h->Nstm - 1]));
+  for (int nst = h->Nstm - 1; nst >= 1; --nst) {
+    RET(wrapul(h, h->stab_nt[nst + 1], h->stab_nt[nst]));
+    RET(udv_copy(h, h->udvst[nst - 1], h->udvl));
+  }
+  RET(wrapul(h, h->stab_nt[1], 0));
+  RET(stabilise(h, 1, 0));
+  RET(check_err(h));
+  if (phase_out) CK(cudaMemcpy(phase_out, h->phase, h->C * sizeof(zd), cudaMemcpyDeviceToHost));
+  h->state_ok = true;
+  return 0;
+}
+
+int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  if (!h->state_ok) return ALFGPU_ERROR_ARGUMENT;
+  (void)cb; (void)ctx;
+  CK(cudaSetDevice(h->dev));
+  const int L = h->L, M = h->M, Nstm = h->Nstm;
+  const double* dr = nullptr;
+  if (uniforms) {
+    CK(cudaMemcpyAsync(h->draws, uniforms, (size_t)h->C * 6 * M * L * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    dr = h->draws;
+  } else {
+    CK(cudaMemcpyAsync(h->rngkey, h->h_key.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->rngctr, h->h_ctr.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
+  }
+  h->rec_stab = 0;
+  // up pass (main.F90:717-774)
+  RET(udv_reset(h, h->udvr));
+  int NST = 1;
+  int pending = 0;
+  for (int ntau = 0; ntau < L; ++ntau) {
+    const int ntau1 = ntau + 1;
+    RET(hop(h, 1, pending));
+    RET(slice_scale(h, ntau1));  // vertex wraps of this slice use the fields before their update
+    RET(update_slice(h, ntau1, 0, ntau * M, dr));
+    pending = 1;
+    if (ntau1 == h->stab_nt[NST]) {
+      {
+        dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
+        k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
+        CK(cudaGetLastError());
+      }
+      pending = 0;
+      RET(wrapur(h, h->stab_nt[NST - 1], ntau1));
+      RET(udv_copy(h, h->udvl, h->udvst[NST - 1]));
+      RET(udv_copy(h, h->udvst[NST - 1], h->udvr));
+      const int nvar = (ntau1 > L / 2) ? 2 : 1;
+      RET(stabilise(h, nvar, 1));
+      NST++;
+    }
+  }
+  // down pass (main.F90:776-834)
+  RET(udv_reset(h, h->udvl));
+  NST = Nstm - 1;
+  for (int ntau = L; ntau >= 1; --ntau) {
+    const int ntau1 = ntau - 1;
+    RET(update_slice(h, ntau, 1, L * M + (L - ntau) * M, dr));
+    RET(slice_scale(h, ntau));  // Op_Wrapdo N_type=1 uses the updated fields
+    RET(hop(h, 0, 1));
+    if (NST >= 1 && h->stab_nt[NST] == ntau1 && ntau1 != 0) {
+      RET(wrapul(h, h->stab_nt[NST + 1], ntau1));
+      RET(udv_copy(h, h->udvr, h->udvst[NST - 1]));
+      RET(udv_copy(h, h->udvst[NST - 1], h->udvl));
+      const int nvar = (ntau1 > L / 2) ? 2 : 1;
+      RET(stabilise(h, nvar, 1));
+      NST--;
+    }
+  }
+  // G on time slice 0 (main.F90:836-872)
+  RET(wrapul(h, h->stab_nt[1], h->stab_nt[0]));
+  RET(udv_reset(h, h->udvr));
+  RET(stabilise(h, 1, 1));
+  RET(udv_reset(h, h->udvst[Nstm - 1]));
+  if (!uniforms)
+    for (int c = 0; c < h->C; ++c) h->h_ctr[c] += 6ull * M * L;
+  {
+    k_count_sweep<<<(h->C + 127) / 128, 128, 0, h->st>>>(h->stat, h->C);
+    CK(cudaGetLastError());
+  }
+  return check_err(h);
+}
+
+
+int alfgpu_get_green(alfgpu_t* h, int32_t chain, double* G) {
+  if (!h || !G || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  const size_t n = (size_t)h->F * h->N * h->N;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(G, h->G + chain * n, n * sizeof(zd), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int alfgpu_get_phase(alfgpu_t* h, double* phase) {
+  if (!h || !phase) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(phase, h->phase, h->C * sizeof(zd), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int alfgpu_get_stats(alfgpu_t* h, int32_t chain, alfgpu_stats* s) {
+  if (!h || !s || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  long long cn[4];
+  double st[8];
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(cn, h->cnt + 4 * chain, sizeof(cn), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(st, h->stat + 8 * chain, sizeof(st), cudaMemcpyDeviceToHost));
+  memset(s, 0, sizeof(*s));
+  s->n_prop = cn[0]; s->n_acc = cn[1]; s->n_prop_eff = cn[2]; s->n_acc_eff = cn[3];
+  s->ncg = (int64_t)st[0]; s->xmeanG_sum = st[1]; s->xmaxG = st[2]; s->xmaxP = st[3];
+  s->ncg_tau = (int64_t)st[4]; s->xmean_tau_sum = st[5]; s->xmax_tau = st[6]; s->sweeps = (int64_t)st[7];
+  return 0;
+}
+
+int alfgpu_reset_stats(alfgpu_t* h) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaMemsetAsync(h->cnt, 0, 4 * h->C * sizeof(long long), h->st));
+  CK(cudaMemsetAsync(h->stat, 0, 8 * h->C * sizeof(double), h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int alfgpu_set_recording(alfgpu_t* h, int32_t enable) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  if (enable && !h->rec_acc) {
+    const size_t V = (size_t)2 * h->M * h->L, P = 2 * (size_t)h->Nstm, NN = (size_t)h->N * h->N;
+    int r = 0;
+    r |= dalloc(h, &h->rec_acc, h->C * V);
+    r |= dalloc(h, &h->rec_ratio, h->C * V);
+    r |= dalloc(h, &h->rec_G, P * h->B * NN);
+    r |= dalloc(h, &h->rec_Gw, P * h->B * NN);
+    r |= dalloc(h, &h->rec_phase, P * h->C);
+    if (r) return ALFGPU_ERROR_CUDA;
+  }
+  h->recording = enable ? 1 : 0;
+  return 0;
+}
+
+int alfgpu_get_record(alfgpu_t* h, int32_t chain, int8_t* acc, double* ratio, double* G_fresh, double* G_wrapped,
+                      double* phase) {
+  if (!h || chain < 0 || chain >= h->C || !h->rec_acc) return ALFGPU_ERROR_ARGUMENT;
+  const size_t V = (size_t)2 * h->M * h->L, P = 2 * (size_t)h->Nstm, NN = (size_t)h->N * h->N, F = h->F;
+  CK(cudaStreamSynchronize(h->st));
+  if (acc) CK(cudaMemcpy(acc, h->rec_acc + chain * V, V, cudaMemcpyDeviceToHost));
+  if (ratio) CK(cudaMemcpy(ratio, h->rec_ratio + chain * V, V * sizeof(zd), cudaMemcpyDeviceToHost));
+  for (size_t p = 0; p < P; ++p) {
+    const size_t off = (p * h->B + (size_t)chain * F) * NN;
+    if (G_fresh) CK(cudaMemcpy(G_fresh + 2 * p * F * NN, h->rec_G + off, F * NN * sizeof(zd), cudaMemcpyDeviceToHost));
+    if (G_wrapped)
+      CK(cudaMemcpy(G_wrapped + 2 * p * F * NN, h->rec_Gw + off, F * NN * sizeof(zd), cudaMemcpyDeviceToHost));
+    if (phase) CK(cudaMemcpy(phase + 2 * p, h->rec_phase + p * h->C + chain, sizeof(zd), cudaMemcpyDeviceToHost));
+  }
+  return 0;
+}
+
+// ---- one-shot component entry points -------------------------------------------------------
+static int oneshot_handle(int N, alfgpu_s** out) {
+  alfgpu_dims d;
+  memset(&d, 0, sizeof(d));
+  d.ndim = N; d.n_fl = 1; d.n_sun = 1; d.n_op = 1; d.ltrot = 1; d.nwrap = 1; d.n_chains = 1;
+  d.precision = ALFGPU_PRECISION_FP64;
+  return alfgpu_create(out, &d);
+}
+
+int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, const double* VR, const double* UL,
+               const double* DL, const double* VL, double* G, double* phase) {
+  if (ndim < 1 || !UR || !DR || !VR || !UL || !DL || !VL || !G || !phase) return ALFGPU_ERROR_ARGUMENT;
+  alfgpu_s* h = nullptr;
+  RET(oneshot_handle(ndim, &h));
+  const size_t N = ndim, NN = N * N;
+  auto run = [&]() -> int {
+    std::vector<double> dr(N), dl(N);
+    for (size_t i = 0; i < N; ++i) { dr[i] = DR[2 * i]; dl[i] = DL[2 * i]; }
+    CK(cudaMemcpy(h->udvr.U, UR, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->udvr.V, VR, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->udvr.D, dr.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->udvl.U, UL, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->udvl.V, VL, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->udvl.D, dl.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    // det(U) of arbitrary inputs: pivoted QR of each U (det = det(Q) prod R_ii sign(P))
+    for (int side = 0; side < 2; ++side) {
+      UDVSet& s = side ? h->udvl : h->udvr;
+      RET(copy_mats(h, h->TP, s.U, NN));
+      RET(launch_qr(h, h->TP, nullptr, 1));
+      QRInfo inf;
+      CK(cudaMemcpyAsync(&inf, h->info, sizeof(inf), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      std::vector<double> dd(N);
+      CK(cudaMemcpy(dd.data(), h->DUP, N * sizeof(double), cudaMemcpyDeviceToHost));
+      zd det = zmul(inf.detQ, inf.prodR);
+      if (inf.psign < 0) det = zneg(det);
+      CK(cudaMemcpy(s.detU, &det, sizeof(zd), cudaMemcpyHostToDevice));
+    }
+    RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
+    CK(cudaMemsetAsync(h->opang, 0, sizeof(double), h->st));
+    StabFinishParams sp;
+    memset(&sp, 0, sizeof(sp));
+    sp.C = 1; sp.F = 1; sp.NSUN = 1; sp.nvar = nvar; sp.compare = 0;
+    sp.detUR = h->udvr.detU; sp.detUL = h->udvl.detU; sp.info = h->info; sp.opang = h->opang; sp.cmp = h->cmp;
+    sp.phase = h->phase; sp.stat = h->stat; sp.err = h->err;
+    k_stab_finish<<<1, 32, 0, h->st>>>(sp);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaMemcpy(G, h->G, NN * sizeof(zd), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(phase, h->phase, sizeof(zd), cudaMemcpyDeviceToHost));
+    return 0;
+  };
+  int rc = run();
+  alfgpu_destroy(h);
+  return rc;
+}
+
+int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V) {
+  if (ndim < 1 || !U || !D || !V) return ALFGPU_ERROR_ARGUMENT;
+  const int left = (side == 'l' || side == 'L');
+  alfgpu_s* h = nullptr;
+  RET(oneshot_handle(ndim, &h));
+  const size_t N = ndim, NN = N * N;
+  auto run = [&]() -> int {
+    std::vector<double> dd(N);
+    for (size_t i = 0; i < N; ++i) dd[i] = D[2 * i];
+    UDVSet& s = h->udvr;
+    CK(cudaMemcpy(s.U, U, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.V, V, NN * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.D, dd.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    RET(decompose(h, s, left));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaMemcpy(U, s.U, NN * sizeof(zd), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(V, s.V, NN * sizeof(zd), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dd.data(), s.D, N * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < N; ++i) { D[2 * i] = dd[i]; D[2 * i + 1] = 0.0; }
+    return 0;
+  };
+  int rc = run();
+  alfgpu_destroy(h);
+  return rc;
+}
+
+}  // extern "C"

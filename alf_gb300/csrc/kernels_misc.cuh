@@ -1,0 +1,207 @@
+// Small per-slice and per-stabilisation kernels.
+#pragma once
+#include "common.cuh"
+#include "linalg.cuh"
+
+// Diagonal product of all single-site vertex exponentials of slice nt1 (1-based):
+//   S(i) = prod_{n: P(n)=i} E_exp(1, s(n,nt1)),  Sinv(i) = prod E_exp(1, -s(n,nt1)).
+// This is Op_mmultR / Op_Wrapup for diagonal operators (Operator_mod.F90:686-693,
+// 776-781) for every vertex of the slice at once.  grid (B), block 256.
+__global__ void k_slice_scale(const int8_t* fields, int L, int M, int N, int F, int nt1, const int* site,
+                              const zd* Eexp, zd* S, zd* Sinv) {
+  const int b = blockIdx.x, c = b / F, f = b % F;
+  const int8_t* fl = fields + (long long)c * L * M + (long long)(nt1 - 1) * M;
+  const int* st = site + (long long)c * F * M + (long long)f * M;
+  const zd* ee = Eexp + ((long long)c * F * M + (long long)f * M) * 5;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    zd s = zmk(1.0, 0.0), si = zmk(1.0, 0.0);
+    for (int n = 0; n < M; ++n) {
+      if (st[n] == i) {
+        int sp = fl[n];
+        s = zmul(s, ee[(long long)n * 5 + sp + 2]);
+        si = zmul(si, ee[(long long)n * 5 - sp + 2]);
+      }
+    }
+    S[(long long)b * N + i] = s;
+    Sinv[(long long)b * N + i] = si;
+  }
+}
+
+// G(i,j) <- S(i) G(i,j) Sinv(j)  (deferred vertex wraps of one slice), grid (ceil(N*N/256), B)
+__global__ void k_apply_scale(zd* G, const zd* S, const zd* Sinv, int N) {
+  const int b = blockIdx.y;
+  const long long NN = (long long)N * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < NN; e += (long long)gridDim.x * blockDim.x) {
+    int i = e % N, j = e / N;
+    zd* g = G + b * NN + e;
+    *g = zmul(zmul(S[(long long)b * N + i], *g), Sinv[(long long)b * N + j]);
+  }
+}
+
+// U = I, V = I, D = 1, det(U) = 1 (reset_UDV_state, udv_state_mod.F90:320-345)
+__global__ void k_udv_reset(zd* U, zd* V, double* D, zd* detU, int N) {
+  const int b = blockIdx.y;
+  const long long NN = (long long)N * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < NN; e += (long long)gridDim.x * blockDim.x) {
+    int i = e % N, j = e / N;
+    zd v = zmk(i == j ? 1.0 : 0.0, 0.0);
+    U[b * NN + e] = v;
+    V[b * NN + e] = v;
+    if (e < N) D[(long long)b * N + e] = 1.0;
+    if (e == 0) detU[b] = zmk(1.0, 0.0);
+  }
+}
+
+// decompose_UDV_state phase handling (udv_state_mod.F90:481-492): phase = prod R_ii *
+// pivot sign (conjugated on the L side); R(1,:) /= phase; det(U) = det(Q) * phase.
+__global__ void k_decomp_phase(zd* R, long long ldr, int N, const QRInfo* info, int left, zd* phase_out, zd* detU) {
+  const int b = blockIdx.x;
+  __shared__ zd s_beta;
+  if (threadIdx.x == 0) {
+    zd ph = info[b].prodR;
+    if (info[b].psign < 0) ph = zneg(ph);
+    if (left) ph = zconj(ph);
+    phase_out[b] = ph;
+    detU[b] = zmul(info[b].detQ, ph);
+    s_beta = zdiv(zmk(1.0, 0.0), ph);
+  }
+  __syncthreads();
+  zd* Rb = R + (long long)b * ldr * N;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) Rb[(long long)j * ldr] = zmul(s_beta, Rb[(long long)j * ldr]);
+}
+
+// U(:,1) *= phase
+__global__ void k_scale_col0(zd* U, int N, const zd* phase) {
+  const int b = blockIdx.x;
+  zd* u = U + (long long)b * N * N;
+  zd ph = phase[b];
+  for (int r = threadIdx.x; r < N; r += blockDim.x) u[r] = zmul(u[r], ph);
+}
+
+// COMPARE_C (mymats_mod.F90:683-704) with the NaN test of Control_PrecisionG
+// (control_mod.F90:219-263).  grid (B), block 256; out[b] = {xmax, xmean}.
+__global__ void k_compare(const zd* A, const zd* Bm, int N, double* out, int* err) {
+  const int b = blockIdx.x;
+  const long long NN = (long long)N * N;
+  const zd* a = A + b * NN;
+  const zd* c = Bm + b * NN;
+  double mx = 0.0, sm = 0.0;
+  int nan = 0;
+  for (long long e = threadIdx.x; e < NN; e += blockDim.x) {
+    zd x = a[e], y = c[e];
+    if (x.x != x.x || x.y != x.y || y.x != y.x || y.y != y.y) nan = 1;
+    double d = hypot(x.x - y.x, x.y - y.y);
+    mx = fmax(mx, d);
+    sm += d;
+  }
+  __shared__ double rm[8], rs[8];
+  __shared__ int rn[8];
+  mx = warp_max(mx);
+  sm = warp_sum(sm);
+  nan = __any_sync(0xffffffffu, nan);
+  if ((threadIdx.x & 31) == 0) { rm[threadIdx.x >> 5] = mx; rs[threadIdx.x >> 5] = sm; rn[threadIdx.x >> 5] = nan; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0, s = 0.0;
+    int nn = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { m = fmax(m, rm[w]); s += rs[w]; nn |= rn[w]; }
+    out[2 * b] = m;
+    out[2 * b + 1] = s / (double)NN;
+    if (nn) atomicOr(err, 1);
+  }
+}
+
+// Op_phase angle sum (Operator_mod.F90:160-181): sum over n, nt of Im(g alpha phi).
+__global__ void k_opphase(const int8_t* fields, int L, int M, int F, const zd* g, const zd* alpha, const int8_t* type,
+                          FieldTables ft, double* out) {
+  const int b = blockIdx.x, c = b / F, f = b % F;
+  const int8_t* fl = fields + (long long)c * L * M;
+  const long long k0 = (long long)c * F * M + (long long)f * M;
+  double s = 0.0;
+  for (long long e = threadIdx.x; e < (long long)L * M; e += blockDim.x) {
+    int n = e % M;
+    int sp = fl[e];
+    zd ga = zmul(g[k0 + n], alpha[k0 + n]);
+    s += ga.y * ft.phi[type[(long long)c * F * M + n] - 1][sp + 2];
+  }
+  __shared__ double r[8];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += r[w];
+    out[b] = t;
+  }
+}
+
+// Phase and precision bookkeeping after CGR on all flavours of a chain
+// (main.F90:734-753, control_mod.F90:207-320).  stat layout per chain:
+// [0] ncg [1] xmeanG_sum [2] xmaxG [3] xmaxP [4] ncg_tau [5] xmean_tau_sum [6] xmax_tau [7] sweeps
+struct StabFinishParams {
+  int C, F, NSUN, nvar, compare, init;
+  const zd* detUR; const zd* detUL;   // [B]
+  const QRInfo* info;                 // [B]
+  const double* opang;                // [B]
+  const double* cmp;                  // [B][2]
+  zd* phase;                          // [C]
+  double* stat;                       // [C][8]
+  int* err;
+  zd* rec_phase;                      // [C] slot for this point or null
+};
+
+__global__ void k_stab_finish(StabFinishParams p) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= p.C) return;
+  zd Z = zmk(1.0, 0.0);
+  double* st = p.stat + 8ll * c;
+  for (int f = 0; f < p.F; ++f) {
+    const int b = c * p.F + f;
+    zd ph = zmul(p.detUR[b], zconj(p.detUL[b]));  // conj(det(U_R^H U_L))
+    ph = zscale(ph, 1.0 / zabs(ph));
+    if (p.info[b].psign < 0) ph = zneg(ph);
+    zd q = zmul(p.info[b].prodR, p.info[b].detQ);
+    if (p.nvar != 1) q = zconj(q);
+    ph = zmul(ph, q);
+    double s, co;
+    sincos(p.opang[b], &s, &co);
+    ph = zmul(ph, zmk(co, s));
+    Z = zmul(Z, ph);
+    if (p.compare) {
+      double xmax = p.cmp[2 * b], xmean = p.cmp[2 * b + 1];
+      st[0] += 1.0;
+      if (xmax > 10.0) atomicOr(p.err, 2);
+      if (xmax > st[2]) st[2] = xmax;
+      st[1] += xmean;
+    }
+  }
+  zd Zp = Z;
+  for (int e = 1; e < p.NSUN; ++e) Zp = zmul(Zp, Z);
+  if (p.compare) {
+    double X = zabs(zsub(Zp, p.phase[c]));
+    if (X > st[3]) st[3] = X;
+  }
+  p.phase[c] = Zp;
+  if (p.rec_phase) p.rec_phase[c] = Zp;
+}
+
+__global__ void k_real_to_complex(const double* a, zd* out, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = zmk(a[i], 0.0);
+}
+__global__ void k_real_to_complex2(const double* a, const double* b, zd* oa, zd* ob, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) {
+    oa[i] = zmk(a[i], 0.0);
+    ob[i] = zmk(b[i], 0.0);
+  }
+}
+// per-batch flush rank: out[c*F + f] = m[c]
+__global__ void k_expand_m(const int* m, int* out, int C, int F) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < C * F) out[b] = m[b / F];
+}
+__global__ void k_count_sweep(double* stat, int C) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < C) stat[8 * c + 7] += 1.0;
+}

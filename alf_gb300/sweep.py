@@ -1,0 +1,155 @@
+"""Host-side API over the GPU library, mirroring ALF's sweep interface.
+
+``Chains`` owns one library handle (``alfgpu_create``) for ``n_chains``
+Markov chains that share lattice size, Ltrot and Nwrap.  Its methods map onto
+the Fortran driver's steps:
+
+=========================  =============================================
+``Chains.init_state()``    Prog/main.F90:589-631 (WRAPUL chain + CGR)
+``Chains.sweep()``         Prog/main.F90:714-887 (up pass, down pass,
+                           stabilisations, TAU_M when enabled)
+``Chains.green(c)``        GR(:,:,:) of chain c
+``Chains.stats(c)``        Control_upgrade / Control_Precision* counters
+=========================  =============================================
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .model import Model
+
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Chains:
+    def __init__(self, model: Model, n_chains: int = 1, precision: str = "fp64", delay_k: int = 0,
+                 device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None):
+        self.L = _lib.lib()
+        self.model = model
+        self.C = n_chains
+        self.N, self.F, self.M, self.Lt = model.ndim, model.n_fl, model.n_op, model.ltrot
+        d = _lib.Dims(model.ndim, model.n_fl, model.n_sun, model.n_op, model.ltrot, model.nwrap, n_chains,
+                      PRECISIONS[precision], delay_k, ltau, device)
+        h = C.c_void_p()
+        _lib.check(self.L.alfgpu_create(C.byref(h), C.byref(d)), "alfgpu_create")
+        self.h = h
+        self._keep = []
+        pk = model.pack()
+        _lib.check(self.L.alfgpu_upload_hopping(self.h, _p(pk["expT"]), _p(pk["expTinv"])), "alfgpu_upload_hopping")
+        if models is None:
+            self._upload_vertices(-1, pk)
+        else:
+            assert len(models) == n_chains
+            for c, m in enumerate(models):
+                self._upload_vertices(c, m.pack())
+
+    def _upload_vertices(self, chain: int, pk: dict):
+        v = _lib.Vertices(*[_p(np.ascontiguousarray(pk[k])).value for k in
+                            ("op_n", "op_nz", "op_diag", "op_type", "op_P", "op_g", "op_alpha", "op_E",
+                             "op_U", "op_Eexp", "op_Mexp")])
+        self._keep.append(pk)
+        _lib.check(self.L.alfgpu_upload_vertices(self.h, chain, C.byref(v)), "alfgpu_upload_vertices")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.alfgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # --- fields and draws -------------------------------------------------------------------
+    def set_fields(self, chain: int, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.int8)
+        assert f.shape == (self.Lt, self.M)
+        _lib.check(self.L.alfgpu_set_fields(self.h, chain, _p(f)), "alfgpu_set_fields")
+
+    def fields(self, chain: int) -> np.ndarray:
+        f = np.zeros((self.Lt, self.M), np.int8)
+        _lib.check(self.L.alfgpu_get_fields(self.h, chain, _p(f)), "alfgpu_get_fields")
+        return f
+
+    def set_rng(self, chain: int, seed: int, counter: int):
+        _lib.check(self.L.alfgpu_set_rng(self.h, chain, seed, counter), "alfgpu_set_rng")
+
+    # --- the sweep -----------------------------------------------------------------------------
+    def init_state(self) -> np.ndarray:
+        ph = np.zeros(self.C, np.complex128)
+        _lib.check(self.L.alfgpu_init_state(self.h, _p(ph)), "alfgpu_init_state")
+        return ph
+
+    def sweep(self, uniforms: Optional[np.ndarray] = None):
+        if uniforms is not None:
+            u = np.ascontiguousarray(uniforms, dtype=np.float64)
+            assert u.size == self.C * 6 * self.M * self.Lt
+            rc = self.L.alfgpu_sweep(self.h, _p(u), _lib.OBS_CB(), None)
+        else:
+            rc = self.L.alfgpu_sweep(self.h, None, _lib.OBS_CB(), None)
+        _lib.check(rc, "alfgpu_sweep")
+
+    # --- readback --------------------------------------------------------------------------------
+    def green(self, chain: int = 0) -> np.ndarray:
+        G = np.zeros((self.F, self.N, self.N), np.complex128)
+        _lib.check(self.L.alfgpu_get_green(self.h, chain, _p(G)), "alfgpu_get_green")
+        return np.transpose(G, (0, 2, 1)).copy()
+
+    def phase(self) -> np.ndarray:
+        ph = np.zeros(self.C, np.complex128)
+        _lib.check(self.L.alfgpu_get_phase(self.h, _p(ph)), "alfgpu_get_phase")
+        return ph
+
+    def stats(self, chain: int = 0) -> _lib.Stats:
+        s = _lib.Stats()
+        _lib.check(self.L.alfgpu_get_stats(self.h, chain, C.byref(s)), "alfgpu_get_stats")
+        return s
+
+    def reset_stats(self):
+        _lib.check(self.L.alfgpu_reset_stats(self.h), "alfgpu_reset_stats")
+
+    def set_recording(self, enable: bool = True):
+        _lib.check(self.L.alfgpu_set_recording(self.h, int(enable)), "alfgpu_set_recording")
+
+    def record(self, chain: int = 0) -> dict:
+        V = 2 * self.M * self.Lt
+        P = 2 * self.model.nstm
+        acc = np.zeros(V, np.int8)
+        ratio = np.zeros(V, np.complex128)
+        G = np.zeros((P, self.F, self.N, self.N), np.complex128)
+        Gw = np.zeros((P, self.F, self.N, self.N), np.complex128)
+        ph = np.zeros(P, np.complex128)
+        _lib.check(self.L.alfgpu_get_record(self.h, chain, _p(acc), _p(ratio), _p(G), _p(Gw), _p(ph)),
+                   "alfgpu_get_record")
+        return dict(acc=acc, ratio=ratio, G=np.transpose(G, (0, 1, 3, 2)).copy(),
+                    Gwrap=np.transpose(Gw, (0, 1, 3, 2)).copy(), phase=ph)
+
+
+def cgr(nvar: int, UR, DR, VR, UL, DL, VL):
+    """GPU ``CGR`` on explicit UDV factors (row-major numpy in/out)."""
+    L = _lib.lib()
+    N = UR.shape[0]
+    cm = lambda A: np.ascontiguousarray(np.asarray(A, np.complex128).T)
+    args = [cm(UR), np.ascontiguousarray(DR, np.complex128), cm(VR), cm(UL), np.ascontiguousarray(DL, np.complex128),
+            cm(VL)]
+    G = np.zeros((N, N), np.complex128)
+    ph = np.zeros(1, np.complex128)
+    _lib.check(L.alfgpu_cgr(N, nvar, *[_p(a) for a in args], _p(G), _p(ph)), "alfgpu_cgr")
+    return G.T.copy(), complex(ph[0])
+
+
+def decompose(side: str, U, D, V):
+    """GPU ``decompose_UDV_state`` on explicit factors (row-major numpy in/out)."""
+    L = _lib.lib()
+    N = U.shape[0]
+    Uc = np.ascontiguousarray(np.asarray(U, np.complex128).T)
+    Vc = np.ascontiguousarray(np.asarray(V, np.complex128).T)
+    Dc = np.ascontiguousarray(D, np.complex128).copy()
+    _lib.check(L.alfgpu_decompose(N, C.c_char(side.encode()), _p(Uc), _p(Dc), _p(Vc)), "alfgpu_decompose")
+    return Uc.T.copy(), Dc, Vc.T.copy()

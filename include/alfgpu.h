@@ -1,0 +1,165 @@
+/*
+ * alfgpu -- GB300-native finite-temperature AFQMC sweep (ALF drop-in).
+ *
+ * C ABI of the GPU library.  All matrices are complex128 stored Fortran-style
+ * (column-major, interleaved real/imaginary doubles), i.e. the memory layout of
+ * ALF's `Complex(Kind=Kind(0.d0)) :: GR(Ndim,Ndim,N_FL)`.  Every entry point
+ * returns an int status from ALF's runtime_error_mod enumeration
+ * (Libraries/Modules/runtime_error_mod.F90:57-66) or one of the library codes
+ * >= 100; the library never aborts the process and never traps on the device.
+ *
+ * One handle holds n_chains independent Markov chains that share Ndim, N_FL,
+ * N_SUN, the number of vertices and Ltrot; each chain has its own vertex tables
+ * (so U may differ per chain), its own fields, G, UDV stack and draw stream.
+ * All sweep state stays resident on the GPU between calls.
+ *
+ * Replaced reference interfaces (paths inside the ALF tree):
+ *   alfgpu_init_state  <- Prog/main.F90:589-631 (WRAPUL chain + CGR + Op_phase)
+ *   alfgpu_sweep       <- Prog/main.F90:714-887 (the `If (get_sequential())` block:
+ *                         WRAPGRUP Prog/Wrapgr_mod.F90:81, WRAPGRDO :160,
+ *                         WRAPUR Prog/wrapur_mod.F90:37, WRAPUL Prog/wrapul_mod.F90:36,
+ *                         CGR Prog/cgr1_mod.F90:36, Upgrade2 Prog/upgrade_mod.F90:105,
+ *                         and TAU_M Prog/tau_m_mod.F90:56 when ltau = 1)
+ *   alfgpu_cgr         <- CGR(PHASE, NVAR, GRUP, udvr, udvl), Prog/cgr1_mod.F90:36
+ *   alfgpu_decompose   <- decompose_UDV_state, Prog/udv_state_mod.F90:448
+ */
+#ifndef ALFGPU_H
+#define ALFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: 0..9 mirror runtime_error_mod.F90:57-66. */
+enum {
+  ALFGPU_ERROR_NONE = 0,
+  ALFGPU_ERROR_GENERIC = 1,
+  ALFGPU_ERROR_FILE_NOT_FOUND = 2,
+  ALFGPU_ERROR_UNSTABLE_MATRIX = 3, /* Precision Green > 10 (control_mod.F90:267-294) */
+  ALFGPU_ERROR_MISSING_OBS = 4,
+  ALFGPU_ERROR_FIELDS = 5,          /* field value outside {+-1, +-2} */
+  ALFGPU_ERROR_HAMILTONIAN = 6,     /* invalid operator tables */
+  ALFGPU_ERROR_GLOBAL_UPDATES = 7,
+  ALFGPU_ERROR_MAXENT = 8,
+  ALFGPU_ERROR_RUNNING_FILE_FOUND = 9,
+  ALFGPU_ERROR_CUDA = 100,          /* a CUDA runtime call failed */
+  ALFGPU_ERROR_ARGUMENT = 101,      /* bad pointer / size / index */
+  ALFGPU_ERROR_UNSUPPORTED = 102,   /* model feature not implemented on the GPU */
+  ALFGPU_ERROR_NAN = 103,           /* NaN in G (control_mod.F90:219-263 aborts with ERROR_GENERIC) */
+  ALFGPU_ERROR_TIMEOUT = 104        /* a bounded device-side wait gave up */
+};
+
+enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
+
+typedef struct alfgpu_s alfgpu_t;
+
+typedef struct {
+  int32_t ndim;      /* Ndim */
+  int32_t n_fl;      /* N_FL (= N_FL_eff; flavour reconstruction is not used) */
+  int32_t n_sun;     /* N_SUN after the model's own adjustment */
+  int32_t n_op;      /* Size(Op_V,1): vertices per time slice */
+  int32_t ltrot;     /* Ltrot */
+  int32_t nwrap;     /* Nwrap; Stab_nt follows main.F90:446-457 */
+  int32_t n_chains;  /* independent Markov chains in this handle */
+  int32_t precision; /* ALFGPU_PRECISION_FP64 or ALFGPU_PRECISION_MIXED */
+  int32_t delay_k;   /* vertex visits per delayed-update block (0: library default) */
+  int32_t ltau;      /* 1: time-displaced Green functions (TAU_M) after every sweep */
+  int32_t device;    /* CUDA device ordinal */
+  int32_t reserved[5];
+} alfgpu_dims;
+
+/* Interaction vertices Op_V(n,nf) after Op_set (Prog/Operator_mod.F90:259-472),
+ * struct-of-arrays with index k = nf*n_op + n.  Complex arrays are interleaved.
+ *   op_n[k]      Op%N (1 or 2 sites)          op_nz[k]   Op%N_non_zero
+ *   op_diag[k]   Op%diag                       op_type[k] Op%type (1 or 2)
+ *   op_P[2k+a]   Op%P(a+1) - 1 (0-based site)  op_g[k], op_alpha[k]   complex
+ *   op_E[2k+m]   Op%E(m+1)                     op_U[k]    2x2 column-major
+ *   op_Eexp[k]   [m][s+2] = E_exp(m+1, s)      op_Mexp[k] [s+2] 2x2 column-major M_exp */
+typedef struct {
+  const int32_t* op_n;
+  const int32_t* op_nz;
+  const int32_t* op_diag;
+  const int32_t* op_type;
+  const int32_t* op_P;
+  const double* op_g;
+  const double* op_alpha;
+  const double* op_E;
+  const double* op_U;
+  const double* op_Eexp;
+  const double* op_Mexp;
+} alfgpu_vertices;
+
+typedef struct {
+  int64_t n_prop, n_acc;          /* Control_upgrade counters (upgrade_mod.F90:295-298) */
+  int64_t n_prop_eff, n_acc_eff;  /* Control_upgrade_eff */
+  int64_t ncg;                    /* number of Precision Green comparisons */
+  double xmeanG_sum, xmaxG;       /* Control_PrecisionG: sum of mean, max |G_wrap - G_fresh| */
+  double xmaxP;                   /* Control_PrecisionP: max |phase_wrap - phase_fresh| */
+  int64_t ncg_tau;
+  double xmean_tau_sum, xmax_tau; /* Control_Precision_tau */
+  int64_t sweeps;
+} alfgpu_stats;
+
+/* Observable callback: the Fortran side's ham%Obser (kind 0, G = GR(N,N,N_FL)) or
+ * ham%ObserT (kind 1, G = [GT0, G0T, G00, GTT] each N x N x N_FL).  Buffers are
+ * library-owned pinned memory, valid only during the call. */
+typedef void (*alfgpu_obs_cb)(void* ctx, int32_t chain, int32_t ntau, int32_t kind, const double* G,
+                              const double* phase);
+
+/* Handle lifetime. */
+int alfgpu_create(alfgpu_t** h, const alfgpu_dims* dims);
+void alfgpu_destroy(alfgpu_t* h);
+const char* alfgpu_error_string(int code);
+
+/* Model upload.  expT / expTinv are the real `mat` / `invmat` of RealExpOpT
+ * (Prog/OpTTypes_mod.F90:92-133), n_fl x Ndim x Ndim column-major, shared by all
+ * chains.  Vertex tables are per chain (chain = -1 uploads the same tables to all). */
+int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv);
+int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v);
+
+/* Fields nsigma%f(n, nt): int8 values in {+-1, +-2}, Ltrot x n_op (n fastest). */
+int alfgpu_set_fields(alfgpu_t* h, int32_t chain, const int8_t* f);
+/* Same, from ALF's complex storage (real parts are the field values). */
+int alfgpu_set_fields_c128(alfgpu_t* h, int32_t chain, const double* f);
+int alfgpu_get_fields(alfgpu_t* h, int32_t chain, int8_t* f);
+
+/* Per-chain draw stream used when alfgpu_sweep gets uniforms = NULL. */
+int alfgpu_set_rng(alfgpu_t* h, int32_t chain, uint64_t seed, uint64_t counter);
+
+/* Initial UDV stack and G (main.F90:589-631); phase_out: complex per chain (may be NULL). */
+int alfgpu_init_state(alfgpu_t* h, double* phase_out);
+
+/* One sequential sweep on every chain.  uniforms: host array n_chains x (6*n_op*Ltrot),
+ * three draws per vertex visit in visit order (up pass nt=1..L, n=1..M; down pass
+ * nt=L..1, n=M..1; slots: flip choice, T0 test, Metropolis), or NULL for the
+ * device stream.  cb may be NULL (no measurements). */
+int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx);
+
+/* State readback. */
+int alfgpu_get_green(alfgpu_t* h, int32_t chain, double* G);  /* Ndim x Ndim x N_FL */
+int alfgpu_get_phase(alfgpu_t* h, double* phase);             /* complex per chain */
+int alfgpu_get_stats(alfgpu_t* h, int32_t chain, alfgpu_stats* s);
+int alfgpu_reset_stats(alfgpu_t* h);
+
+/* Parity recording (diagnostics): while enabled, every vertex visit's ratio and
+ * accept bit, and G and the phase at every stabilisation point are kept on the
+ * device for the next sweep; alfgpu_get_record copies them out for one chain.
+ * Sizes per sweep: visits = 2*n_op*Ltrot, points = 2*Nstm. */
+int alfgpu_set_recording(alfgpu_t* h, int32_t enable);
+int alfgpu_get_record(alfgpu_t* h, int32_t chain, int8_t* acc, double* ratio, double* G_fresh,
+                      double* G_wrapped, double* phase);
+
+/* Stream the library launches on (a cudaStream_t), for callers that overlap work. */
+void* alfgpu_stream(alfgpu_t* h);
+
+/* One-shot component entry points on host buffers (allocate their own device memory). */
+int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, const double* VR, const double* UL,
+               const double* DL, const double* VL, double* G, double* phase);
+int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALFGPU_H */

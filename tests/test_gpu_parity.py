@@ -1,0 +1,162 @@
+"""GPU parity tests: the CUDA path (called through the C ABI) against the CPU oracle.
+
+Tolerances follow the acceptance criteria for the plain complex128 form:
+G at every stabilisation point and every Metropolis ratio within 1e-10
+relative, identical accept/reject sequences and final fields from the same
+draws.  All tests run on cuda:0 and are skipped without a GPU.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from alf_gb300 import model as mdl, rng
+from alf_gb300.sweep import Chains, cgr as gpu_cgr, decompose as gpu_decompose
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _relmax(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_decompose_matches_oracle_and_reconstructs():
+    rs = np.random.default_rng(4782347)
+    N = 32
+    for side in ("r", "l"):
+        U, D, V = np.eye(N, dtype=complex), np.ones(N, complex), np.eye(N, dtype=complex)
+        Uo, Do, Vo = U.copy(), D.copy(), V.copy()
+        P = np.eye(N, dtype=complex)
+        for _ in range(6):
+            X = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+            U, Uo, P = X @ U, X @ Uo, X @ P
+            U, D, V = gpu_decompose(side, U, D, V)
+            Uo, Do, Vo = oracle.decompose(side, Uo, Do, Vo)
+            R = U @ np.diag(D) @ (V if side == "r" else V.conj().T)
+            assert _relmax(R, P) < 1e-10
+            assert np.max(np.abs(U.conj().T @ U - np.eye(N))) < 1e-12
+            assert _relmax(D, Do) < 1e-10
+
+
+def test_cgr_matches_naive_15cgr_and_oracle():
+    N = 5
+    for nvar in (1, 2):
+        UR = np.eye(N, dtype=complex)
+        UL = np.eye(N, dtype=complex)
+        VR = np.array([[complex(i, j) for j in range(1, N + 1)] for i in range(1, N + 1)])
+        VL = np.array([[complex(i + j, 0) for j in range(1, N + 1)] for i in range(1, N + 1)])
+        for i in range(N):
+            VR[i, i] = 1 + 1j
+            VL[i, i] = 1 + 1j
+        DL = np.ones(N, complex)
+        DR = np.arange(1, N + 1).astype(complex)
+        G, ph = gpu_cgr(nvar, UR, DR, VR, UL, DL, VL)
+        M = np.eye(N) + UR @ np.diag(DR) @ VR @ VL @ np.diag(DL) @ UL.conj().T
+        assert _relmax(G, np.linalg.inv(M)) < 1e-10
+        d = np.linalg.det(M)
+        assert abs(ph - d / abs(d)) < 1e-13
+    # random unitary U's and graded D's, against the oracle
+    rs = np.random.default_rng(7)
+    N = 48
+    q = lambda: np.linalg.qr(rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N)))[0]
+    UR, UL = q(), q()
+    VR = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+    VL = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+    DR = np.exp(np.linspace(8, -8, N)).astype(complex)
+    DL = np.exp(np.linspace(6, -6, N)).astype(complex)
+    for nvar in (1, 2):
+        G, ph = gpu_cgr(nvar, UR, DR, VR, UL, DL, VL)
+        Go, pho = oracle.cgr(nvar, UR, DR, VR, UL, DL, VL)
+        assert _relmax(G, Go) < 1e-10
+        assert abs(ph - pho) < 1e-10
+
+
+def _run_pair(m, seed=5, sweeps=1, chain=0):
+    f0 = rng.initial_fields(seed, chain, m.n_op, m.ltrot)
+    o = oracle.Oracle(m)
+    o.set_fields(f0)
+    ph_o = o.init_state()
+    g = Chains(m, n_chains=1)
+    g.set_fields(0, f0)
+    ph_g = g.init_state()[0]
+    assert abs(ph_g - ph_o) < 1e-10
+    assert _relmax(g.green(0), o.green()) < RTOL
+    g.set_recording(True)
+    for s in range(sweeps):
+        u = rng.sweep_uniforms(seed, chain, m.n_op, m.ltrot, s)
+        ro = o.record(1)
+        o.sweep(u)
+        g.sweep(u[None, :])
+        rg = g.record(0)
+        np.testing.assert_array_equal(rg["acc"], ro["acc"])
+        acc = ro["acc"].astype(bool)
+        r_o, r_g = ro["ratio"], rg["ratio"]
+        assert np.max(np.abs(r_g - r_o) / np.maximum(np.abs(r_o), 1e-300)) < RTOL
+        for p in range(ro["G"].shape[0]):
+            assert _relmax(rg["G"][p], ro["G"][p]) < RTOL, (s, p)
+            assert _relmax(rg["Gwrap"][p], ro["Gwrap"][p]) < 1e-8, (s, p)
+        np.testing.assert_array_equal(g.fields(0), o.fields())
+        assert _relmax(g.green(0), o.green()) < RTOL
+        assert abs(g.phase()[0] - o.phase()) < 1e-10
+    so, sg = o.stats(), g.stats(0)
+    assert sg.n_acc == so.n_acc and sg.n_prop == so.n_prop
+    assert abs(sg.xmaxG - so.xmaxG) <= 1e-8 + 1e-3 * so.xmaxG
+    return g, o
+
+
+def test_init_and_sweep_hubbard_4x4_parity():
+    # the small reference configuration: 4x4 square Hubbard, U=4, beta=4, dtau=0.1, Nwrap=10
+    _run_pair(mdl.config("hubbard4x4"), sweeps=3)
+
+
+def test_sweep_hubbard_odd_sizes_parity():
+    # ragged blocks (M not a multiple of the delay block), odd Nwrap remainder
+    m = mdl.hubbard("square", 6, 4, U=6.0, beta=1.3, dtau=0.1, nwrap=4)
+    _run_pair(m, seed=9, sweeps=2)
+
+
+def test_sweep_honeycomb_parity():
+    m = mdl.hubbard("honeycomb", 3, 3, U=5.0, beta=1.0, dtau=0.05, nwrap=5)
+    _run_pair(m, seed=3, sweeps=2)
+
+
+def test_twenty_sweeps_identical_accept_sequence():
+    m = mdl.hubbard("square", 4, 4, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    _run_pair(m, seed=17, sweeps=20)
+
+
+def test_device_stream_matches_host_draws():
+    m = mdl.config("hubbard4x4")
+    seed = 23
+    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+    a = Chains(m)
+    a.set_fields(0, f0)
+    a.init_state()
+    a.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    a.sweep(None)
+    b = Chains(m)
+    b.set_fields(0, f0)
+    b.init_state()
+    b.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)[None, :])
+    np.testing.assert_array_equal(a.fields(0), b.fields(0))
+    assert _relmax(a.green(0), b.green(0)) == 0.0
+
+
+def test_batched_chains_match_single_chains():
+    m = mdl.config("hubbard4x4")
+    C = 3
+    g = Chains(m, n_chains=C)
+    fs = [rng.initial_fields(100 + c, c, m.n_op, m.ltrot) for c in range(C)]
+    for c in range(C):
+        g.set_fields(c, fs[c])
+    g.init_state()
+    u = np.stack([rng.sweep_uniforms(100 + c, c, m.n_op, m.ltrot, 0) for c in range(C)])
+    g.sweep(u)
+    for c in range(C):
+        o = oracle.Oracle(m)
+        o.set_fields(fs[c])
+        o.init_state()
+        o.sweep(u[c])
+        np.testing.assert_array_equal(g.fields(c), o.fields())
+        assert _relmax(g.green(c), o.green()) < RTOL
