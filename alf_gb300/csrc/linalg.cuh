@@ -203,16 +203,14 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
         dq = zmul(dq, zscale(h, 1.0 / zabs(h)));
       }
     }
-    // permutation sign by cycle lengths
+    // permutation sign by cycle lengths (visited flags reuse the vector buffer)
+    int* vis = reinterpret_cast<int*>(vsh);
+    for (int i = 0; i < N; ++i) vis[i] = 0;
     int sgn = 1;
     for (int i = 0; i < N; ++i) {
+      if (vis[i]) continue;
       int next = i, len = 0;
-      // cycle start = smallest index of the cycle
-      bool first = true;
-      int x = i;
-      do { if (x < i) { first = false; break; } x = jpvt[x] - 1; } while (x != i);
-      if (!first) continue;
-      do { len++; next = jpvt[next] - 1; } while (next != i);
+      while (!vis[next]) { vis[next] = 1; len++; next = jpvt[next] - 1; }
       if (len % 2 == 0) sgn = -sgn;
     }
     p.info[b].detQ = dq;
