@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
     for (int i = 0; i < N; ++i) {
       if (vis[i]) continue;
       int next = i, len = 0;
-      while (!vis[next]) { vis[next] = 1; len++; next = jpvt[next] - 1; }
+      while (next >= 0 && next < N && !vis[next]) { vis[next] = 1; len++; next = jpvt[next] - 1; }
       if (len % 2 == 0) sgn = -sgn;
     }
     p.info[b].detQ = dq;
