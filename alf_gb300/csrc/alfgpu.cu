@@ -241,22 +241,10 @@ static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
     RET(slice_scale(h, nt));
     GemmParams p = gsq(h, B);
-    p.A = h->expT; p.realA = 1; p.sA = 0;  // replaced by flavour offsets below
+    p.A = h->expT; p.realA = 1; p.modA = h->F;
     p.B = h->udvr.U; p.C = h->T1;
     p.rs = h->S; p.sRS = N;
-    if (h->F == 1) {
-      RET(gemm(h, p));
-    } else {
-      for (int f = 0; f < h->F; ++f) {  // per flavour: A = expT[f], batch over chains (stride F)
-        GemmParams q = p;
-        q.A = h->expT + (long long)f * N * N;
-        q.B = h->udvr.U + (long long)f * N * N; q.sB = (long long)h->F * N * N;
-        q.C = h->T1 + (long long)f * N * N; q.sC = (long long)h->F * N * N;
-        q.rs = h->S + (long long)f * N; q.sRS = (long long)h->F * N;
-        q.batch = h->C;
-        RET(gemm(h, q));
-      }
-    }
+    RET(gemm(h, p));
     RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
   }
   return decompose(h, h->udvr, 0);
@@ -264,18 +252,15 @@ static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
 
 // WRAPUL (wrapul_mod.F90:108-131): U <- prod_nt [expT conj(D_nt)] U (descending nt), decompose (side L)
 static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
-  const int N = h->N;
+  const int N = h->N, B = h->B;
   for (int nt = ntau1; nt >= ntau + 1; --nt) {
     RET(slice_scale(h, nt));
-    for (int f = 0; f < h->F; ++f) {
-      GemmParams q = gsq(h, h->C);
-      q.A = h->expT + (long long)f * N * N; q.realA = 1; q.sA = 0;
-      q.B = h->udvl.U + (long long)f * N * N; q.sB = (long long)h->F * N * N;
-      q.C = h->T1 + (long long)f * N * N; q.sC = (long long)h->F * N * N;
-      q.ks = h->S + (long long)f * N; q.sKS = (long long)h->F * N; q.ksConj = 1;
-      RET(gemm(h, q));
-    }
-    RET(copy_mats(h, h->udvl.U, h->T1, (size_t)h->B * N * N));
+    GemmParams q = gsq(h, B);
+    q.A = h->expT; q.realA = 1; q.modA = h->F;
+    q.B = h->udvl.U; q.C = h->T1;
+    q.ks = h->S; q.sKS = N; q.ksConj = 1;
+    RET(gemm(h, q));
+    RET(copy_mats(h, h->udvl.U, h->T1, (size_t)B * N * N));
   }
   return decompose(h, h->udvl, 1);
 }
@@ -385,44 +370,31 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
 // Hopping wraps with the slice's deferred vertex scalings (Wrapgr_mod.F90:110-114, 237-241).
 // up:   G <- expT (S G Sinv) expTinv      down: G <- expTinv (Sinv G S) expT
 static int hop(alfgpu_s* h, int up, int with_scale) {
-  const int N = h->N, F = h->F;
+  const int N = h->N, F = h->F, B = h->B;
   const long long NN = (long long)N * N;
-  for (int f = 0; f < F; ++f) {
-    const double* E1 = (up ? h->expT : h->expTinv) + f * NN;
-    const double* E2 = (up ? h->expTinv : h->expT) + f * NN;
-    const zd* s1 = up ? h->S : h->Sinv;  // applied next to the first (left) factor
-    const zd* s2 = up ? h->Sinv : h->S;
-    if (up) {
-      // T1 = expT * diag(S) * G
-      GemmParams p = gsq(h, h->C);
-      p.A = E1; p.realA = 1; p.sA = 0;
-      p.B = h->G + f * NN; p.sB = F * NN;
-      p.C = h->T1 + f * NN; p.sC = F * NN;
-      if (with_scale) { p.ks = s1 + (long long)f * N; p.sKS = (long long)F * N; p.ksOnA = 0; }
-      RET(gemm(h, p));
-      // G = T1 * diag(Sinv) * expTinv
-      GemmParams q = gsq(h, h->C);
-      q.A = h->T1 + f * NN; q.sA = F * NN;
-      q.B = E2; q.realB = 1; q.sB = 0;
-      q.C = h->G + f * NN; q.sC = F * NN;
-      if (with_scale) { q.ks = s2 + (long long)f * N; q.sKS = (long long)F * N; q.ksOnA = 1; }
-      RET(gemm(h, q));
-    } else {
-      // T1 = G * diag(S) * expT
-      GemmParams p = gsq(h, h->C);
-      p.A = h->G + f * NN; p.sA = F * NN;
-      p.B = E2; p.realB = 1; p.sB = 0;
-      p.C = h->T1 + f * NN; p.sC = F * NN;
-      if (with_scale) { p.ks = s2 + (long long)f * N; p.sKS = (long long)F * N; p.ksOnA = 1; }
-      RET(gemm(h, p));
-      // G = expTinv * diag(Sinv) * T1
-      GemmParams q = gsq(h, h->C);
-      q.A = E1; q.realA = 1; q.sA = 0;
-      q.B = h->T1 + f * NN; q.sB = F * NN;
-      q.C = h->G + f * NN; q.sC = F * NN;
-      if (with_scale) { q.ks = s1 + (long long)f * N; q.sKS = (long long)F * N; q.ksOnA = 0; }
-      RET(gemm(h, q));
-    }
+  const double* E1 = up ? h->expT : h->expTinv;   // left factor
+  const double* E2 = up ? h->expTinv : h->expT;   // right factor
+  if (up) {
+    // T1 = expT * diag(S) * G ; G = T1 * diag(Sinv) * expTinv
+    GemmParams p = gsq(h, B);
+    p.A = E1; p.realA = 1; p.modA = F;
+    p.B = h->G; p.C = h->T1;
+    if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 0; }
+    RET(gemm(h, p));
+    GemmParams q = gsq(h, B);
+    q.A = h->T1; q.B = E2; q.realB = 1; q.modB = F; q.C = h->G;
+    if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 1; }
+    RET(gemm(h, q));
+  } else {
+    // T1 = G * diag(S) * expT ; G = expTinv * diag(Sinv) * T1
+    GemmParams p = gsq(h, B);
+    p.A = h->G; p.B = E2; p.realB = 1; p.modB = F; p.C = h->T1;
+    if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 1; }
+    RET(gemm(h, p));
+    GemmParams q = gsq(h, B);
+    q.A = E1; q.realA = 1; q.modA = F; q.B = h->T1; q.C = h->G;
+    if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 0; }
+    RET(gemm(h, q));
   }
   return 0;
 }
@@ -448,8 +420,10 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.ft = h->ft;
     k_update_block<<<h->C, 64, UPD_SMEM_BYTES, h->st>>>(u);
     CK(cudaGetLastError());
-    k_flush_prep<<<dim3((N + 127) / 128, F, h->C), 128, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->X,
-                                                                     h->Y);
+    k_flush_x<<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites,
+                                                                                 h->X);
+    CK(cudaGetLastError());
+    k_flush_y<<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->Y);
     CK(cudaGetLastError());
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();

@@ -27,6 +27,7 @@ struct GemmParams {
   const int* permB; long long sPB;
   const int* kdyn;  // per-batch K (<= k) or null
   int batch;
+  int modA, modB;   // if > 0, operand batch index = b % mod (an operand shared across chains)
 };
 
 static inline GemmParams gemm_defaults() {
@@ -79,8 +80,9 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
   const int g = lane >> 2, t = lane & 3;
 
   const int K = p.kdyn ? min(p.kdyn[b], p.k) : p.k;
-  const void* A = p.realA ? (const void*)((const double*)p.A + b * p.sA) : (const void*)((const zd*)p.A + b * p.sA);
-  const void* B = p.realB ? (const void*)((const double*)p.B + b * p.sB) : (const void*)((const zd*)p.B + b * p.sB);
+  const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
+  const void* A = p.realA ? (const void*)((const double*)p.A + bA * p.sA) : (const void*)((const zd*)p.A + bA * p.sA);
+  const void* B = p.realB ? (const void*)((const double*)p.B + bB * p.sB) : (const void*)((const zd*)p.B + bB * p.sB);
   zd* C = p.C + b * p.sC;
   const zd* ks = p.ks ? p.ks + b * p.sKS : nullptr;
   const int* pA = p.permA ? p.permA + b * p.sPA : nullptr;

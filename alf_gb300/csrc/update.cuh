@@ -76,6 +76,10 @@ __global__ void __launch_bounds__(64) k_update_block(UpdParams p) {
   __shared__ int sites[UPD_KMAX];                 // site of block position
   __shared__ int vtx[UPD_KMAX];                   // vertex n of block position
   __shared__ zd yv[2][UPD_KMAX];
+  __shared__ zd v_g[2][UPD_KMAX], v_al[2][UPD_KMAX];
+  __shared__ double v_E[2][UPD_KMAX];
+  __shared__ int v_s[UPD_KMAX], v_t[UPD_KMAX];
+  __shared__ double v_u[UPD_KMAX][3];
   __shared__ zd Dcand[2], Rf[2], delta_new[2];
   __shared__ int s_m, s_acc, s_snew;
   __shared__ zd s_phase;
@@ -93,6 +97,21 @@ __global__ void __launch_bounds__(64) k_update_block(UpdParams p) {
     int n = p.dir == 0 ? pos : M - 1 - pos;
     vtx[q] = n;
     sites[q] = site[n];  // flavour 0 site; single-site diagonal vertices share P across flavours
+    v_s[q] = fl[n];
+    v_t[q] = ty[n];
+    for (int f = 0; f < F; ++f) {
+      v_g[f][q] = gg[f * M + n];
+      v_al[f][q] = al[f * M + n];
+      v_E[f][q] = EE[f * M + n];
+    }
+    const int v = p.visit_base + pos;
+    if (p.draws) {
+      const double* d = p.draws + (long long)c * p.sDraws + 3ll * v;
+      v_u[q][0] = d[0]; v_u[q][1] = d[1]; v_u[q][2] = d[2];
+    } else {
+      unsigned long long key = p.rngkey[c], ctr = p.rngctr[c] + 3ull * v;
+      v_u[q][0] = alf_uniform(key, ctr); v_u[q][1] = alf_uniform(key, ctr + 1); v_u[q][2] = alf_uniform(key, ctr + 2);
+    }
   }
   if (threadIdx.x == 0) { s_m = 0; s_phase = p.phase[c]; }
   __syncthreads();
@@ -109,24 +128,16 @@ __global__ void __launch_bounds__(64) k_update_block(UpdParams p) {
     const int n = vtx[q];
     const int v = p.visit_base + p.q0 + q;
     const int m = s_m;
-    double u0, u1, u2;
-    if (p.draws) {
-      const double* d = p.draws + (long long)c * p.sDraws + 3ll * v;
-      u0 = d[0]; u1 = d[1]; u2 = d[2];
-    } else {
-      unsigned long long key = p.rngkey[c], ctr = p.rngctr[c] + 3ull * v;
-      u0 = alf_uniform(key, ctr); u1 = alf_uniform(key, ctr + 1); u2 = alf_uniform(key, ctr + 2);
-    }
-    const int s_old = fl[n];
-    const int tp = ty[n];
+    const double u0 = v_u[q][0], u1 = v_u[q][1], u2 = v_u[q][2];
+    const int s_old = v_s[q];
+    const int tp = v_t[q];
     const int s_new = (tp == 1) ? -s_old : (int)p.ft.flip[s_old + 2][nranf3(u0) - 1];
     const bool propose = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
     if (w < F) {
       const int f = w;
-      const int k = f * M + n;
       const double dphi = p.ft.phi[tp - 1][s_new + 2] - p.ft.phi[tp - 1][s_old + 2];
-      const zd Z1 = zscale(gg[k], dphi);
-      const zd myexp = zexp(zscale(Z1, EE[k]));
+      const zd Z1 = zscale(v_g[f][q], dphi);
+      const zd myexp = zexp(zscale(Z1, v_E[f][q]));
       const zd Dj = zsub(myexp, zmk(1.0, 0.0));
       // y = Gamma^-1 g, g_l = G0(s_l, j)
       zd corr_l = zmk(0.0, 0.0);
@@ -141,7 +152,7 @@ __global__ void __launch_bounds__(64) k_update_block(UpdParams p) {
         zd gcur = zadd(Gs[f][q][q], corr);
         zd mat = zadd(myexp, zneg(zmul(Dj, gcur)));  // Mat(1,1) = myexp - Z*G(P,P)
         Dcand[f] = mat;
-        Rf[f] = zmul(mat, zexp(zmul(Z1, al[k])));
+        Rf[f] = zmul(mat, zexp(zmul(Z1, v_al[f][q])));
         delta_new[f] = Dj;
       }
     }
@@ -220,34 +231,46 @@ __global__ void __launch_bounds__(64) k_update_block(UpdParams p) {
   }
 }
 
-// Flush operands: X(:, l) = G0(:, s_l) and Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :)).
-// grid: (ceil(N/128), F, chains), 128 threads; X: [chain][F][N][KMAX] col-major (ld N),
-// Y: [chain][F][KMAX][N] col-major (ld KMAX).
-__global__ void k_flush_prep(const zd* G, long long sG, int N, int F, const int* m_in, const int* sites,
-                             const zd* W, zd* X, zd* Y) {
-  const int c = blockIdx.z, f = blockIdx.y;
+// Flush operands, spread over the GPU:
+//   X(:, l) = G0(:, s_l)                           (k_flush_x: one thread per (row, l))
+//   Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :))  (k_flush_y: one thread per (l, column))
+// X: [chain][2][N][KMAX] col-major (ld N); Y: [chain][2][KMAX][N] col-major (ld KMAX).
+__global__ void k_flush_x(const zd* G, long long sG, int N, int F, const int* m_in, const int* sites, zd* X) {
+  const int b = blockIdx.y, c = b / F, f = b % F;
+  const int m = m_in[c];
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)N * m) return;
+  const int row = e % N, l = e / N;
+  const int s = sites[(long long)c * UPD_KMAX + l];
+  X[((long long)c * 2 + f) * N * UPD_KMAX + row + (long long)l * N] =
+      G[(long long)c * sG + (long long)f * N * N + row + (long long)s * N];
+}
+
+// block: 32 x 8 threads = (l, column); grid (ceil(N/8), B)
+__global__ void k_flush_y(const zd* G, long long sG, int N, int F, const int* m_in, const int* sites, const zd* W,
+                          zd* Y) {
+  const int b = blockIdx.y, c = b / F, f = b % F;
   const int m = m_in[c];
   if (m == 0) return;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ zd Ws[UPD_KMAX][UPD_KMAX + 1];
+  __shared__ zd gb[8][UPD_KMAX];
   __shared__ int st[UPD_KMAX];
-  __shared__ zd Ws[UPD_KMAX][UPD_KMAX];
-  for (int l = threadIdx.x; l < m; l += blockDim.x) st[l] = sites[(long long)c * UPD_KMAX + l];
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x)
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+  for (int l = tid; l < m; l += 256) st[l] = sites[(long long)c * UPD_KMAX + l];
+  for (int e = tid; e < m * m; e += 256)
     Ws[e / m][e % m] = W[(((long long)c * 2 + f) * UPD_KMAX + e / m) * UPD_KMAX + e % m];
   __syncthreads();
-  if (col >= N) return;
+  const int col = blockIdx.x * 8 + ty;
   const zd* Gf = G + (long long)c * sG + (long long)f * N * N;
-  zd* Xf = X + ((long long)c * 2 + f) * N * UPD_KMAX;
-  zd* Yf = Y + ((long long)c * 2 + f) * N * UPD_KMAX;
-  zd gcol[UPD_KMAX];
-  for (int l = 0; l < m; ++l) {
-    Xf[col + (long long)l * N] = Gf[col + (long long)st[l] * N];  // X(col, l)
-    zd gv = Gf[st[l] + (long long)col * N];                        // G0(s_l, col)
-    gcol[l] = zsub(zmk(st[l] == col ? 1.0 : 0.0, 0.0), gv);       // (E_S - G0(S,:))(l, col)
+  if (col < N && tx < m) {
+    const int s = st[tx];
+    zd gv = Gf[s + (long long)col * N];
+    gb[ty][tx] = zsub(zmk(s == col ? 1.0 : 0.0, 0.0), gv);
   }
-  for (int l = 0; l < m; ++l) {
+  __syncthreads();
+  if (col < N && tx < m) {
     zd y = zmk(0.0, 0.0);
-    for (int l2 = 0; l2 < m; ++l2) y = zadd(y, zmul(Ws[l][l2], gcol[l2]));
-    Yf[l + (long long)col * UPD_KMAX] = y;
+    for (int l2 = 0; l2 < m; ++l2) y = zadd(y, zmul(Ws[tx][l2], gb[ty][l2]));
+    Y[((long long)c * 2 + f) * N * UPD_KMAX + tx + (long long)col * UPD_KMAX] = y;
   }
 }

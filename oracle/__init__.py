@@ -67,8 +67,15 @@ def lib():
                  "oracle_set_fields", "oracle_get_fields", "oracle_wrapgrup", "oracle_wrapgrdo"):
         getattr(L, name).restype = _c.c_int
     L.oracle_set_threads.argtypes = [_c.c_int]
+    L.oracle_set_variant.argtypes = [_c.c_int]
     _lib = L
     return L
+
+
+def set_variant(v: int) -> None:
+    """Summation order of the hopping products: 0 = OpenBLAS (as linked by the
+    reference), 1 = plain loops (what another BLAS build of the reference gives)."""
+    lib().oracle_set_variant(v)
 
 
 class OracleStats(_c.Structure):
@@ -139,6 +146,14 @@ class Oracle:
         lib().oracle_set_recording(self.h, _ptr(r["acc"]), _ptr(r["ratio"]),
                                    _ptr(r["G"]) if green else None, _ptr(r["Gwrap"]) if green else None,
                                    _ptr(r["phase"]))
+        return r
+
+    def recorded(self) -> dict:
+        """Recorded data of the armed sweeps; G arrays as [point][nf][row][col]."""
+        r = dict(self._rec)
+        for k in ("G", "Gwrap"):
+            if r[k] is not None:
+                r[k] = np.transpose(r[k], (0, 1, 3, 2)).copy()
         return r
 
     def sweep(self, u: np.ndarray) -> None:

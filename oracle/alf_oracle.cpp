@@ -178,15 +178,38 @@ struct Oracle {
 // ---------------------------------------------------------------------------
 // Hop_mod (dense real Op_T; ZDSLSYMM dense branch uses ZLARCM / ZLACRM)
 // ---------------------------------------------------------------------------
+// Summation-order variant: 0 = OpenBLAS ZLARCM/ZLACRM (as the reference links), 1 = plain loops.
+// Used only to measure how much two valid BLAS builds of the reference differ.
+static int g_variant = 0;
+extern "C" void oracle_set_variant(int v) { g_variant = v; }
+
 static void lmult_real(Oracle& o, const double* A, zc* X) {  // X = A * X
   int N = o.N;
   o.tmp.assign(X, X + (size_t)N * N);
+  if (g_variant == 1) {
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        double re = 0.0, im = 0.0;
+        for (int k = N - 1; k >= 0; --k) { re += A[i + (size_t)k * N] * o.tmp[k + (size_t)j * N].real(); im += A[i + (size_t)k * N] * o.tmp[k + (size_t)j * N].imag(); }
+        X[i + (size_t)j * N] = zc(re, im);
+      }
+    return;
+  }
   o.rwork.resize((size_t)2 * N * N);
   LA.zlarcm(&N, &N, A, &N, o.tmp.data(), &N, X, &N, o.rwork.data());
 }
 static void rmult_real(Oracle& o, const double* A, zc* X) {  // X = X * A
   int N = o.N;
   o.tmp.assign(X, X + (size_t)N * N);
+  if (g_variant == 1) {
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        double re = 0.0, im = 0.0;
+        for (int k = N - 1; k >= 0; --k) { re += o.tmp[i + (size_t)k * N].real() * A[k + (size_t)j * N]; im += o.tmp[i + (size_t)k * N].imag() * A[k + (size_t)j * N]; }
+        X[i + (size_t)j * N] = zc(re, im);
+      }
+    return;
+  }
   o.rwork.resize((size_t)2 * N * N);
   LA.zlacrm(&N, &N, o.tmp.data(), &N, A, &N, X, &N, o.rwork.data());
 }
