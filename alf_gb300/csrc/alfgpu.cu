@@ -57,7 +57,7 @@ struct alfgpu_s {
   QRInfo* info = nullptr;
   // delayed update
   int *m = nullptr, *sites = nullptr;
-  zd *W = nullptr, *X = nullptr, *Y = nullptr;
+  zd *W = nullptr, *X = nullptr, *Y = nullptr, *dlt = nullptr;
   // per chain
   zd* phase = nullptr;
   long long* cnt = nullptr;
@@ -415,15 +415,18 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.fields = h->fields;
     u.draws = draws_dev; u.sDraws = 6ll * M * h->L;
     u.rngkey = h->rngkey; u.rngctr = h->rngctr;
-    u.phase = h->phase; u.m_out = h->m; u.sites_out = h->sites; u.W_out = h->W; u.cnt = h->cnt;
+    u.phase = h->phase; u.m_out = h->m; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
-    k_update_block<<<h->C, 64, UPD_SMEM_BYTES, h->st>>>(u);
+    k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
     CK(cudaGetLastError());
-    k_flush_x<<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites,
-                                                                                 h->X);
+    k_flush_w<double2><<<h->B, 256, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
     CK(cudaGetLastError());
-    k_flush_y<<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->Y);
+    k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(h->G, F * NN, N, F, h->m,
+                                                                                         h->sites, h->X);
+    CK(cudaGetLastError());
+    k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
+                                                                            h->Y);
     CK(cudaGetLastError());
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();
@@ -442,7 +445,6 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
   }
   return 0;
 }
-
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -495,7 +497,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
         cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
       return fail(ALFGPU_ERROR_CUDA);
   }
-  if (cudaFuncSetAttribute(k_update_block, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM_BYTES) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_update_block<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)upd_smem_bytes<double2>()) != cudaSuccess)
     return fail(ALFGPU_ERROR_CUDA);
   // shrink the QR cluster until at least one cluster fits on the device
   while (h->CL > 1) {
@@ -538,7 +541,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->info, B); r |= dalloc(h, &h->dphase, B); r |= dalloc(h, &h->cmp, 2 * B);
   r |= dalloc(h, &h->opang, B);
   r |= dalloc(h, &h->m, C + B); r |= dalloc(h, &h->sites, C * UPD_KMAX);
-  r |= dalloc(h, &h->W, C * 2 * UPD_KMAX * UPD_KMAX);
+  r |= dalloc(h, &h->W, C * 2 * UPD_KMAX * UPD_KMAX); r |= dalloc(h, &h->dlt, C * 2 * UPD_KMAX);
   r |= dalloc(h, &h->X, C * 2 * N * UPD_KMAX); r |= dalloc(h, &h->Y, C * 2 * N * UPD_KMAX);
   r |= dalloc(h, &h->phase, C); r |= dalloc(h, &h->cnt, 4 * C); r |= dalloc(h, &h->stat, 8 * C);
   r |= dalloc(h, &h->err, 1);

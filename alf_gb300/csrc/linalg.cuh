@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
       // norm downdate (ZLAQP2)
       double v1 = vn1[c];
       if (v1 != 0.0) {
-        double tmp = zabs(col[j]) / v1;
-        tmp = fmax(1.0 - tmp * tmp, 0.0);
+        const zd a = col[j];
+        double tmp = fmax(1.0 - (a.x * a.x + a.y * a.y) / (v1 * v1), 0.0);
         double r2 = v1 / vn2[c];
         double tmp2 = tmp * r2 * r2;
         double nv1, nv2 = vn2[c];
@@ -285,20 +285,20 @@ __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
   __syncthreads();
   if (!p.lower) {
     for (int i = N - 1; i >= 0; --i) {
-      zd xi = zdiv(xs[i], T[i + (long long)i * p.ldt]);
+      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], T[i + (long long)i * p.ldt]);
       __syncthreads();
+      const zd xi = xs[i];
       const zd* ci = T + (long long)i * p.ldt;
       for (int r = threadIdx.x; r < i; r += blockDim.x) xs[r] = zsub(xs[r], zmul(ci[r], xi));
-      if (threadIdx.x == 0) xs[i] = xi;
       __syncthreads();
     }
   } else {
     for (int i = 0; i < N; ++i) {
-      zd xi = zdiv(xs[i], T[i + (long long)i * p.ldt]);
+      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], T[i + (long long)i * p.ldt]);
       __syncthreads();
+      const zd xi = xs[i];
       const zd* ci = T + (long long)i * p.ldt;
       for (int r = i + 1 + threadIdx.x; r < N; r += blockDim.x) xs[r] = zsub(xs[r], zmul(ci[r], xi));
-      if (threadIdx.x == 0) xs[i] = xi;
       __syncthreads();
     }
   }

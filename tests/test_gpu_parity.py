@@ -124,9 +124,11 @@ def _run_pair(m, seed=5, sweeps=1, chain=0):
         spread = np.max(np.abs(var[s] - r_o) / np.maximum(np.abs(r_o), 1e-300))
         assert np.median(rel) <= 1e-12, np.median(rel)
         assert rel.max() <= max(RTOL, 10.0 * spread), (rel.max(), spread)
+        # wrapped G just before each stabilisation: within 10x the oracle's own drift
+        drift = max(np.max(np.abs(ro["Gwrap"][p] - ro["G"][p])) for p in range(ro["G"].shape[0]))
         for p in range(ro["G"].shape[0]):
             assert _relmax(rg["G"][p], ro["G"][p]) < RTOL, (s, p)
-            assert _relmax(rg["Gwrap"][p], ro["Gwrap"][p]) < 1e-8, (s, p)
+            assert np.max(np.abs(rg["Gwrap"][p] - ro["Gwrap"][p])) <= 10.0 * drift + 1e-12, (s, p)
         np.testing.assert_array_equal(g.fields(0), o.fields())
         assert _relmax(g.green(0), o.green()) < RTOL
         assert abs(g.phase()[0] - o.phase()) < 1e-10
