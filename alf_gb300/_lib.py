@@ -32,6 +32,8 @@ class Stats(C.Structure):
                 ("sweeps", C.c_int64)]
 
 
+PROF_PHASES = ["hop", "update", "flush", "propagate", "qr", "orgqr", "solve"]
+
 OBS_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_double),
                      C.POINTER(C.c_double))
 
@@ -85,6 +87,9 @@ def lib(build_if_missing: bool = True):
         "alfgpu_set_recording": ([vp, C.c_int32], C.c_int),
         "alfgpu_get_record": ([vp, C.c_int32, vp, vp, vp, vp, vp], C.c_int),
         "alfgpu_stream": ([vp], vp),
+        "alfgpu_set_profiling": ([vp, C.c_int32], C.c_int),
+        "alfgpu_get_profile": ([vp, vp, vp], C.c_int),
+        "alfgpu_launch_count": ([vp], C.c_int64),
         "alfgpu_cgr": ([C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "alfgpu_decompose": ([C.c_int32, C.c_char, vp, vp, vp], C.c_int),
     }

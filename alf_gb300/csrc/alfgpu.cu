@@ -72,7 +72,45 @@ struct alfgpu_s {
   zd *rec_ratio = nullptr, *rec_G = nullptr, *rec_Gw = nullptr, *rec_phase = nullptr;
   FieldTables ft;
   std::vector<void*> allocs;
+  // phase profiling (CUDA events on the library stream)
+  int profiling = 0;
+  long long launches = 0;  // kernel launches issued by this handle
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<int> prof_cat;  // category of event pair i (events 2i, 2i+1)
+  double prof_ms[ALFGPU_PROF_N] = {0};
+  long long prof_n[ALFGPU_PROF_N] = {0};
 };
+
+static cudaEvent_t prof_event(alfgpu_s* h) {
+  if (h->ev_used == h->ev_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    h->ev_pool.push_back(e);
+  }
+  return h->ev_pool[h->ev_used++];
+}
+static void prof_begin(alfgpu_s* h, int cat) {
+  if (!h->profiling) return;
+  h->prof_cat.push_back(cat);
+  cudaEventRecord(prof_event(h), h->st);
+}
+static void prof_end(alfgpu_s* h) {
+  if (!h->profiling) return;
+  cudaEventRecord(prof_event(h), h->st);
+}
+static void prof_collect(alfgpu_s* h) {
+  if (h->prof_cat.empty()) return;
+  cudaStreamSynchronize(h->st);
+  for (size_t i = 0; i < h->prof_cat.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev_pool[2 * i], h->ev_pool[2 * i + 1]);
+    h->prof_ms[h->prof_cat[i]] += ms;
+    h->prof_n[h->prof_cat[i]] += 1;
+  }
+  h->prof_cat.clear();
+  h->ev_used = 0;
+}
 
 #define CK(x)                                   \
   do {                                          \
@@ -81,6 +119,11 @@ struct alfgpu_s {
       h->last_cuda = e_;                        \
       return ALFGPU_ERROR_CUDA;                 \
     }                                           \
+  } while (0)
+#define CKL()           \
+  do {                  \
+    h->launches++;      \
+    CK(cudaGetLastError()); \
   } while (0)
 #define RET(x)                \
   do {                        \
@@ -121,6 +164,7 @@ static int cluster_size(int N) {
 // Kernel launch helpers
 // ---------------------------------------------------------------------------
 static int launch_qr(alfgpu_s* h, zd* A, const double* colscale, int nb) {
+  prof_begin(h, ALFGPU_PROF_QR);
   QRParams q;
   memset(&q, 0, sizeof(q));
   const int N = h->N;
@@ -141,11 +185,14 @@ static int launch_qr(alfgpu_s* h, zd* A, const double* colscale, int nb) {
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
   cfg.attrs = at; cfg.numAttrs = 1;
+  h->launches++;
   CK(cudaLaunchKernelEx(&cfg, k_qrp, q));
+  prof_end(h);
   return 0;
 }
 
 static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
+  prof_begin(h, ALFGPU_PROF_ORGQR);
   OrgqrParams q;
   const int N = h->N;
   q.A = A; q.lda = N; q.sA = (long long)N * N; q.tau = h->tau; q.sT = N; q.N = N;
@@ -159,11 +206,14 @@ static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
   cfg.attrs = at; cfg.numAttrs = 1;
+  h->launches++;
   CK(cudaLaunchKernelEx(&cfg, k_orgqr, q));
+  prof_end(h);
   return 0;
 }
 
 static int gemm(alfgpu_s* h, const GemmParams& p) {
+  h->launches++;
   CK(launch_zgemm(p, h->st));
   return 0;
 }
@@ -196,7 +246,7 @@ static int udv_reset(alfgpu_s* h, UDVSet& s) {
   const int N = h->N;
   dim3 grid((unsigned)(((long long)N * N + 255) / 256), h->B);
   k_udv_reset<<<grid, 256, 0, h->st>>>(s.U, s.V, s.D, s.detU, N);
-  CK(cudaGetLastError());
+  CKL();
   return 0;
 }
 
@@ -204,7 +254,7 @@ static int udv_reset(alfgpu_s* h, UDVSet& s) {
 static int slice_scale(alfgpu_s* h, int nt1) {
   k_slice_scale<<<h->B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->N, h->F, nt1, h->v_site, h->v_Eexp, h->S,
                                           h->Sinv);
-  CK(cudaGetLastError());
+  CKL();
   return 0;
 }
 
@@ -214,9 +264,9 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   const long long NN = (long long)N * N;
   RET(launch_qr(h, s.U, s.D, B));
   k_decomp_phase<<<B, 256, 0, h->st>>>(s.U, N, N, h->info, left, h->dphase, s.detU);
-  CK(cudaGetLastError());
+  CKL();
   k_perm0<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->perm, N, N);
-  CK(cudaGetLastError());
+  CKL();
   GemmParams p = gsq(h, B);
   if (!left) {  // V = R * P^T V   (ZLAPMR forward, ZTRMM L,U,N)
     p.A = s.U; p.opA = OP_N; p.triA = 1;
@@ -231,13 +281,14 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   RET(launch_orgqr(h, s.U, B));
   k_scale_col0<<<B, 256, 0, h->st>>>(s.U, N, h->dphase);
-  CK(cudaGetLastError());
+  CKL();
   return 0;
 }
 
 // WRAPUR (wrapur_mod.F90:101-124): U <- prod_nt [D_nt expT] U, then decompose (side R)
 static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
   const int N = h->N, B = h->B;
+  prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
     RET(slice_scale(h, nt));
     GemmParams p = gsq(h, B);
@@ -247,12 +298,14 @@ static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
     RET(gemm(h, p));
     RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
   }
+  prof_end(h);
   return decompose(h, h->udvr, 0);
 }
 
 // WRAPUL (wrapul_mod.F90:108-131): U <- prod_nt [expT conj(D_nt)] U (descending nt), decompose (side L)
 static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
   const int N = h->N, B = h->B;
+  prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau1; nt >= ntau + 1; --nt) {
     RET(slice_scale(h, nt));
     GemmParams q = gsq(h, B);
@@ -262,6 +315,7 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
     RET(gemm(h, q));
     RET(copy_mats(h, h->udvl.U, h->T1, (size_t)B * N * N));
   }
+  prof_end(h);
   return decompose(h, h->udvl, 1);
 }
 
@@ -278,7 +332,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
   // TPUP = D_R (V_R V_L) D_L + RHS  (D's packed as complex scale vectors in S / Sinv)
   RET(copy_mats(h, h->TP, h->RHS, (size_t)B * NN));
   k_real_to_complex2<<<(unsigned)((B * N + 255) / 256), 256, 0, h->st>>>(ur.D, ul.D, h->S, h->Sinv, (long long)B * N);
-  CK(cudaGetLastError());
+  CKL();
   {
     GemmParams p = gsq(h, B);
     p.A = ur.V; p.B = ul.V; p.C = h->TP; p.beta = zmk(1.0, 0.0);
@@ -290,7 +344,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
   if (nvar != 1) {
     dim3 grid((N + 31) / 32, (N + 31) / 32, B);
     k_transpose<<<grid, dim3(32, 8), 0, h->st>>>(h->TP, N, NN, h->Qb, N, NN, N, 1);
-    CK(cudaGetLastError());
+    CKL();
     QR = h->Qb;
   }
   RET(launch_qr(h, QR, nullptr, B));
@@ -299,9 +353,9 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
   RET(copy_mats(h, Q, QR, (size_t)B * NN));
   RET(launch_orgqr(h, Q, B));
   k_invperm<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->iperm, N, N);
-  CK(cudaGetLastError());
+  CKL();
   k_real_to_complex<<<(B * N + 255) / 256, 256, 0, h->st>>>(h->DUP, h->S, (long long)B * N);
-  CK(cudaGetLastError());
+  CKL();
   if (nvar == 1) {
     // RHS = Q^H U_R^H, rows divided by DUP
     GemmParams p = gsq(h, B);
@@ -312,8 +366,10 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     TrsvParams t;
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
+    prof_begin(h, ALFGPU_PROF_SOLVE);
     k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
-    CK(cudaGetLastError());
+    prof_end(h);
+    CKL();
     // G = U_L * P RHS (ZLAPMR backward folded into the B load)
     GemmParams g = gsq(h, B);
     g.A = ul.U; g.B = h->RHS; g.permB = h->iperm; g.sPB = N; g.C = Gout;
@@ -328,8 +384,10 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     TrsvParams t;
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 1;
+    prof_begin(h, ALFGPU_PROF_SOLVE);
     k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
-    CK(cudaGetLastError());
+    prof_end(h);
+    CKL();
     // G = (RHS P) U_R^H (ZLAPMT backward folded into the A load)
     GemmParams g = gsq(h, B);
     g.A = h->RHS; g.permA = h->iperm; g.sPA = N; g.B = ur.U; g.opB = OP_C; g.C = Gout;
@@ -347,10 +405,10 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
   RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
   if (compare) {
     k_compare<<<B, 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
-    CK(cudaGetLastError());
+    CKL();
   }
   k_opphase<<<B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->F, h->v_g, h->v_alpha, h->v_type, h->ft, h->opang);
-  CK(cudaGetLastError());
+  CKL();
   StabFinishParams sp;
   sp.C = h->C; sp.F = h->F; sp.NSUN = h->NSUN; sp.nvar = nvar; sp.compare = compare; sp.init = !compare;
   sp.detUR = h->udvr.detU; sp.detUL = h->udvl.detU; sp.info = h->info; sp.opang = h->opang; sp.cmp = h->cmp;
@@ -363,15 +421,21 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
     h->rec_stab++;
   }
   k_stab_finish<<<(h->C + 127) / 128, 128, 0, h->st>>>(sp);
-  CK(cudaGetLastError());
+  CKL();
   return 0;
 }
 
 // Hopping wraps with the slice's deferred vertex scalings (Wrapgr_mod.F90:110-114, 237-241).
 // up:   G <- expT (S G Sinv) expTinv      down: G <- expTinv (Sinv G S) expT
+static int hop_impl(alfgpu_s* h, int up, int with_scale);
 static int hop(alfgpu_s* h, int up, int with_scale) {
+  prof_begin(h, ALFGPU_PROF_HOP);
+  int r = hop_impl(h, up, with_scale);
+  prof_end(h);
+  return r;
+}
+static int hop_impl(alfgpu_s* h, int up, int with_scale) {
   const int N = h->N, F = h->F, B = h->B;
-  const long long NN = (long long)N * N;
   const double* E1 = up ? h->expT : h->expTinv;   // left factor
   const double* E2 = up ? h->expTinv : h->expT;   // right factor
   if (up) {
@@ -418,16 +482,19 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.phase = h->phase; u.m_out = h->m; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
+    prof_begin(h, ALFGPU_PROF_UPDATE);
     k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
-    CK(cudaGetLastError());
+    prof_end(h);
+    CKL();
+    prof_begin(h, ALFGPU_PROF_FLUSH);
     k_flush_w<double2><<<h->B, 256, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
-    CK(cudaGetLastError());
+    CKL();
     k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(h->G, F * NN, N, F, h->m,
                                                                                          h->sites, h->X);
-    CK(cudaGetLastError());
+    CKL();
     k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
                                                                             h->Y);
-    CK(cudaGetLastError());
+    CKL();
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();
     p.m = N; p.n = N; p.k = UPD_KMAX;
@@ -439,9 +506,10 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
     k_expand_m<<<(h->B + 127) / 128, 128, 0, h->st>>>(h->m, h->m + h->C, h->C, F);
-    CK(cudaGetLastError());
+    CKL();
     p.kdyn = h->m + h->C;
     RET(gemm(h, p));
+    prof_end(h);
   }
   return 0;
 }
@@ -559,11 +627,29 @@ void alfgpu_destroy(alfgpu_t* h) {
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
   for (void* p : h->allocs) cudaFree(p);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
 
 void* alfgpu_stream(alfgpu_t* h) { return h ? (void*)h->st : nullptr; }
+
+int alfgpu_set_profiling(alfgpu_t* h, int32_t enable) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  prof_collect(h);
+  h->profiling = enable ? 1 : 0;
+  for (int i = 0; i < ALFGPU_PROF_N; ++i) { h->prof_ms[i] = 0.0; h->prof_n[i] = 0; }
+  return 0;
+}
+
+int64_t alfgpu_launch_count(alfgpu_t* h) { return h ? (int64_t)h->launches : -1; }
+
+int alfgpu_get_profile(alfgpu_t* h, double* ms, int64_t* launches) {
+  if (!h || !ms || !launches) return ALFGPU_ERROR_ARGUMENT;
+  prof_collect(h);
+  for (int i = 0; i < ALFGPU_PROF_N; ++i) { ms[i] = h->prof_ms[i]; launches[i] = h->prof_n[i]; }
+  return 0;
+}
 
 int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv) {
   if (!h || !expT || !expTinv) return ALFGPU_ERROR_ARGUMENT;
@@ -724,7 +810,7 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
       {
         dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
         k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
-        CK(cudaGetLastError());
+        CKL();
       }
       pending = 0;
       RET(wrapur(h, h->stab_nt[NST - 1], ntau1));
@@ -761,9 +847,11 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
     for (int c = 0; c < h->C; ++c) h->h_ctr[c] += 6ull * M * L;
   {
     k_count_sweep<<<(h->C + 127) / 128, 128, 0, h->st>>>(h->stat, h->C);
-    CK(cudaGetLastError());
+    CKL();
   }
-  return check_err(h);
+  int rc = check_err(h);
+  prof_collect(h);
+  return rc;
 }
 
 
@@ -883,7 +971,7 @@ int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, c
     sp.detUR = h->udvr.detU; sp.detUL = h->udvl.detU; sp.info = h->info; sp.opang = h->opang; sp.cmp = h->cmp;
     sp.phase = h->phase; sp.stat = h->stat; sp.err = h->err;
     k_stab_finish<<<1, 32, 0, h->st>>>(sp);
-    CK(cudaGetLastError());
+    CKL();
     CK(cudaStreamSynchronize(h->st));
     CK(cudaMemcpy(G, h->G, NN * sizeof(zd), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(phase, h->phase, sizeof(zd), cudaMemcpyDeviceToHost));

@@ -114,6 +114,17 @@ class Chains:
     def reset_stats(self):
         _lib.check(self.L.alfgpu_reset_stats(self.h), "alfgpu_reset_stats")
 
+    def set_profiling(self, enable: bool = True):
+        _lib.check(self.L.alfgpu_set_profiling(self.h, int(enable)), "alfgpu_set_profiling")
+
+    def profile(self) -> dict:
+        """Per-phase device time (ms) and launch-group counts since profiling was enabled."""
+        n = len(_lib.PROF_PHASES)
+        ms = np.zeros(n, np.float64)
+        cnt = np.zeros(n, np.int64)
+        _lib.check(self.L.alfgpu_get_profile(self.h, _p(ms), _p(cnt)), "alfgpu_get_profile")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.PROF_PHASES)}
+
     def set_recording(self, enable: bool = True):
         _lib.check(self.L.alfgpu_set_recording(self.h, int(enable)), "alfgpu_set_recording")
 

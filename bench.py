@@ -1,0 +1,291 @@
+#!/usr/bin/env python
+"""Benchmark: AFQMC sweeps/s of ALF's finite-temperature sweep on a GB300.
+
+Workload (default): Hubbard model on a 16x16 square lattice, N_dim = 256,
+t = 1, U = 4, mu = 0, beta = 10, dtau = 0.1 (Ltrot = 100), Nwrap = 10, Mz
+decoupling with four-valued fields, one Markov chain.  A step is one full
+sequential sweep (up pass, down pass, 2*Nstm stabilisations).
+
+value: sweeps/s with all state resident on the device, timed with CUDA events
+       on the library's stream (device draw stream, no host traffic).
+e2e:   the same metric through the C ABI with host buffers: each step copies
+       the host draws in (6*M*Ltrot doubles) and reads G back (N^2*N_FL complex),
+       both inside the timed region.
+--impl reference: ALF's algorithm on the host cores (the CPU restatement that
+       calls the same LAPACK; the Fortran reference cannot be built here), one
+       chain, all host threads given to its BLAS, each step a bounded sample of
+       a sweep (a fixed number of time slices with their stabilisations) scaled
+       to sweeps/s.
+Multi-GPU (torchrun): every rank runs an independent chain (replicas); value is
+the total sweeps of all ranks / the max over ranks of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "AFQMC sweeps/s (per chain & aggregate), mixed vs FP64 GPU at max|dG|<=1e-5"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# Measured on this machine's GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
+FP64_DMMA_TFLOPS = 1.048
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="hubbard16x16")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                parts = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(parts) >= 8:
+                    self.samples.append(parts)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_flops(m, phase: str, launches: int, n_acc: int) -> float:
+    """Algorithmic FLOPs of one phase over `launches` launch groups (real-flop convention:
+    complex MAC = 8, real x complex MAC = 4; LAPACK counts for QR)."""
+    N, F = m.ndim, m.n_fl
+    if phase == "hop":        # 2 real x complex N^3 products per flavour per group
+        return launches * 2 * F * 4.0 * N ** 3
+    if phase == "propagate":  # per group: Nwrap (or fewer) slices of one real x complex product per flavour
+        return None
+    if phase in ("qr", "orgqr"):
+        return launches * F * (16.0 / 3.0) * N ** 3
+    if phase == "solve":
+        return launches * F * 4.0 * N ** 3
+    if phase == "flush":
+        return 8.0 * N * N * n_acc * 1.0  # rank-1 equivalents, both flavours counted in n_acc per flavour
+    return None
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    from alf_gb300 import model as mdl, rng
+    from alf_gb300.sweep import Chains
+
+    torch.cuda.set_device(local)
+    m = mdl.config(args.config)
+    seed = args.seed + 1000 * rank
+    ch = Chains(m, n_chains=1, precision=args.precision, device=local)
+    ch.set_fields(0, rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    ch.init_state()
+    ch.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    stream = torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local)
+    l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > 129 MB L2
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        ch.sweep(None)
+    ch.reset_stats()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    n0 = ch.L.alfgpu_launch_count(ch.h)
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            l2.add_(1.0)  # flush L2 between timed steps (outside the timed region)
+            torch.cuda.synchronize()
+            ev[i][0].record(stream)
+            ch.sweep(None)
+            ev[i][1].record(stream)
+        barrier()
+    n_launch = ch.L.alfgpu_launch_count(ch.h) - n0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    st = ch.stats(0)
+    n_acc = st.n_acc
+    # e2e through the C ABI with host buffers
+    u_host = [rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 1000 + i)[None, :] for i in range(args.steps)]
+    G_host = np.zeros((m.n_fl, m.ndim, m.ndim), np.complex128)
+    h2d = u_host[0].nbytes
+    d2h = G_host.nbytes
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ch.sweep(u_host[i])
+        G_host = ch.green(0)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    # phase profile of two sweeps (separate pass; events on the library stream)
+    ch.set_profiling(True)
+    for _ in range(2):
+        ch.sweep(None)
+    prof = ch.profile()
+    ch.set_profiling(False)
+    # launch count per sweep from the profile pass
+    times = torch.tensor([ms / 1e3, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+    if ws > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    t_dev, t_e2e = float(times[0]), float(times[1])
+    return dict(m=m, t_dev=t_dev, t_e2e=t_e2e, clocks=clk.summary(), prof=prof, n_acc=n_acc, h2d=h2d, d2h=d2h,
+                stats=st, chains=ch, launches=n_launch)
+
+
+def cpu_oracle_rate(m, seed: int, threads: int, slices: int):
+    """Sweeps/s of the CPU restatement on a bounded sample (slices time slices incl. stabilisations)."""
+    import oracle
+    from alf_gb300 import rng
+    o = oracle.Oracle(m, threads=threads)
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
+    t0 = time.perf_counter()
+    o.sweep_chunk(u, slices)
+    dt = time.perf_counter() - t0
+    return (slices / (2.0 * m.ltrot)) / dt, dt
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    from alf_gb300 import model as mdl
+    m = mdl.config(args.config)
+    workload = {"workload": f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
+                            f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
+                            f"Nwrap={m.nwrap}, Mz four-valued fields, one chain per GPU",
+                "chains_per_gpu": 1, "precision": args.precision, "l2": "flushed between timed steps (256 MB write)",
+                "draws": "device counter stream (value); host arrays through the C ABI (e2e)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        slices = 20 if m.ndim >= 200 else 2 * m.ltrot
+        rates = []
+        for i in range(args.warmup + args.steps):
+            r, dt = cpu_oracle_rate(m, args.seed, cores, slices)
+            if i >= args.warmup:
+                rates.append(r)
+        v = float(np.mean(rates))
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded fields and draws)",
+                "config": dict(workload, chains_per_gpu=1, parallelism="host cores"),
+                "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                                 "sample": f"{slices} time slices of one sweep (with their stabilisations) per step, "
+                                           f"CPU restatement of ALF's default-STAB sweep calling OpenBLAS LAPACK "
+                                           f"with {cores} threads; the Fortran reference has no compiler here"},
+                "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    r = run_ours(args, ws, rank, local)
+    if rank != 0:
+        return
+    m = r["m"]
+    total_sweeps = args.steps * ws
+    value = total_sweeps / r["t_dev"]
+    e2e = total_sweeps / r["t_e2e"]
+    prof = r["prof"]
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dn) = dom
+    n_acc_2 = r["stats"].n_acc / max(args.steps, 1) * 2
+    flops = algorithmic_flops(m, dname, dn, int(n_acc_2))
+    if flops is not None and dms > 0:
+        achieved = flops / (dms / 1e3) / 1e12
+        roof = {"bound": "tensor", "kernel": dname, "achieved": achieved, "peak": FP64_DMMA_TFLOPS,
+                "unit": "TFLOP/s", "frac": achieved / FP64_DMMA_TFLOPS, "traffic": None,
+                "peak_source": "measured FP64 mma.sync m8n8k4 throughput (profiles/fp64_throughput_gb300.md); "
+                               "MEASURED_PEAKS.json has no FP64 figure"}
+    else:
+        roof = {"bound": "latency", "kernel": dname, "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None}
+    phases = {k: {"ms_per_sweep": v[0] / 2.0, "launch_groups_per_sweep": v[1] / 2.0} for k, v in prof.items()}
+    launches = int(r["launches"])
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            rate, dt = cpu_oracle_rate(m, args.seed, 1, 20 if m.ndim >= 200 else 2 * m.ltrot)
+            cpu = {"value": rate, "unit": "sweeps/s", "cores": 1, "kind": "port",
+                   "sample": f"{20 if m.ndim >= 200 else 2 * m.ltrot} time slices with their stabilisations "
+                             f"({dt:.1f} s), CPU restatement of ALF's sweep with single-threaded OpenBLAS"}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+    st = r["stats"]
+    line = {
+        "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
+        "data": "synthetic (seeded fields and draws)",
+        "config": dict(workload, parallelism=f"replicas x{ws}"),
+        "e2e": {"value": e2e, "unit": "sweeps/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "roofline": roof, "cpu_baseline": cpu, "clocks": r["clocks"], "gpu_launches": launches,
+        "phases": phases,
+        "precision_green": {"xmaxG": st.xmaxG, "xmeanG": st.xmeanG_sum / max(st.ncg, 1), "xmaxP": st.xmaxP},
+        "acceptance": st.n_acc / max(st.n_prop, 1),
+    }
+    print(json.dumps(line))
+    r["chains"].close()
+
+
+if __name__ == "__main__":
+    main()

@@ -154,6 +154,24 @@ int alfgpu_get_record(alfgpu_t* h, int32_t chain, int8_t* acc, double* ratio, do
 /* Stream the library launches on (a cudaStream_t), for callers that overlap work. */
 void* alfgpu_stream(alfgpu_t* h);
 
+/* Phase profiling (diagnostics): while enabled, CUDA events on the library
+ * stream time each group of launches by phase; alfgpu_get_profile returns the
+ * accumulated milliseconds and launch-group counts per phase. */
+enum {
+  ALFGPU_PROF_HOP = 0,       /* exp(-dtau T) wraps of G (Wrapgr_mod.F90:110-114, 237-241) */
+  ALFGPU_PROF_UPDATE = 1,    /* Metropolis blocks (Upgrade2) */
+  ALFGPU_PROF_FLUSH = 2,     /* delayed-update flushes */
+  ALFGPU_PROF_PROPAGATE = 3, /* UDV propagation of WRAPUR / WRAPUL */
+  ALFGPU_PROF_QR = 4,        /* pivoted QR (QDRP_decompose) */
+  ALFGPU_PROF_ORGQR = 5,     /* explicit Q */
+  ALFGPU_PROF_SOLVE = 6,     /* triangular solves of CGR */
+  ALFGPU_PROF_N = 7
+};
+int alfgpu_set_profiling(alfgpu_t* h, int32_t enable);
+int alfgpu_get_profile(alfgpu_t* h, double* ms, int64_t* launches);
+/* Number of kernel launches this handle has issued so far. */
+int64_t alfgpu_launch_count(alfgpu_t* h);
+
 /* One-shot component entry points on host buffers (allocate their own device memory). */
 int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, const double* VR, const double* UL,
                const double* DL, const double* VL, double* G, double* phase);

@@ -63,6 +63,8 @@ def lib():
     L.oracle_create.restype = _p
     L.oracle_create.argtypes = [_c.c_int] * 7
     L.oracle_destroy.argtypes = [_p]
+    L.oracle_sweep_chunk.argtypes = [_p, _p, _c.c_int]
+    L.oracle_sweep_chunk.restype = _c.c_int
     for name in ("oracle_init_state", "oracle_sweep", "oracle_get_green", "oracle_set_green",
                  "oracle_set_fields", "oracle_get_fields", "oracle_wrapgrup", "oracle_wrapgrdo"):
         getattr(L, name).restype = _c.c_int
@@ -162,6 +164,14 @@ class Oracle:
         rc = lib().oracle_sweep(self.h, _ptr(u))
         if rc:
             raise RuntimeError(f"oracle_sweep rc={rc}")
+
+    def sweep_chunk(self, u: np.ndarray, nslices: int) -> bool:
+        """Advance the current sweep by nslices time slices (with their stabilisations).
+        Returns True once the sweep is complete."""
+        rc = lib().oracle_sweep_chunk(self.h, u.ctypes.data_as(_p), nslices)
+        if rc < 0:
+            raise RuntimeError(f"oracle_sweep_chunk rc={-rc}")
+        return rc == 1
 
     def green(self) -> np.ndarray:
         G = np.zeros((self.F, self.N, self.N), np.complex128)  # [nf][col][row] memory = col-major per flavour

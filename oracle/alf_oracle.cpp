@@ -144,8 +144,14 @@ struct Stats {
   int64_t ncg_tau; double xmean_tau_sum, xmax_tau;
 };
 
+struct SweepCursor {
+  bool active = false;
+  int phase = 0, ntau = 0, NST = 1;
+};
+
 struct Oracle {
   int N, F, NSUN, M, L, Nwrap, Nstm, ltau;
+  SweepCursor cur;
   vector<int> stab_nt;
   vector<double> expT, expTinv;  // F x N x N
   // vertices, k = nf*M + n
@@ -921,53 +927,75 @@ int oracle_init_state(void* h, zc* phase_out) {
 
 static int oracle_tau_m(Oracle& o);
 
-// One sequential sweep (main.F90:714-887).  u: 3*2*M*L draws in visit order.
-int oracle_sweep(void* h, const double* u) {
+// One sequential sweep (main.F90:714-887), resumable in chunks of time slices so that a
+// bounded sample of sweep work can be timed.  u: 3*2*M*L draws in visit order.
+// Returns 1 when the sweep (including the final stabilisation and TAU_M) is complete,
+// 0 when more slices remain, or an ALF error code (>1 is returned negated).
+int oracle_sweep_chunk(void* h, const double* u, int nslices) {
   Oracle& o = *(Oracle*)h;
   const size_t per_slice = (size_t)3 * o.M;
-  for (int nf = 0; nf < o.F; ++nf) o.udvr[nf].reset(o.N, 'r');
-  int NST = 1;
-  for (int ntau = 0; ntau < o.L; ++ntau) {
-    int ntau1 = ntau + 1;
-    wrapgrup(o, ntau, u + (size_t)ntau * per_slice);
-    if (ntau1 == o.stab_nt[NST]) {
-      int nt1 = o.stab_nt[NST - 1];
-      wrapur(o, nt1, ntau1, o.udvr);
-      for (int nf = 0; nf < o.F; ++nf) {
-        o.udvl[nf] = o.udvst[(size_t)(NST - 1) * o.F + nf];
-        o.udvst[(size_t)(NST - 1) * o.F + nf] = o.udvr[nf];
-      }
-      int nvar = (ntau1 > o.L / 2) ? 2 : 1;
-      int e = stabilise(o, nvar);
-      if (e) return e;
-      NST++;
-    }
+  SweepCursor& cur = o.cur;
+  if (!cur.active) {
+    for (int nf = 0; nf < o.F; ++nf) o.udvr[nf].reset(o.N, 'r');
+    cur.active = true; cur.phase = 0; cur.ntau = 0; cur.NST = 1;
   }
-  for (int nf = 0; nf < o.F; ++nf) o.udvl[nf].reset(o.N, 'l');
-  NST = o.Nstm - 1;
-  for (int ntau = o.L; ntau >= 1; --ntau) {
-    int ntau1 = ntau - 1;
-    wrapgrdo(o, ntau, u + (size_t)o.L * per_slice + (size_t)(o.L - ntau) * per_slice);
-    if (NST >= 1 && o.stab_nt[NST] == ntau1 && ntau1 != 0) {
-      int nt1 = o.stab_nt[NST + 1];
-      wrapul(o, nt1, ntau1, o.udvl);
-      for (int nf = 0; nf < o.F; ++nf) {
-        o.udvr[nf] = o.udvst[(size_t)(NST - 1) * o.F + nf];
-        o.udvst[(size_t)(NST - 1) * o.F + nf] = o.udvl[nf];
+  int done = 0;
+  while (done < nslices && cur.phase < 2) {
+    if (cur.phase == 0) {
+      const int ntau = cur.ntau, ntau1 = ntau + 1;
+      wrapgrup(o, ntau, u + (size_t)ntau * per_slice);
+      if (ntau1 == o.stab_nt[cur.NST]) {
+        wrapur(o, o.stab_nt[cur.NST - 1], ntau1, o.udvr);
+        for (int nf = 0; nf < o.F; ++nf) {
+          o.udvl[nf] = o.udvst[(size_t)(cur.NST - 1) * o.F + nf];
+          o.udvst[(size_t)(cur.NST - 1) * o.F + nf] = o.udvr[nf];
+        }
+        int e = stabilise(o, (ntau1 > o.L / 2) ? 2 : 1);
+        if (e) { cur.active = false; return -e; }
+        cur.NST++;
       }
-      int nvar = (ntau1 > o.L / 2) ? 2 : 1;
-      int e = stabilise(o, nvar);
-      if (e) return e;
-      NST--;
+      cur.ntau++;
+      if (cur.ntau == o.L) {
+        for (int nf = 0; nf < o.F; ++nf) o.udvl[nf].reset(o.N, 'l');
+        cur.phase = 1; cur.ntau = o.L; cur.NST = o.Nstm - 1;
+      }
+    } else {
+      const int ntau = cur.ntau, ntau1 = ntau - 1;
+      wrapgrdo(o, ntau, u + (size_t)o.L * per_slice + (size_t)(o.L - ntau) * per_slice);
+      if (cur.NST >= 1 && o.stab_nt[cur.NST] == ntau1 && ntau1 != 0) {
+        wrapul(o, o.stab_nt[cur.NST + 1], ntau1, o.udvl);
+        for (int nf = 0; nf < o.F; ++nf) {
+          o.udvr[nf] = o.udvst[(size_t)(cur.NST - 1) * o.F + nf];
+          o.udvst[(size_t)(cur.NST - 1) * o.F + nf] = o.udvl[nf];
+        }
+        int e = stabilise(o, (ntau1 > o.L / 2) ? 2 : 1);
+        if (e) { cur.active = false; return -e; }
+        cur.NST--;
+      }
+      cur.ntau--;
+      if (cur.ntau == 0) cur.phase = 2;
     }
+    ++done;
   }
+  if (cur.phase < 2) return 0;
   wrapul(o, o.stab_nt[1], o.stab_nt[0], o.udvl);
   for (int nf = 0; nf < o.F; ++nf) o.udvr[nf].reset(o.N, 'r');
+  cur.active = false;
   int e = stabilise(o, 1);
-  if (e) return e;
+  if (e) return -e;
   for (int nf = 0; nf < o.F; ++nf) o.udvst[(size_t)(o.Nstm - 1) * o.F + nf].reset(o.N, 'l');
-  if (o.ltau == 1) return oracle_tau_m(o);
-  return 0;
+  if (o.ltau == 1) {
+    e = oracle_tau_m(o);
+    if (e) return -e;
+  }
+  return 1;
+}
+
+int oracle_sweep(void* h, const double* u) {
+  int r;
+  while ((r = oracle_sweep_chunk(h, u, 1 << 30)) == 0) {
+  }
+  return r == 1 ? 0 : -r;
 }
 
 // Component entry points for unit tests -------------------------------------------------------
