@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "gemm.cuh"
+#include "gemm32.cuh"
 #include "kernels_misc.cuh"
 #include "linalg.cuh"
 #include "update.cuh"
@@ -34,6 +35,8 @@ struct UDVSet {  // one UDV state for all B = C*F (chain, flavour) pairs
 struct alfgpu_s {
   alfgpu_dims d;
   int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
+  int mixed = 0;           // complex64 G, FP32 wraps / updates / flushes, FP64 stabilisation
+  int mixed_propagate = 0; // mixed form: UDV propagation products computed in FP32
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
@@ -47,6 +50,7 @@ struct alfgpu_s {
   int8_t* fields = nullptr;
   // state
   zd *G = nullptr, *Gw = nullptr, *T1 = nullptr;
+  float2 *G32 = nullptr, *T32 = nullptr, *X32 = nullptr, *Y32 = nullptr;  // mixed form
   zd *S = nullptr, *Sinv = nullptr;
   UDVSet udvl, udvr;
   std::vector<UDVSet> udvst;  // index nst-1
@@ -218,6 +222,25 @@ static int gemm(alfgpu_s* h, const GemmParams& p) {
   return 0;
 }
 
+static int gemm32(alfgpu_s* h, const GemmParams& g, int tA, int tB, int tC) {
+  Gemm32Params P;
+  P.g = g; P.tA = tA; P.tB = tB; P.tC = tC;
+  h->launches++;
+  CK(launch_cgemm32(P, h->st));
+  return 0;
+}
+
+static int to32(alfgpu_s* h, const zd* in, float2* out, size_t n) {
+  k_c128_to_c64<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, h->st>>>(in, out, (long long)n);
+  CKL();
+  return 0;
+}
+static int to64(alfgpu_s* h, const float2* in, zd* out, size_t n) {
+  k_c64_to_c128<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, h->st>>>(in, out, (long long)n);
+  CKL();
+  return 0;
+}
+
 static GemmParams gsq(alfgpu_s* h, int batch) {  // N x N x N square product, batch strides N*N
   GemmParams p = gemm_defaults();
   const int N = h->N;
@@ -295,7 +318,8 @@ static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
     p.A = h->expT; p.realA = 1; p.modA = h->F;
     p.B = h->udvr.U; p.C = h->T1;
     p.rs = h->S; p.sRS = N;
-    RET(gemm(h, p));
+    if (h->mixed_propagate) RET(gemm32(h, p, ST_R64, ST_C128, ST_C128));
+    else RET(gemm(h, p));
     RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
   }
   prof_end(h);
@@ -312,7 +336,8 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
     q.A = h->expT; q.realA = 1; q.modA = h->F;
     q.B = h->udvl.U; q.C = h->T1;
     q.ks = h->S; q.sKS = N; q.ksConj = 1;
-    RET(gemm(h, q));
+    if (h->mixed_propagate) RET(gemm32(h, q, ST_R64, ST_C128, ST_C128));
+    else RET(gemm(h, q));
     RET(copy_mats(h, h->udvl.U, h->T1, (size_t)B * N * N));
   }
   prof_end(h);
@@ -401,8 +426,12 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
 static int stabilise(alfgpu_s* h, int nvar, int compare) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
-  if (compare) RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
+  if (compare) {
+    if (h->mixed) RET(to64(h, h->G32, h->Gw, (size_t)B * NN));
+    else RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
+  }
   RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
+  if (h->mixed) RET(to32(h, h->G, h->G32, (size_t)B * NN));
   if (compare) {
     k_compare<<<B, 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
     CKL();
@@ -436,6 +465,30 @@ static int hop(alfgpu_s* h, int up, int with_scale) {
 }
 static int hop_impl(alfgpu_s* h, int up, int with_scale) {
   const int N = h->N, F = h->F, B = h->B;
+  if (h->mixed) {
+    const double* E1 = up ? h->expT : h->expTinv;
+    const double* E2 = up ? h->expTinv : h->expT;
+    if (up) {
+      GemmParams p = gsq(h, B);
+      p.A = E1; p.modA = F; p.B = h->G32; p.C = (zd*)h->T32;
+      if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 0; }
+      RET(gemm32(h, p, ST_R64, ST_C64, ST_C64));
+      GemmParams q = gsq(h, B);
+      q.A = h->T32; q.B = E2; q.modB = F; q.C = (zd*)h->G32;
+      if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 1; }
+      RET(gemm32(h, q, ST_C64, ST_R64, ST_C64));
+    } else {
+      GemmParams p = gsq(h, B);
+      p.A = h->G32; p.B = E2; p.modB = F; p.C = (zd*)h->T32;
+      if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 1; }
+      RET(gemm32(h, p, ST_C64, ST_R64, ST_C64));
+      GemmParams q = gsq(h, B);
+      q.A = E1; q.modA = F; q.B = h->T32; q.C = (zd*)h->G32;
+      if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 0; }
+      RET(gemm32(h, q, ST_R64, ST_C64, ST_C64));
+    }
+    return 0;
+  }
   const double* E1 = up ? h->expT : h->expTinv;   // left factor
   const double* E2 = up ? h->expTinv : h->expT;   // right factor
   if (up) {
@@ -483,24 +536,43 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
     prof_begin(h, ALFGPU_PROF_UPDATE);
-    k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
+    if (h->mixed) {
+      u.G = h->G32;
+      k_update_block<float2><<<h->C, UPD_THREADS, upd_smem_bytes<float2>(), h->st>>>(u);
+    } else {
+      k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
+    }
     prof_end(h);
     CKL();
     prof_begin(h, ALFGPU_PROF_FLUSH);
-    k_flush_w<double2><<<h->B, 256, 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
-    CKL();
-    k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(h->G, F * NN, N, F, h->m,
-                                                                                         h->sites, h->X);
-    CKL();
-    k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
-                                                                            h->Y);
-    CKL();
+    void* Gst = h->mixed ? (void*)h->G32 : (void*)h->G;
+    void* Xst = h->mixed ? (void*)h->X32 : (void*)h->X;
+    void* Yst = h->mixed ? (void*)h->Y32 : (void*)h->Y;
+    if (h->mixed) {
+      k_flush_w32<<<h->B, 256, 0, h->st>>>(h->G32, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
+      CKL();
+      k_flush_x<float2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
+                                                                                          h->sites, Xst);
+      CKL();
+      k_flush_y<float2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->W,
+                                                                             Yst);
+      CKL();
+    } else {
+      k_flush_w<double2><<<h->B, 256, 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
+      CKL();
+      k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
+                                                                                           h->sites, Xst);
+      CKL();
+      k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites,
+                                                                              h->W, Yst);
+      CKL();
+    }
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();
     p.m = N; p.n = N; p.k = UPD_KMAX;
-    p.A = h->X; p.lda = N; p.sA = (long long)N * UPD_KMAX;
-    p.B = h->Y; p.ldb = UPD_KMAX; p.sB = (long long)N * UPD_KMAX;
-    p.C = h->G; p.ldc = N; p.sC = NN;
+    p.A = Xst; p.lda = N; p.sA = (long long)N * UPD_KMAX;
+    p.B = Yst; p.ldb = UPD_KMAX; p.sB = (long long)N * UPD_KMAX;
+    p.C = (zd*)Gst; p.ldc = N; p.sC = NN;
     p.alpha = zmk(-1.0, 0.0); p.beta = zmk(1.0, 0.0);
     p.batch = h->B;
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
@@ -508,7 +580,8 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     k_expand_m<<<(h->B + 127) / 128, 128, 0, h->st>>>(h->m, h->m + h->C, h->C, F);
     CKL();
     p.kdyn = h->m + h->C;
-    RET(gemm(h, p));
+    if (h->mixed) RET(gemm32(h, p, ST_C64, ST_C64, ST_C64));
+    else RET(gemm(h, p));
     prof_end(h);
   }
   return 0;
@@ -542,7 +615,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   if (d.ndim < 1 || d.ndim > 4096 || d.n_fl < 1 || d.n_fl > 2 || d.n_sun < 1 || d.n_op < 1 || d.ltrot < 1 ||
       d.nwrap < 1 || d.n_chains < 1)
     return ALFGPU_ERROR_ARGUMENT;
-  if (d.precision != ALFGPU_PRECISION_FP64) return ALFGPU_ERROR_UNSUPPORTED;
+  if (d.precision != ALFGPU_PRECISION_FP64 && d.precision != ALFGPU_PRECISION_MIXED) return ALFGPU_ERROR_ARGUMENT;
   if (d.ltau) return ALFGPU_ERROR_UNSUPPORTED;
   alfgpu_s* h = new alfgpu_s();
   h->d = d;
@@ -556,6 +629,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->CL = cluster_size(h->N);
   h->kblk = (d.delay_k > 0 && d.delay_k <= UPD_KMAX) ? d.delay_k : UPD_KMAX;
   h->dev = d.device;
+  h->mixed = d.precision == ALFGPU_PRECISION_MIXED;
+  h->mixed_propagate = h->mixed && !(d.reserved[0] & ALFGPU_FLAG_FP64_PROPAGATION);
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
@@ -565,6 +640,9 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
         cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
       return fail(ALFGPU_ERROR_CUDA);
   }
+  if (cudaFuncSetAttribute(k_update_block<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)upd_smem_bytes<float2>()) != cudaSuccess)
+    return fail(ALFGPU_ERROR_CUDA);
   if (cudaFuncSetAttribute(k_update_block<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)upd_smem_bytes<double2>()) != cudaSuccess)
     return fail(ALFGPU_ERROR_CUDA);
@@ -594,6 +672,10 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->fields, C * L * M);
   r |= dalloc(h, &h->G, B * NN); r |= dalloc(h, &h->Gw, B * NN); r |= dalloc(h, &h->T1, B * NN);
   r |= dalloc(h, &h->S, B * N); r |= dalloc(h, &h->Sinv, B * N);
+  if (h->mixed) {
+    r |= dalloc(h, &h->G32, B * NN); r |= dalloc(h, &h->T32, B * NN);
+    r |= dalloc(h, &h->X32, C * 2 * N * UPD_KMAX); r |= dalloc(h, &h->Y32, C * 2 * N * UPD_KMAX);
+  }
   auto mk_udv = [&](UDVSet& s) {
     int q = 0;
     q |= dalloc(h, &s.U, B * NN); q |= dalloc(h, &s.V, B * NN); q |= dalloc(h, &s.D, B * N); q |= dalloc(h, &s.detU, B);
@@ -809,7 +891,8 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
     if (ntau1 == h->stab_nt[NST]) {
       {
         dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
-        k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
+        if (h->mixed) k_apply_scale32<<<grid, 256, 0, h->st>>>(h->G32, h->S, h->Sinv, h->N);
+        else k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
         CKL();
       }
       pending = 0;

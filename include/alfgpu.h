@@ -51,7 +51,13 @@ enum {
   ALFGPU_ERROR_TIMEOUT = 104        /* a bounded device-side wait gave up */
 };
 
+/* Precision forms.  FP64: complex128 throughout.  MIXED: G in complex64; the G wraps,
+ * the Metropolis-block submatrix updates, the delayed-update flushes and (unless
+ * ALFGPU_FLAG_FP64_PROPAGATION is set in dims.reserved[0]) the UDV propagation
+ * products are computed in FP32; the pivoted QR, CGR and its determinant phase,
+ * and the Metropolis ratio / phase arithmetic stay FP64. */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
+enum { ALFGPU_FLAG_FP64_PROPAGATION = 1 };
 
 typedef struct alfgpu_s alfgpu_t;
 

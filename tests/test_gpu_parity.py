@@ -134,7 +134,8 @@ def _run_pair(m, seed=5, sweeps=1, chain=0):
         assert abs(g.phase()[0] - o.phase()) < 1e-10
     so, sg = o.stats(), g.stats(0)
     assert sg.n_acc == so.n_acc and sg.n_prop == so.n_prop
-    assert abs(sg.xmaxG - so.xmaxG) <= 1e-8 + 1e-3 * so.xmaxG
+    # Precision Green (max |G_wrapped - G_fresh|) is rounding drift: same band as above
+    assert sg.xmaxG <= 10.0 * so.xmaxG + 1e-12 and so.xmaxG <= 10.0 * sg.xmaxG + 1e-12
     return g, o
 
 
