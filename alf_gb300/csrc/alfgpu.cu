@@ -36,7 +36,7 @@ struct alfgpu_s {
   alfgpu_dims d;
   int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
   int mixed = 0;           // complex64 G, FP32 wraps / updates / flushes, FP64 stabilisation
-  int mixed_propagate = 0; // mixed form: UDV propagation products computed in FP32
+  int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products computed in FP32
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
@@ -630,7 +630,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->kblk = (d.delay_k > 0 && d.delay_k <= UPD_KMAX) ? d.delay_k : UPD_KMAX;
   h->dev = d.device;
   h->mixed = d.precision == ALFGPU_PRECISION_MIXED;
-  h->mixed_propagate = h->mixed && !(d.reserved[0] & ALFGPU_FLAG_FP64_PROPAGATION);
+  h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_FP32_PROPAGATION);
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);

@@ -52,12 +52,14 @@ enum {
 };
 
 /* Precision forms.  FP64: complex128 throughout.  MIXED: G in complex64; the G wraps,
- * the Metropolis-block submatrix updates, the delayed-update flushes and (unless
- * ALFGPU_FLAG_FP64_PROPAGATION is set in dims.reserved[0]) the UDV propagation
- * products are computed in FP32; the pivoted QR, CGR and its determinant phase,
- * and the Metropolis ratio / phase arithmetic stay FP64. */
+ * the Metropolis-block submatrix updates and the delayed-update flushes are
+ * computed in FP32; the UDV propagation (WRAPUR/WRAPUL), the pivoted QR, CGR and
+ * its determinant phase, and the Metropolis ratio / phase arithmetic stay FP64.
+ * ALFGPU_FLAG_FP32_PROPAGATION in dims.reserved[0] also moves the propagation
+ * products to FP32; the product of Nwrap slices is ill-conditioned, so this is
+ * only usable for small beta / Nwrap. */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
-enum { ALFGPU_FLAG_FP64_PROPAGATION = 1 };
+enum { ALFGPU_FLAG_FP32_PROPAGATION = 1 };
 
 typedef struct alfgpu_s alfgpu_t;
 
