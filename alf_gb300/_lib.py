@@ -39,7 +39,7 @@ OBS_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTE
 
 ERRORS = {0: "ERROR_NONE", 1: "ERROR_GENERIC", 3: "ERROR_UNSTABLE_MATRIX", 5: "ERROR_FIELDS",
           6: "ERROR_HAMILTONIAN", 100: "ERROR_CUDA", 101: "ERROR_ARGUMENT", 102: "ERROR_UNSUPPORTED",
-          103: "ERROR_NAN", 104: "ERROR_TIMEOUT"}
+          103: "ERROR_NAN", 104: "ERROR_TIMEOUT", 105: "ERROR_SIZE"}
 
 
 class AlfGpuError(RuntimeError):
@@ -92,6 +92,7 @@ def lib(build_if_missing: bool = True):
         "alfgpu_launch_count": ([vp], C.c_int64),
         "alfgpu_cgr": ([C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "alfgpu_decompose": ([C.c_int32, C.c_char, vp, vp, vp], C.c_int),
+        "alfgpu_decompose_noalloc": ([C.c_int32, C.c_char, vp, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -604,6 +604,7 @@ const char* alfgpu_error_string(int code) {
     case ALFGPU_ERROR_UNSUPPORTED: return "model feature not supported on the GPU path";
     case ALFGPU_ERROR_NAN: return "NaN in the Green function";
     case ALFGPU_ERROR_TIMEOUT: return "device wait timed out";
+    case ALFGPU_ERROR_SIZE: return "Ndim exceeds the static scratch of the no-allocation entry point";
     default: return "unknown error";
   }
 }
@@ -1092,3 +1093,64 @@ int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V) {
 }
 
 }  // extern "C"
+
+// ---- decompose without device allocation -----------------------------------------------------
+// Scratch of alfgpu_decompose_noalloc: a file-scope device array (held by every GPU that loads
+// the library, ~1.06 MiB).  Host code must not take the address of g_noalloc_scratch directly:
+// in host code the symbol is only a stand-in for the device copy, so each device's address is
+// obtained with cudaGetSymbolAddress while that device is current.
+struct NoallocScratch {
+  zd Vtmp[ALFGPU_NOALLOC_MAX_NDIM * ALFGPU_NOALLOC_MAX_NDIM];
+  zd tau[ALFGPU_NOALLOC_MAX_NDIM];
+  int jpvt[ALFGPU_NOALLOC_MAX_NDIM];
+  int perm[ALFGPU_NOALLOC_MAX_NDIM];
+  double DUP[ALFGPU_NOALLOC_MAX_NDIM];
+  double vn[2 * ALFGPU_NOALLOC_MAX_NDIM];
+  QRInfo info;
+  zd dphase;
+  zd detU;
+};
+static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
+
+namespace {
+struct NoallocDevice {
+  NoallocScratch* scratch = nullptr;
+  int cl16 = 0;  // non-portable 16-CTA clusters enabled for the QR kernels
+};
+NoallocDevice g_noalloc_dev[64];
+}  // namespace
+
+extern "C" int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, double* V, double* detU,
+                                        void* stream) {
+  if (ndim < 1 || !U || !D || !V) return ALFGPU_ERROR_ARGUMENT;
+  if (ndim > ALFGPU_NOALLOC_MAX_NDIM) return ALFGPU_ERROR_SIZE;
+  if (side != 'r' && side != 'R' && side != 'l' && side != 'L') return ALFGPU_ERROR_ARGUMENT;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ALFGPU_ERROR_CUDA;
+  NoallocDevice& nd = g_noalloc_dev[dev];
+  if (!nd.scratch) {  // first call on this device: resolve the device address of the scratch array
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return ALFGPU_ERROR_CUDA;
+    if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+        cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+      nd.cl16 = 1;
+    cudaGetLastError();
+    nd.scratch = static_cast<NoallocScratch*>(p);
+  }
+  NoallocScratch* s = nd.scratch;
+  alfgpu_s ctx;  // host-side bookkeeping only; all device memory below is the caller's or the scratch
+  ctx.N = ndim; ctx.F = 1; ctx.C = 1; ctx.B = 1; ctx.M = 1; ctx.L = 1; ctx.NSUN = 1; ctx.dev = dev;
+  ctx.CL = cluster_size(ndim);
+  if (ctx.CL > 8 && !nd.cl16) ctx.CL = 8;
+  ctx.st = (cudaStream_t)stream;
+  ctx.Vtmp = s->Vtmp; ctx.tau = s->tau; ctx.jpvt = s->jpvt; ctx.perm = s->perm; ctx.DUP = s->DUP; ctx.vn = s->vn;
+  ctx.info = &s->info; ctx.dphase = &s->dphase;
+  UDVSet u;
+  u.U = reinterpret_cast<zd*>(U);
+  u.V = reinterpret_cast<zd*>(V);
+  u.D = D;
+  u.detU = detU ? reinterpret_cast<zd*>(detU) : &s->detU;
+  const int rc = decompose(&ctx, u, (side == 'l' || side == 'L') ? 1 : 0);
+  ctx.st = nullptr;  // the caller owns the stream
+  return rc;
+}

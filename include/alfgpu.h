@@ -48,7 +48,8 @@ enum {
   ALFGPU_ERROR_ARGUMENT = 101,      /* bad pointer / size / index */
   ALFGPU_ERROR_UNSUPPORTED = 102,   /* model feature not implemented on the GPU */
   ALFGPU_ERROR_NAN = 103,           /* NaN in G (control_mod.F90:219-263 aborts with ERROR_GENERIC) */
-  ALFGPU_ERROR_TIMEOUT = 104        /* a bounded device-side wait gave up */
+  ALFGPU_ERROR_TIMEOUT = 104,       /* a bounded device-side wait gave up */
+  ALFGPU_ERROR_SIZE = 105           /* size above a fixed maximum (see alfgpu_decompose_noalloc) */
 };
 
 /* Precision forms.  FP64: complex128 throughout.  MIXED: G in complex64; the G wraps,
@@ -184,6 +185,29 @@ int64_t alfgpu_launch_count(alfgpu_t* h);
 int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, const double* VR, const double* UL,
                const double* DL, const double* VL, double* G, double* phase);
 int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V);
+
+/* decompose_UDV_state on DEVICE buffers without allocating any device memory.
+ * This entry point has no counterpart in the reference.  It exists for callers
+ * that cannot or must not allocate: a host program whose device memory is
+ * already owned by another allocator (a framework's caching pool), or one that
+ * must not trigger the implicit device synchronisation of cudaMalloc/cudaFree
+ * in the middle of its stream work.  The caller passes its own device
+ * pointers: U (ndim x ndim complex128, column-major, in/out), D (ndim doubles,
+ * in/out: the scales, real), V (ndim x ndim complex128, in/out), detU (one
+ * complex128, out: det(U) after the decomposition; may be NULL) and the
+ * cudaStream_t to launch on (NULL = legacy default stream).  All scratch lives
+ * in one file-scope device array sized for ndim <= ALFGPU_NOALLOC_MAX_NDIM
+ * (about 1.06 MiB, held by every GPU that loads the library until the process
+ * exits); larger ndim returns ALFGPU_ERROR_SIZE without touching the buffers.
+ * The first call on each device resolves the array's device address
+ * (cudaGetSymbolAddress) with that device current, so make the first call on
+ * a device before any stream capture.  Every call reuses the same array, and
+ * each call writes every scratch word it later reads, so no state carries over;
+ * calls that overlap on the GPU (different streams or host threads) race on
+ * the shared array and must be serialised by the caller.  The call is
+ * stream-ordered: results are ready when the stream reaches them. */
+#define ALFGPU_NOALLOC_MAX_NDIM 256
+int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, double* V, double* detU, void* stream);
 
 #ifdef __cplusplus
 }
