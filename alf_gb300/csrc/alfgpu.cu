@@ -35,8 +35,8 @@ struct UDVSet {  // one UDV state for all B = C*F (chain, flavour) pairs
 struct alfgpu_s {
   alfgpu_dims d;
   int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
-  int mixed = 0;           // complex64 G, FP32 wraps / updates / flushes, FP64 stabilisation
-  int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products computed in FP32
+  int mixed = 0;           // double-float G wraps and flush GEMMs on the FP32 pipes, FP64 elsewhere
+  int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products in double-float too
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
@@ -50,7 +50,6 @@ struct alfgpu_s {
   int8_t* fields = nullptr;
   // state
   zd *G = nullptr, *Gw = nullptr, *T1 = nullptr;
-  float2 *G32 = nullptr, *T32 = nullptr, *X32 = nullptr, *Y32 = nullptr;  // mixed form
   zd *S = nullptr, *Sinv = nullptr;
   UDVSet udvl, udvr;
   std::vector<UDVSet> udvst;  // index nst-1
@@ -226,18 +225,7 @@ static int gemm32(alfgpu_s* h, const GemmParams& g, int tA, int tB, int tC) {
   Gemm32Params P;
   P.g = g; P.tA = tA; P.tB = tB; P.tC = tC;
   h->launches++;
-  CK(launch_cgemm32(P, h->st));
-  return 0;
-}
-
-static int to32(alfgpu_s* h, const zd* in, float2* out, size_t n) {
-  k_c128_to_c64<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, h->st>>>(in, out, (long long)n);
-  CKL();
-  return 0;
-}
-static int to64(alfgpu_s* h, const float2* in, zd* out, size_t n) {
-  k_c64_to_c128<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, h->st>>>(in, out, (long long)n);
-  CKL();
+  CK(launch_dfgemm(P, h->st));
   return 0;
 }
 
@@ -426,12 +414,8 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
 static int stabilise(alfgpu_s* h, int nvar, int compare) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
-  if (compare) {
-    if (h->mixed) RET(to64(h, h->G32, h->Gw, (size_t)B * NN));
-    else RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
-  }
+  if (compare) RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
   RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
-  if (h->mixed) RET(to32(h, h->G, h->G32, (size_t)B * NN));
   if (compare) {
     k_compare<<<B, 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
     CKL();
@@ -470,22 +454,22 @@ static int hop_impl(alfgpu_s* h, int up, int with_scale) {
     const double* E2 = up ? h->expTinv : h->expT;
     if (up) {
       GemmParams p = gsq(h, B);
-      p.A = E1; p.modA = F; p.B = h->G32; p.C = (zd*)h->T32;
+      p.A = E1; p.modA = F; p.B = h->G; p.C = h->T1;
       if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 0; }
-      RET(gemm32(h, p, ST_R64, ST_C64, ST_C64));
+      RET(gemm32(h, p, ST_R64, ST_C128, ST_C128));
       GemmParams q = gsq(h, B);
-      q.A = h->T32; q.B = E2; q.modB = F; q.C = (zd*)h->G32;
+      q.A = h->T1; q.B = E2; q.modB = F; q.C = h->G;
       if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 1; }
-      RET(gemm32(h, q, ST_C64, ST_R64, ST_C64));
+      RET(gemm32(h, q, ST_C128, ST_R64, ST_C128));
     } else {
       GemmParams p = gsq(h, B);
-      p.A = h->G32; p.B = E2; p.modB = F; p.C = (zd*)h->T32;
+      p.A = h->G; p.B = E2; p.modB = F; p.C = h->T1;
       if (with_scale) { p.ks = h->S; p.sKS = N; p.ksOnA = 1; }
-      RET(gemm32(h, p, ST_C64, ST_R64, ST_C64));
+      RET(gemm32(h, p, ST_C128, ST_R64, ST_C128));
       GemmParams q = gsq(h, B);
-      q.A = E1; q.modA = F; q.B = h->T32; q.C = (zd*)h->G32;
+      q.A = E1; q.modA = F; q.B = h->T1; q.C = h->G;
       if (with_scale) { q.ks = h->Sinv; q.sKS = N; q.ksOnA = 0; }
-      RET(gemm32(h, q, ST_R64, ST_C64, ST_C64));
+      RET(gemm32(h, q, ST_R64, ST_C128, ST_C128));
     }
     return 0;
   }
@@ -536,37 +520,21 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
     prof_begin(h, ALFGPU_PROF_UPDATE);
-    if (h->mixed) {
-      u.G = h->G32;
-      k_update_block<float2><<<h->C, UPD_THREADS, upd_smem_bytes<float2>(), h->st>>>(u);
-    } else {
-      k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
-    }
+    k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
     prof_end(h);
     CKL();
     prof_begin(h, ALFGPU_PROF_FLUSH);
-    void* Gst = h->mixed ? (void*)h->G32 : (void*)h->G;
-    void* Xst = h->mixed ? (void*)h->X32 : (void*)h->X;
-    void* Yst = h->mixed ? (void*)h->Y32 : (void*)h->Y;
-    if (h->mixed) {
-      k_flush_w32<<<h->B, 256, 0, h->st>>>(h->G32, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
-      CKL();
-      k_flush_x<float2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
-                                                                                          h->sites, Xst);
-      CKL();
-      k_flush_y<float2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->W,
-                                                                             Yst);
-      CKL();
-    } else {
-      k_flush_w<double2><<<h->B, 256, 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
-      CKL();
-      k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
-                                                                                           h->sites, Xst);
-      CKL();
-      k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites,
-                                                                              h->W, Yst);
-      CKL();
-    }
+    void* Gst = h->G;
+    void* Xst = h->X;
+    void* Yst = h->Y;
+    k_flush_w<double2><<<h->B, 256, 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
+    CKL();
+    k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
+                                                                                         h->sites, Xst);
+    CKL();
+    k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->W,
+                                                                            Yst);
+    CKL();
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();
     p.m = N; p.n = N; p.k = UPD_KMAX;
@@ -580,7 +548,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     k_expand_m<<<(h->B + 127) / 128, 128, 0, h->st>>>(h->m, h->m + h->C, h->C, F);
     CKL();
     p.kdyn = h->m + h->C;
-    if (h->mixed) RET(gemm32(h, p, ST_C64, ST_C64, ST_C64));
+    if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
     else RET(gemm(h, p));
     prof_end(h);
   }
@@ -631,7 +599,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->kblk = (d.delay_k > 0 && d.delay_k <= UPD_KMAX) ? d.delay_k : UPD_KMAX;
   h->dev = d.device;
   h->mixed = d.precision == ALFGPU_PRECISION_MIXED;
-  h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_FP32_PROPAGATION);
+  h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_PROPAGATION);
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
@@ -641,9 +609,6 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
         cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
       return fail(ALFGPU_ERROR_CUDA);
   }
-  if (cudaFuncSetAttribute(k_update_block<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)upd_smem_bytes<float2>()) != cudaSuccess)
-    return fail(ALFGPU_ERROR_CUDA);
   if (cudaFuncSetAttribute(k_update_block<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)upd_smem_bytes<double2>()) != cudaSuccess)
     return fail(ALFGPU_ERROR_CUDA);
@@ -673,10 +638,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->fields, C * L * M);
   r |= dalloc(h, &h->G, B * NN); r |= dalloc(h, &h->Gw, B * NN); r |= dalloc(h, &h->T1, B * NN);
   r |= dalloc(h, &h->S, B * N); r |= dalloc(h, &h->Sinv, B * N);
-  if (h->mixed) {
-    r |= dalloc(h, &h->G32, B * NN); r |= dalloc(h, &h->T32, B * NN);
-    r |= dalloc(h, &h->X32, C * 2 * N * UPD_KMAX); r |= dalloc(h, &h->Y32, C * 2 * N * UPD_KMAX);
-  }
+
   auto mk_udv = [&](UDVSet& s) {
     int q = 0;
     q |= dalloc(h, &s.U, B * NN); q |= dalloc(h, &s.V, B * NN); q |= dalloc(h, &s.D, B * N); q |= dalloc(h, &s.detU, B);
@@ -892,8 +854,7 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
     if (ntau1 == h->stab_nt[NST]) {
       {
         dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
-        if (h->mixed) k_apply_scale32<<<grid, 256, 0, h->st>>>(h->G32, h->S, h->Sinv, h->N);
-        else k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
+        k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
         CKL();
       }
       pending = 0;

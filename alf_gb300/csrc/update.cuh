@@ -19,8 +19,8 @@
 //   Gamma = 1 + (1 - G0(S,S)) Delta_S   (S = accepted sites, in accept order),
 // applied by one rank-m GEMM flush; Gamma^-1 is formed by k_flush_w.
 //
-// T is the storage type of G: double2 (plain complex128 form) or float2 (mixed
-// form, complex64 G).  Ratios, phases and the Metropolis test are always FP64.
+// T is the storage type of G (double2: complex128, used by both precision
+// forms).  Ratios, phases and the Metropolis test are always FP64.
 #pragma once
 #include "common.cuh"
 
@@ -63,10 +63,6 @@ template <typename T> struct CT;
 template <> struct CT<double2> {
   static ALF_DEV double2 mk(zd a) { return a; }
   static ALF_DEV zd wide(double2 a) { return a; }
-};
-template <> struct CT<float2> {
-  static ALF_DEV float2 mk(zd a) { return make_float2((float)a.x, (float)a.y); }
-  static ALF_DEV zd wide(float2 a) { return zmk((double)a.x, (double)a.y); }
 };
 template <typename T> ALF_DEV T tmul(T a, T b) { T r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
 template <typename T> ALF_DEV T tadd(T a, T b) { T r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
@@ -314,72 +310,6 @@ __global__ void k_flush_y(const void* Gv, long long sG, int N, int F, const int*
     zd y = zmk(0.0, 0.0);
     for (int l2 = 0; l2 < m; ++l2) y = zadd(y, zmul(Ws[tx][l2], gb[ty][l2]));
     reinterpret_cast<T*>(Yv)[((long long)c * 2 + f) * N * UPD_KMAX + tx + (long long)col * UPD_KMAX] = CT<T>::mk(y);
-  }
-}
-
-// complex64 variant of k_flush_w for the mixed form (same algorithm in FP32).
-__global__ void __launch_bounds__(256) k_flush_w32(const float2* Gv, long long sG, int N, int F, const int* m_in,
-                                                   const int* sites, const zd* delta, zd* W) {
-  const int b = blockIdx.x, c = b / F, f = b % F;
-  const int m = m_in[c];
-  if (m == 0) return;
-  const float2* G = Gv + (long long)c * sG + (long long)f * N * N;
-  __shared__ float2 A[UPD_KMAX][2 * UPD_KMAX + 1];
-  __shared__ int st[UPD_KMAX];
-  __shared__ float2 dl[UPD_KMAX];
-  __shared__ int piv;
-  __shared__ float2 pinv;
-  auto fm = [](float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
-  for (int l = threadIdx.x; l < m; l += blockDim.x) {
-    st[l] = sites[(long long)c * UPD_KMAX + l];
-    const zd d = delta[((long long)c * 2 + f) * UPD_KMAX + l];
-    dl[l] = make_float2((float)d.x, (float)d.y);
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    const int r = e % m, col = e / m;
-    const float2 g = G[st[col] + (long long)st[r] * N];
-    float2 v = fm(make_float2((col == r ? 1.f : 0.f) - g.x, -g.y), dl[r]);
-    if (col == r) v.x += 1.f;
-    A[r][col] = v;
-    A[r][m + col] = make_float2(r == col ? 1.f : 0.f, 0.f);
-  }
-  __syncthreads();
-  for (int k = 0; k < m; ++k) {
-    if (threadIdx.x == 0) {
-      int pv = k;
-      float best = A[k][k].x * A[k][k].x + A[k][k].y * A[k][k].y;
-      for (int r = k + 1; r < m; ++r) {
-        const float v = A[r][k].x * A[r][k].x + A[r][k].y * A[r][k].y;
-        if (v > best) { best = v; pv = r; }
-      }
-      piv = pv;
-      const float2 a = A[pv][k];
-      const float d = a.x * a.x + a.y * a.y;
-      pinv = make_float2(a.x / d, -a.y / d);
-    }
-    __syncthreads();
-    const int pv = piv;
-    if (pv != k)
-      for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) { float2 t = A[k][j]; A[k][j] = A[pv][j]; A[pv][j] = t; }
-    __syncthreads();
-    const float2 inv = pinv;
-    for (int j = threadIdx.x; j < 2 * m; j += blockDim.x)
-      if (j != k) A[k][j] = fm(A[k][j], inv);
-    __syncthreads();
-    for (int e = threadIdx.x; e < m * 2 * m; e += blockDim.x) {
-      const int r = e / (2 * m), j = e % (2 * m);
-      if (r != k && j != k) {
-        const float2 t = fm(A[r][k], A[k][j]);
-        A[r][j] = make_float2(A[r][j].x - t.x, A[r][j].y - t.y);
-      }
-    }
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    const int l = e / m, l2 = e % m;
-    const float2 w = fm(dl[l], A[l2][m + l]);
-    W[(((long long)c * 2 + f) * UPD_KMAX + l) * UPD_KMAX + l2] = zmk(w.x, w.y);
   }
 }
 

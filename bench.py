@@ -274,7 +274,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "df64+c128",
         "data": "synthetic (seeded fields and draws)",
         "config": dict(workload, parallelism=f"replicas x{ws}"),
         "e2e": {"value": e2e, "unit": "sweeps/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},

@@ -52,15 +52,16 @@ enum {
   ALFGPU_ERROR_SIZE = 105           /* size above a fixed maximum (see alfgpu_decompose_noalloc) */
 };
 
-/* Precision forms.  FP64: complex128 throughout.  MIXED: G in complex64; the G wraps,
- * the Metropolis-block submatrix updates and the delayed-update flushes are
- * computed in FP32; the UDV propagation (WRAPUR/WRAPUL), the pivoted QR, CGR and
- * its determinant phase, and the Metropolis ratio / phase arithmetic stay FP64.
- * ALFGPU_FLAG_FP32_PROPAGATION in dims.reserved[0] also moves the propagation
- * products to FP32; the product of Nwrap slices is ill-conditioned, so this is
- * only usable for small beta / Nwrap. */
+/* Precision forms.  FP64: complex128 throughout (FP64 tensor cores for the products).
+ * MIXED: the G wraps through exp(-dtau T) and the delayed-update flush GEMMs run in
+ * double-float arithmetic (FP32 hi/lo pairs, ~2^-44 relative rounding) on the FP32
+ * pipes; G and all state stay complex128; the UDV propagation, pivoted QR, CGR and its
+ * determinant phase, and the Metropolis ratio / phase arithmetic stay FP64.
+ * ALFGPU_FLAG_DF_PROPAGATION in dims.reserved[0] also moves the UDV propagation
+ * products to double-float; the product of Nwrap slices is ill-conditioned
+ * (1e5-1e10 at beta = 10), so this is only usable for small beta / Nwrap. */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
-enum { ALFGPU_FLAG_FP32_PROPAGATION = 1 };
+enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
 
 typedef struct alfgpu_s alfgpu_t;
 

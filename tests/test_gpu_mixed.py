@@ -1,6 +1,7 @@
-"""Mixed-precision form (complex64 G; FP32 wraps, block updates, flushes and UDV
-propagation; FP64 pivoted QR, CGR and ratio/phase arithmetic) against the
-FP64 CPU oracle on the same fields and draws.
+"""Mixed-precision form (double-float G wraps and delayed-update flush GEMMs on
+the FP32 pipes; complex128 storage; FP64 UDV propagation, pivoted QR, CGR and
+ratio/phase arithmetic) against the FP64 CPU oracle on the same fields and
+draws.
 
 Acceptance bound: max |G_mixed - G_fp64| <= 1e-5 at every stabilisation point
 (the freshly computed CGR result) while the accept/reject sequences agree, and
