@@ -35,7 +35,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(s) <= t for s in srcs):
             return LIB
-    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared",
            "-o", LIB + ".tmp", os.path.join(CSRC, "alfgpu.cu")]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

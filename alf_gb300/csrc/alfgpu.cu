@@ -12,11 +12,13 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <complex>
 #include <vector>
 
 #include "common.cuh"
 #include "gemm.cuh"
 #include "gemm32.cuh"
+#include "qr_blocked.cuh"
 #include "kernels_misc.cuh"
 #include "linalg.cuh"
 #include "update.cuh"
@@ -37,6 +39,9 @@ struct alfgpu_s {
   int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
   int mixed = 0;           // double-float G wraps and flush GEMMs on the FP32 pipes, FP64 elsewhere
   int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products in double-float too
+  int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
+  int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
+  int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
@@ -45,6 +50,8 @@ struct alfgpu_s {
   double *expT = nullptr, *expTinv = nullptr;
   int* v_site = nullptr;
   zd *v_g = nullptr, *v_alpha = nullptr, *v_Eexp = nullptr;
+  UpdTab* v_tab = nullptr;  // [chain][F*M][5][3] transition factors of every (vertex, old field, flip choice)
+  int *v_sptr = nullptr, *v_slist = nullptr;  // [chain][F][N+1], [chain][F][M]: vertices of each site (CSR)
   double* v_E = nullptr;
   int8_t* v_type = nullptr;
   int8_t* fields = nullptr;
@@ -55,6 +62,8 @@ struct alfgpu_s {
   std::vector<UDVSet> udvst;  // index nst-1
   // stabilisation work
   zd *TP = nullptr, *Qb = nullptr, *RHS = nullptr, *tau = nullptr, *Vtmp = nullptr, *dphase = nullptr;
+  zd* QRw = nullptr;         // factored matrix (R above, reflectors below) of the last QR
+  double* qkeys = nullptr;   // column keys of the pre-pivoting
   int *jpvt = nullptr, *perm = nullptr, *iperm = nullptr;
   double *DUP = nullptr, *vn = nullptr, *cmp = nullptr, *opang = nullptr;
   QRInfo* info = nullptr;
@@ -153,6 +162,9 @@ static void fill_tables(FieldTables& ft) {
   ft.gama[1][3] = 1.0 + sq6 / 3.0; ft.gama[1][4] = 1.0 - sq6 / 3.0;
   const int8_t fl[5][3] = {{-1, 1, 2}, {1, 2, -2}, {0, 0, 0}, {2, -2, -1}, {-2, -1, 1}};
   memcpy(ft.flip, fl, sizeof(fl));
+  for (int t = 0; t < 2; ++t)
+    for (int so = 0; so < 5; ++so)
+      for (int sn = 0; sn < 5; ++sn) ft.grat[t][so][sn] = ft.gama[t][sn] / ft.gama[t][so];
 }
 
 static int cluster_size(int N) {
@@ -215,6 +227,7 @@ static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
   return 0;
 }
 
+
 static int gemm(alfgpu_s* h, const GemmParams& p) {
   h->launches++;
   CK(launch_zgemm(p, h->st));
@@ -263,14 +276,107 @@ static int udv_reset(alfgpu_s* h, UDVSet& s) {
 
 // Slice scale vectors S / Sinv of slice nt1 from the current fields.
 static int slice_scale(alfgpu_s* h, int nt1) {
-  k_slice_scale<<<h->B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->N, h->F, nt1, h->v_site, h->v_Eexp, h->S,
-                                          h->Sinv);
+  k_slice_scale<<<h->B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->N, h->F, nt1, h->v_sptr, h->v_slist, h->v_Eexp,
+                                         h->S, h->Sinv);
   CKL();
   return 0;
 }
 
 // decompose_UDV_state (udv_state_mod.F90:466-578) on all B pairs; s.U holds the propagated A.
-static int decompose(alfgpu_s* h, UDVSet& s, int left) {
+// QR of Ain * diag(colscale) into Aout (Aout != Ain): R above the diagonal (rows
+// normalised by D = DUP), reflectors below, tau, jpvt, info.
+static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, int exact) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  h->exact_qrp = exact;
+  const dim3 g8((N + 7) / 8, B);
+  if (exact && !h->qrr_ok) {
+    RET(copy_mats(h, Aout, Ain, (size_t)B * NN));
+    return launch_qr(h, Aout, colscale, B);
+  }
+  prof_begin(h, ALFGPU_PROF_QR);
+  if (exact) {
+    QRRowsParams q;
+    q.Ain = Ain; q.A = Aout; q.lda = N; q.sA = NN; q.N = N;
+    q.colscale = colscale; q.sCS = N;
+    q.tau = h->tau; q.sT = N; q.jpvt = h->jpvt; q.sP = N; q.D = h->DUP; q.sD = N; q.info = h->info;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(h->CL, B, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = qrr_smem_bytes(N, h->CL);
+    cfg.stream = h->st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    cfg.attrs = at; cfg.numAttrs = 1;
+    h->launches++;
+    CK(cudaLaunchKernelEx(&cfg, k_qrp_rows, q));
+    k_bqr_finish<<<g8, 256, (size_t)N * sizeof(double), h->st>>>(Aout, N, NN, N, h->tau, N, h->DUP, N, h->info);
+    CKL();
+    prof_end(h);
+    return 0;
+  }
+  k_bqr_keys<<<g8, 256, 0, h->st>>>(Ain, N, NN, N, colscale, N, h->qkeys);
+  CKL();
+  k_bqr_permute<<<g8, 256, (size_t)N * (sizeof(double) + sizeof(int)), h->st>>>(Ain, N, NN, N, colscale, N, h->qkeys,
+                                                                                  Aout, NN, h->jpvt, N, h->info);
+  CKL();
+  for (int j0 = 0; j0 < N; j0 += BQR_NB) {
+    const int w = (N - j0 < BQR_NB) ? N - j0 : BQR_NB;
+    BQRPanel pp;
+    pp.A = Aout; pp.lda = N; pp.sA = NN; pp.N = N; pp.j0 = j0; pp.nb = w;
+    pp.tau = h->tau; pp.sT = N; pp.D = h->DUP; pp.sD = N;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(h->CL, B, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.stream = h->st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    cfg.attrs = at; cfg.numAttrs = 1;
+    h->launches++;
+    CK(cudaLaunchKernelEx(&cfg, k_bqr_panel, pp));
+    if (j0 + w < N) {
+      BQRApply ap;
+      ap.V = Aout; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
+      ap.C = Aout; ap.ldc = N; ap.sC = NN;
+      ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0 + w; ap.conj_tau = 1;
+      k_bqr_apply<<<dim3(N - j0 - w, B), 128, 0, h->st>>>(ap);
+      CKL();
+    }
+  }
+  k_bqr_finish<<<g8, 256, (size_t)N * sizeof(double), h->st>>>(Aout, N, NN, N, h->tau, N, h->DUP, N, h->info);
+  CKL();
+  prof_end(h);
+  return 0;
+}
+
+// Explicit Q (first N columns of H_1 ... H_N) of the factored matrix F into Q (Q != F).
+static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  if (N > 32 * BQR_LROWS) {
+    RET(copy_mats(h, Q, F, (size_t)B * NN));
+    return launch_orgqr(h, Q, B);
+  }
+  prof_begin(h, ALFGPU_PROF_ORGQR);
+  for (int j0 = ((N - 1) / BQR_NB) * BQR_NB; j0 >= 0; j0 -= BQR_NB) {
+    const int w = (N - j0 < BQR_NB) ? N - j0 : BQR_NB;
+    BQRApply ap;
+    ap.V = F; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
+    ap.C = Q; ap.ldc = N; ap.sC = NN;
+    ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0; ap.conj_tau = 0;
+    k_bqr_apply<<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
+    CKL();
+  }
+  prof_end(h);
+  return 0;
+}
+
+// Decompose with ZGEQP3 in place on s.U (no work matrix): the allocation-free entry point.
+static int decompose_inplace(alfgpu_s* h, UDVSet& s, int left) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
   RET(launch_qr(h, s.U, s.D, B));
@@ -291,6 +397,34 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   RET(copy_mats(h, s.V, h->Vtmp, (size_t)B * NN));
   CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   RET(launch_orgqr(h, s.U, B));
+  k_scale_col0<<<B, 256, 0, h->st>>>(s.U, N, h->dphase);
+  CKL();
+  return 0;
+}
+
+// decompose_UDV_state (udv_state_mod.F90:448-582): QR of U*D, phase of det(R) moved into U(:,1),
+// V <- R P^-1 V, U <- Q.  The factored matrix goes to the work matrix QRw; Q is formed into s.U.
+static int decompose(alfgpu_s* h, UDVSet& s, int left) {
+  if (!h->QRw) return decompose_inplace(h, s, left);
+  const int N = h->N, B = h->B;
+  RET(qr_any(h, s.U, s.D, h->QRw, h->exact_dec));
+  k_decomp_phase<<<B, 256, 0, h->st>>>(h->QRw, N, N, h->info, left, h->dphase, s.detU);
+  CKL();
+  k_perm0<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->perm, N, N);
+  CKL();
+  GemmParams p = gsq(h, B);
+  if (!left) {  // V = R * P^T V   (ZLAPMR forward, ZTRMM L,U,N)
+    p.A = h->QRw; p.opA = OP_N; p.triA = 1;
+    p.B = s.V; p.opB = OP_N; p.permB = h->perm; p.sPB = N;
+  } else {      // V = (V P) * R^H (ZLAPMT forward, ZTRMM R,U,C)
+    p.A = s.V; p.opA = OP_N; p.permA = h->perm; p.sPA = N;
+    p.B = h->QRw; p.opB = OP_C; p.triB = 1;
+  }
+  p.C = h->Vtmp;
+  RET(gemm(h, p));
+  std::swap(s.V, h->Vtmp);
+  CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  RET(orgqr_any(h, h->QRw, s.U));
   k_scale_col0<<<B, 256, 0, h->st>>>(s.U, N, h->dphase);
   CKL();
   return 0;
@@ -360,11 +494,10 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     CKL();
     QR = h->Qb;
   }
-  RET(launch_qr(h, QR, nullptr, B));
-  // keep R: copy the factored matrix, form Q in the copy
-  zd* Q = (QR == h->TP) ? h->Qb : h->TP;
-  RET(copy_mats(h, Q, QR, (size_t)B * NN));
-  RET(launch_orgqr(h, Q, B));
+  RET(qr_any(h, QR, nullptr, h->QRw, h->exact_cgr));
+  zd* Q = QR;  // the input is no longer needed
+  RET(orgqr_any(h, h->QRw, Q));
+  QR = h->QRw;
   k_invperm<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->iperm, N, N);
   CKL();
   k_real_to_complex<<<(B * N + 255) / 256, 256, 0, h->st>>>(h->DUP, h->S, (long long)B * N);
@@ -417,7 +550,8 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
   if (compare) RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
   RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
   if (compare) {
-    k_compare<<<B, 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
+    CK(cudaMemsetAsync(h->cmp, 0, 2 * (size_t)B * sizeof(double), h->st));
+    k_compare<<<dim3(CMP_BLOCKS, B), 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
     CKL();
   }
   k_opphase<<<B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->F, h->v_g, h->v_alpha, h->v_type, h->ft, h->opang);
@@ -510,31 +644,28 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.N = N; u.F = F; u.M = M; u.L = h->L; u.NSUN = h->NSUN;
     u.nt1 = nt1; u.dir = dir; u.q0 = q0; u.nq = (M - q0 < h->kblk) ? M - q0 : h->kblk;
     u.visit_base = visit_base;
+    u.nChains = h->C;
     u.G = h->G; u.sG = F * NN;
-    u.V.site = h->v_site; u.V.g = h->v_g; u.V.alpha = h->v_alpha; u.V.E = h->v_E; u.V.type = h->v_type;
-    u.V.Eexp = h->v_Eexp; u.V.sK = (long long)F * M;
+    u.V.site = h->v_site; u.V.type = h->v_type; u.V.sK = (long long)F * M;
+    u.tab = h->v_tab;
     u.fields = h->fields;
     u.draws = draws_dev; u.sDraws = 6ll * M * h->L;
     u.rngkey = h->rngkey; u.rngctr = h->rngctr;
-    u.phase = h->phase; u.m_out = h->m; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
+    u.phase = h->phase; u.m_out = h->m; u.W = h->W; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
     prof_begin(h, ALFGPU_PROF_UPDATE);
-    k_update_block<double2><<<h->C, UPD_THREADS, upd_smem_bytes<double2>(), h->st>>>(u);
+    if (h->mixed) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
+    else k_update<ArD><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
     prof_end(h);
     CKL();
     prof_begin(h, ALFGPU_PROF_FLUSH);
+    k_flush_xy<<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->X,
+                                                                  h->Y);
+    CKL();
     void* Gst = h->G;
     void* Xst = h->X;
     void* Yst = h->Y;
-    k_flush_w<double2><<<h->B, 256, 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->dlt, h->W);
-    CKL();
-    k_flush_x<double2><<<dim3((unsigned)((N * u.nq + 255) / 256), h->B), 256, 0, h->st>>>(Gst, F * NN, N, F, h->m,
-                                                                                         h->sites, Xst);
-    CKL();
-    k_flush_y<double2><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(Gst, F * NN, N, F, h->m, h->sites, h->W,
-                                                                            Yst);
-    CKL();
     // G -= X Y, rank m per chain
     GemmParams p = gemm_defaults();
     p.m = N; p.n = N; p.k = UPD_KMAX;
@@ -545,9 +676,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     p.batch = h->B;
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
-    k_expand_m<<<(h->B + 127) / 128, 128, 0, h->st>>>(h->m, h->m + h->C, h->C, F);
-    CKL();
-    p.kdyn = h->m + h->C;
+    p.kdyn = h->m + h->C;  // per-(chain, flavour) rank, written by k_update
     if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
     else RET(gemm(h, p));
     prof_end(h);
@@ -600,17 +729,22 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->dev = d.device;
   h->mixed = d.precision == ALFGPU_PRECISION_MIXED;
   h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_PROPAGATION);
+  h->exact_dec = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_DECOMPOSE)) ? 1 : 0;
+  h->exact_cgr = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_CGR)) ? 1 : 0;
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
   if (h->CL > 8) {
     if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-        cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(k_bqr_panel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
       return fail(ALFGPU_ERROR_CUDA);
   }
-  if (cudaFuncSetAttribute(k_update_block<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)upd_smem_bytes<double2>()) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_update<ArD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes()) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_update<ArF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes()) !=
+          cudaSuccess)
     return fail(ALFGPU_ERROR_CUDA);
   // shrink the QR cluster until at least one cluster fits on the device
   while (h->CL > 1) {
@@ -624,17 +758,46 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
     cfg.attrs = at; cfg.numAttrs = 1;
     int n1 = 0, n2 = 0;
+    int n3 = 0;
+    cudaLaunchConfig_t cfg3 = cfg;
+    cfg3.dynamicSmemBytes = 0;
     if (cudaOccupancyMaxActiveClusters(&n1, k_qrp, &cfg) == cudaSuccess &&
-        cudaOccupancyMaxActiveClusters(&n2, k_orgqr, &cfg) == cudaSuccess && n1 > 0 && n2 > 0)
+        cudaOccupancyMaxActiveClusters(&n2, k_orgqr, &cfg) == cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&n3, k_bqr_panel, &cfg3) == cudaSuccess && n1 > 0 && n2 > 0 && n3 > 0)
       break;
     cudaGetLastError();
     h->CL /= 2;
   }
+  // exact pivoting on the row-distributed cluster kernel when its row block fits in shared memory
+  {
+    const size_t sm = qrr_smem_bytes(h->N, h->CL);
+    if (sm <= 227 * 1024 &&
+        cudaFuncSetAttribute(k_qrp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
+        (h->CL <= 8 ||
+         cudaFuncSetAttribute(k_qrp_rows, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)) {
+      cudaLaunchConfig_t cfg;
+      memset(&cfg, 0, sizeof(cfg));
+      cfg.gridDim = dim3(h->CL, 1, 1);
+      cfg.blockDim = dim3(256, 1, 1);
+      cfg.dynamicSmemBytes = sm;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+      cfg.attrs = at; cfg.numAttrs = 1;
+      int n = 0;
+      h->qrr_ok = cudaOccupancyMaxActiveClusters(&n, k_qrp_rows, &cfg) == cudaSuccess && n > 0;
+    }
+    cudaGetLastError();
+  }
+  // the blocked QR keeps at most BQR_ROWS panel rows per CTA and BQR_LROWS rows per lane
+  if (h->N > 32 * BQR_LROWS || (h->N + h->CL - 1) / h->CL > BQR_ROWS) h->exact_dec = h->exact_cgr = 1;
   const size_t N = h->N, NN = N * N, B = h->B, C = h->C, F = h->F, M = h->M, L = h->L;
   int r = 0;
   r |= dalloc(h, &h->expT, F * NN); r |= dalloc(h, &h->expTinv, F * NN);
   r |= dalloc(h, &h->v_site, C * F * M); r |= dalloc(h, &h->v_g, C * F * M); r |= dalloc(h, &h->v_alpha, C * F * M);
   r |= dalloc(h, &h->v_E, C * F * M); r |= dalloc(h, &h->v_type, C * F * M); r |= dalloc(h, &h->v_Eexp, C * F * M * 5);
+  r |= dalloc(h, &h->v_tab, C * F * M * 15);
+  r |= dalloc(h, &h->v_sptr, C * F * (N + 1)); r |= dalloc(h, &h->v_slist, C * F * M);
   r |= dalloc(h, &h->fields, C * L * M);
   r |= dalloc(h, &h->G, B * NN); r |= dalloc(h, &h->Gw, B * NN); r |= dalloc(h, &h->T1, B * NN);
   r |= dalloc(h, &h->S, B * N); r |= dalloc(h, &h->Sinv, B * N);
@@ -648,6 +811,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->udvst.resize(h->Nstm);
   for (auto& s : h->udvst) r |= mk_udv(s);
   r |= dalloc(h, &h->TP, B * NN); r |= dalloc(h, &h->Qb, B * NN); r |= dalloc(h, &h->RHS, B * NN);
+  r |= dalloc(h, &h->QRw, B * NN); r |= dalloc(h, &h->qkeys, B * N);
   r |= dalloc(h, &h->Vtmp, B * NN);
   r |= dalloc(h, &h->tau, B * N); r |= dalloc(h, &h->jpvt, B * N); r |= dalloc(h, &h->perm, B * N);
   r |= dalloc(h, &h->iperm, B * N); r |= dalloc(h, &h->DUP, B * N); r |= dalloc(h, &h->vn, B * 2 * N);
@@ -743,8 +907,38 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
       seen[s] = 1;
     }
   }
+  // transition factors for every (vertex, old field, flip choice); type-1 fields flip sign
+  std::vector<UpdTab> tab(K * 15);
+  for (size_t k = 0; k < K; ++k) {
+    const int t = ty[k] - 1;
+    for (int so = -2; so <= 2; ++so)
+      for (int ch = 0; ch < 3; ++ch) {
+        const int sn = (t == 0) ? -so : h->ft.flip[so + 2][ch];
+        UpdTab& e = tab[(k * 5 + so + 2) * 3 + ch];
+        if (sn < -2 || sn > 2) { e.myexp = zmk(1.0, 0.0); e.dlt = zmk(0.0, 0.0); e.expal = zmk(1.0, 0.0); continue; }
+        const double dphi = h->ft.phi[t][sn + 2] - h->ft.phi[t][so + 2];
+        const std::complex<double> Z1(g[k].x * dphi, g[k].y * dphi);
+        const std::complex<double> me = std::exp(Z1 * E[k]);
+        const std::complex<double> ea = std::exp(Z1 * std::complex<double>(al[k].x, al[k].y));
+        e.myexp = zmk(me.real(), me.imag());
+        e.dlt = zmk(me.real() - 1.0, me.imag());
+        e.expal = zmk(ea.real(), ea.imag());
+      }
+  }
+  // vertices of each site, ascending, per flavour
+  std::vector<int> sptr((size_t)F * (N + 1), 0), slist(K);
+  for (int f = 0; f < F; ++f) {
+    int* ptr = &sptr[(size_t)f * (N + 1)];
+    for (int n = 0; n < M; ++n) ptr[site[(size_t)f * M + n] + 1]++;
+    for (int i = 0; i < N; ++i) ptr[i + 1] += ptr[i];
+    std::vector<int> fill(ptr, ptr + N);
+    for (int n = 0; n < M; ++n) slist[(size_t)f * M + fill[site[(size_t)f * M + n]]++] = n;
+  }
   int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->C : chain + 1;
   for (int c = c0; c < c1; ++c) {
+    CK(cudaMemcpy(h->v_tab + c * K * 15, tab.data(), K * 15 * sizeof(UpdTab), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_sptr + (size_t)c * F * (N + 1), sptr.data(), sptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_slist + (size_t)c * K, slist.data(), K * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_site + c * K, site.data(), K * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_g + c * K, g.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_alpha + c * K, al.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
@@ -976,6 +1170,7 @@ static int oneshot_handle(int N, alfgpu_s** out) {
   memset(&d, 0, sizeof(d));
   d.ndim = N; d.n_fl = 1; d.n_sun = 1; d.n_op = 1; d.ltrot = 1; d.nwrap = 1; d.n_chains = 1;
   d.precision = ALFGPU_PRECISION_FP64;
+  d.reserved[0] = ALFGPU_FLAG_EXACT_QRP;  // decompose_UDV_state / CGR default branch: ZGEQP3 pivoting
   return alfgpu_create(out, &d);
 }
 
@@ -997,8 +1192,7 @@ int alfgpu_cgr(int32_t ndim, int32_t nvar, const double* UR, const double* DR, c
     // det(U) of arbitrary inputs: pivoted QR of each U (det = det(Q) prod R_ii sign(P))
     for (int side = 0; side < 2; ++side) {
       UDVSet& s = side ? h->udvl : h->udvr;
-      RET(copy_mats(h, h->TP, s.U, NN));
-      RET(launch_qr(h, h->TP, nullptr, 1));
+      RET(qr_any(h, s.U, nullptr, h->QRw, 1));
       QRInfo inf;
       CK(cudaMemcpyAsync(&inf, h->info, sizeof(inf), cudaMemcpyDeviceToHost, h->st));
       CK(cudaStreamSynchronize(h->st));

@@ -102,5 +102,6 @@ ALF_HD double alf_uniform(uint64_t key, uint64_t counter) {
 struct FieldTables {
   double phi[2][5];   // [type-1][s+2]
   double gama[2][5];
+  double grat[2][5][5];  // [type-1][s_old+2][s_new+2] = gama(s_new) / gama(s_old)
   int8_t flip[5][3];  // type 2
 };

@@ -7,20 +7,22 @@
 //   S(i) = prod_{n: P(n)=i} E_exp(1, s(n,nt1)),  Sinv(i) = prod E_exp(1, -s(n,nt1)).
 // This is Op_mmultR / Op_Wrapup for diagonal operators (Operator_mod.F90:686-693,
 // 776-781) for every vertex of the slice at once.  grid (B), block 256.
-__global__ void k_slice_scale(const int8_t* fields, int L, int M, int N, int F, int nt1, const int* site,
-                              const zd* Eexp, zd* S, zd* Sinv) {
+// sptr/slist: per (chain, flavour) the vertices of each site in ascending order
+// (CSR, built at upload).
+__global__ void k_slice_scale(const int8_t* fields, int L, int M, int N, int F, int nt1, const int* sptr,
+                              const int* slist, const zd* Eexp, zd* S, zd* Sinv) {
   const int b = blockIdx.x, c = b / F, f = b % F;
   const int8_t* fl = fields + (long long)c * L * M + (long long)(nt1 - 1) * M;
-  const int* st = site + (long long)c * F * M + (long long)f * M;
+  const int* ptr = sptr + (long long)b * (N + 1);
+  const int* lst = slist + (long long)b * M;
   const zd* ee = Eexp + ((long long)c * F * M + (long long)f * M) * 5;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     zd s = zmk(1.0, 0.0), si = zmk(1.0, 0.0);
-    for (int n = 0; n < M; ++n) {
-      if (st[n] == i) {
-        int sp = fl[n];
-        s = zmul(s, ee[(long long)n * 5 + sp + 2]);
-        si = zmul(si, ee[(long long)n * 5 - sp + 2]);
-      }
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+      const int n = lst[e];
+      const int sp = fl[n];
+      s = zmul(s, ee[(long long)n * 5 + sp + 2]);
+      si = zmul(si, ee[(long long)n * 5 - sp + 2]);
     }
     S[(long long)b * N + i] = s;
     Sinv[(long long)b * N + i] = si;
@@ -79,34 +81,53 @@ __global__ void k_scale_col0(zd* U, int N, const zd* phase) {
 }
 
 // COMPARE_C (mymats_mod.F90:683-704) with the NaN test of Control_PrecisionG
-// (control_mod.F90:219-263).  grid (B), block 256; out[b] = {xmax, xmean}.
-__global__ void k_compare(const zd* A, const zd* Bm, int N, double* out, int* err) {
-  const int b = blockIdx.x;
+// (control_mod.F90:219-263).  grid (CMP_BLOCKS, B), block 256; out[b] = {xmax, xmean},
+// zeroed by the caller.  The maximum is taken over |d|^2 as an integer on the IEEE bit
+// pattern (non-negative doubles order like their bits) and rooted once; the mean adds
+// FP32 square roots per element (a diagnostic) in FP64 partial sums.  Per element this
+// costs five FP64-pipe instructions instead of a hypot.
+#define CMP_BLOCKS 32
+__global__ void __launch_bounds__(256) k_compare(const zd* A, const zd* Bm, int N, double* out, int* err) {
+  const int b = blockIdx.y;
   const long long NN = (long long)N * N;
   const zd* a = A + b * NN;
   const zd* c = Bm + b * NN;
-  double mx = 0.0, sm = 0.0;
+  unsigned long long mx = 0ull;
+  float sm = 0.f;
   int nan = 0;
-  for (long long e = threadIdx.x; e < NN; e += blockDim.x) {
-    zd x = a[e], y = c[e];
-    if (x.x != x.x || x.y != x.y || y.x != y.x || y.y != y.y) nan = 1;
-    double d = hypot(x.x - y.x, x.y - y.y);
-    mx = fmax(mx, d);
-    sm += d;
+  for (long long e = blockIdx.x * 256ll + threadIdx.x; e < NN; e += 256ll * CMP_BLOCKS) {
+    const zd x = a[e], y = c[e];
+    const unsigned long long bits[4] = {(unsigned long long)__double_as_longlong(x.x),
+                                        (unsigned long long)__double_as_longlong(x.y),
+                                        (unsigned long long)__double_as_longlong(y.x),
+                                        (unsigned long long)__double_as_longlong(y.y)};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) nan |= (bits[t] & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+    const double dx = x.x - y.x, dy = x.y - y.y;
+    const double d2 = fma(dx, dx, dy * dy);
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d2);
+    mx = u > mx ? u : mx;
+    sm += sqrtf(__double2float_rn(d2));
   }
-  __shared__ double rm[8], rs[8];
+  __shared__ unsigned long long rm[8];
+  __shared__ float rs[8];
   __shared__ int rn[8];
-  mx = warp_max(mx);
-  sm = warp_sum(sm);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long om = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = om > mx ? om : mx;
+    sm += __shfl_xor_sync(0xffffffffu, sm, o);
+  }
   nan = __any_sync(0xffffffffu, nan);
   if ((threadIdx.x & 31) == 0) { rm[threadIdx.x >> 5] = mx; rs[threadIdx.x >> 5] = sm; rn[threadIdx.x >> 5] = nan; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double m = 0.0, s = 0.0;
+    unsigned long long m = 0ull;
+    double s = 0.0;
     int nn = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { m = fmax(m, rm[w]); s += rs[w]; nn |= rn[w]; }
-    out[2 * b] = m;
-    out[2 * b + 1] = s / (double)NN;
+    for (int w = 0; w < 8; ++w) { m = rm[w] > m ? rm[w] : m; s += (double)rs[w]; nn |= rn[w]; }
+    if (m > 0x7ff0000000000000ull) nn = 1;
+    atomicMax(reinterpret_cast<unsigned long long*>(out + 2 * b), m);  // |d|^2 bits; rooted by k_stab_finish
+    atomicAdd(out + 2 * b + 1, s / (double)NN);
     if (nn) atomicOr(err, 1);
   }
 }
@@ -168,7 +189,7 @@ __global__ void k_stab_finish(StabFinishParams p) {
     ph = zmul(ph, zmk(co, s));
     Z = zmul(Z, ph);
     if (p.compare) {
-      double xmax = p.cmp[2 * b], xmean = p.cmp[2 * b + 1];
+      double xmax = sqrt(p.cmp[2 * b]), xmean = p.cmp[2 * b + 1];  // k_compare leaves max |d|^2
       st[0] += 1.0;
       if (xmax > 10.0) atomicOr(p.err, 2);
       if (xmax > st[2]) st[2] = xmax;

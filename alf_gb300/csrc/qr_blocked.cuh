@@ -1,0 +1,593 @@
+// Blocked Householder QR with norm pre-pivoting, and the explicit Q.
+//
+// Pivoting follows ALF's STABLOG branch of decompose_UDV_state
+// (Prog/udv_state_mod.F90:503-542): the columns are ordered once by their
+// norms (log|A(:,j)| + log(scale_j)), then factored without pivoting
+// (QDRP_decompose with IPVT = 1).  Each Householder step is ZLARFG (beta,
+// tau, 1/(alpha-beta)) and the left application of H^H = I - conj(tau) v v^H
+// (LAPACK ZGEQR2 as vendored in Libraries/libqrref), followed by QDRP's
+// D = |R_ii| and row normalisation (Prog/QDRP_decompose_mod.F90:85-100).
+//
+// GB300 layout of the work: FP64 DMMA and DFMA run at the same ~1 TFLOP/s,
+// so a GEMM-shaped trailing update buys nothing over applying the panel's
+// reflectors column by column; what matters is that the trailing work is
+// spread over all SMs and that the sequential chain per column is short.
+//   k_bqr_keys     column keys (one warp per column, all SMs)
+//   k_bqr_permute  rank sort of the keys, permuted + scaled copy, jpvt, sign
+//   k_bqr_panel    one panel of nb <= 32 columns on a thread-block cluster:
+//                  rows dealt in contiguous chunks to the CTAs, ONE
+//                  distributed-shared-memory exchange per column carries the
+//                  norm, all dot products v^H a_j of the panel and the pivot row
+//   k_bqr_apply    the panel's reflectors applied to every later column, one
+//                  warp per column, all SMs (also used for Q, in reverse)
+//   k_bqr_finish   D, row normalisation, det(Q) and prod R_ii/|R_ii|
+#pragma once
+#include "common.cuh"
+#include "linalg.cuh"
+
+#define BQR_NB 32
+#define BQR_ROWS 32   // max rows of a panel per CTA (N <= 32 * cluster size)
+#define BQR_LROWS 16  // max rows per lane in k_bqr_apply (N <= 512)
+
+// 1/d for real d != 0: float seed and two Newton-Raphson steps (an FP64 division
+// costs ~560 dependent cycles on GB300); falls back to division outside float range.
+ALF_DEV double bqr_rcp(double d) {
+  const double a = fabs(d);
+  if (!(a > 1e-30 && a < 1e30)) return 1.0 / d;
+  double r = (double)__frcp_rn(__double2float_rn(d));
+  r = fma(r, fma(-d, r, 1.0), r);
+  return fma(r, fma(-d, r, 1.0), r);
+}
+ALF_DEV zd bqr_zrcp(zd a) {
+  const double s = bqr_rcp(a.x * a.x + a.y * a.y);
+  return zmk(a.x * s, -a.y * s);
+}
+
+// keys[b][j] = log ||A(:,j)|| + log |scale_j|  (-inf for a zero column)
+__global__ void __launch_bounds__(256) k_bqr_keys(const zd* A, long long lda, long long sA, int N,
+                                                  const double* scale, long long sS, double* keys) {
+  const int b = blockIdx.y, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (c >= N) return;
+  const zd* col = A + b * sA + (long long)c * lda;
+  double s = 0.0;
+  for (int r = lane; r < N; r += 32) s = fma(col[r].x, col[r].x, fma(col[r].y, col[r].y, s));
+  s = warp_sum(s);
+  if (lane == 0) {
+    double k = (s > 0.0) ? 0.5 * log(s) : -INFINITY;
+    if (scale) k += log(fabs(scale[b * sS + c]));
+    keys[(long long)b * N + c] = k;
+  }
+}
+
+// Rank sort (descending key, ties by index), Out(:, i) = A(:, jpvt_i - 1) * scale,
+// jpvt 1-based like LAPACK; block x == 0 also writes jpvt and the permutation sign.
+// grid (ceil(N/8), B), 256 threads; dynamic smem: N doubles + N ints.
+__global__ void __launch_bounds__(256) k_bqr_permute(const zd* A, long long lda, long long sA, int N,
+                                                     const double* scale, long long sS, const double* keys,
+                                                     zd* Out, long long sO, int* jpvt, long long sP, QRInfo* info) {
+  const int b = blockIdx.y, tid = threadIdx.x;
+  extern __shared__ double kbuf[];
+  int* src = reinterpret_cast<int*>(kbuf + N);  // src[rank] = original column
+  __shared__ int inv_cnt;
+  for (int j = tid; j < N; j += 256) {
+    double v = keys[(long long)b * N + j];
+    kbuf[j] = (v != v) ? -INFINITY : v;  // NaN keys sort last
+  }
+  if (tid == 0) inv_cnt = 0;
+  __syncthreads();
+  for (int j = tid; j < N; j += 256) {
+    const double kj = kbuf[j];
+    int r = 0;
+    for (int i = 0; i < N; ++i) {
+      const double ki = kbuf[i];
+      r += (ki > kj) || (ki == kj && i < j);
+    }
+    src[r] = j;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    int cnt = 0;  // inversions of src, for the sign
+    for (int j = tid; j < N; j += 256) {
+      const int sj = src[j];
+      for (int i = 0; i < j; ++i) cnt += src[i] > sj;
+      jpvt[b * sP + j] = sj + 1;
+    }
+    atomicAdd(&inv_cnt, cnt & 1);
+    __syncthreads();
+    if (tid == 0) info[b].psign = (inv_cnt & 1) ? -1 : 1;
+  }
+  const int lane = tid & 31;
+  const int i = blockIdx.x * 8 + (tid >> 5);
+  if (i >= N) return;
+  const int s = src[i];
+  const double sc = scale ? scale[b * sS + s] : 1.0;
+  const zd* in = A + b * sA + (long long)s * lda;
+  zd* out = Out + b * sO + (long long)i * lda;
+  for (int r = lane; r < N; r += 32) out[r] = scale ? zscale(in[r], sc) : in[r];
+}
+
+struct BQRPanel {
+  zd* A; long long lda, sA;  // factored in place
+  int N, j0, nb;
+  zd* tau; long long sT;
+  double* D; long long sD;   // |R(kc,kc)| of the panel's columns
+};
+
+// One panel, columns [j0, j0+nb), rows [j0, N), on a cluster of CL CTAs of 256 threads.
+// Thread (j = tid % 32, g = tid / 32) handles panel column j on the CTA's rows g, g+8, ...
+__global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
+  const unsigned rank = cluster_ctarank(), CL = cluster_nctarank();
+  const int b = blockIdx.y, N = p.N, j0 = p.j0, nb = p.nb;
+  const int tid = threadIdx.x, j = tid & 31, g = tid >> 5;
+  const int mp = N - j0;
+  const int rpc = (mp + (int)CL - 1) / (int)CL;
+  const int r0 = j0 + (int)rank * rpc;
+  const int nr = max(0, min(N, r0 + rpc) - r0);
+  zd* A = p.A + b * p.sA;
+  const long long lda = p.lda;
+  __shared__ zd P[BQR_ROWS][BQR_NB + 1];
+  __shared__ zd red[8][BQR_NB];
+  __shared__ zd xs[2][BQR_NB];  // this CTA's column partial sums (read remotely)
+  __shared__ zd xr[2][BQR_NB];  // the pivot row, published by its owner
+  __shared__ zd tot[BQR_NB], prow[BQR_NB];
+  for (int il = g; il < nr; il += 8)
+    if (j < nb) P[il][j] = A[(r0 + il) + (long long)(j0 + j) * lda];
+  __syncthreads();
+
+  for (int k = 0; k < nb; ++k) {
+    const int kc = j0 + k, par = k & 1;
+    const unsigned owner = (unsigned)(k / rpc);
+    // partials over own rows i > kc: column k -> sum |a_ik|^2, column j > k -> sum conj(a_ik) a_ij
+    zd acc = zmk(0.0, 0.0);
+    if (j >= k && j < nb)
+      for (int il = g; il < nr; il += 8)
+        if (r0 + il > kc) acc = zadd(acc, zmul(zconj(P[il][k]), P[il][j]));
+    red[g][j] = acc;
+    if (rank == owner && j < nb && g == 0) xr[par][j] = P[kc - r0][j];
+    __syncthreads();
+    if (g == 0) {
+      const zd s = zadd(zadd(zadd(red[0][j], red[1][j]), zadd(red[2][j], red[3][j])),
+                        zadd(zadd(red[4][j], red[5][j]), zadd(red[6][j], red[7][j])));
+      xs[par][j] = s;
+    }
+    cluster_sync();
+    if (g == 0 && j >= k && j < nb) {
+      zd s0 = zmk(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+      for (unsigned q = 0; q < CL; q += 4) {
+        const unsigned a0 = dsmem_addr(&xs[par][j], q);
+        s0 = zadd(s0, zmk(dsmem_ld_f64(a0), dsmem_ld_f64(a0 + 8)));
+        if (q + 1 < CL) { const unsigned a = dsmem_addr(&xs[par][j], q + 1); s1 = zadd(s1, zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8))); }
+        if (q + 2 < CL) { const unsigned a = dsmem_addr(&xs[par][j], q + 2); s2 = zadd(s2, zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8))); }
+        if (q + 3 < CL) { const unsigned a = dsmem_addr(&xs[par][j], q + 3); s3 = zadd(s3, zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8))); }
+      }
+      tot[j] = zadd(zadd(s0, s1), zadd(s2, s3));
+      const unsigned ar = dsmem_addr(&xr[par][j], owner);
+      prow[j] = zmk(dsmem_ld_f64(ar), dsmem_ld_f64(ar + 8));
+    }
+    __syncthreads();
+    // ZLARFG on (alpha, x), x = A(kc+1:N, kc)
+    const zd alpha = prow[k];
+    const double xn2 = tot[k].x;
+    const bool trivial = (xn2 == 0.0 && alpha.y == 0.0);
+    double beta = alpha.x;
+    zd t = zmk(0.0, 0.0), scal = zmk(0.0, 0.0);
+    if (!trivial) {
+      beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn2))), alpha.x);
+      const double ib = bqr_rcp(beta);
+      t = zmk((beta - alpha.x) * ib, -alpha.y * ib);
+      scal = bqr_zrcp(zmk(alpha.x - beta, alpha.y));
+    }
+    // H^H applied to the panel's later columns: a_j -= conj(tau) v (v^H a_j),
+    // v^H a_j = a_kc,j + conj(scal) sum_{i>kc} conj(a_ik) a_ij
+    // v_i = scal a_ik for the warp's rows, read before any lane overwrites column k
+    zd vi[BQR_ROWS / 8];
+#pragma unroll
+    for (int q = 0; q < BQR_ROWS / 8; ++q) {
+      const int il = g + 8 * q;
+      vi[q] = (il < nr) ? zmul(scal, P[il][k]) : zmk(0.0, 0.0);
+    }
+    __syncwarp();
+    if (!trivial && j >= k && j < nb) {
+      const zd f = (j > k) ? zmul(zconj(t), zadd(prow[j], zmul(zconj(scal), tot[j]))) : zmk(0.0, 0.0);
+#pragma unroll
+      for (int q = 0; q < BQR_ROWS / 8; ++q) {
+        const int il = g + 8 * q;
+        if (il >= nr) continue;
+        const int i = r0 + il;
+        if (i > kc) {
+          if (j == k) P[il][k] = vi[q];
+          else P[il][j] = zsub(P[il][j], zmul(vi[q], f));
+        } else if (i == kc) {
+          if (j == k) P[il][k] = zmk(beta, 0.0);
+          else P[il][j] = zsub(P[il][j], f);
+        }
+      }
+    }
+    if (rank == owner && tid == 0) {
+      p.tau[b * p.sT + kc] = t;
+      p.D[b * p.sD + kc] = trivial ? zabs(alpha) : fabs(beta);
+    }
+    __syncthreads();
+  }
+  for (int il = g; il < nr; il += 8)
+    if (j < nb) A[(r0 + il) + (long long)(j0 + j) * lda] = P[il][j];
+  cluster_sync();  // no CTA leaves while its shared memory may still be read
+}
+
+struct BQRApply {
+  const zd* V; long long ldv, sV;  // reflectors: column kc holds v below row kc (v_kc = 1 implicit)
+  const zd* tau; long long sT;
+  zd* C; long long ldc, sC;        // columns c0 .. N-1 are updated, rows j0 .. N-1
+  int N, j0, nb, c0;
+  int conj_tau;  // 1: QR trailing update, H^H in order k = 0..nb-1
+                 // 0: explicit Q, H in reverse order; columns [j0, j0+nb) start as e_c
+};
+
+// One column per CTA of 4 warps (one per SMSP: on GB300 a warp issues at most one
+// FP64 instruction every ~64 cycles); grid (N - c0, B), 128 threads.  Warp w holds the
+// 32-row blocks w, w+4, ... of rows j0..N-1 (lane l: row j0 + l + 32 (w + 4 q)); row
+// blocks above the reflector are skipped warp-uniformly; the four warp partials of
+// v^H x meet in shared memory (double-buffered: one barrier per reflector); the next
+// reflector is prefetched.
+#define BQR_QW (BQR_LROWS / 4)
+__global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
+  const int b = blockIdx.y, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c = p.c0 + blockIdx.x;
+  if (c >= p.N) return;
+  const int N = p.N, j0 = p.j0, nb = p.nb;
+  const int nblk = (N - j0 + 31) >> 5;  // 32-row blocks
+  const zd* V = p.V + b * p.sV;
+  const zd* tau = p.tau + b * p.sT;
+  zd* col = p.C + b * p.sC + (long long)c * p.ldc;
+  const bool fresh = !p.conj_tau && c < j0 + nb;
+  __shared__ zd red[2][4];
+  zd x[BQR_QW], vn[BQR_QW];
+#pragma unroll
+  for (int q = 0; q < BQR_QW; ++q) {
+    const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
+    x[q] = zmk(0.0, 0.0);
+    vn[q] = zmk(0.0, 0.0);
+    if (blk < nblk && r < N) x[q] = fresh ? zmk(r == c ? 1.0 : 0.0, 0.0) : col[r];
+  }
+  auto load_v = [&](int k) {
+    const int kc = j0 + k, blo = (kc - j0) >> 5;
+    const zd* v = V + (long long)kc * p.ldv;
+#pragma unroll
+    for (int q = 0; q < BQR_QW; ++q) {
+      const int blk = w + 4 * q;
+      if (blk < blo || blk >= nblk) continue;
+      const int r = j0 + lane + 32 * blk;
+      vn[q] = (r < kc || r >= N) ? zmk(0.0, 0.0) : (r == kc ? zmk(1.0, 0.0) : v[r]);
+    }
+  };
+  load_v(p.conj_tau ? 0 : nb - 1);
+  int par = 0;  // parity of the reduction buffer: flips once per barrier
+  for (int kk = 0; kk < nb; ++kk) {
+    const int k = p.conj_tau ? kk : nb - 1 - kk;
+    const int kc = j0 + k, blo = (kc - j0) >> 5;
+    zd vr[BQR_QW];
+#pragma unroll
+    for (int q = 0; q < BQR_QW; ++q) vr[q] = vn[q];
+    if (kk + 1 < nb) load_v(p.conj_tau ? kk + 1 : nb - 2 - kk);
+    zd t = tau[kc];
+    if (t.x == 0.0 && t.y == 0.0) continue;  // uniform over the block
+    if (p.conj_tau) t.y = -t.y;
+    zd s = zmk(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < BQR_QW; ++q) {
+      const int blk = w + 4 * q;
+      if (blk < blo || blk >= nblk) continue;
+      s = zadd(s, zmul(zconj(vr[q]), x[q]));
+    }
+    s = warp_zsum(s);
+    if (lane == 0) red[par][w] = s;
+    __syncthreads();
+    const zd f = zmul(t, zadd(zadd(red[par][0], red[par][1]), zadd(red[par][2], red[par][3])));
+    par ^= 1;
+#pragma unroll
+    for (int q = 0; q < BQR_QW; ++q) {
+      const int blk = w + 4 * q;
+      if (blk < blo || blk >= nblk) continue;
+      x[q] = zsub(x[q], zmul(vr[q], f));
+    }
+  }
+  if (fresh)
+    for (int r = threadIdx.x; r < j0; r += 128) col[r] = zmk(0.0, 0.0);
+#pragma unroll
+  for (int q = 0; q < BQR_QW; ++q) {
+    const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
+    if (blk < nblk && r < N) col[r] = x[q];
+  }
+}
+
+// R(i, j) /= D(i) for j >= i (QDRP row normalisation); block x == 0 also forms
+// det(Q) = prod det(H_i) (unit-modulus factors) and prod R_ii / D_i, then
+// normalises the diagonal (the other blocks touch only the strict upper part).
+// grid (ceil(N/8), B), 256 threads; dynamic smem: N doubles.
+__global__ void __launch_bounds__(256) k_bqr_finish(zd* A, long long lda, long long sA, int N, const zd* tau,
+                                                    long long sT, const double* D, long long sD, QRInfo* info) {
+  const int b = blockIdx.y, tid = threadIdx.x, lane = tid & 31;
+  zd* M = A + b * sA;
+  const double* Db = D + b * sD;
+  extern __shared__ double invD[];
+  for (int i = tid; i < N; i += 256) invD[i] = bqr_rcp(Db[i]);
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    __shared__ zd pq[256], pr[256];
+    zd q = zmk(1.0, 0.0), r = zmk(1.0, 0.0);
+    for (int i = tid; i < N; i += 256) {
+      const zd z = tau[b * sT + i];
+      if (z.x != 0.0 || z.y != 0.0) {
+        const double iX = 1.0 / zabs(z);
+        const zd h = zsub(zmk(1.0, 0.0), zscale(zscale(z, iX), 2.0 * z.x * iX));
+        q = zmul(q, zscale(h, 1.0 / zabs(h)));
+      }
+      r = zmul(r, zscale(M[i + (long long)i * lda], invD[i]));
+    }
+    pq[tid] = q; pr[tid] = r;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+      if (tid < s) { pq[tid] = zmul(pq[tid], pq[tid + s]); pr[tid] = zmul(pr[tid], pr[tid + s]); }
+      __syncthreads();
+    }
+    if (tid == 0) { info[b].detQ = pq[0]; info[b].prodR = pr[0]; }
+    for (int i = tid; i < N; i += 256) M[i + (long long)i * lda] = zscale(M[i + (long long)i * lda], invD[i]);
+  }
+  const int c = blockIdx.x * 8 + (tid >> 5);
+  if (c >= N) return;
+  zd* col = M + (long long)c * lda;
+  for (int r = lane; r < c; r += 32) col[r] = zscale(col[r], invD[r]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Exact ZGEQP3 (ZLAQP2: dynamic column pivoting with norm downdates,
+// Prog/QDRP_decompose_mod.F90:60-101) on one thread-block cluster per matrix.
+// Rows are dealt cyclically to the CL CTAs (row i -> CTA i % CL, local row i / CL)
+// and kept in shared memory.  Per step j one distributed-shared-memory exchange
+// carries, for every column c >= j, the CTA's partial sum_{i>j} conj(a_ij) a_ic
+// (c == j: sum |a_ij|^2) and the pivot row; every CTA then holds the same totals,
+// applies the reflector to its rows, and downdates its own copy of the column
+// norms (identical in all CTAs: same inputs, same summation order), so the pivot
+// search needs no exchange.  A column whose downdate loses accuracy (ZLAQP2's
+// tol3z test) gets its norm recomputed through one more exchange.
+// Outputs as k_qrp before normalisation: R above, reflectors below, tau, jpvt,
+// D = |R_jj|, info.psign; k_bqr_finish then normalises and forms the products.
+struct QRRowsParams {
+  const zd* Ain;             // input (may equal A)
+  zd* A; long long lda, sA;  // output
+  int N;
+  const double* colscale; long long sCS;
+  zd* tau; long long sT;
+  int* jpvt; long long sP;
+  double* D; long long sD;
+  QRInfo* info;
+};
+
+static inline size_t qrr_smem_bytes(int N, int CL) {
+  const size_t nrl = (size_t)((N + CL - 1) / CL);
+  return nrl * N * sizeof(zd) + 6ull * N * sizeof(zd) + 2ull * N * sizeof(double) + (size_t)N * sizeof(int) +
+         nrl * sizeof(zd) + 64;
+}
+
+ALF_DEV void qrr_argmax(double& v, int& i) {  // warp argmax, first index on ties
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
+  const unsigned rank = cluster_ctarank(), CL = cluster_nctarank();
+  const int b = blockIdx.y, N = p.N, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nrl = (N + (int)CL - 1) / (int)CL;
+  const int nmine = (N - (int)rank + (int)CL - 1) / (int)CL;  // rows rank, rank+CL, ...
+  extern __shared__ __align__(16) unsigned char qrr_raw[];
+  zd* Ar = reinterpret_cast<zd*>(qrr_raw);  // [nrl][N] row-major: Ar[il*N + c] = A(rank + il*CL, c)
+  zd* xs = Ar + (size_t)nrl * N;           // [2][N] partial sums (read remotely)
+  zd* xr = xs + 2 * N;                     // [2][N] pivot row (owner)
+  zd* tot = xr + 2 * N;                    // [N]
+  zd* prow = tot + N;                      // [N]
+  double* vn1 = reinterpret_cast<double*>(prow + N);
+  double* vn2 = vn1 + N;
+  zd* vsh = reinterpret_cast<zd*>(vn2 + N);  // [nrl]
+  int* jp = reinterpret_cast<int*>(vsh + nrl);
+  __shared__ double s_bv[8];
+  __shared__ int s_bi[8], s_pv, s_cnt;
+  const double tol3z = 1.0536712127723509e-08;  // sqrt(dlamch('Epsilon'))
+  zd* A = p.A + b * p.sA;
+  const long long lda = p.lda;
+
+  for (long long e = tid; e < (long long)nmine * N; e += 256) {
+    const int il = (int)(e / N), c = (int)(e % N);
+    zd v = p.Ain[b * p.sA + (rank + (long long)il * CL) + c * lda];
+    if (p.colscale) v = zscale(v, p.colscale[b * p.sCS + c]);
+    Ar[(size_t)il * N + c] = v;
+  }
+  __syncthreads();
+  // initial column norms: exchange 0
+  for (int c = tid; c < N; c += 256) {
+    double s0 = 0.0, s1 = 0.0;
+    int il = 0;
+    for (; il + 1 < nmine; il += 2) {
+      const zd a = Ar[(size_t)il * N + c], d = Ar[(size_t)(il + 1) * N + c];
+      s0 = fma(a.x, a.x, fma(a.y, a.y, s0));
+      s1 = fma(d.x, d.x, fma(d.y, d.y, s1));
+    }
+    if (il < nmine) { const zd a = Ar[(size_t)il * N + c]; s0 = fma(a.x, a.x, fma(a.y, a.y, s0)); }
+    xs[c] = zmk(s0 + s1, 0.0);
+    jp[c] = c + 1;
+  }
+  cluster_sync();
+  for (int c = tid; c < N; c += 256) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (q < (int)CL) s[q & 3] += dsmem_ld_f64(dsmem_addr(&xs[c], q));
+    const double nrm = sqrt((s[0] + s[1]) + (s[2] + s[3]));
+    vn1[c] = nrm; vn2[c] = nrm;
+  }
+  int par = 1;
+  __syncthreads();
+
+  for (int j = 0; j < N; ++j) {
+    // pivot: first maximum of vn1[j..N)
+    double bv = -1.0;
+    int bi = N;
+    for (int c = j + tid; c < N; c += 256) {
+      const double v = vn1[c];
+      if (v > bv) { bv = v; bi = c; }
+    }
+    qrr_argmax(bv, bi);
+    if (lane == 0) { s_bv[warp] = bv; s_bi[warp] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double v = s_bv[0];
+      int i = s_bi[0];
+      for (int w = 1; w < 8; ++w)
+        if (s_bv[w] > v || (s_bv[w] == v && s_bi[w] < i)) { v = s_bv[w]; i = s_bi[w]; }
+      s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
+    }
+    __syncthreads();
+    const int pv = s_pv;
+    if (pv != j) {
+      for (int il = tid; il < nmine; il += 256) {
+        const zd t = Ar[(size_t)il * N + pv];
+        Ar[(size_t)il * N + pv] = Ar[(size_t)il * N + j];
+        Ar[(size_t)il * N + j] = t;
+      }
+      if (tid == 0) {
+        const int t = jp[pv]; jp[pv] = jp[j]; jp[j] = t;
+        vn1[pv] = vn1[j]; vn2[pv] = vn2[j];
+      }
+      __syncthreads();
+    }
+    // partials over own rows i > j; the owner of row j publishes it
+    const unsigned owner = (unsigned)(j % (int)CL);
+    const int ilj = j / (int)CL;
+    const int il0 = (j >= (int)rank) ? (j - (int)rank) / (int)CL + 1 : 0;  // first own row > j
+    zd* xsp = xs + par * N;
+    zd* xrp = xr + par * N;
+    for (int c = j + tid; c < N; c += 256) {
+      zd s0 = zmk(0.0, 0.0), s1 = s0;
+      int il = il0;
+      for (; il + 1 < nmine; il += 2) {
+        s0 = zadd(s0, zmul(zconj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]));
+        s1 = zadd(s1, zmul(zconj(Ar[(size_t)(il + 1) * N + j]), Ar[(size_t)(il + 1) * N + c]));
+      }
+      if (il < nmine) s0 = zadd(s0, zmul(zconj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]));
+      xsp[c] = zadd(s0, s1);
+      if (rank == owner) xrp[c] = Ar[(size_t)ilj * N + c];
+    }
+    cluster_sync();
+    for (int c = j + tid; c < N; c += 256) {
+      zd s[4] = {zmk(0.0, 0.0), zmk(0.0, 0.0), zmk(0.0, 0.0), zmk(0.0, 0.0)};
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (q < (int)CL) {
+          const uint32_t a = dsmem_addr(&xsp[c], q);
+          s[q & 3] = zadd(s[q & 3], zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8)));
+        }
+      tot[c] = zadd(zadd(s[0], s[1]), zadd(s[2], s[3]));
+      const uint32_t a = dsmem_addr(&xrp[c], owner);
+      prow[c] = zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8));
+    }
+    par ^= 1;
+    __syncthreads();
+    // ZLARFG on (alpha, x), x = A(j+1:N, j)
+    const zd alpha = prow[j];
+    const double xn2 = tot[j].x;
+    const bool trivial = (xn2 == 0.0 && alpha.y == 0.0);
+    double beta = alpha.x;
+    zd t = zmk(0.0, 0.0), scal = zmk(0.0, 0.0);
+    if (!trivial) {
+      beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn2))), alpha.x);
+      const double ib = bqr_rcp(beta);
+      t = zmk((beta - alpha.x) * ib, -alpha.y * ib);
+      scal = bqr_zrcp(zmk(alpha.x - beta, alpha.y));
+    }
+    for (int il = il0 + tid; il < nmine; il += 256) vsh[il] = zmul(scal, Ar[(size_t)il * N + j]);
+    __syncthreads();
+    // H^H on columns c > j (a_c -= conj(tau) v (v^H a_c)), reflector into column j,
+    // and the norm downdate with the updated pivot-row entry
+    int need = 0;
+    for (int c = j + tid; c < N; c += 256) {
+      if (c == j) {
+        if (!trivial) {
+          for (int il = il0; il < nmine; ++il) Ar[(size_t)il * N + j] = vsh[il];
+          if (rank == owner) Ar[(size_t)ilj * N + j] = zmk(beta, 0.0);
+        }
+        continue;
+      }
+      zd anew = prow[c];
+      if (!trivial) {
+        const zd f = zmul(zconj(t), zadd(prow[c], zmul(zconj(scal), tot[c])));
+        for (int il = il0; il < nmine; ++il)
+          Ar[(size_t)il * N + c] = zsub(Ar[(size_t)il * N + c], zmul(vsh[il], f));
+        anew = zsub(anew, f);
+        if (rank == owner) Ar[(size_t)ilj * N + c] = anew;
+      }
+      const double v1 = vn1[c];
+      if (v1 != 0.0) {
+        const double r = zabs(anew) * bqr_rcp(v1);
+        const double temp = fmax(1.0 - r * r, 0.0);
+        const double q = v1 * bqr_rcp(vn2[c]);
+        const double temp2 = temp * q * q;
+        if (temp2 <= tol3z) {
+          if (j < N - 1) { need = 1; vn1[c] = -1.0; }  // recomputed below
+          else { vn1[c] = 0.0; vn2[c] = 0.0; }
+        } else {
+          vn1[c] = v1 * sqrt(temp);
+        }
+      }
+    }
+    if (rank == owner && tid == 0) {
+      p.tau[b * p.sT + j] = t;
+      p.D[b * p.sD + j] = trivial ? zabs(alpha) : fabs(beta);
+    }
+    if (__syncthreads_or(need)) {
+      // exact norms of the flagged columns over rows > j (post-update)
+      zd* xq = xs + par * N;
+      for (int c = j + 1 + tid; c < N; c += 256) {
+        double s0 = 0.0;
+        if (vn1[c] < 0.0)
+          for (int il = il0; il < nmine; ++il) {
+            const zd a = Ar[(size_t)il * N + c];
+            s0 = fma(a.x, a.x, fma(a.y, a.y, s0));
+          }
+        xq[c] = zmk(s0, 0.0);
+      }
+      cluster_sync();
+      for (int c = j + 1 + tid; c < N; c += 256) {
+        if (vn1[c] >= 0.0) continue;
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (q < (int)CL) s[q & 3] += dsmem_ld_f64(dsmem_addr(&xq[c], q));
+        const double nrm = sqrt((s[0] + s[1]) + (s[2] + s[3]));
+        vn1[c] = nrm; vn2[c] = nrm;
+      }
+      par ^= 1;
+      __syncthreads();
+    }
+  }
+  for (long long e = tid; e < (long long)nmine * N; e += 256) {
+    const int il = (int)(e / N), c = (int)(e % N);
+    A[(rank + (long long)il * CL) + c * lda] = Ar[(size_t)il * N + c];
+  }
+  if (rank == 0) {
+    if (tid == 0) s_cnt = 0;
+    __syncthreads();
+    int cnt = 0;
+    for (int c = tid; c < N; c += 256) {
+      const int sc = jp[c];
+      for (int i = 0; i < c; ++i) cnt += jp[i] > sc;
+      p.jpvt[b * p.sP + c] = sc;
+    }
+    atomicAdd(&s_cnt, cnt & 1);
+    __syncthreads();
+    if (tid == 0) p.info[b].psign = (s_cnt & 1) ? -1 : 1;
+  }
+  cluster_sync();  // no CTA leaves while its shared memory may still be read
+}

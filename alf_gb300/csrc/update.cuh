@@ -17,26 +17,30 @@
 // on the full matrix is the Woodbury form of the same updates,
 //   G = G0 - G0(:,S) Delta_S Gamma^-1 (E_S - G0(S,:)),
 //   Gamma = 1 + (1 - G0(S,S)) Delta_S   (S = accepted sites, in accept order),
-// applied by one rank-m GEMM flush; Gamma^-1 is formed by k_flush_w.
+// applied by one rank-m GEMM flush; W = Delta_S Gamma^-1 is formed at block
+// end by the same kernel.
 //
-// T is the storage type of G (double2: complex128, used by both precision
-// forms).  Ratios, phases and the Metropolis test are always FP64.
+// G is complex128 in both precision forms.  The sequential chain (ratios,
+// Metropolis test, phase), the Ghat rank-1 updates and Gamma^-1 run in FP64
+// (plain form) or double-float (mixed form, dfloat.cuh, ~2^-46 relative
+// rounding).  GB300's FP64 dependent latency (63-76 cycles, ~560 for a
+// division) sets the cost of every visit, so the chain avoids divisions and
+// square roots: the Metropolis test is division-free, the reciprocal is a
+// Newton iteration, and the phase stays unnormalised until the block ends.
 #pragma once
 #include "common.cuh"
+#include "dfloat.cuh"
 
 #define UPD_KMAX 32
-#define UPD_THREADS 128
+#define UPD_THREADS 256
 
 struct VertexDev {
   // per chain: K = F*M entries, index k = nf*M + n
   const int* site;       // P(1), 0-based
-  const zd* g;
-  const zd* alpha;
-  const double* E;       // E(1)
   const int8_t* type;    // 1 or 2
-  const zd* Eexp;        // [k][5] = E_exp(1, s) at s+2
   long long sK;          // per-chain stride in entries (F*M)
 };
+struct UpdTab;
 
 struct UpdParams {
   int N, F, M, L, NSUN;
@@ -44,28 +48,23 @@ struct UpdParams {
   int dir;        // 0: up pass (n = pos), 1: down pass (n = M-1-pos)
   int q0, nq;     // visit positions q0 .. q0+nq-1 of this slice
   int visit_base; // visit index (within the sweep) of position 0 of this slice
-  void* G; long long sG;  // [chain][F][N][N] of T
+  int nChains;
+  const void* G; long long sG;  // [chain][F][N][N] complex128
   VertexDev V;
+  const UpdTab* tab;    // [chain][F*M][5][3]
   int8_t* fields;       // [chain][L][M]
   const double* draws; long long sDraws;  // [chain][6*M*L] or null
   const unsigned long long* rngkey;      // [chain]
   const unsigned long long* rngctr;      // [chain] counter of draw 0 of this sweep
   zd* phase;            // [chain]
-  int* m_out;           // [chain]
+  int* m_out;           // [chain], then [chain][F] (per-GEMM-batch rank)
+  zd* W;                // [chain][2][UPD_KMAX][UPD_KMAX]  Delta_S Gamma^-1
   int* sites_out;       // [chain][UPD_KMAX]  accepted sites, accept order
   zd* delta_out;        // [chain][2][UPD_KMAX] Delta of accepted sites
   long long* cnt;       // [chain][4] n_prop, n_acc, n_prop_eff, n_acc_eff
   int8_t* rec_acc; zd* rec_ratio; long long sRec;
   FieldTables ft;
 };
-
-template <typename T> struct CT;
-template <> struct CT<double2> {
-  static ALF_DEV double2 mk(zd a) { return a; }
-  static ALF_DEV zd wide(double2 a) { return a; }
-};
-template <typename T> ALF_DEV T tmul(T a, T b) { T r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
-template <typename T> ALF_DEV T tadd(T a, T b) { T r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 
 ALF_DEV int nranf3(double r) {
   // nint(r*3 + 0.5) clamped to [1,3] (random_wrap_mod.F90:159-168); no contraction.
@@ -74,37 +73,134 @@ ALF_DEV int nranf3(double r) {
   return v < 1 ? 1 : (v > 3 ? 3 : v);
 }
 
-// One CTA per chain.  Dynamic shared memory: Ghat[F][UPD_KMAX][UPD_KMAX+1] of T.
-template <typename T>
-__global__ void __launch_bounds__(UPD_THREADS) k_update_block(UpdParams p) {
-  const int c = blockIdx.x;
+// Per-visit transition data, precomputed per (vertex k, old field s, flip choice):
+//   myexp = exp(Z E), dlt = myexp - 1, expal = exp(Z alpha),  Z = g (phi(s_new) - phi(s_old))
+// (Upgrade2's Mat(1,1) = myexp - dlt G(P,P), Hamiltonian_main_mod.F90 ratio factors).
+struct UpdTab {
+  zd myexp, dlt, expal;
+};
+
+// Scalar arithmetic of the update kernel.  ArD: FP64 complex (the plain form:
+// the ratios must agree with an FP64 reference to ~1e-10 even where
+// 1 + Delta (1 - G_jj) cancels).  ArF: double-float (the mixed form).
+struct ArD {
+  typedef zd Z;
+  typedef double R;
+  static ALF_DEV Z mk(zd a) { return a; }
+  static ALF_DEV zd wide(Z a) { return a; }
+  static ALF_DEV R mkr(double a) { return a; }
+  static ALF_DEV Z one() { return zmk(1.0, 0.0); }
+  static ALF_DEV Z zero() { return zmk(0.0, 0.0); }
+  static ALF_DEV Z mul(Z a, Z b) { return zmul(a, b); }
+  static ALF_DEV Z sub(Z a, Z b) { return zsub(a, b); }
+  static ALF_DEV Z add(Z a, Z b) { return zadd(a, b); }
+  static ALF_DEV Z neg(Z a) { return zmk(-a.x, -a.y); }
+  static ALF_DEV Z mac(Z c, Z a, Z b) { return zadd(c, zmul(a, b)); }
+  static ALF_DEV Z scale(Z a, R s) { return zscale(a, s); }
+  static ALF_DEV R re_mul(Z a, Z b) { return a.x * b.x - a.y * b.y; }
+  static ALF_DEV R re(Z a) { return a.x; }
+  static ALF_DEV R absr(R a) { return fabs(a); }
+  static ALF_DEV R mulr(R a, R b) { return a * b; }
+  static ALF_DEV bool gt(R a, R b) { return a > b; }
+  // 1/d, d > 0 real: float seed, two Newton-Raphson steps r <- r + r (1 - d r) (quadratic
+  // convergence, 2^-24 -> 2^-48 -> below 2^-53); an FP64 division costs ~560 cycles here.
+  static ALF_DEV double rcp_pos(double d) {
+    if (!(d > 1e-30 && d < 1e30)) return 1.0 / d;
+    double r = (double)__frcp_rn(__double2float_rn(d));
+    r = fma(r, fma(-d, r, 1.0), r);
+    return fma(r, fma(-d, r, 1.0), r);
+  }
+  static ALF_DEV Z rcp(Z a) {
+    const double s = rcp_pos(a.x * a.x + a.y * a.y);
+    return zmk(a.x * s, -a.y * s);
+  }
+  // positive rescaling towards |a| ~ 1 (direction unchanged)
+  static ALF_DEV Z renorm(Z a) {
+    const float m2 = __double2float_rn(a.x * a.x + a.y * a.y);
+    return (m2 > 0.f && m2 < 3e38f) ? zscale(a, (double)rsqrtf(m2)) : a;
+  }
+  static ALF_DEV zd unit(Z a) { const double r = sqrt(a.x * a.x + a.y * a.y); return zmk(a.x / r, a.y / r); }
+  static ALF_DEV Z shfl(Z a, int src) {
+    return zmk(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));
+  }
+};
+struct ArF {
+  typedef dfz Z;
+  typedef dff R;
+  static ALF_DEV Z mk(zd a) { return dz_make(a); }
+  static ALF_DEV zd wide(Z a) { return dz_wide(a); }
+  static ALF_DEV R mkr(double a) { return df_make(a); }
+  static ALF_DEV Z one() { return dfz{{1.f, 0.f}, {0.f, 0.f}}; }
+  static ALF_DEV Z zero() { return dfz{{0.f, 0.f}, {0.f, 0.f}}; }
+  static ALF_DEV Z mul(Z a, Z b) { return dz_mul(a, b); }
+  static ALF_DEV Z sub(Z a, Z b) { return dz_sub(a, b); }
+  static ALF_DEV Z add(Z a, Z b) { return dz_add(a, b); }
+  static ALF_DEV Z neg(Z a) { return dfz{df_neg(a.r), df_neg(a.i)}; }
+  static ALF_DEV Z mac(Z c, Z a, Z b) { return dz_mac(c, a, b); }
+  static ALF_DEV Z scale(Z a, R s) { return dz_scale(a, s); }
+  static ALF_DEV R re_mul(Z a, Z b) { return df_dot2(a.r, b.r, df_neg(a.i), b.i); }
+  static ALF_DEV R re(Z a) { return a.r; }
+  static ALF_DEV R absr(R a) { return df_abs(a); }
+  static ALF_DEV R mulr(R a, R b) { return df_mul(a, b); }
+  static ALF_DEV bool gt(R a, R b) { return df_gt(a, b); }
+  static ALF_DEV Z rcp(Z a) { return dz_rcp(a); }
+  static ALF_DEV Z renorm(Z a) {
+    const float m2 = a.r.h * a.r.h + a.i.h * a.i.h;
+    return (m2 > 0.f && m2 < 3e38f) ? dz_scale(a, df_f(rsqrtf(m2))) : a;
+  }
+  static ALF_DEV zd unit(Z a) { return dz_wide(dz_unit(a)); }
+  static ALF_DEV Z shfl(Z a, int src) {
+    Z r;
+    r.r.h = __shfl_sync(0xffffffffu, a.r.h, src); r.r.l = __shfl_sync(0xffffffffu, a.r.l, src);
+    r.i.h = __shfl_sync(0xffffffffu, a.i.h, src); r.i.l = __shfl_sync(0xffffffffu, a.i.l, src);
+    return r;
+  }
+};
+
+// One CTA of UPD_THREADS threads per chain.  Dynamic shared memory:
+//   Gh[F][KMAX][KMAX+1]  the block Ghat, updated in place (arithmetic A)
+//   G0[F][KMAX][KMAX+1]  Ghat at block entry; reused as the ping-pong buffer of the
+//                        Gauss-Jordan inversion of Gamma.
+// Warp 0 runs the sequential Metropolis chain (all lanes compute the same scalars;
+// lane a handles row a of a column).  While warps 1..7 apply the rank-1 update of
+// an accepted visit q to rows a > q and columns b > q+1, warp 0 updates column q+1
+// itself and already decides visit q+1 from its new diagonal: one block barrier
+// per visit.  At block end, W = Delta_S Gamma^-1 is formed by Gauss-Jordan
+// elimination without pivoting: the pivots in accept order are the accepted
+// visits' own 1 + Delta (1 - G_jj) factors (the Sherman-Morrison sequence is the LU
+// factorisation of Gamma in that order), non-zero because a zero factor gives
+// weight 0 and is rejected.
+template <class A>
+__global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
+  typedef typename A::Z Z;
+  typedef typename A::R R;
+  constexpr int KM = UPD_KMAX, LD = UPD_KMAX + 1, NW = UPD_THREADS / 32;
+  const int c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int N = p.N, F = p.F, M = p.M, nq = p.nq;
   extern __shared__ __align__(16) unsigned char upd_raw[];
-  T* Gh = reinterpret_cast<T*>(upd_raw);  // Gh[(f*UPD_KMAX + a)*LD + b] = G(site_a, site_b)
-  constexpr int LD = UPD_KMAX + 1;
-  __shared__ int sites[UPD_KMAX], vtx[UPD_KMAX], s_new[UPD_KMAX], prop[UPD_KMAX];
-  __shared__ zd myexp[2][UPD_KMAX], dlt[2][UPD_KMAX], expal[2][UPD_KMAX];
-  __shared__ double gr[UPD_KMAX], u2[UPD_KMAX];
-  __shared__ zd xfac[2];
-  __shared__ int s_acc, s_m;
-  __shared__ zd s_phase;
+  Z* Gh = reinterpret_cast<Z*>(upd_raw);
+  Z* G0 = Gh + 2 * KM * LD;
+  __shared__ Z s_mye[2][KM], s_dlt[2][KM], s_tcol[2][2][KM], s_K[KM], s_rowt[2][KM], s_piv[2][2];
+  __shared__ zd s_dlt64[2][KM];
+  __shared__ R s_u2[KM], s_gr[KM];
+  __shared__ int s_site[KM], s_vtx[KM], s_snew[KM], s_prop[KM], s_accq[KM], s_acc[2];
+  __shared__ short s_ij[KM * KM];
+  __shared__ int s_m;
 
-  const T* G = reinterpret_cast<const T*>(p.G) + (long long)c * p.sG;
+  const double2* G = reinterpret_cast<const double2*>(p.G) + (long long)c * p.sG;
   const int* site = p.V.site + (long long)c * p.V.sK;
-  const zd* gg = p.V.g + (long long)c * p.V.sK;
-  const zd* al = p.V.alpha + (long long)c * p.V.sK;
-  const double* EE = p.V.E + (long long)c * p.V.sK;
   const int8_t* ty = p.V.type + (long long)c * p.V.sK;
+  const UpdTab* tab = p.tab + (long long)c * p.V.sK * 15;
   int8_t* fl = p.fields + (long long)c * p.L * M + (long long)(p.nt1 - 1) * M;
+  const long long NN = (long long)N * N;
 
-  // Prologue: every visit of the block is known in advance (each vertex is visited once
-  // per block, so its old field is the field at block start); all FP64 transcendental
-  // work is done here in parallel, off the sequential chain.
-  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-    const int pos = p.q0 + q;
+  // Prologue: each vertex is visited once per block, so its old field is the field at
+  // block start and every visit's proposal, draws and transition factors are known.
+  if (tid < nq) {
+    const int q = tid, pos = p.q0 + q;
     const int n = p.dir == 0 ? pos : M - 1 - pos;
-    vtx[q] = n;
-    sites[q] = site[n];
+    s_vtx[q] = n;
+    s_site[q] = site[n];
     const int v = p.visit_base + pos;
     double u0, u1, uu2;
     if (p.draws) {
@@ -115,178 +211,189 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update_block(UpdParams p) {
       u0 = alf_uniform(key, ctr); u1 = alf_uniform(key, ctr + 1); uu2 = alf_uniform(key, ctr + 2);
     }
     const int so = fl[n], tp = ty[n];
-    const int sn = (tp == 1) ? -so : (int)p.ft.flip[so + 2][nranf3(u0) - 1];
-    s_new[q] = sn;
-    prop[q] = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
-    u2[q] = uu2;
-    gr[q] = p.ft.gama[tp - 1][sn + 2] / p.ft.gama[tp - 1][so + 2];
-    const double dphi = p.ft.phi[tp - 1][sn + 2] - p.ft.phi[tp - 1][so + 2];
+    const int ch = (tp == 1) ? 0 : nranf3(u0) - 1;
+    const int sn = (tp == 1) ? -so : (int)p.ft.flip[so + 2][ch];
+    s_snew[q] = sn;
+    s_prop[q] = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
+    s_u2[q] = A::mkr(uu2);
+    s_gr[q] = A::mkr(p.ft.grat[tp - 1][so + 2][sn + 2]);
+    zd K = zmk(1.0, 0.0);
     for (int f = 0; f < F; ++f) {
-      const int k = f * M + n;
-      const zd Z1 = zscale(gg[k], dphi);
-      const zd me = zexp(zscale(Z1, EE[k]));
-      myexp[f][q] = me;
-      dlt[f][q] = zsub(me, zmk(1.0, 0.0));
-      expal[f][q] = zexp(zmul(Z1, al[k]));
+      const UpdTab e = tab[((long long)(f * M + n) * 5 + so + 2) * 3 + ch];
+      s_mye[f][q] = A::mk(e.myexp);
+      s_dlt[f][q] = A::mk(e.dlt);
+      s_dlt64[f][q] = e.dlt;
+      K = (f == 0) ? e.expal : zmul(K, e.expal);
     }
+    s_K[q] = A::mk(K);
   }
-  if (threadIdx.x == 0) { s_m = 0; s_phase = p.phase[c]; }
   __syncthreads();
-  for (int e = threadIdx.x; e < F * nq * nq; e += blockDim.x) {
-    const int f = e / (nq * nq), r = e % (nq * nq), a = r % nq, b = r / nq;
-    Gh[(f * UPD_KMAX + a) * LD + b] = G[(long long)f * N * N + sites[a] + (long long)sites[b] * N];
-  }
+  for (int a = warp; a < nq; a += NW)
+    if (lane < nq)
+      for (int f = 0; f < F; ++f) {
+        const Z v = A::mk(G[f * NN + s_site[a] + (long long)s_site[lane] * N]);
+        Gh[(f * KM + a) * LD + lane] = v;
+        G0[(f * KM + a) * LD + lane] = v;
+      }
   __syncthreads();
 
-  long long n_prop = 0, n_acc = 0;
-  for (int q = 0; q < nq; ++q) {
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      zd R = zmk(0.0, 0.0);
-      if (prop[q]) {
-        zd D[2];
-        for (int f = 0; f < F; ++f) {
-          const zd gjj = CT<T>::wide(Gh[(f * UPD_KMAX + q) * LD + q]);
-          D[f] = zsub(myexp[f][q], zmul(dlt[f][q], gjj));  // Mat(1,1) = myexp - Z*G(P,P)
-          const zd Rf = zmul(D[f], expal[f][q]);
-          R = (f == 0) ? Rf : zmul(R, Rf);
-        }
-        zd Rp = R;
-        for (int e = 1; e < p.NSUN; ++e) Rp = zmul(Rp, R);
-        R = zscale(Rp, gr[q]);
-        const zd ph = s_phase;
-        const double weight = fabs(zmul(ph, R).x / ph.x);
-        acc = weight > u2[q];
-        if (acc) {
-          const double ar = sqrt(zmul(R, zconj(R)).x);
-          const zd pr = zmul(ph, R);
-          s_phase = zmk(pr.x / ar, pr.y / ar);
-          for (int f = 0; f < F; ++f) xfac[f] = zdiv(dlt[f][q], D[f]);  // x = Delta / (1 + Delta (1 - G_jj))
-        }
+  // warp-0 state (identical in all lanes)
+  Z ph = A::mk(p.phase[c]);  // kept unnormalised (only its direction enters the weight)
+  int m = 0;
+  long long n_prop = 0;
+  // Decide visit v from the current Ghat(v,v) (gd) and column Ghat(lane, v) (gc, lanes > v).
+  auto decide = [&](int v, const Z* gd, const Z* gc) {
+    int acc = 0;
+    Z Rt = A::zero();
+    if (s_prop[v]) {
+      Z D[2];
+#pragma unroll
+      for (int f = 0; f < 2; ++f)  // Mat(1,1) = myexp - Delta G(P,P)
+        if (f < F) D[f] = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));
+      Rt = (F == 2) ? A::mul(D[0], D[1]) : D[0];
+      Rt = A::mul(Rt, s_K[v]);
+      Z Rp = Rt;
+      for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
+      Rt = A::scale(Rp, s_gr[v]);
+      // weight = |Re(phase R) / Re(phase)| > u  (Wrapgr_mod.F90:141-143), division-free
+      const R num = A::absr(A::re_mul(ph, Rt));
+      const R den = A::mulr(A::absr(A::re(ph)), s_u2[v]);
+      acc = A::gt(num, den);
+      if (acc) {
+        ph = A::renorm(A::mul(ph, Rt));
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+          if (f < F) {
+            const Z x = A::mul(s_dlt[f][v], A::rcp(D[f]));  // Delta / Mat(1,1)
+            if (lane > v && lane < nq) s_tcol[v & 1][f][lane] = A::mul(x, gc[f]);
+          }
       }
+    }
+    n_prop += s_prop[v];
+    if (lane == 0) {
       if (p.rec_acc) {
-        const int v = p.visit_base + p.q0 + q;
-        p.rec_acc[(long long)c * p.sRec + v] = (int8_t)acc;
-        p.rec_ratio[(long long)c * p.sRec + v] = R;
+        const long long r = (long long)c * p.sRec + p.visit_base + p.q0 + v;
+        p.rec_acc[r] = (int8_t)acc;
+        p.rec_ratio[r] = A::wide(Rt);
       }
-      s_acc = acc;
+      if (acc) {
+        s_accq[m] = v;
+        p.sites_out[(long long)c * KM + m] = s_site[v];
+        for (int f = 0; f < F; ++f) p.delta_out[((long long)c * 2 + f) * KM + m] = s_dlt64[f][v];
+        fl[s_vtx[v]] = (int8_t)s_snew[v];
+      }
+      s_acc[v & 1] = acc;
+    }
+    m += acc;
+  };
+
+  if (warp == 0) {
+    Z gd[2], gc[2];
+#pragma unroll
+    for (int f = 0; f < 2; ++f)
+      if (f < F) {
+        gc[f] = (lane < nq) ? Gh[(f * KM + lane) * LD] : A::zero();
+        gd[f] = Gh[f * KM * LD];
+      }
+    decide(0, gd, gc);
+  }
+  __syncthreads();
+  for (int q = 0; q < nq; ++q) {
+    const int acc = s_acc[q & 1];
+    if (warp == 0) {
+      if (q + 1 < nq) {
+        const int v = q + 1;
+        Z gd[2], gc[2];
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+          if (f < F) {
+            Z col = (lane < nq) ? Gh[(f * KM + lane) * LD + v] : A::zero();
+            if (acc && lane > q && lane < nq) {  // column v of the rank-1 update of visit q
+              col = A::mac(col, s_tcol[q & 1][f][lane], Gh[(f * KM + q) * LD + v]);
+              Gh[(f * KM + lane) * LD + v] = col;
+            }
+            gc[f] = col;
+            gd[f] = A::shfl(col, v);
+          }
+        decide(v, gd, gc);
+      }
+    } else if (acc) {
+      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b), rows a > q, columns b > q+1
+      const int b = lane;
+      if (b > q + 1 && b < nq)
+        for (int f = 0; f < F; ++f)
+          for (int a = q + warp; a < nq; a += NW - 1) {
+            Z* g = Gh + (f * KM + a) * LD + b;
+            *g = A::mac(*g, s_tcol[q & 1][f][a], Gh[(f * KM + q) * LD + b]);
+          }
     }
     __syncthreads();
-    n_prop += prop[q];
-    if (s_acc) {
-      ++n_acc;
-      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b) for the positions still to be visited (a, b > q)
-      const int rem = nq - q - 1;
-      for (int e = threadIdx.x; e < F * rem * rem; e += blockDim.x) {
-        const int f = e / (rem * rem), r = e % (rem * rem), a = q + 1 + r % rem, b = q + 1 + r / rem;
-        const T x = CT<T>::mk(xfac[f]);
-        const T gaq = Gh[(f * UPD_KMAX + a) * LD + q];
-        const T gqb = Gh[(f * UPD_KMAX + q) * LD + b];
-        Gh[(f * UPD_KMAX + a) * LD + b] = tadd(Gh[(f * UPD_KMAX + a) * LD + b], tmul(x, tmul(gaq, gqb)));
-      }
-      if (threadIdx.x == 0) {
-        const int m = s_m;
-        p.sites_out[(long long)c * UPD_KMAX + m] = sites[q];
-        for (int f = 0; f < F; ++f) p.delta_out[((long long)c * 2 + f) * UPD_KMAX + m] = dlt[f][q];
-        s_m = m + 1;
-        fl[vtx[q]] = (int8_t)s_new[q];
-      }
+  }
+  if (tid == 0) s_m = m;
+  __syncthreads();
+  m = s_m;
+  if (m > 0) {
+    const int FMM = F * m * m;
+    for (int e = tid; e < m * m; e += UPD_THREADS) s_ij[e] = (short)(((e / m) << 6) | (e % m));
+    // Gamma(l,l') = delta_ll' + (delta_ll' - G0(s_l, s_l')) Delta_l'  in Gh (accept order)
+    for (int l = warp; l < m; l += NW)
+      if (lane < m)
+        for (int f = 0; f < F; ++f) {
+          const int l2 = lane;
+          const Z g = G0[(f * KM + s_accq[l]) * LD + s_accq[l2]];
+          Z v = A::mul(A::sub(l == l2 ? A::one() : A::zero(), g), s_dlt[f][s_accq[l2]]);
+          if (l == l2) v = A::add(v, A::one());
+          Gh[(f * KM + l) * LD + l2] = v;
+        }
+    __syncthreads();
+    if (tid < F) s_piv[0][tid] = A::rcp(Gh[(tid * KM) * LD]);
+    // in-place Gauss-Jordan inversion, ping-pong between Gh and G0
+    Z* Ga = Gh;
+    Z* Gb = G0;
+    for (int k = 0; k < m; ++k) {
       __syncthreads();
-    }
-  }
-  if (threadIdx.x == 0) {
-    p.m_out[c] = s_m;
-    p.phase[c] = s_phase;
-    long long* cn = p.cnt + 4ll * c;
-    cn[0] += n_prop; cn[1] += n_acc; cn[2] += nq; cn[3] += n_acc;
-  }
-}
-
-// W = Delta_S Gamma^-1, Gamma = 1 + (1 - G0(S,S)) Delta_S: Gauss-Jordan elimination with
-// partial pivoting on [Gamma^T | I] (so the right half becomes Gamma^-T).  One CTA per
-// (chain, flavour); W: [chain][2][KMAX][KMAX] row-major (l, l').
-template <typename T>
-__global__ void __launch_bounds__(256) k_flush_w(const void* Gv, long long sG, int N, int F, const int* m_in,
-                                                 const int* sites, const zd* delta, zd* W) {
-  const int b = blockIdx.x, c = b / F, f = b % F;
-  const int m = m_in[c];
-  if (m == 0) return;
-  const T* G = reinterpret_cast<const T*>(Gv) + (long long)c * sG + (long long)f * N * N;
-  __shared__ zd A[UPD_KMAX][2 * UPD_KMAX + 1];
-  __shared__ int st[UPD_KMAX];
-  __shared__ zd dl[UPD_KMAX];
-  __shared__ int piv;
-  __shared__ zd pinv;
-  for (int l = threadIdx.x; l < m; l += blockDim.x) {
-    st[l] = sites[(long long)c * UPD_KMAX + l];
-    dl[l] = delta[((long long)c * 2 + f) * UPD_KMAX + l];
-  }
-  __syncthreads();
-  // A(r, col) = Gamma(col, r) = delta + (delta - G0(s_col, s_r)) Delta_r
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    const int r = e % m, col = e / m;
-    const zd g = CT<T>::wide(G[st[col] + (long long)st[r] * N]);
-    zd v = zmul(zsub(zmk(col == r ? 1.0 : 0.0, 0.0), g), dl[r]);
-    if (col == r) v = zadd(v, zmk(1.0, 0.0));
-    A[r][col] = v;
-    A[r][m + col] = zmk(r == col ? 1.0 : 0.0, 0.0);
-  }
-  __syncthreads();
-  for (int k = 0; k < m; ++k) {
-    if (threadIdx.x == 0) {
-      int pv = k;
-      double best = A[k][k].x * A[k][k].x + A[k][k].y * A[k][k].y;
-      for (int r = k + 1; r < m; ++r) {
-        const double v = A[r][k].x * A[r][k].x + A[r][k].y * A[r][k].y;
-        if (v > best) { best = v; pv = r; }
+      if (warp < F && lane < m) s_rowt[warp][lane] = A::mul(Ga[(warp * KM + lane) * LD + k], s_piv[k & 1][warp]);
+      __syncthreads();
+      for (int e = tid; e < FMM; e += UPD_THREADS) {
+        const int f = e >= m * m, r = e - f * m * m;
+        const int i = s_ij[r] >> 6, j = s_ij[r] & 63;
+        const Z pinv = s_piv[k & 1][f];
+        Z v;
+        if (i == k && j == k) v = pinv;
+        else if (i == k) v = A::mul(Ga[(f * KM + k) * LD + j], pinv);
+        else if (j == k) v = A::neg(s_rowt[f][i]);
+        else v = A::mac(Ga[(f * KM + i) * LD + j], A::neg(s_rowt[f][i]), Ga[(f * KM + k) * LD + j]);
+        Gb[(f * KM + i) * LD + j] = v;
+        if (i == k + 1 && j == k + 1) s_piv[(k + 1) & 1][f] = A::rcp(v);
       }
-      piv = pv;
-      pinv = zinv(A[pv][k]);
+      Z* t = Ga; Ga = Gb; Gb = t;
     }
     __syncthreads();
-    const int pv = piv;
-    if (pv != k)
-      for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) { zd t = A[k][j]; A[k][j] = A[pv][j]; A[pv][j] = t; }
-    __syncthreads();
-    const zd inv = pinv;
-    for (int j = threadIdx.x; j < 2 * m; j += blockDim.x)
-      if (j != k) A[k][j] = zmul(A[k][j], inv);
-    __syncthreads();
-    for (int e = threadIdx.x; e < m * 2 * m; e += blockDim.x) {
-      const int r = e / (2 * m), j = e % (2 * m);
-      if (r != k && j != k) A[r][j] = zsub(A[r][j], zmul(A[r][k], A[k][j]));
-    }
-    __syncthreads();
+    // W(l, l') = Delta_l Gamma^-1(l, l')
+    for (int l = warp; l < m; l += NW)
+      if (lane < m)
+        for (int f = 0; f < F; ++f)
+          p.W[(((long long)c * 2 + f) * KM + l) * KM + lane] =
+              zmul(s_dlt64[f][s_accq[l]], A::wide(Ga[(f * KM + l) * LD + lane]));
   }
-  // Gamma^-1(l, l') = A(l', m + l);  W(l, l') = Delta_l Gamma^-1(l, l')
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    const int l = e / m, l2 = e % m;
-    W[(((long long)c * 2 + f) * UPD_KMAX + l) * UPD_KMAX + l2] = zmul(dl[l], A[l2][m + l]);
+  if (tid == 0) {
+    p.m_out[c] = m;
+    for (int f = 0; f < F; ++f) p.m_out[p.nChains + c * F + f] = m;
+    if (m > 0) p.phase[c] = A::unit(ph);
+    long long* cn = p.cnt + 4ll * c;
+    cn[0] += n_prop; cn[1] += m; cn[2] += nq; cn[3] += m;
   }
 }
 
-// Flush operands, spread over the GPU:
-//   X(:, l) = G0(:, s_l)                                   (k_flush_x: one thread per (row, l))
-//   Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :))      (k_flush_y: one thread per (l, column))
-// X: [chain][2][N][KMAX] col-major (ld N); Y: [chain][2][KMAX][N] col-major (ld KMAX), type T.
-template <typename T>
-__global__ void k_flush_x(const void* Gv, long long sG, int N, int F, const int* m_in, const int* sites, void* Xv) {
-  const int b = blockIdx.y, c = b / F, f = b % F;
-  const int m = m_in[c];
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= (long long)N * m) return;
-  const int row = e % N, l = e / N;
-  const int s = sites[(long long)c * UPD_KMAX + l];
-  const T* G = reinterpret_cast<const T*>(Gv);
-  T* X = reinterpret_cast<T*>(Xv);
-  X[((long long)c * 2 + f) * N * UPD_KMAX + row + (long long)l * N] =
-      G[(long long)c * sG + (long long)f * N * N + row + (long long)s * N];
-}
+constexpr size_t upd_smem_bytes() { return 2ull * 2 * UPD_KMAX * (UPD_KMAX + 1) * 16; }  // Z is 16 bytes
 
-// block: 32 x 8 threads = (l, column); grid (ceil(N/8), B)
-template <typename T>
-__global__ void k_flush_y(const void* Gv, long long sG, int N, int F, const int* m_in, const int* sites, const zd* W,
-                          void* Yv) {
+// Flush operands for G = G0 - X Y (one launch, spread over the GPU):
+//   X(:, l) = G0(:, s_l)
+//   Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :))
+// block 32 x 8 threads = (l, column / row); grid (ceil(N/8), chains*flavours).
+// X: [chain][2][N][KMAX] col-major (ld N); Y: [chain][2][KMAX][N] col-major (ld KMAX).
+__global__ void k_flush_xy(const zd* Gv, long long sG, int N, int F, const int* m_in, const int* sites, const zd* W,
+                           zd* X, zd* Y) {
   const int b = blockIdx.y, c = b / F, f = b % F;
   const int m = m_in[c];
   if (m == 0) return;
@@ -299,18 +406,18 @@ __global__ void k_flush_y(const void* Gv, long long sG, int N, int F, const int*
     Ws[e / m][e % m] = W[(((long long)c * 2 + f) * UPD_KMAX + e / m) * UPD_KMAX + e % m];
   __syncthreads();
   const int col = blockIdx.x * 8 + ty;
-  const T* Gf = reinterpret_cast<const T*>(Gv) + (long long)c * sG + (long long)f * N * N;
+  const zd* Gf = Gv + (long long)c * sG + (long long)f * N * N;
+  const long long xy = ((long long)c * 2 + f) * N * UPD_KMAX;
   if (col < N && tx < m) {
     const int s = st[tx];
-    const zd gv = CT<T>::wide(Gf[s + (long long)col * N]);
-    gb[ty][tx] = zsub(zmk(s == col ? 1.0 : 0.0, 0.0), gv);
+    X[xy + col + (long long)tx * N] = Gf[col + (long long)s * N];  // row `col` of X
+    gb[ty][tx] = zsub(zmk(s == col ? 1.0 : 0.0, 0.0), Gf[s + (long long)col * N]);
   }
   __syncthreads();
   if (col < N && tx < m) {
     zd y = zmk(0.0, 0.0);
     for (int l2 = 0; l2 < m; ++l2) y = zadd(y, zmul(Ws[tx][l2], gb[ty][l2]));
-    reinterpret_cast<T*>(Yv)[((long long)c * 2 + f) * N * UPD_KMAX + tx + (long long)col * UPD_KMAX] = CT<T>::mk(y);
+    Y[xy + tx + (long long)col * UPD_KMAX] = y;
   }
 }
 
-template <typename T> constexpr size_t upd_smem_bytes() { return 2 * UPD_KMAX * (UPD_KMAX + 1) * sizeof(T); }

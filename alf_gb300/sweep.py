@@ -23,6 +23,13 @@ from . import _lib
 from .model import Model
 
 PRECISIONS = {"fp64": 0, "mixed": 1}
+# dims.reserved[0] flags (include/alfgpu.h)
+FLAG_DF_PROPAGATION = 1
+FLAG_EXACT_QRP = 2
+FLAG_EXACT_QRP_CGR = 4
+FLAG_EXACT_QRP_DECOMPOSE = 8
+PIVOTING = {"norms": 0, "exact": FLAG_EXACT_QRP, "exact-cgr": FLAG_EXACT_QRP_CGR,
+            "exact-decompose": FLAG_EXACT_QRP_DECOMPOSE}
 
 
 def _p(a: np.ndarray):
@@ -31,13 +38,18 @@ def _p(a: np.ndarray):
 
 class Chains:
     def __init__(self, model: Model, n_chains: int = 1, precision: str = "fp64", delay_k: int = 0,
-                 device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None):
+                 device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None,
+                 pivoting: str = "norms", flags: int = 0):
+        """``pivoting``: "norms" orders the columns of every stabilisation QR once by
+        their norms (ALF's STABLOG pivoting) and factors them with the blocked QR;
+        "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)."""
         self.L = _lib.lib()
         self.model = model
         self.C = n_chains
         self.N, self.F, self.M, self.Lt = model.ndim, model.n_fl, model.n_op, model.ltrot
         d = _lib.Dims(model.ndim, model.n_fl, model.n_sun, model.n_op, model.ltrot, model.nwrap, n_chains,
                       PRECISIONS[precision], delay_k, ltau, device)
+        d.reserved[0] = PIVOTING[pivoting] | flags
         h = C.c_void_p()
         _lib.check(self.L.alfgpu_create(C.byref(h), C.byref(d)), "alfgpu_create")
         self.h = h

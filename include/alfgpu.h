@@ -62,6 +62,15 @@ enum {
  * (1e5-1e10 at beta = 10), so this is only usable for small beta / Nwrap. */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
 enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
+/* Column pivoting of the stabilisation QRs.  Default: the columns are ordered once by
+ * their norms and factored by a blocked unpivoted Householder QR (the pivoting of
+ * ALF's STABLOG branch, Prog/udv_state_mod.F90:503-542), whose trailing work runs on
+ * all SMs.  ALFGPU_FLAG_EXACT_QRP in dims.reserved[0] selects ZGEQP3's dynamic
+ * pivoting with norm downdates (Prog/QDRP_decompose_mod.F90:60-101, the default
+ * branch), run on one thread-block cluster per matrix, for every QR; _CGR and
+ * _DECOMPOSE select it for the QR of CGR (cgr1_mod.F90:223) or of
+ * decompose_UDV_state only.  ZGEQP3 pivoting is always used for Ndim > 512. */
+enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_EXACT_QRP_CGR = 4, ALFGPU_FLAG_EXACT_QRP_DECOMPOSE = 8 };
 
 typedef struct alfgpu_s alfgpu_t;
 

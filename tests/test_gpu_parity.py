@@ -98,13 +98,13 @@ def _variant_ratios(m, f0, seed, sweeps, chain):
         oracle.set_variant(0)
 
 
-def _run_pair(m, seed=5, sweeps=1, chain=0):
+def _run_pair(m, seed=5, sweeps=1, chain=0, pivoting="norms"):
     f0 = rng.initial_fields(seed, chain, m.n_op, m.ltrot)
     var = _variant_ratios(m, f0, seed, sweeps, chain)
     o = oracle.Oracle(m)
     o.set_fields(f0)
     ph_o = o.init_state()
-    g = Chains(m, n_chains=1)
+    g = Chains(m, n_chains=1, pivoting=pivoting)
     g.set_fields(0, f0)
     ph_g = g.init_state()[0]
     assert abs(ph_g - ph_o) < 1e-10
@@ -139,9 +139,17 @@ def _run_pair(m, seed=5, sweeps=1, chain=0):
     return g, o
 
 
-def test_init_and_sweep_hubbard_4x4_parity():
-    # the small reference configuration: 4x4 square Hubbard, U=4, beta=4, dtau=0.1, Nwrap=10
-    _run_pair(mdl.config("hubbard4x4"), sweeps=3)
+@pytest.mark.parametrize("pivoting", ["norms", "exact"])
+def test_init_and_sweep_hubbard_4x4_parity(pivoting):
+    # the small reference configuration: 4x4 square Hubbard, U=4, beta=4, dtau=0.1, Nwrap=10;
+    # the oracle pivots like ZGEQP3: with "norms" only G (not the UDV factors) is comparable
+    _run_pair(mdl.config("hubbard4x4"), sweeps=3, pivoting=pivoting)
+
+
+def test_sweep_hubbard_8x8_parity():
+    # 8x8 (N_dim = 64): four panels of the blocked QR on a 4-CTA cluster
+    m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    _run_pair(m, seed=4, sweeps=1)
 
 
 def test_sweep_hubbard_odd_sizes_parity():
