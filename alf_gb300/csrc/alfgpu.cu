@@ -42,6 +42,10 @@ struct alfgpu_s {
   int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
   int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
   int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
+  int df_stab = 0;                   // mixed form: stabilisation products in double-float
+  int df_qr = 0;                     // mixed form: decompose QR and Q formation in double-float
+  int qr_df = 0;                     // the last QR left double-float reflectors in QRdf
+  zd* QRdf = nullptr;                // [B][N][N] reflectors in double-float (16-byte elements)
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
@@ -242,6 +246,13 @@ static int gemm32(alfgpu_s* h, const GemmParams& g, int tA, int tB, int tC) {
   return 0;
 }
 
+// Stabilisation products (UDV propagation, decompose, CGR): double-float in the mixed
+// form, FP64 otherwise.
+static int gemm_s(alfgpu_s* h, const GemmParams& g) {
+  if (!h->df_stab) return gemm(h, g);
+  return gemm32(h, g, g.realA ? ST_R64 : ST_C128, g.realB ? ST_R64 : ST_C128, ST_C128);
+}
+
 static GemmParams gsq(alfgpu_s* h, int batch) {  // N x N x N square product, batch strides N*N
   GemmParams p = gemm_defaults();
   const int N = h->N;
@@ -285,10 +296,11 @@ static int slice_scale(alfgpu_s* h, int nt1) {
 // decompose_UDV_state (udv_state_mod.F90:466-578) on all B pairs; s.U holds the propagated A.
 // QR of Ain * diag(colscale) into Aout (Aout != Ain): R above the diagonal (rows
 // normalised by D = DUP), reflectors below, tau, jpvt, info.
-static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, int exact) {
+static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, int exact, int df = 0) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
   h->exact_qrp = exact;
+  h->qr_df = 0;
   const dim3 g8((N + 7) / 8, B);
   if (exact && !h->qrr_ok) {
     RET(copy_mats(h, Aout, Ain, (size_t)B * NN));
@@ -298,6 +310,7 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
   if (exact) {
     QRRowsParams q;
     q.Ain = Ain; q.A = Aout; q.lda = N; q.sA = NN; q.N = N;
+    q.Araw = df ? h->QRdf : nullptr;
     q.colscale = colscale; q.sCS = N;
     q.tau = h->tau; q.sT = N; q.jpvt = h->jpvt; q.sP = N; q.D = h->DUP; q.sD = N; q.info = h->info;
     cudaLaunchConfig_t cfg;
@@ -311,7 +324,9 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
     at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
     cfg.attrs = at; cfg.numAttrs = 1;
     h->launches++;
-    CK(cudaLaunchKernelEx(&cfg, k_qrp_rows, q));
+    if (df) CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArF>, q));
+    else CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArD>, q));
+    h->qr_df = df;
     k_bqr_finish<<<g8, 256, (size_t)N * sizeof(double), h->st>>>(Aout, N, NN, N, h->tau, N, h->DUP, N, h->info);
     CKL();
     prof_end(h);
@@ -343,12 +358,13 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
       ap.V = Aout; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
       ap.C = Aout; ap.ldc = N; ap.sC = NN;
       ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0 + w; ap.conj_tau = 1;
-      k_bqr_apply<<<dim3(N - j0 - w, B), 128, 0, h->st>>>(ap);
+      k_bqr_apply<ArD><<<dim3(N - j0 - w, B), 128, 0, h->st>>>(ap);
       CKL();
     }
   }
   k_bqr_finish<<<g8, 256, (size_t)N * sizeof(double), h->st>>>(Aout, N, NN, N, h->tau, N, h->DUP, N, h->info);
   CKL();
+  h->qr_df = 0;
   prof_end(h);
   return 0;
 }
@@ -365,10 +381,11 @@ static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
   for (int j0 = ((N - 1) / BQR_NB) * BQR_NB; j0 >= 0; j0 -= BQR_NB) {
     const int w = (N - j0 < BQR_NB) ? N - j0 : BQR_NB;
     BQRApply ap;
-    ap.V = F; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
+    ap.V = h->qr_df ? (const void*)h->QRdf : (const void*)F; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
     ap.C = Q; ap.ldc = N; ap.sC = NN;
     ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0; ap.conj_tau = 0;
-    k_bqr_apply<<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
+    if (h->qr_df) k_bqr_apply<ArF><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
+    else k_bqr_apply<ArD><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
     CKL();
   }
   prof_end(h);
@@ -407,7 +424,7 @@ static int decompose_inplace(alfgpu_s* h, UDVSet& s, int left) {
 static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   if (!h->QRw) return decompose_inplace(h, s, left);
   const int N = h->N, B = h->B;
-  RET(qr_any(h, s.U, s.D, h->QRw, h->exact_dec));
+  RET(qr_any(h, s.U, s.D, h->QRw, h->exact_dec, h->df_qr && h->exact_dec));
   k_decomp_phase<<<B, 256, 0, h->st>>>(h->QRw, N, N, h->info, left, h->dphase, s.detU);
   CKL();
   k_perm0<<<dim3((N + 255) / 256, B), 256, 0, h->st>>>(h->jpvt, N, h->perm, N, N);
@@ -421,7 +438,7 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
     p.B = h->QRw; p.opB = OP_C; p.triB = 1;
   }
   p.C = h->Vtmp;
-  RET(gemm(h, p));
+  RET(gemm_s(h, p));
   std::swap(s.V, h->Vtmp);
   CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   RET(orgqr_any(h, h->QRw, s.U));
@@ -441,7 +458,7 @@ static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
     p.B = h->udvr.U; p.C = h->T1;
     p.rs = h->S; p.sRS = N;
     if (h->mixed_propagate) RET(gemm32(h, p, ST_R64, ST_C128, ST_C128));
-    else RET(gemm(h, p));
+    else RET(gemm_s(h, p));
     RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
   }
   prof_end(h);
@@ -459,7 +476,7 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
     q.B = h->udvl.U; q.C = h->T1;
     q.ks = h->S; q.sKS = N; q.ksConj = 1;
     if (h->mixed_propagate) RET(gemm32(h, q, ST_R64, ST_C128, ST_C128));
-    else RET(gemm(h, q));
+    else RET(gemm_s(h, q));
     RET(copy_mats(h, h->udvl.U, h->T1, (size_t)B * N * N));
   }
   prof_end(h);
@@ -474,7 +491,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
   {
     GemmParams p = gsq(h, B);
     p.A = ur.U; p.opA = OP_C; p.B = ul.U; p.opB = OP_N; p.C = h->RHS;
-    RET(gemm(h, p));
+    RET(gemm_s(h, p));
   }
   // TPUP = D_R (V_R V_L) D_L + RHS  (D's packed as complex scale vectors in S / Sinv)
   RET(copy_mats(h, h->TP, h->RHS, (size_t)B * NN));
@@ -485,7 +502,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     p.A = ur.V; p.B = ul.V; p.C = h->TP; p.beta = zmk(1.0, 0.0);
     p.rs = h->S; p.sRS = N;
     p.cs = h->Sinv; p.sCS = N;
-    RET(gemm(h, p));
+    RET(gemm_s(h, p));
   }
   zd* QR = h->TP;
   if (nvar != 1) {
@@ -507,7 +524,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     GemmParams p = gsq(h, B);
     p.A = Q; p.opA = OP_C; p.B = ur.U; p.opB = OP_C; p.C = h->RHS;
     p.rs = h->S; p.sRS = N; p.rsInv = 1;
-    RET(gemm(h, p));
+    RET(gemm_s(h, p));
     // R y = RHS (ZTRSM L,U,N), columns of RHS
     TrsvParams t;
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
@@ -519,13 +536,13 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     // G = U_L * P RHS (ZLAPMR backward folded into the B load)
     GemmParams g = gsq(h, B);
     g.A = ul.U; g.B = h->RHS; g.permB = h->iperm; g.sPB = N; g.C = Gout;
-    RET(gemm(h, g));
+    RET(gemm_s(h, g));
   } else {
     // RHS = U_L Q, columns divided by DUP
     GemmParams p = gsq(h, B);
     p.A = ul.U; p.B = Q; p.C = h->RHS;
     p.cs = h->S; p.sCS = N; p.csInv = 1;
-    RET(gemm(h, p));
+    RET(gemm_s(h, p));
     // y R^H = RHS (ZTRSM R,U,C): rows of RHS, conjugated, upper solve
     TrsvParams t;
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
@@ -537,7 +554,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     // G = (RHS P) U_R^H (ZLAPMT backward folded into the A load)
     GemmParams g = gsq(h, B);
     g.A = h->RHS; g.permA = h->iperm; g.sPA = N; g.B = ur.U; g.opB = OP_C; g.C = Gout;
-    RET(gemm(h, g));
+    RET(gemm_s(h, g));
   }
   return 0;
 }
@@ -731,6 +748,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_PROPAGATION);
   h->exact_dec = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_DECOMPOSE)) ? 1 : 0;
   h->exact_cgr = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_CGR)) ? 1 : 0;
+  h->df_stab = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_GEMM);
+  h->df_qr = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_QR);
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
@@ -772,9 +791,11 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   {
     const size_t sm = qrr_smem_bytes(h->N, h->CL);
     if (sm <= 227 * 1024 &&
-        cudaFuncSetAttribute(k_qrp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
+        cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
+        cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
         (h->CL <= 8 ||
-         cudaFuncSetAttribute(k_qrp_rows, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)) {
+         (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+          cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess))) {
       cudaLaunchConfig_t cfg;
       memset(&cfg, 0, sizeof(cfg));
       cfg.gridDim = dim3(h->CL, 1, 1);
@@ -785,7 +806,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
       at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
       cfg.attrs = at; cfg.numAttrs = 1;
       int n = 0;
-      h->qrr_ok = cudaOccupancyMaxActiveClusters(&n, k_qrp_rows, &cfg) == cudaSuccess && n > 0;
+      h->qrr_ok = cudaOccupancyMaxActiveClusters(&n, k_qrp_rows<ArD>, &cfg) == cudaSuccess && n > 0;
     }
     cudaGetLastError();
   }
@@ -812,6 +833,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   for (auto& s : h->udvst) r |= mk_udv(s);
   r |= dalloc(h, &h->TP, B * NN); r |= dalloc(h, &h->Qb, B * NN); r |= dalloc(h, &h->RHS, B * NN);
   r |= dalloc(h, &h->QRw, B * NN); r |= dalloc(h, &h->qkeys, B * N);
+  if (h->df_qr) r |= dalloc(h, &h->QRdf, B * NN);
   r |= dalloc(h, &h->Vtmp, B * NN);
   r |= dalloc(h, &h->tau, B * N); r |= dalloc(h, &h->jpvt, B * N); r |= dalloc(h, &h->perm, B * N);
   r |= dalloc(h, &h->iperm, B * N); r |= dalloc(h, &h->DUP, B * N); r |= dalloc(h, &h->vn, B * 2 * N);

@@ -24,6 +24,7 @@
 #pragma once
 #include "common.cuh"
 #include "linalg.cuh"
+#include "arith.cuh"
 
 #define BQR_NB 32
 #define BQR_ROWS 32   // max rows of a panel per CTA (N <= 32 * cluster size)
@@ -216,9 +217,10 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
 }
 
 struct BQRApply {
-  const zd* V; long long ldv, sV;  // reflectors: column kc holds v below row kc (v_kc = 1 implicit)
+  const void* V; long long ldv, sV;  // reflectors (column kc holds v below row kc, v_kc = 1 implicit),
+                                     // stored in the kernel's arithmetic (FP64 or double-float)
   const zd* tau; long long sT;
-  zd* C; long long ldc, sC;        // columns c0 .. N-1 are updated, rows j0 .. N-1
+  zd* C; long long ldc, sC;          // columns c0 .. N-1 are updated, rows j0 .. N-1 (FP64)
   int N, j0, nb, c0;
   int conj_tau;  // 1: QR trailing update, H^H in order k = 0..nb-1
                  // 0: explicit Q, H in reverse order; columns [j0, j0+nb) start as e_c
@@ -229,36 +231,38 @@ struct BQRApply {
 // 32-row blocks w, w+4, ... of rows j0..N-1 (lane l: row j0 + l + 32 (w + 4 q)); row
 // blocks above the reflector are skipped warp-uniformly; the four warp partials of
 // v^H x meet in shared memory (double-buffered: one barrier per reflector); the next
-// reflector is prefetched.
+// reflector is prefetched.  Arithmetic A: ArD or ArF.
 #define BQR_QW (BQR_LROWS / 4)
+template <class A>
 __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
+  typedef typename A::Z Z;
   const int b = blockIdx.y, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int c = p.c0 + blockIdx.x;
   if (c >= p.N) return;
   const int N = p.N, j0 = p.j0, nb = p.nb;
   const int nblk = (N - j0 + 31) >> 5;  // 32-row blocks
-  const zd* V = p.V + b * p.sV;
+  const Z* V = reinterpret_cast<const Z*>(p.V) + b * p.sV;
   const zd* tau = p.tau + b * p.sT;
   zd* col = p.C + b * p.sC + (long long)c * p.ldc;
   const bool fresh = !p.conj_tau && c < j0 + nb;
-  __shared__ zd red[2][4];
-  zd x[BQR_QW], vn[BQR_QW];
+  __shared__ Z red[2][4];
+  Z x[BQR_QW], vn[BQR_QW];
 #pragma unroll
   for (int q = 0; q < BQR_QW; ++q) {
     const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
-    x[q] = zmk(0.0, 0.0);
-    vn[q] = zmk(0.0, 0.0);
-    if (blk < nblk && r < N) x[q] = fresh ? zmk(r == c ? 1.0 : 0.0, 0.0) : col[r];
+    x[q] = A::zero();
+    vn[q] = A::zero();
+    if (blk < nblk && r < N) x[q] = fresh ? (r == c ? A::one() : A::zero()) : A::mk(col[r]);
   }
   auto load_v = [&](int k) {
     const int kc = j0 + k, blo = (kc - j0) >> 5;
-    const zd* v = V + (long long)kc * p.ldv;
+    const Z* v = V + (long long)kc * p.ldv;
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
       const int blk = w + 4 * q;
       if (blk < blo || blk >= nblk) continue;
       const int r = j0 + lane + 32 * blk;
-      vn[q] = (r < kc || r >= N) ? zmk(0.0, 0.0) : (r == kc ? zmk(1.0, 0.0) : v[r]);
+      vn[q] = (r < kc || r >= N) ? A::zero() : (r == kc ? A::one() : v[r]);
     }
   };
   load_v(p.conj_tau ? 0 : nb - 1);
@@ -266,30 +270,31 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
   for (int kk = 0; kk < nb; ++kk) {
     const int k = p.conj_tau ? kk : nb - 1 - kk;
     const int kc = j0 + k, blo = (kc - j0) >> 5;
-    zd vr[BQR_QW];
+    Z vr[BQR_QW];
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) vr[q] = vn[q];
     if (kk + 1 < nb) load_v(p.conj_tau ? kk + 1 : nb - 2 - kk);
     zd t = tau[kc];
     if (t.x == 0.0 && t.y == 0.0) continue;  // uniform over the block
     if (p.conj_tau) t.y = -t.y;
-    zd s = zmk(0.0, 0.0);
+    Z s = A::zero();
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
       const int blk = w + 4 * q;
       if (blk < blo || blk >= nblk) continue;
-      s = zadd(s, zmul(zconj(vr[q]), x[q]));
+      s = A::mac(s, A::conj(vr[q]), x[q]);
     }
-    s = warp_zsum(s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = A::add(s, A::shfl_xor(s, o));
     if (lane == 0) red[par][w] = s;
     __syncthreads();
-    const zd f = zmul(t, zadd(zadd(red[par][0], red[par][1]), zadd(red[par][2], red[par][3])));
+    const Z f = A::neg(A::mul(A::mk(t), A::add(A::add(red[par][0], red[par][1]), A::add(red[par][2], red[par][3]))));
     par ^= 1;
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
       const int blk = w + 4 * q;
       if (blk < blo || blk >= nblk) continue;
-      x[q] = zsub(x[q], zmul(vr[q], f));
+      x[q] = A::mac(x[q], vr[q], f);
     }
   }
   if (fresh)
@@ -297,7 +302,7 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
 #pragma unroll
   for (int q = 0; q < BQR_QW; ++q) {
     const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
-    if (blk < nblk && r < N) col[r] = x[q];
+    if (blk < nblk && r < N) col[r] = A::wide(x[q]);
   }
 }
 
@@ -355,7 +360,8 @@ __global__ void __launch_bounds__(256) k_bqr_finish(zd* A, long long lda, long l
 // D = |R_jj|, info.psign; k_bqr_finish then normalises and forms the products.
 struct QRRowsParams {
   const zd* Ain;             // input (may equal A)
-  zd* A; long long lda, sA;  // output
+  zd* A; long long lda, sA;  // output: R above the diagonal, reflectors below (FP64)
+  void* Araw;                // optional: the same in the kernel's arithmetic (for k_bqr_apply)
   int N;
   const double* colscale; long long sCS;
   zd* tau; long long sT;
@@ -366,100 +372,145 @@ struct QRRowsParams {
 
 static inline size_t qrr_smem_bytes(int N, int CL) {
   const size_t nrl = (size_t)((N + CL - 1) / CL);
-  return nrl * N * sizeof(zd) + 6ull * N * sizeof(zd) + 2ull * N * sizeof(double) + (size_t)N * sizeof(int) +
-         nrl * sizeof(zd) + 64;
+  const size_t npad = (size_t)((N + 1) & ~1);  // keeps the 16-byte arrays after it aligned
+  return nrl * N * 16 + 6ull * N * 16 + 2ull * N * 8 + npad * 8 + (size_t)N * sizeof(int) + nrl * 16 + 64;
 }
 
-ALF_DEV void qrr_argmax(double& v, int& i) {  // warp argmax, first index on ties
+template <class Z>
+ALF_DEV Z dsm_ld16(uint32_t addr) {  // 16-byte value from a peer CTA's shared memory
+  const double v[2] = {dsmem_ld_f64(addr), dsmem_ld_f64(addr + 8)};
+  Z z;
+  memcpy(&z, v, 16);
+  return z;
+}
+
+template <class A>
+ALF_DEV void qrr_argmax(typename A::R& v, int& i) {  // warp argmax, first index on ties
   for (int o = 16; o > 0; o >>= 1) {
-    const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const typename A::R ov = A::rshfl_xor(v, o);
     const int oi = __shfl_xor_sync(0xffffffffu, i, o);
-    if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
+    if (A::gt(ov, v) || (!A::gt(v, ov) && oi < i)) { v = ov; i = oi; }
   }
 }
 
+// Arithmetic A: ArD (FP64) or ArF (double-float).  A norm of -1 marks a column whose
+// norm is recomputed in the extra exchange of the step.
+// Column scales: FP64 multiplies A(:,c) by colscale_c on load, like QDRP's caller.
+// Double-float has FP32's exponent range, and the UDV scales reach far beyond it, so
+// ArF factors the unscaled columns instead: with the same pivots QR(U D) = Q (R_U D)
+// (a Householder reflector does not change when its column is scaled), so only the
+// pivot keys ||U_c|| d_c (FP64), D and the R output carry the scales.
+template <class A>
 __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
+  typedef typename A::Z Z;
+  typedef typename A::R R;
   const unsigned rank = cluster_ctarank(), CL = cluster_nctarank();
   const int b = blockIdx.y, N = p.N, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrl = (N + (int)CL - 1) / (int)CL;
   const int nmine = (N - (int)rank + (int)CL - 1) / (int)CL;  // rows rank, rank+CL, ...
   extern __shared__ __align__(16) unsigned char qrr_raw[];
-  zd* Ar = reinterpret_cast<zd*>(qrr_raw);  // [nrl][N] row-major: Ar[il*N + c] = A(rank + il*CL, c)
-  zd* xs = Ar + (size_t)nrl * N;           // [2][N] partial sums (read remotely)
-  zd* xr = xs + 2 * N;                     // [2][N] pivot row (owner)
-  zd* tot = xr + 2 * N;                    // [N]
-  zd* prow = tot + N;                      // [N]
-  double* vn1 = reinterpret_cast<double*>(prow + N);
-  double* vn2 = vn1 + N;
-  zd* vsh = reinterpret_cast<zd*>(vn2 + N);  // [nrl]
+  Z* Ar = reinterpret_cast<Z*>(qrr_raw);  // [nrl][N] row-major: Ar[il*N + c] = A(rank + il*CL, c)
+  Z* xs = Ar + (size_t)nrl * N;           // [2][N] partial sums (read remotely)
+  Z* xr = xs + 2 * N;                     // [2][N] pivot row (owner)
+  Z* tot = xr + 2 * N;                    // [N]
+  Z* prow = tot + N;                      // [N]
+  R* vn1 = reinterpret_cast<R*>(prow + N);
+  R* vn2 = vn1 + N;
+  double* cs = reinterpret_cast<double*>(vn2 + N);  // [N] column scales (ArF), padded to even length
+  Z* vsh = reinterpret_cast<Z*>(cs + ((N + 1) & ~1));  // [nrl], 16-byte aligned
   int* jp = reinterpret_cast<int*>(vsh + nrl);
-  __shared__ double s_bv[8];
+  constexpr bool sep = A::kDoubleFloat;
+  const bool scaled = p.colscale != nullptr;
+  __shared__ R s_bv[8];
+  __shared__ double s_bvd[8];
   __shared__ int s_bi[8], s_pv, s_cnt;
-  const double tol3z = 1.0536712127723509e-08;  // sqrt(dlamch('Epsilon'))
-  zd* A = p.A + b * p.sA;
+  const R tol3z = A::mkr(1.0536712127723509e-08);  // sqrt(dlamch('Epsilon'))
+  const R mone = A::mkr(-1.0);
+  zd* Aout = p.A + b * p.sA;
   const long long lda = p.lda;
 
   for (long long e = tid; e < (long long)nmine * N; e += 256) {
     const int il = (int)(e / N), c = (int)(e % N);
     zd v = p.Ain[b * p.sA + (rank + (long long)il * CL) + c * lda];
-    if (p.colscale) v = zscale(v, p.colscale[b * p.sCS + c]);
-    Ar[(size_t)il * N + c] = v;
+    if (scaled && !sep) v = zscale(v, p.colscale[b * p.sCS + c]);
+    Ar[(size_t)il * N + c] = A::mk(v);
   }
+  for (int c = tid; c < N; c += 256) cs[c] = (scaled && sep) ? fabs(p.colscale[b * p.sCS + c]) : 1.0;
   __syncthreads();
   // initial column norms: exchange 0
   for (int c = tid; c < N; c += 256) {
-    double s0 = 0.0, s1 = 0.0;
+    R s0 = A::rzero(), s1 = A::rzero();
     int il = 0;
     for (; il + 1 < nmine; il += 2) {
-      const zd a = Ar[(size_t)il * N + c], d = Ar[(size_t)(il + 1) * N + c];
-      s0 = fma(a.x, a.x, fma(a.y, a.y, s0));
-      s1 = fma(d.x, d.x, fma(d.y, d.y, s1));
+      s0 = A::radd(s0, A::abs2(Ar[(size_t)il * N + c]));
+      s1 = A::radd(s1, A::abs2(Ar[(size_t)(il + 1) * N + c]));
     }
-    if (il < nmine) { const zd a = Ar[(size_t)il * N + c]; s0 = fma(a.x, a.x, fma(a.y, a.y, s0)); }
-    xs[c] = zmk(s0 + s1, 0.0);
+    if (il < nmine) s0 = A::radd(s0, A::abs2(Ar[(size_t)il * N + c]));
+    xs[c] = A::mkz(A::radd(s0, s1), A::rzero());
     jp[c] = c + 1;
   }
   cluster_sync();
   for (int c = tid; c < N; c += 256) {
-    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    Z s[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
 #pragma unroll
     for (int q = 0; q < 16; ++q)
-      if (q < (int)CL) s[q & 3] += dsmem_ld_f64(dsmem_addr(&xs[c], q));
-    const double nrm = sqrt((s[0] + s[1]) + (s[2] + s[3]));
+      if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xs[c], q)));
+    const R nrm = A::rsqrt_(A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3]))));
     vn1[c] = nrm; vn2[c] = nrm;
   }
   int par = 1;
   __syncthreads();
 
   for (int j = 0; j < N; ++j) {
-    // pivot: first maximum of vn1[j..N)
-    double bv = -1.0;
-    int bi = N;
-    for (int c = j + tid; c < N; c += 256) {
-      const double v = vn1[c];
-      if (v > bv) { bv = v; bi = c; }
+    // pivot: first maximum of the norms vn1[j..N) (times the column scales, ArF)
+    int pv;
+    if (sep && scaled) {
+      double bv = -1.0;
+      int bi = N;
+      for (int c = j + tid; c < N; c += 256) {
+        const double v = A::rwide(vn1[c]) * cs[c];
+        if (v > bv) { bv = v; bi = c; }
+      }
+      qrr_argmax<ArD>(bv, bi);
+      if (lane == 0) { s_bvd[warp] = bv; s_bi[warp] = bi; }
+      __syncthreads();
+      if (tid == 0) {
+        double v = s_bvd[0];
+        int i = s_bi[0];
+        for (int w = 1; w < 8; ++w)
+          if (s_bvd[w] > v || (s_bvd[w] == v && s_bi[w] < i)) { v = s_bvd[w]; i = s_bi[w]; }
+        s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
+      }
+    } else {
+      R bv = mone;
+      int bi = N;
+      for (int c = j + tid; c < N; c += 256) {
+        const R v = vn1[c];
+        if (A::gt(v, bv)) { bv = v; bi = c; }
+      }
+      qrr_argmax<A>(bv, bi);
+      if (lane == 0) { s_bv[warp] = bv; s_bi[warp] = bi; }
+      __syncthreads();
+      if (tid == 0) {
+        R v = s_bv[0];
+        int i = s_bi[0];
+        for (int w = 1; w < 8; ++w)
+          if (A::gt(s_bv[w], v) || (!A::gt(v, s_bv[w]) && s_bi[w] < i)) { v = s_bv[w]; i = s_bi[w]; }
+        s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
+      }
     }
-    qrr_argmax(bv, bi);
-    if (lane == 0) { s_bv[warp] = bv; s_bi[warp] = bi; }
     __syncthreads();
-    if (tid == 0) {
-      double v = s_bv[0];
-      int i = s_bi[0];
-      for (int w = 1; w < 8; ++w)
-        if (s_bv[w] > v || (s_bv[w] == v && s_bi[w] < i)) { v = s_bv[w]; i = s_bi[w]; }
-      s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
-    }
-    __syncthreads();
-    const int pv = s_pv;
+    pv = s_pv;
     if (pv != j) {
       for (int il = tid; il < nmine; il += 256) {
-        const zd t = Ar[(size_t)il * N + pv];
+        const Z t = Ar[(size_t)il * N + pv];
         Ar[(size_t)il * N + pv] = Ar[(size_t)il * N + j];
         Ar[(size_t)il * N + j] = t;
       }
       if (tid == 0) {
         const int t = jp[pv]; jp[pv] = jp[j]; jp[j] = t;
         vn1[pv] = vn1[j]; vn2[pv] = vn2[j];
+        const double ts = cs[pv]; cs[pv] = cs[j]; cs[j] = ts;
       }
       __syncthreads();
     }
@@ -467,47 +518,43 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
     const unsigned owner = (unsigned)(j % (int)CL);
     const int ilj = j / (int)CL;
     const int il0 = (j >= (int)rank) ? (j - (int)rank) / (int)CL + 1 : 0;  // first own row > j
-    zd* xsp = xs + par * N;
-    zd* xrp = xr + par * N;
+    Z* xsp = xs + par * N;
+    Z* xrp = xr + par * N;
     for (int c = j + tid; c < N; c += 256) {
-      zd s0 = zmk(0.0, 0.0), s1 = s0;
+      Z s0 = A::zero(), s1 = s0;
       int il = il0;
       for (; il + 1 < nmine; il += 2) {
-        s0 = zadd(s0, zmul(zconj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]));
-        s1 = zadd(s1, zmul(zconj(Ar[(size_t)(il + 1) * N + j]), Ar[(size_t)(il + 1) * N + c]));
+        s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
+        s1 = A::mac(s1, A::conj(Ar[(size_t)(il + 1) * N + j]), Ar[(size_t)(il + 1) * N + c]);
       }
-      if (il < nmine) s0 = zadd(s0, zmul(zconj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]));
-      xsp[c] = zadd(s0, s1);
+      if (il < nmine) s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
+      xsp[c] = A::add(s0, s1);
       if (rank == owner) xrp[c] = Ar[(size_t)ilj * N + c];
     }
     cluster_sync();
     for (int c = j + tid; c < N; c += 256) {
-      zd s[4] = {zmk(0.0, 0.0), zmk(0.0, 0.0), zmk(0.0, 0.0), zmk(0.0, 0.0)};
+      Z s[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
 #pragma unroll
       for (int q = 0; q < 16; ++q)
-        if (q < (int)CL) {
-          const uint32_t a = dsmem_addr(&xsp[c], q);
-          s[q & 3] = zadd(s[q & 3], zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8)));
-        }
-      tot[c] = zadd(zadd(s[0], s[1]), zadd(s[2], s[3]));
-      const uint32_t a = dsmem_addr(&xrp[c], owner);
-      prow[c] = zmk(dsmem_ld_f64(a), dsmem_ld_f64(a + 8));
+        if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xsp[c], q)));
+      tot[c] = A::add(A::add(s[0], s[1]), A::add(s[2], s[3]));
+      prow[c] = dsm_ld16<Z>(dsmem_addr(&xrp[c], owner));
     }
     par ^= 1;
     __syncthreads();
     // ZLARFG on (alpha, x), x = A(j+1:N, j)
-    const zd alpha = prow[j];
-    const double xn2 = tot[j].x;
-    const bool trivial = (xn2 == 0.0 && alpha.y == 0.0);
-    double beta = alpha.x;
-    zd t = zmk(0.0, 0.0), scal = zmk(0.0, 0.0);
+    const Z alpha = prow[j];
+    const R xn2 = A::re(tot[j]);
+    const bool trivial = A::rzero_p(xn2) && A::rzero_p(A::im(alpha));
+    R beta = A::re(alpha);
+    Z t = A::zero(), scal = A::zero();
     if (!trivial) {
-      beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn2))), alpha.x);
-      const double ib = bqr_rcp(beta);
-      t = zmk((beta - alpha.x) * ib, -alpha.y * ib);
-      scal = bqr_zrcp(zmk(alpha.x - beta, alpha.y));
+      beta = A::rneg(A::rcopysign(A::rsqrt_(A::radd(A::abs2(alpha), xn2)), A::re(alpha)));
+      const R ib = A::rrcp(beta);
+      t = A::mkz(A::mulr(A::rsub(beta, A::re(alpha)), ib), A::rneg(A::mulr(A::im(alpha), ib)));
+      scal = A::rcp(A::mkz(A::rsub(A::re(alpha), beta), A::im(alpha)));
     }
-    for (int il = il0 + tid; il < nmine; il += 256) vsh[il] = zmul(scal, Ar[(size_t)il * N + j]);
+    for (int il = il0 + tid; il < nmine; il += 256) vsh[il] = A::mul(scal, Ar[(size_t)il * N + j]);
     __syncthreads();
     // H^H on columns c > j (a_c -= conj(tau) v (v^H a_c)), reflector into column j,
     // and the norm downdate with the updated pivot-row entry
@@ -516,65 +563,68 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
       if (c == j) {
         if (!trivial) {
           for (int il = il0; il < nmine; ++il) Ar[(size_t)il * N + j] = vsh[il];
-          if (rank == owner) Ar[(size_t)ilj * N + j] = zmk(beta, 0.0);
+          if (rank == owner) Ar[(size_t)ilj * N + j] = A::mkz(beta, A::rzero());
         }
         continue;
       }
-      zd anew = prow[c];
+      Z anew = prow[c];
       if (!trivial) {
-        const zd f = zmul(zconj(t), zadd(prow[c], zmul(zconj(scal), tot[c])));
+        const Z f = A::mul(A::conj(t), A::mac(prow[c], A::conj(scal), tot[c]));
+        const Z nf = A::neg(f);
         for (int il = il0; il < nmine; ++il)
-          Ar[(size_t)il * N + c] = zsub(Ar[(size_t)il * N + c], zmul(vsh[il], f));
-        anew = zsub(anew, f);
+          Ar[(size_t)il * N + c] = A::mac(Ar[(size_t)il * N + c], vsh[il], nf);
+        anew = A::sub(anew, f);
         if (rank == owner) Ar[(size_t)ilj * N + c] = anew;
       }
-      const double v1 = vn1[c];
-      if (v1 != 0.0) {
-        const double r = zabs(anew) * bqr_rcp(v1);
-        const double temp = fmax(1.0 - r * r, 0.0);
-        const double q = v1 * bqr_rcp(vn2[c]);
-        const double temp2 = temp * q * q;
-        if (temp2 <= tol3z) {
-          if (j < N - 1) { need = 1; vn1[c] = -1.0; }  // recomputed below
-          else { vn1[c] = 0.0; vn2[c] = 0.0; }
+      const R v1 = vn1[c];
+      if (!A::rzero_p(v1)) {
+        const R iv = A::rrcp(v1);
+        const R temp = A::rmax0(A::rsub(A::mkr(1.0), A::mulr(A::abs2(anew), A::mulr(iv, iv))));
+        const R q = A::mulr(v1, A::rrcp(vn2[c]));
+        const R temp2 = A::mulr(temp, A::mulr(q, q));
+        if (!A::gt(temp2, tol3z)) {
+          if (j < N - 1) { need = 1; vn1[c] = mone; }  // recomputed below
+          else { vn1[c] = A::rzero(); vn2[c] = A::rzero(); }
         } else {
-          vn1[c] = v1 * sqrt(temp);
+          vn1[c] = A::mulr(v1, A::rsqrt_(temp));
         }
       }
     }
     if (rank == owner && tid == 0) {
-      p.tau[b * p.sT + j] = t;
-      p.D[b * p.sD + j] = trivial ? zabs(alpha) : fabs(beta);
+      p.tau[b * p.sT + j] = A::wide(t);
+      p.D[b * p.sD + j] = (trivial ? sqrt(A::rwide(A::abs2(alpha))) : fabs(A::rwide(beta))) * cs[j];
     }
     if (__syncthreads_or(need)) {
       // exact norms of the flagged columns over rows > j (post-update)
-      zd* xq = xs + par * N;
+      Z* xq = xs + par * N;
       for (int c = j + 1 + tid; c < N; c += 256) {
-        double s0 = 0.0;
-        if (vn1[c] < 0.0)
-          for (int il = il0; il < nmine; ++il) {
-            const zd a = Ar[(size_t)il * N + c];
-            s0 = fma(a.x, a.x, fma(a.y, a.y, s0));
-          }
-        xq[c] = zmk(s0, 0.0);
+        R s0 = A::rzero();
+        if (A::rneg_p(vn1[c]))
+          for (int il = il0; il < nmine; ++il) s0 = A::radd(s0, A::abs2(Ar[(size_t)il * N + c]));
+        xq[c] = A::mkz(s0, A::rzero());
       }
       cluster_sync();
       for (int c = j + 1 + tid; c < N; c += 256) {
-        if (vn1[c] >= 0.0) continue;
-        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        if (!A::rneg_p(vn1[c])) continue;
+        Z s[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
 #pragma unroll
         for (int q = 0; q < 16; ++q)
-          if (q < (int)CL) s[q & 3] += dsmem_ld_f64(dsmem_addr(&xq[c], q));
-        const double nrm = sqrt((s[0] + s[1]) + (s[2] + s[3]));
+          if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xq[c], q)));
+        const R nrm = A::rsqrt_(A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3]))));
         vn1[c] = nrm; vn2[c] = nrm;
       }
       par ^= 1;
       __syncthreads();
     }
   }
+  Z* raw = p.Araw ? reinterpret_cast<Z*>(p.Araw) + b * p.sA : nullptr;
   for (long long e = tid; e < (long long)nmine * N; e += 256) {
     const int il = (int)(e / N), c = (int)(e % N);
-    A[(rank + (long long)il * CL) + c * lda] = Ar[(size_t)il * N + c];
+    const long long g = (rank + (long long)il * CL) + c * lda;
+    const Z v = Ar[(size_t)il * N + c];
+    const long long i = rank + (long long)il * CL;
+    Aout[g] = (i <= c) ? zscale(A::wide(v), cs[c]) : A::wide(v);  // R part carries the scales
+    if (raw) raw[g] = v;
   }
   if (rank == 0) {
     if (tid == 0) s_cnt = 0;

@@ -29,7 +29,7 @@
 // Newton iteration, and the phase stays unnormalised until the block ends.
 #pragma once
 #include "common.cuh"
-#include "dfloat.cuh"
+#include "arith.cuh"
 
 #define UPD_KMAX 32
 #define UPD_THREADS 256
@@ -78,83 +78,6 @@ ALF_DEV int nranf3(double r) {
 // (Upgrade2's Mat(1,1) = myexp - dlt G(P,P), Hamiltonian_main_mod.F90 ratio factors).
 struct UpdTab {
   zd myexp, dlt, expal;
-};
-
-// Scalar arithmetic of the update kernel.  ArD: FP64 complex (the plain form:
-// the ratios must agree with an FP64 reference to ~1e-10 even where
-// 1 + Delta (1 - G_jj) cancels).  ArF: double-float (the mixed form).
-struct ArD {
-  typedef zd Z;
-  typedef double R;
-  static ALF_DEV Z mk(zd a) { return a; }
-  static ALF_DEV zd wide(Z a) { return a; }
-  static ALF_DEV R mkr(double a) { return a; }
-  static ALF_DEV Z one() { return zmk(1.0, 0.0); }
-  static ALF_DEV Z zero() { return zmk(0.0, 0.0); }
-  static ALF_DEV Z mul(Z a, Z b) { return zmul(a, b); }
-  static ALF_DEV Z sub(Z a, Z b) { return zsub(a, b); }
-  static ALF_DEV Z add(Z a, Z b) { return zadd(a, b); }
-  static ALF_DEV Z neg(Z a) { return zmk(-a.x, -a.y); }
-  static ALF_DEV Z mac(Z c, Z a, Z b) { return zadd(c, zmul(a, b)); }
-  static ALF_DEV Z scale(Z a, R s) { return zscale(a, s); }
-  static ALF_DEV R re_mul(Z a, Z b) { return a.x * b.x - a.y * b.y; }
-  static ALF_DEV R re(Z a) { return a.x; }
-  static ALF_DEV R absr(R a) { return fabs(a); }
-  static ALF_DEV R mulr(R a, R b) { return a * b; }
-  static ALF_DEV bool gt(R a, R b) { return a > b; }
-  // 1/d, d > 0 real: float seed, two Newton-Raphson steps r <- r + r (1 - d r) (quadratic
-  // convergence, 2^-24 -> 2^-48 -> below 2^-53); an FP64 division costs ~560 cycles here.
-  static ALF_DEV double rcp_pos(double d) {
-    if (!(d > 1e-30 && d < 1e30)) return 1.0 / d;
-    double r = (double)__frcp_rn(__double2float_rn(d));
-    r = fma(r, fma(-d, r, 1.0), r);
-    return fma(r, fma(-d, r, 1.0), r);
-  }
-  static ALF_DEV Z rcp(Z a) {
-    const double s = rcp_pos(a.x * a.x + a.y * a.y);
-    return zmk(a.x * s, -a.y * s);
-  }
-  // positive rescaling towards |a| ~ 1 (direction unchanged)
-  static ALF_DEV Z renorm(Z a) {
-    const float m2 = __double2float_rn(a.x * a.x + a.y * a.y);
-    return (m2 > 0.f && m2 < 3e38f) ? zscale(a, (double)rsqrtf(m2)) : a;
-  }
-  static ALF_DEV zd unit(Z a) { const double r = sqrt(a.x * a.x + a.y * a.y); return zmk(a.x / r, a.y / r); }
-  static ALF_DEV Z shfl(Z a, int src) {
-    return zmk(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));
-  }
-};
-struct ArF {
-  typedef dfz Z;
-  typedef dff R;
-  static ALF_DEV Z mk(zd a) { return dz_make(a); }
-  static ALF_DEV zd wide(Z a) { return dz_wide(a); }
-  static ALF_DEV R mkr(double a) { return df_make(a); }
-  static ALF_DEV Z one() { return dfz{{1.f, 0.f}, {0.f, 0.f}}; }
-  static ALF_DEV Z zero() { return dfz{{0.f, 0.f}, {0.f, 0.f}}; }
-  static ALF_DEV Z mul(Z a, Z b) { return dz_mul(a, b); }
-  static ALF_DEV Z sub(Z a, Z b) { return dz_sub(a, b); }
-  static ALF_DEV Z add(Z a, Z b) { return dz_add(a, b); }
-  static ALF_DEV Z neg(Z a) { return dfz{df_neg(a.r), df_neg(a.i)}; }
-  static ALF_DEV Z mac(Z c, Z a, Z b) { return dz_mac(c, a, b); }
-  static ALF_DEV Z scale(Z a, R s) { return dz_scale(a, s); }
-  static ALF_DEV R re_mul(Z a, Z b) { return df_dot2(a.r, b.r, df_neg(a.i), b.i); }
-  static ALF_DEV R re(Z a) { return a.r; }
-  static ALF_DEV R absr(R a) { return df_abs(a); }
-  static ALF_DEV R mulr(R a, R b) { return df_mul(a, b); }
-  static ALF_DEV bool gt(R a, R b) { return df_gt(a, b); }
-  static ALF_DEV Z rcp(Z a) { return dz_rcp(a); }
-  static ALF_DEV Z renorm(Z a) {
-    const float m2 = a.r.h * a.r.h + a.i.h * a.i.h;
-    return (m2 > 0.f && m2 < 3e38f) ? dz_scale(a, df_f(rsqrtf(m2))) : a;
-  }
-  static ALF_DEV zd unit(Z a) { return dz_wide(dz_unit(a)); }
-  static ALF_DEV Z shfl(Z a, int src) {
-    Z r;
-    r.r.h = __shfl_sync(0xffffffffu, a.r.h, src); r.r.l = __shfl_sync(0xffffffffu, a.r.l, src);
-    r.i.h = __shfl_sync(0xffffffffu, a.i.h, src); r.i.l = __shfl_sync(0xffffffffu, a.i.l, src);
-    return r;
-  }
 };
 
 // One CTA of UPD_THREADS threads per chain.  Dynamic shared memory:

@@ -28,6 +28,9 @@ FLAG_DF_PROPAGATION = 1
 FLAG_EXACT_QRP = 2
 FLAG_EXACT_QRP_CGR = 4
 FLAG_EXACT_QRP_DECOMPOSE = 8
+FLAG_DF_STAB_QR = 16
+FLAG_DF_STAB_GEMM = 32
+FLAG_DF_STAB = 48
 PIVOTING = {"norms": 0, "exact": FLAG_EXACT_QRP, "exact-cgr": FLAG_EXACT_QRP_CGR,
             "exact-decompose": FLAG_EXACT_QRP_DECOMPOSE}
 
@@ -39,7 +42,7 @@ def _p(a: np.ndarray):
 class Chains:
     def __init__(self, model: Model, n_chains: int = 1, precision: str = "fp64", delay_k: int = 0,
                  device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None,
-                 pivoting: str = "norms", flags: int = 0):
+                 pivoting: str = "exact", flags: int = 0):
         """``pivoting``: "norms" orders the columns of every stabilisation QR once by
         their norms (ALF's STABLOG pivoting) and factors them with the blocked QR;
         "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)."""

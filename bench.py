@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="hubbard16x16")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--pivoting", default="norms", choices=["norms", "exact", "exact-cgr", "exact-decompose"])
+    ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
+    ap.add_argument("--pivoting", default="exact", choices=["norms", "exact", "exact-cgr", "exact-decompose"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -132,7 +133,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     m = mdl.config(args.config)
     seed = args.seed + 1000 * rank
-    ch = Chains(m, n_chains=1, precision=args.precision, device=local, pivoting=args.pivoting)
+    ch = Chains(m, n_chains=1, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags)
     ch.set_fields(0, rng.initial_fields(seed, 0, m.n_op, m.ltrot))
     ch.init_state()
     ch.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
@@ -214,7 +215,7 @@ def main():
     workload = {"workload": f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
                             f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
                             f"Nwrap={m.nwrap}, Mz four-valued fields, one chain per GPU",
-                "chains_per_gpu": 1, "precision": args.precision, "pivoting": args.pivoting, "l2": "flushed between timed steps (256 MB write)",
+                "chains_per_gpu": 1, "precision": args.precision, "pivoting": args.pivoting, "flags": args.flags, "l2": "flushed between timed steps (256 MB write)",
                 "draws": "device counter stream (value); host arrays through the C ABI (e2e)"}
     if args.impl == "reference":
         if rank != 0:

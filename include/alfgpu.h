@@ -71,6 +71,13 @@ enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
  * _DECOMPOSE select it for the QR of CGR (cgr1_mod.F90:223) or of
  * decompose_UDV_state only.  ZGEQP3 pivoting is always used for Ndim > 512. */
 enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_EXACT_QRP_CGR = 4, ALFGPU_FLAG_EXACT_QRP_DECOMPOSE = 8 };
+/* Mixed form only, opt-in: run parts of the stabilisation in double-float instead of
+ * FP64.  _QR: the pivoted QR and explicit Q of decompose_UDV_state (the columns are
+ * factored unscaled, exact in exponent range); _GEMM: the UDV propagation, decompose
+ * and CGR products.  Measured on the 16x16 beta = 10 Hubbard chain, Precision Green
+ * rises from 2.5e-6 (FP64) to 7.9e-6 (_QR) and 2.1e-5 (both): double-float keeps 48
+ * of FP64's 53 mantissa bits, and the UDV products amplify rounding. */
+enum { ALFGPU_FLAG_DF_STAB_QR = 16, ALFGPU_FLAG_DF_STAB_GEMM = 32, ALFGPU_FLAG_DF_STAB = 48 };
 
 typedef struct alfgpu_s alfgpu_t;
 

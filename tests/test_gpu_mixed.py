@@ -1,7 +1,7 @@
-"""Mixed-precision form (double-float G wraps and delayed-update flush GEMMs on
-the FP32 pipes; complex128 storage; FP64 UDV propagation, pivoted QR, CGR and
-ratio/phase arithmetic) against the FP64 CPU oracle on the same fields and
-draws.
+"""Mixed-precision form (double-float G wraps, delayed-update flush GEMMs and
+per-visit Metropolis arithmetic on the FP32 pipes; complex128 storage; FP64 UDV
+propagation, pivoted QR and CGR) against the FP64 CPU oracle on the same fields
+and draws.
 
 Acceptance bound: max |G_mixed - G_fp64| <= 1e-5 at every stabilisation point
 (the freshly computed CGR result) while the accept/reject sequences agree, and
@@ -19,12 +19,12 @@ pytestmark = pytest.mark.gpu
 BOUND = 1e-5
 
 
-def _compare(m, seed, sweeps):
+def _compare(m, seed, sweeps, flags=0):
     f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
     o = oracle.Oracle(m)
     o.set_fields(f0)
     o.init_state()
-    g = Chains(m, precision="mixed")
+    g = Chains(m, precision="mixed", flags=flags)
     g.set_fields(0, f0)
     g.init_state()
     assert np.max(np.abs(g.green(0) - o.green())) < BOUND
@@ -70,4 +70,18 @@ def test_mixed_hubbard_8x8_vs_fp64_oracle():
 def test_mixed_honeycomb_vs_fp64_oracle():
     m = mdl.hubbard("honeycomb", 3, 3, U=5.0, beta=2.0, dtau=0.05, nwrap=5)
     w = _compare(m, seed=3, sweeps=2)
+    assert w < BOUND
+
+
+def test_mixed_hubbard_16x16_vs_fp64_oracle():
+    # the 16x16 (N_dim = 256) beta = 10 configuration, one sweep: 20 stabilisation points
+    w = _compare(mdl.config("hubbard16x16"), seed=1, sweeps=1)
+    assert w < BOUND
+
+
+def test_mixed_double_float_stabilisation_small():
+    # opt-in double-float QR and stabilisation products (scale-free column factoring)
+    from alf_gb300.sweep import FLAG_DF_STAB
+    w = _compare(mdl.hubbard("square", 8, 8, U=4.0, beta=4.0, dtau=0.1, nwrap=10), seed=2, sweeps=1,
+                 flags=FLAG_DF_STAB)
     assert w < BOUND

@@ -98,7 +98,7 @@ def _variant_ratios(m, f0, seed, sweeps, chain):
         oracle.set_variant(0)
 
 
-def _run_pair(m, seed=5, sweeps=1, chain=0, pivoting="norms"):
+def _run_pair(m, seed=5, sweeps=1, chain=0, pivoting="exact"):
     f0 = rng.initial_fields(seed, chain, m.n_op, m.ltrot)
     var = _variant_ratios(m, f0, seed, sweeps, chain)
     o = oracle.Oracle(m)
@@ -146,10 +146,12 @@ def test_init_and_sweep_hubbard_4x4_parity(pivoting):
     _run_pair(mdl.config("hubbard4x4"), sweeps=3, pivoting=pivoting)
 
 
-def test_sweep_hubbard_8x8_parity():
-    # 8x8 (N_dim = 64): four panels of the blocked QR on a 4-CTA cluster
+@pytest.mark.parametrize("pivoting", ["exact", "norms"])
+def test_sweep_hubbard_8x8_parity(pivoting):
+    # 8x8 (N_dim = 64): exact pivoting on a 4-CTA cluster; norm pivoting runs the
+    # blocked QR (two panels)
     m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
-    _run_pair(m, seed=4, sweeps=1)
+    _run_pair(m, seed=4, sweeps=1, pivoting=pivoting)
 
 
 def test_sweep_hubbard_odd_sizes_parity():
