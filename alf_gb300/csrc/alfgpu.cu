@@ -22,6 +22,7 @@
 #include "kernels_misc.cuh"
 #include "linalg.cuh"
 #include "update.cuh"
+#include "tau.cuh"
 
 namespace {
 
@@ -42,6 +43,19 @@ struct alfgpu_s {
   int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
   int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
   int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
+  // time-displaced Green functions (ltau = 1)
+  int ltau = 0;
+  zd *GT0 = nullptr, *G0T = nullptr, *G00 = nullptr, *GTT = nullptr, *Hn[4] = {nullptr, nullptr, nullptr, nullptr};
+  UDVSet udvr_tau;
+  zd *HB1 = nullptr, *HB2 = nullptr, *HLP = nullptr, *tau2 = nullptr, *V1I = nullptr, *Qt = nullptr;
+  int *jpvt2 = nullptr, *first2 = nullptr;
+  double *D3 = nullptr, *vn2 = nullptr, *cmp_tau = nullptr;
+  QRInfo* info2 = nullptr;
+  // measurement staging (pinned host memory, allocated on first use)
+  double* obs_host = nullptr;
+  double* tau_host = nullptr;
+  double* phase_host = nullptr;
+  zd* Gq = nullptr;  // [chain][4][F][N][N] device staging of the ObserT quartet
   int df_stab = 0;                   // mixed form: stabilisation products in double-float
   int df_qr = 0;                     // mixed form: decompose QR and Q formation in double-float
   int qr_df = 0;                     // the last QR left double-float reflectors in QRdf
@@ -357,7 +371,7 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
       BQRApply ap;
       ap.V = Aout; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
       ap.C = Aout; ap.ldc = N; ap.sC = NN;
-      ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0 + w; ap.conj_tau = 1;
+      ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0 + w; ap.conj_tau = 1; ap.init = 0;
       k_bqr_apply<ArD><<<dim3(N - j0 - w, B), 128, 0, h->st>>>(ap);
       CKL();
     }
@@ -373,7 +387,7 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
 static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
-  if (N > 32 * BQR_LROWS) {
+  if (N > 32 * BQR_LROWS) {  // beyond the rows a lane of k_bqr_apply holds
     RET(copy_mats(h, Q, F, (size_t)B * NN));
     return launch_orgqr(h, Q, B);
   }
@@ -383,7 +397,7 @@ static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
     BQRApply ap;
     ap.V = h->qr_df ? (const void*)h->QRdf : (const void*)F; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
     ap.C = Q; ap.ldc = N; ap.sC = NN;
-    ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0; ap.conj_tau = 0;
+    ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0; ap.conj_tau = 0; ap.init = 1;
     if (h->qr_df) k_bqr_apply<ArF><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
     else k_bqr_apply<ArD><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
     CKL();
@@ -448,22 +462,23 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
 }
 
 // WRAPUR (wrapur_mod.F90:101-124): U <- prod_nt [D_nt expT] U, then decompose (side R)
-static int wrapur(alfgpu_s* h, int ntau, int ntau1) {
+static int wrapur_u(alfgpu_s* h, UDVSet& u, int ntau, int ntau1) {
   const int N = h->N, B = h->B;
   prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
     RET(slice_scale(h, nt));
     GemmParams p = gsq(h, B);
     p.A = h->expT; p.realA = 1; p.modA = h->F;
-    p.B = h->udvr.U; p.C = h->T1;
+    p.B = u.U; p.C = h->T1;
     p.rs = h->S; p.sRS = N;
     if (h->mixed_propagate) RET(gemm32(h, p, ST_R64, ST_C128, ST_C128));
     else RET(gemm_s(h, p));
-    RET(copy_mats(h, h->udvr.U, h->T1, (size_t)B * N * N));
+    RET(copy_mats(h, u.U, h->T1, (size_t)B * N * N));
   }
   prof_end(h);
-  return decompose(h, h->udvr, 0);
+  return decompose(h, u, 0);
 }
+static int wrapur(alfgpu_s* h, int ntau, int ntau1) { return wrapur_u(h, h->udvr, ntau, ntau1); }
 
 // WRAPUL (wrapul_mod.F90:108-131): U <- prod_nt [expT conj(D_nt)] U (descending nt), decompose (side L)
 static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
@@ -526,7 +541,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     p.rs = h->S; p.sRS = N; p.rsInv = 1;
     RET(gemm_s(h, p));
     // R y = RHS (ZTRSM L,U,N), columns of RHS
-    TrsvParams t;
+    TrsvParams t{};
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
     prof_begin(h, ALFGPU_PROF_SOLVE);
@@ -544,7 +559,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     p.cs = h->S; p.sCS = N; p.csInv = 1;
     RET(gemm_s(h, p));
     // y R^H = RHS (ZTRSM R,U,C): rows of RHS, conjugated, upper solve
-    TrsvParams t;
+    TrsvParams t{};
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 1;
     prof_begin(h, ALFGPU_PROF_SOLVE);
@@ -586,6 +601,205 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
   }
   k_stab_finish<<<(h->C + 127) / 128, 128, 0, h->st>>>(sp);
   CKL();
+  return 0;
+}
+
+// ---- measurements ---------------------------------------------------------------------------
+static int ensure_obs_host(alfgpu_s* h) {
+  const size_t NN = (size_t)h->N * h->N;
+  if (!h->obs_host) CK(cudaMallocHost(&h->obs_host, (size_t)h->B * NN * sizeof(zd)));
+  if (!h->phase_host) CK(cudaMallocHost(&h->phase_host, (size_t)h->C * sizeof(zd)));
+  if (h->ltau && !h->tau_host) CK(cudaMallocHost(&h->tau_host, 4 * (size_t)h->B * NN * sizeof(zd)));
+  return 0;
+}
+
+// ham%Obser(GR, PHASE, ntau1) for every chain (main.F90:757-772, 788-803).  With a pending
+// vertex scaling (up pass), G in ALF's frame is S G Sinv, formed into the work matrix Gw.
+static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pending) {
+  if (!cb) return 0;
+  RET(ensure_obs_host(h));
+  const long long NN = (long long)h->N * h->N;
+  const zd* src = h->G;
+  if (pending) {
+    RET(copy_mats(h, h->Gw, h->G, (size_t)h->B * NN));
+    dim3 grid((unsigned)((NN + 255) / 256), h->B);
+    k_apply_scale<<<grid, 256, 0, h->st>>>(h->Gw, h->S, h->Sinv, h->N);
+    CKL();
+    src = h->Gw;
+  }
+  CK(cudaMemcpyAsync(h->obs_host, src, (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->phase_host, h->phase, (size_t)h->C * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int c = 0; c < h->C; ++c)
+    cb(ctx, c, ntau1, 0, h->obs_host + (size_t)c * h->F * NN * 2, h->phase_host + 2 * c);
+  return 0;
+}
+
+// ham%ObserT(NT, GT0, G0T, G00, GTT, PHASE) for every chain (tau_m_mod.F90:116, 168)
+static int obs_tau(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int nt) {
+  if (!cb) return 0;
+  RET(ensure_obs_host(h));
+  const long long NN = (long long)h->N * h->N;
+  dim3 grid((unsigned)((NN + 255) / 256), h->B);
+  k_gather_quartet<<<grid, 256, 0, h->st>>>(h->GT0, h->G0T, h->G00, h->GTT, h->Gq, h->N, h->F);
+  CKL();
+  CK(cudaMemcpyAsync(h->tau_host, h->Gq, 4 * (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->phase_host, h->phase, (size_t)h->C * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int c = 0; c < h->C; ++c)
+    cb(ctx, c, nt, 1, h->tau_host + (size_t)c * 4 * h->F * NN * 2, h->phase_host + 2 * c);
+  return 0;
+}
+
+// ---- CGR2_2 ---------------------------------------------------------------------------------
+// Column-pivoted QR (ZGEQP3 semantics, cluster kernel) of the N2 x N2 matrices A in place.
+static int qrp_n(alfgpu_s* h, zd* A, int N2, zd* tau, int* jpvt, double* D, double* vn, QRInfo* info) {
+  QRParams q;
+  memset(&q, 0, sizeof(q));
+  q.A = A; q.lda = N2; q.sA = (long long)N2 * N2; q.N = N2;
+  q.tau = tau; q.sT = N2; q.jpvt = jpvt; q.sP = N2; q.D = D; q.sD = N2; q.vn = vn; q.sV = 2 * N2;
+  q.info = info;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(h->CL, h->B, 1);
+  cfg.blockDim = dim3(QR_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = (size_t)N2 * sizeof(zd);
+  cfg.stream = h->st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  h->launches++;
+  CK(cudaLaunchKernelEx(&cfg, k_qrp, q));
+  return 0;
+}
+
+// Q C for the reflectors of the factored N2 x N2 matrix F (ZUNMQR 'L','N'), all columns of C.
+static int unmqr_n(alfgpu_s* h, const zd* F, const zd* tau, zd* Cm, int N2) {
+  const long long NN2 = (long long)N2 * N2;
+  for (int j0 = ((N2 - 1) / BQR_NB) * BQR_NB; j0 >= 0; j0 -= BQR_NB) {
+    const int w = (N2 - j0 < BQR_NB) ? N2 - j0 : BQR_NB;
+    BQRApply ap;
+    ap.V = F; ap.ldv = N2; ap.sV = NN2; ap.tau = tau; ap.sT = N2;
+    ap.C = Cm; ap.ldc = N2; ap.sC = NN2;
+    ap.N = N2; ap.j0 = j0; ap.nb = w; ap.c0 = 0; ap.conj_tau = 0; ap.init = 0;
+    k_bqr_apply<ArD><<<dim3(N2, h->B), 128, 0, h->st>>>(ap);
+    CKL();
+  }
+  return 0;
+}
+
+// CGR2_2, default branch (cgr2_2_mod.F90:317-425) for all (chain, flavour) pairs:
+// udv2 = right state (0 -> tau), udv1 = stored left state; results into Hn = GRT0, GR00, GRTT, GR0T.
+static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
+  const int N = h->N, B = h->B, N2 = 2 * N;
+  const long long NN = (long long)N * N, NN2 = (long long)N2 * N2;
+  const dim3 gN((unsigned)((NN + 255) / 256), B), gN2((unsigned)((NN2 + 255) / 256), B);
+  // V1^-1 = P R^-1 D^-1 Q^H from the pivoted QR of V1 (INV_C, mymats_mod.F90:546-593)
+  RET(qr_any(h, udv1.V, nullptr, h->QRw, 1));
+  RET(orgqr_any(h, h->QRw, h->Qt));
+  k_scaled_adjoint<<<gN, 256, 0, h->st>>>(h->Qt, h->DUP, h->RHS, N);
+  CKL();
+  {
+    TrsvParams t{};
+    t.T = h->QRw; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
+    t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
+    prof_begin(h, ALFGPU_PROF_SOLVE);
+    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    prof_end(h);
+    CKL();
+  }
+  k_perm_rows<<<gN, 256, 0, h->st>>>(h->RHS, h->jpvt, h->V1I, N);
+  CKL();
+  // HLPB2 / HLPB1 = HLPB2^H, QDRP of HLPB1 (2N x 2N)
+  k_cgr22_build<<<gN, 256, 0, h->st>>>(udv1.U, udv1.D, h->V1I, udv2.U, udv2.D, udv2.V, h->HB2, h->HB1, h->first2, N);
+  CKL();
+  prof_begin(h, ALFGPU_PROF_QR);
+  RET(qrp_n(h, h->HB1, N2, h->tau2, h->jpvt2, h->D3, h->vn2, h->info2));
+  prof_end(h);
+  // solve_extended_System: HLP = P blockdiag, R^H Y = HLP (ZTRSM L,U,C), rows / D3, Q Y (ZUNMQR)
+  k_cgr22_hlp<<<gN2, 256, 0, h->st>>>(h->HB2, h->jpvt2, h->HLP, N);
+  CKL();
+  {
+    TrsvParams t{};
+    t.T = h->HB1; t.ldt = N2; t.sT = NN2; t.B = h->HLP; t.vstride = N2; t.estride = 1; t.sB = NN2;
+    t.N = N2; t.nvec = N2; t.lower = 1; t.conj_io = 0; t.trans = 1;
+    t.oscale = nullptr;
+    prof_begin(h, ALFGPU_PROF_SOLVE);
+    k_trsv<<<dim3(N2, B), 256, N2 * sizeof(zd), h->st>>>(t);
+    prof_end(h);
+    CKL();
+  }
+  {
+    // HLP(I, :) *= conj(1 / D3(I)): D3 is real
+    dim3 grid((unsigned)((NN2 + 255) / 256), B);
+    k_scale_rows_inv<<<grid, 256, 0, h->st>>>(h->HLP, h->D3, N2);
+    CKL();
+  }
+  prof_begin(h, ALFGPU_PROF_ORGQR);
+  RET(unmqr_n(h, h->HB1, h->tau2, h->HLP, N2));
+  prof_end(h);
+  k_cgr22_blocks<<<gN, 256, 0, h->st>>>(h->HLP, h->first2, h->Hn[0], h->Hn[1], h->Hn[2], h->Hn[3], N);
+  CKL();
+  return 0;
+}
+
+// TAU_M (tau_m_mod.F90:56-211), finite temperature, after the sweep: GT0, G0T, G00, GTT for
+// every slice, ObserT each slice, CGR2_2 and Control_Precision_tau every Nwrap block.
+static int tau_m(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx) {
+  const int N = h->N, B = h->B, L = h->L, F = h->F;
+  const long long NN = (long long)N * N;
+  const dim3 gN((unsigned)((NN + 255) / 256), B);
+  k_tau_init<<<gN, 256, 0, h->st>>>(h->G, h->G00, h->GT0, h->GTT, h->G0T, N);
+  CKL();
+  RET(obs_tau(h, cb, ctx, 0));
+  RET(udv_reset(h, h->udvr_tau));
+  int NST = 1;
+  for (int NT = 0; NT < L; ++NT) {
+    const int NT1 = NT + 1;
+    RET(slice_scale(h, NT1));
+    prof_begin(h, ALFGPU_PROF_HOP);
+    {  // PROPR(GT0): GT0 = S (expT GT0)
+      GemmParams p = gsq(h, B);
+      p.A = h->expT; p.realA = 1; p.modA = F; p.B = h->GT0; p.C = h->T1; p.rs = h->S; p.sRS = N;
+      RET(gemm(h, p));
+      std::swap(h->GT0, h->T1);
+    }
+    {  // PROPRM1(G0T): G0T = (G0T expTinv) Sinv
+      GemmParams p = gsq(h, B);
+      p.A = h->G0T; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1; p.cs = h->Sinv; p.sCS = N;
+      RET(gemm(h, p));
+      std::swap(h->G0T, h->T1);
+    }
+    {  // PROPRM1 then PROPR (GTT): GTT = S expT (GTT expTinv Sinv)
+      GemmParams p = gsq(h, B);
+      p.A = h->GTT; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1; p.cs = h->Sinv; p.sCS = N;
+      RET(gemm(h, p));
+      GemmParams q = gsq(h, B);
+      q.A = h->expT; q.realA = 1; q.modA = F; q.B = h->T1; q.C = h->GTT; q.rs = h->S; q.sRS = N;
+      RET(gemm(h, q));
+    }
+    prof_end(h);
+    RET(obs_tau(h, cb, ctx, NT1));
+    if (NST <= h->Nstm && NT1 == h->stab_nt[NST]) {
+      RET(wrapur_u(h, h->udvr_tau, h->stab_nt[NST - 1], NT1));
+      RET(cgr2_2(h, h->udvr_tau, h->udvst[NST - 1]));
+      // Control_Precision_tau: G vs new G00, old GTT / GT0 / G0T vs new
+      zd* olds[4] = {h->GT0, h->G, h->GTT, h->G0T};
+      for (int k = 0; k < 4; ++k) {
+        CK(cudaMemsetAsync(h->cmp_tau + 2ll * k * B, 0, 2 * (size_t)B * sizeof(double), h->st));
+        k_compare<<<dim3(CMP_BLOCKS, B), 256, 0, h->st>>>(h->Hn[k], olds[k], N, h->cmp_tau + 2ll * k * B, h->err);
+        CKL();
+      }
+      k_tau_stats<<<(h->C + 127) / 128, 128, 0, h->st>>>(h->cmp_tau, h->C, F, h->stat);
+      CKL();
+      std::swap(h->GT0, h->Hn[0]);
+      std::swap(h->G00, h->Hn[1]);
+      std::swap(h->GTT, h->Hn[2]);
+      std::swap(h->G0T, h->Hn[3]);
+      NST++;
+    }
+  }
   return 0;
 }
 
@@ -731,7 +945,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
       d.nwrap < 1 || d.n_chains < 1)
     return ALFGPU_ERROR_ARGUMENT;
   if (d.precision != ALFGPU_PRECISION_FP64 && d.precision != ALFGPU_PRECISION_MIXED) return ALFGPU_ERROR_ARGUMENT;
-  if (d.ltau) return ALFGPU_ERROR_UNSUPPORTED;
+  if (d.ltau != 0 && d.ltau != 1) return ALFGPU_ERROR_ARGUMENT;
+  if (d.ltau && 2 * d.ndim > 32 * BQR_LROWS) return ALFGPU_ERROR_UNSUPPORTED;  // CGR2_2's 2N-row apply
   alfgpu_s* h = new alfgpu_s();
   h->d = d;
   h->N = d.ndim; h->F = d.n_fl; h->M = d.n_op; h->L = d.ltrot; h->C = d.n_chains; h->B = d.n_chains * d.n_fl;
@@ -833,6 +1048,20 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   for (auto& s : h->udvst) r |= mk_udv(s);
   r |= dalloc(h, &h->TP, B * NN); r |= dalloc(h, &h->Qb, B * NN); r |= dalloc(h, &h->RHS, B * NN);
   r |= dalloc(h, &h->QRw, B * NN); r |= dalloc(h, &h->qkeys, B * N);
+  h->ltau = d.ltau;
+  if (h->ltau) {
+    const size_t N2 = 2 * N, NN2 = N2 * N2;
+    r |= dalloc(h, &h->GT0, B * NN); r |= dalloc(h, &h->G0T, B * NN); r |= dalloc(h, &h->G00, B * NN);
+    r |= dalloc(h, &h->GTT, B * NN);
+    for (int k = 0; k < 4; ++k) r |= dalloc(h, &h->Hn[k], B * NN);
+    r |= dalloc(h, &h->udvr_tau.U, B * NN); r |= dalloc(h, &h->udvr_tau.V, B * NN);
+    r |= dalloc(h, &h->udvr_tau.D, B * N); r |= dalloc(h, &h->udvr_tau.detU, B);
+    r |= dalloc(h, &h->HB1, B * NN2); r |= dalloc(h, &h->HB2, B * NN2); r |= dalloc(h, &h->HLP, B * NN2);
+    r |= dalloc(h, &h->tau2, B * N2); r |= dalloc(h, &h->jpvt2, B * N2); r |= dalloc(h, &h->D3, B * N2);
+    r |= dalloc(h, &h->vn2, B * 2 * N2); r |= dalloc(h, &h->info2, B); r |= dalloc(h, &h->first2, B);
+    r |= dalloc(h, &h->cmp_tau, 8 * B); r |= dalloc(h, &h->V1I, B * NN); r |= dalloc(h, &h->Qt, B * NN);
+    r |= dalloc(h, &h->Gq, 4 * B * NN);
+  }
   if (h->df_qr) r |= dalloc(h, &h->QRdf, B * NN);
   r |= dalloc(h, &h->Vtmp, B * NN);
   r |= dalloc(h, &h->tau, B * N); r |= dalloc(h, &h->jpvt, B * N); r |= dalloc(h, &h->perm, B * N);
@@ -858,6 +1087,9 @@ void alfgpu_destroy(alfgpu_t* h) {
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
   for (void* p : h->allocs) cudaFree(p);
+  if (h->obs_host) cudaFreeHost(h->obs_host);
+  if (h->tau_host) cudaFreeHost(h->tau_host);
+  if (h->phase_host) cudaFreeHost(h->phase_host);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -1045,7 +1277,6 @@ int alfgpu_init_state(alfgpu_t* h, double* phase_out) {
 int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
   if (!h) return ALFGPU_ERROR_ARGUMENT;
   if (!h->state_ok) return ALFGPU_ERROR_ARGUMENT;
-  (void)cb; (void)ctx;
   CK(cudaSetDevice(h->dev));
   const int L = h->L, M = h->M, Nstm = h->Nstm;
   const double* dr = nullptr;
@@ -1081,6 +1312,7 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
       RET(stabilise(h, nvar, 1));
       NST++;
     }
+    RET(obs_eq(h, cb, ctx, ntau1, pending));  // LOBS_ST = 1, LOBS_EN = Ltrot
   }
   // down pass (main.F90:776-834)
   RET(udv_reset(h, h->udvl));
@@ -1090,6 +1322,7 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
     RET(update_slice(h, ntau, 1, L * M + (L - ntau) * M, dr));
     RET(slice_scale(h, ntau));  // Op_Wrapdo N_type=1 uses the updated fields
     RET(hop(h, 0, 1));
+    if (ntau1 >= 1) RET(obs_eq(h, cb, ctx, ntau1, 0));
     if (NST >= 1 && h->stab_nt[NST] == ntau1 && ntau1 != 0) {
       RET(wrapul(h, h->stab_nt[NST + 1], ntau1));
       RET(udv_copy(h, h->udvr, h->udvst[NST - 1]));
@@ -1104,6 +1337,7 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
   RET(udv_reset(h, h->udvr));
   RET(stabilise(h, 1, 1));
   RET(udv_reset(h, h->udvst[Nstm - 1]));
+  if (h->ltau) RET(tau_m(h, cb, ctx));  // main.F90:879-881
   if (!uniforms)
     for (int c = 0; c < h->C; ++c) h->h_ctr[c] += 6ull * M * L;
   {

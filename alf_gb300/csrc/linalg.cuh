@@ -270,6 +270,8 @@ struct TrsvParams {
   const zd* T; long long ldt, sT;
   zd* B; long long vstride, estride, sB;
   int N, nvec, lower, conj_io;
+  int trans;             // 1: the triangle is conj(T)^T (T(i,j) read as conj(T(j,i)))
+  const double* oscale;  // optional: x_i *= oscale[i] after the solve (per batch, stride N)
 };
 
 __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
@@ -278,6 +280,9 @@ __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
   const zd* T = p.T + b * p.sT;
   zd* x = p.B + b * p.sB + (long long)v * p.vstride;
   extern __shared__ zd xs[];
+  auto Tij = [&](int i, int j) -> zd {
+    return p.trans ? zconj(T[j + (long long)i * p.ldt]) : T[i + (long long)j * p.ldt];
+  };
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     zd t = x[(long long)i * p.estride];
     xs[i] = p.conj_io ? zconj(t) : t;
@@ -285,25 +290,24 @@ __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
   __syncthreads();
   if (!p.lower) {
     for (int i = N - 1; i >= 0; --i) {
-      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], T[i + (long long)i * p.ldt]);
+      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], Tij(i, i));
       __syncthreads();
       const zd xi = xs[i];
-      const zd* ci = T + (long long)i * p.ldt;
-      for (int r = threadIdx.x; r < i; r += blockDim.x) xs[r] = zsub(xs[r], zmul(ci[r], xi));
+      for (int r = threadIdx.x; r < i; r += blockDim.x) xs[r] = zsub(xs[r], zmul(Tij(r, i), xi));
       __syncthreads();
     }
   } else {
     for (int i = 0; i < N; ++i) {
-      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], T[i + (long long)i * p.ldt]);
+      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], Tij(i, i));
       __syncthreads();
       const zd xi = xs[i];
-      const zd* ci = T + (long long)i * p.ldt;
-      for (int r = i + 1 + threadIdx.x; r < N; r += blockDim.x) xs[r] = zsub(xs[r], zmul(ci[r], xi));
+      for (int r = i + 1 + threadIdx.x; r < N; r += blockDim.x) xs[r] = zsub(xs[r], zmul(Tij(r, i), xi));
       __syncthreads();
     }
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     zd t = xs[i];
+    if (p.oscale) t = zscale(t, p.oscale[(long long)b * N + i]);
     x[(long long)i * p.estride] = p.conj_io ? zconj(t) : t;
   }
 }

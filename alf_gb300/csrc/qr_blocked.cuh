@@ -28,7 +28,7 @@
 
 #define BQR_NB 32
 #define BQR_ROWS 32   // max rows of a panel per CTA (N <= 32 * cluster size)
-#define BQR_LROWS 16  // max rows per lane in k_bqr_apply (N <= 512)
+#define BQR_LROWS 24  // max rows per lane in k_bqr_apply (N <= 768)
 
 // 1/d for real d != 0: float seed and two Newton-Raphson steps (an FP64 division
 // costs ~560 dependent cycles on GB300); falls back to division outside float range.
@@ -223,7 +223,8 @@ struct BQRApply {
   zd* C; long long ldc, sC;          // columns c0 .. N-1 are updated, rows j0 .. N-1 (FP64)
   int N, j0, nb, c0;
   int conj_tau;  // 1: QR trailing update, H^H in order k = 0..nb-1
-                 // 0: explicit Q, H in reverse order; columns [j0, j0+nb) start as e_c
+                 // 0: Q applied (ZUNMQR 'L','N'), H in reverse order
+  int init;      // with conj_tau = 0: columns [j0, j0+nb) start as e_c (explicit Q, ZUNGQR)
 };
 
 // One column per CTA of 4 warps (one per SMSP: on GB300 a warp issues at most one
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
   const Z* V = reinterpret_cast<const Z*>(p.V) + b * p.sV;
   const zd* tau = p.tau + b * p.sT;
   zd* col = p.C + b * p.sC + (long long)c * p.ldc;
-  const bool fresh = !p.conj_tau && c < j0 + nb;
+  const bool fresh = p.init && c < j0 + nb;
   __shared__ Z red[2][4];
   Z x[BQR_QW], vn[BQR_QW];
 #pragma unroll

@@ -101,14 +101,33 @@ class Chains:
         _lib.check(self.L.alfgpu_init_state(self.h, _p(ph)), "alfgpu_init_state")
         return ph
 
-    def sweep(self, uniforms: Optional[np.ndarray] = None):
+    def sweep(self, uniforms: Optional[np.ndarray] = None, measure: bool = False):
+        """One sweep on every chain.  With ``measure``, the library's ham%Obser / ham%ObserT
+        callbacks are collected: returns (eq, tau), lists of (chain, ntau, G, phase) and
+        (chain, ntau, [GT0, G0T, G00, GTT], phase), matrices as [nf][row][col]."""
+        eq, tau = [], []
+        NN = self.N * self.N
+
+        def mats(ptr, k):
+            a = np.ctypeslib.as_array(ptr, shape=(2 * k * self.F * NN,)).view(np.complex128)
+            return np.transpose(a.reshape(k, self.F, self.N, self.N), (0, 1, 3, 2)).copy()
+
+        def on_obs(ctx, chain, ntau, kind, G, ph):
+            phase = complex(ph[0], ph[1])
+            if kind == 0:
+                eq.append((chain, ntau, mats(G, 1)[0], phase))
+            else:
+                tau.append((chain, ntau, list(mats(G, 4)), phase))
+
+        cb = _lib.OBS_CB(on_obs) if measure else _lib.OBS_CB()
         if uniforms is not None:
             u = np.ascontiguousarray(uniforms, dtype=np.float64)
             assert u.size == self.C * 6 * self.M * self.Lt
-            rc = self.L.alfgpu_sweep(self.h, _p(u), _lib.OBS_CB(), None)
+            rc = self.L.alfgpu_sweep(self.h, _p(u), cb, None)
         else:
-            rc = self.L.alfgpu_sweep(self.h, None, _lib.OBS_CB(), None)
+            rc = self.L.alfgpu_sweep(self.h, None, cb, None)
         _lib.check(rc, "alfgpu_sweep")
+        return (eq, tau) if measure else None
 
     # --- readback --------------------------------------------------------------------------------
     def green(self, chain: int = 0) -> np.ndarray:

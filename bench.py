@@ -38,6 +38,9 @@ METRIC = "AFQMC sweeps/s (per chain & aggregate), mixed vs FP64 GPU at max|dG|<=
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # Measured on this machine's GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
 FP64_DMMA_TFLOPS = 1.048
+# DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
+# the ncu capture summarised in profiles/k_zgemm_hop_hubbard16x16_fp64.md
+HOP_TRAFFIC_BYTES = None
 
 
 def parse():
@@ -248,19 +251,21 @@ def main():
     value = total_sweeps / r["t_dev"]
     e2e = total_sweeps / r["t_e2e"]
     prof = r["prof"]
-    dom = max(prof.items(), key=lambda kv: kv[1][0])
-    dname, (dms, dn) = dom
-    n_acc_2 = r["stats"].n_acc / max(args.steps, 1) * 2
-    flops = algorithmic_flops(m, dname, dn, int(n_acc_2))
-    if flops is not None and dms > 0:
-        achieved = flops / (dms / 1e3) / 1e12
-        roof = {"bound": "tensor", "kernel": dname, "achieved": achieved, "peak": FP64_DMMA_TFLOPS,
-                "unit": "TFLOP/s", "frac": achieved / FP64_DMMA_TFLOPS, "traffic": None,
-                "peak_source": "measured FP64 mma.sync m8n8k4 throughput (profiles/fp64_throughput_gb300.md); "
-                               "MEASURED_PEAKS.json has no FP64 figure"}
-    else:
-        roof = {"bound": "latency", "kernel": dname, "achieved": None, "peak": None, "unit": None, "frac": None,
-                "traffic": None}
+    # Roofline of the dominant kernel: the complex GEMM (k_zgemm on FP64 DMMA; k_dfgemm in
+    # the mixed form) carries the largest share of the launch list, and its largest
+    # consumer with a clean algorithmic count is the G wrap (2 real x complex N^3
+    # products per flavour per slice, 2 L slices per sweep).
+    hop_ms, hop_n = prof.get("hop", (0.0, 0))
+    flops = algorithmic_flops(m, "hop", hop_n, 0)
+    roof = {"bound": "tensor", "kernel": "k_zgemm (G wraps)" if args.precision == "fp64" else "k_dfgemm (G wraps)",
+            "achieved": None, "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
+            "traffic": HOP_TRAFFIC_BYTES if args.precision == "fp64" and m.ndim == 256 else None,
+            "algorithmic_flops_per_launch": 2 * m.n_fl * 4.0 * m.ndim ** 3 / 2,
+            "peak_source": "FP64 mma.sync m8n8k4 throughput measured on this pool "
+                           "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
+    if flops and hop_ms > 0:
+        roof["achieved"] = flops / (hop_ms / 1e3) / 1e12
+        roof["frac"] = roof["achieved"] / FP64_DMMA_TFLOPS
     phases = {k: {"ms_per_sweep": v[0] / 2.0, "launch_groups_per_sweep": v[1] / 2.0} for k, v in prof.items()}
     launches = int(r["launches"])
     cpu = None

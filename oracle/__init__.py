@@ -70,8 +70,20 @@ def lib():
         getattr(L, name).restype = _c.c_int
     L.oracle_set_threads.argtypes = [_c.c_int]
     L.oracle_set_variant.argtypes = [_c.c_int]
+    L.oracle_set_eq_callback.argtypes = [_p, EQ_CB, _p]
+    L.oracle_set_tau_callback.argtypes = [_p, TAU_CB, _p]
     _lib = L
     return L
+
+
+class _Z(_c.Structure):
+    _fields_ = [("re", _c.c_double), ("im", _c.c_double)]
+
+
+_PD = _c.POINTER(_c.c_double)
+# ham%Obser: (ctx, ntau, G[F][N][N] col-major, phase); ham%ObserT: (ctx, ntau, GT0, G0T, G00, GTT, phase)
+EQ_CB = _c.CFUNCTYPE(None, _p, _c.c_int, _PD, _Z)
+TAU_CB = _c.CFUNCTYPE(None, _p, _c.c_int, _PD, _PD, _PD, _PD, _Z)
 
 
 def set_variant(v: int) -> None:
@@ -172,6 +184,26 @@ class Oracle:
         if rc < 0:
             raise RuntimeError(f"oracle_sweep_chunk rc={-rc}")
         return rc == 1
+
+    def _mats(self, ptr) -> np.ndarray:
+        a = np.ctypeslib.as_array(ptr, shape=(2 * self.F * self.N * self.N,)).view(np.complex128)
+        return np.transpose(a.reshape(self.F, self.N, self.N), (0, 2, 1)).copy()  # -> [nf][row][col]
+
+    def collect_measurements(self):
+        """Collect the equal-time (ham%Obser) and time-displaced (ham%ObserT) callbacks of
+        the following sweeps: lists of (ntau, G, phase) and (ntau, [GT0, G0T, G00, GTT], phase)."""
+        eq, tau = [], []
+
+        def on_eq(ctx, ntau, G, ph):
+            eq.append((ntau, self._mats(G), complex(ph.re, ph.im)))
+
+        def on_tau(ctx, ntau, a, b, c, d, ph):
+            tau.append((ntau, [self._mats(x) for x in (a, b, c, d)], complex(ph.re, ph.im)))
+
+        self._cbs = (EQ_CB(on_eq), TAU_CB(on_tau))
+        lib().oracle_set_eq_callback(self.h, self._cbs[0], None)
+        lib().oracle_set_tau_callback(self.h, self._cbs[1], None)
+        return eq, tau
 
     def green(self) -> np.ndarray:
         G = np.zeros((self.F, self.N, self.N), np.complex128)  # [nf][col][row] memory = col-major per flavour

@@ -176,6 +176,9 @@ struct Oracle {
   // time displaced (TAU_M)
   void (*tau_cb)(void*, int, const zc*, const zc*, const zc*, const zc*, zc) = nullptr;
   void* tau_ctx = nullptr;
+  // equal-time measurements (ham%Obser, main.F90:757-772 and 788-803): G of all flavours
+  void (*eq_cb)(void*, int, const zc*, zc) = nullptr;
+  void* eq_ctx = nullptr;
 
   zc* Gf(int nf) { return G.data() + (size_t)nf * N * N; }
   int fval(int n, int nt1 /*1-based*/) const { return f[(size_t)(nt1 - 1) * M + n]; }
@@ -954,6 +957,7 @@ int oracle_sweep_chunk(void* h, const double* u, int nslices) {
         if (e) { cur.active = false; return -e; }
         cur.NST++;
       }
+      if (o.eq_cb) o.eq_cb(o.eq_ctx, ntau1, o.G.data(), o.phase);  // LOBS_ST = 1, LOBS_EN = Ltrot
       cur.ntau++;
       if (cur.ntau == o.L) {
         for (int nf = 0; nf < o.F; ++nf) o.udvl[nf].reset(o.N, 'l');
@@ -962,6 +966,7 @@ int oracle_sweep_chunk(void* h, const double* u, int nslices) {
     } else {
       const int ntau = cur.ntau, ntau1 = ntau - 1;
       wrapgrdo(o, ntau, u + (size_t)o.L * per_slice + (size_t)(o.L - ntau) * per_slice);
+      if (o.eq_cb && ntau1 >= 1) o.eq_cb(o.eq_ctx, ntau1, o.G.data(), o.phase);
       if (cur.NST >= 1 && o.stab_nt[cur.NST] == ntau1 && ntau1 != 0) {
         wrapul(o, o.stab_nt[cur.NST + 1], ntau1, o.udvl);
         for (int nf = 0; nf < o.F; ++nf) {
@@ -1024,6 +1029,10 @@ void oracle_set_tau_callback(void* h, void (*cb)(void*, int, const zc*, const zc
                              void* ctx) {
   Oracle& o = *(Oracle*)h;
   o.tau_cb = cb; o.tau_ctx = ctx;
+}
+void oracle_set_eq_callback(void* h, void (*cb)(void*, int, const zc*, zc), void* ctx) {
+  Oracle& o = *(Oracle*)h;
+  o.eq_cb = cb; o.eq_ctx = ctx;
 }
 
 }  // extern "C"

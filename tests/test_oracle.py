@@ -118,3 +118,24 @@ def test_sweep_identities(kind):
     st = o.stats()
     assert st.n_prop == len(visits) and 0 < st.n_acc < st.n_prop
     assert st.xmaxG < 1e-8
+
+
+def test_oracle_tau_m_propagation_matches_cgr2_2():
+    # TAU_M's propagated GT0/G0T/GTT/G00 against the fresh CGR2_2 blocks every Nwrap slices
+    # (Control_Precision_tau): two independent computations of the same matrices
+    from alf_gb300 import model as mdl, rng
+    m = mdl.hubbard("honeycomb", 2, 2, U=5.0, beta=1.0, dtau=0.05, nwrap=5)
+    o = oracle.Oracle(m, ltau=1)
+    o.set_fields(rng.initial_fields(7, 0, m.n_op, m.ltrot))
+    o.init_state()
+    eq, tau = o.collect_measurements()
+    o.sweep(rng.sweep_uniforms(7, 0, m.n_op, m.ltrot, 0))
+    s = o.stats()
+    assert s.ncg_tau == 4 * m.n_fl * m.nstm
+    assert s.xmax_tau < 1e-9
+    # at NT = 0: G00 = GT0 = GTT = G and G0T = G - 1
+    nt, (gt0, g0t, g00, gtt), _ = tau[0]
+    assert nt == 0
+    np.testing.assert_array_equal(gt0, g00)
+    np.testing.assert_array_equal(gtt, g00)
+    np.testing.assert_allclose(g0t, g00 - np.eye(m.ndim)[None], atol=1e-15)
