@@ -69,6 +69,14 @@ struct alfgpu_s {
   int* v_site = nullptr;
   zd *v_g = nullptr, *v_alpha = nullptr, *v_Eexp = nullptr;
   UpdTab* v_tab = nullptr;  // [chain][F*M][5][3] transition factors of every (vertex, old field, flip choice)
+  int* v_site2 = nullptr;   // [chain][F*M] site of the second eigen-index (two-site vertices) or -1
+  int8_t* v_nsite = nullptr;  // [chain][F*M] positions (non-zero eigenvalues) of each vertex
+  std::vector<int> blk_start[2], blk_cnt[2];  // delayed-update blocks of the up / down pass (visit positions)
+  std::vector<double> h_expT, h_expTinv;      // hopping exponentials as uploaded (original basis)
+  bool rot = false;                           // two-site vertices: the sweep runs in the rotated basis
+  std::vector<std::pair<int, int>> rot_pairs;
+  double rot_U[4] = {1.0, 0.0, 0.0, 1.0};     // shared real eigenbasis, column-major
+  int* rot_dev = nullptr;                     // pairs on the device
   int *v_sptr = nullptr, *v_slist = nullptr;  // [chain][F][N+1], [chain][F][M]: vertices of each site (CSR)
   double* v_E = nullptr;
   int8_t* v_type = nullptr;
@@ -279,6 +287,19 @@ static GemmParams gsq(alfgpu_s* h, int batch) {  // N x N x N square product, ba
 
 static int copy_mats(alfgpu_s* h, zd* dst, const zd* src, size_t count) {
   CK(cudaMemcpyAsync(dst, src, count * sizeof(zd), cudaMemcpyDeviceToDevice, h->st));
+  return 0;
+}
+
+// count matrices X <- W X W^T (rotated basis -> original basis); no-op without two-site vertices
+static int rotate_out(alfgpu_s* h, zd* X, int count) {
+  if (!h->rot || count <= 0) return 0;
+  const int np = (int)h->rot_pairs.size();
+  dim3 grid((unsigned)(((long long)h->N * np + 255) / 256), count);
+  const double* U = h->rot_U;
+  k_rot_rows<<<grid, 256, 0, h->st>>>(X, h->N, h->rot_dev, np, U[0], U[1], U[2], U[3]);
+  CKL();
+  k_rot_cols<<<grid, 256, 0, h->st>>>(X, h->N, h->rot_dev, np, U[0], U[1], U[2], U[3]);
+  CKL();
   return 0;
 }
 
@@ -582,8 +603,15 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
   if (compare) RET(copy_mats(h, h->Gw, h->G, (size_t)B * NN));
   RET(cgr(h, nvar, h->udvr, h->udvl, h->G));
   if (compare) {
+    const zd* gnew = h->G;
+    if (h->rot) {  // Control_PrecisionG in the original basis
+      RET(copy_mats(h, h->TP, h->G, (size_t)B * NN));
+      RET(rotate_out(h, h->TP, B));
+      RET(rotate_out(h, h->Gw, B));
+      gnew = h->TP;
+    }
     CK(cudaMemsetAsync(h->cmp, 0, 2 * (size_t)B * sizeof(double), h->st));
-    k_compare<<<dim3(CMP_BLOCKS, B), 256, 0, h->st>>>(h->G, h->Gw, N, h->cmp, h->err);
+    k_compare<<<dim3(CMP_BLOCKS, B), 256, 0, h->st>>>(gnew, h->Gw, N, h->cmp, h->err);
     CKL();
   }
   k_opphase<<<B, 256, 0, h->st>>>(h->fields, h->L, h->M, h->F, h->v_g, h->v_alpha, h->v_type, h->ft, h->opang);
@@ -597,6 +625,7 @@ static int stabilise(alfgpu_s* h, int nvar, int compare) {
     sp.rec_phase = h->rec_phase + (long long)h->rec_stab * h->C;
     RET(copy_mats(h, h->rec_G + (long long)h->rec_stab * B * NN, h->G, (size_t)B * NN));
     RET(copy_mats(h, h->rec_Gw + (long long)h->rec_stab * B * NN, h->Gw, (size_t)B * NN));
+    RET(rotate_out(h, h->rec_G + (long long)h->rec_stab * B * NN, B));  // Gw is already rotated
     h->rec_stab++;
   }
   k_stab_finish<<<(h->C + 127) / 128, 128, 0, h->st>>>(sp);
@@ -620,11 +649,14 @@ static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pendi
   RET(ensure_obs_host(h));
   const long long NN = (long long)h->N * h->N;
   const zd* src = h->G;
-  if (pending) {
+  if (pending || h->rot) {
     RET(copy_mats(h, h->Gw, h->G, (size_t)h->B * NN));
-    dim3 grid((unsigned)((NN + 255) / 256), h->B);
-    k_apply_scale<<<grid, 256, 0, h->st>>>(h->Gw, h->S, h->Sinv, h->N);
-    CKL();
+    if (pending) {
+      dim3 grid((unsigned)((NN + 255) / 256), h->B);
+      k_apply_scale<<<grid, 256, 0, h->st>>>(h->Gw, h->S, h->Sinv, h->N);
+      CKL();
+    }
+    RET(rotate_out(h, h->Gw, h->B));
     src = h->Gw;
   }
   CK(cudaMemcpyAsync(h->obs_host, src, (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
@@ -643,6 +675,7 @@ static int obs_tau(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int nt) {
   dim3 grid((unsigned)((NN + 255) / 256), h->B);
   k_gather_quartet<<<grid, 256, 0, h->st>>>(h->GT0, h->G0T, h->G00, h->GTT, h->Gq, h->N, h->F);
   CKL();
+  RET(rotate_out(h, h->Gq, 4 * h->B));
   CK(cudaMemcpyAsync(h->tau_host, h->Gq, 4 * (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->phase_host, h->phase, (size_t)h->C * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -869,15 +902,16 @@ static int hop_impl(alfgpu_s* h, int up, int with_scale) {
 static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const double* draws_dev) {
   const int N = h->N, F = h->F, M = h->M;
   const long long NN = (long long)N * N;
-  for (int q0 = 0; q0 < M; q0 += h->kblk) {
+  for (size_t blk = 0; blk < h->blk_start[dir].size(); ++blk) {
     UpdParams u;
     memset(&u, 0, sizeof(u));
     u.N = N; u.F = F; u.M = M; u.L = h->L; u.NSUN = h->NSUN;
-    u.nt1 = nt1; u.dir = dir; u.q0 = q0; u.nq = (M - q0 < h->kblk) ? M - q0 : h->kblk;
+    u.nt1 = nt1; u.dir = dir; u.q0 = h->blk_start[dir][blk]; u.nq = h->blk_cnt[dir][blk];
     u.visit_base = visit_base;
     u.nChains = h->C;
     u.G = h->G; u.sG = F * NN;
-    u.V.site = h->v_site; u.V.type = h->v_type; u.V.sK = (long long)F * M;
+    u.V.site = h->v_site; u.V.site2 = h->v_site2; u.V.nsite = h->v_nsite; u.V.type = h->v_type;
+    u.V.sK = (long long)F * M;
     u.tab = h->v_tab;
     u.fields = h->fields;
     u.draws = draws_dev; u.sDraws = 6ll * M * h->L;
@@ -1031,9 +1065,10 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   int r = 0;
   r |= dalloc(h, &h->expT, F * NN); r |= dalloc(h, &h->expTinv, F * NN);
   r |= dalloc(h, &h->v_site, C * F * M); r |= dalloc(h, &h->v_g, C * F * M); r |= dalloc(h, &h->v_alpha, C * F * M);
-  r |= dalloc(h, &h->v_E, C * F * M); r |= dalloc(h, &h->v_type, C * F * M); r |= dalloc(h, &h->v_Eexp, C * F * M * 5);
+  r |= dalloc(h, &h->v_E, C * F * M); r |= dalloc(h, &h->v_type, C * F * M); r |= dalloc(h, &h->v_Eexp, C * F * M * 10);
+  r |= dalloc(h, &h->v_site2, C * F * M); r |= dalloc(h, &h->v_nsite, C * F * M);
   r |= dalloc(h, &h->v_tab, C * F * M * 15);
-  r |= dalloc(h, &h->v_sptr, C * F * (N + 1)); r |= dalloc(h, &h->v_slist, C * F * M);
+  r |= dalloc(h, &h->v_sptr, C * F * (N + 1)); r |= dalloc(h, &h->v_slist, C * F * 2 * M);
   r |= dalloc(h, &h->fields, C * L * M);
   r |= dalloc(h, &h->G, B * NN); r |= dalloc(h, &h->Gw, B * NN); r |= dalloc(h, &h->T1, B * NN);
   r |= dalloc(h, &h->S, B * N); r |= dalloc(h, &h->Sinv, B * N);
@@ -1114,13 +1149,51 @@ int alfgpu_get_profile(alfgpu_t* h, double* ms, int64_t* launches) {
   return 0;
 }
 
+// Rotated basis for two-site vertices with one shared eigenbasis on disjoint site pairs
+// (Kondo's J_K vertices): with W = I except the 2x2 block U on every pair, each vertex
+// exponential U diag(exp(g phi E)) U^H is diagonal in x' = W^H x.  Op_Wrapup / Op_Wrapdo
+// with N_type 1 and 2 (Operator_mod.F90:743-951) rotate into and out of this basis
+// around every update; the library stays in it for the whole sweep: expT' = W^H expT W,
+// G' = W^H G W, and every G handed out is rotated back.
+static void rotate_host(const alfgpu_s* h, double* X, int N) {
+  // X <- W^T X W for the real orthogonal W (pairs and U of the handle)
+  const double* U = h->rot_U;
+  for (const auto& pr : h->rot_pairs) {
+    const int a = pr.first, b = pr.second;
+    for (int j = 0; j < N; ++j) {  // rows: W^T X
+      const double xa = X[a + (size_t)j * N], xb = X[b + (size_t)j * N];
+      X[a + (size_t)j * N] = U[0] * xa + U[1] * xb;  // U^T(0,:) = (U00, U10)
+      X[b + (size_t)j * N] = U[2] * xa + U[3] * xb;  // U^T(1,:) = (U01, U11)
+    }
+    for (int i = 0; i < N; ++i) {  // columns: X W
+      const double xa = X[i + (size_t)a * N], xb = X[i + (size_t)b * N];
+      X[i + (size_t)a * N] = xa * U[0] + xb * U[1];
+      X[i + (size_t)b * N] = xa * U[2] + xb * U[3];
+    }
+  }
+}
+
+static int upload_expT(alfgpu_t* h) {
+  const size_t NN = (size_t)h->N * h->N;
+  std::vector<double> a(h->h_expT), b(h->h_expTinv);
+  if (h->rot)
+    for (int f = 0; f < h->F; ++f) {
+      rotate_host(h, a.data() + f * NN, h->N);
+      rotate_host(h, b.data() + f * NN, h->N);
+    }
+  CK(cudaMemcpy(h->expT, a.data(), h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->expTinv, b.data(), h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv) {
   if (!h || !expT || !expTinv) return ALFGPU_ERROR_ARGUMENT;
   const size_t NN = (size_t)h->N * h->N;
   for (size_t i = 0; i < h->F * NN; ++i)
     if (!std::isfinite(expT[i]) || !std::isfinite(expTinv[i])) return ALFGPU_ERROR_HAMILTONIAN;
-  CK(cudaMemcpy(h->expT, expT, h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->expTinv, expTinv, h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  h->h_expT.assign(expT, expT + h->F * NN);
+  h->h_expTinv.assign(expTinv, expTinv + h->F * NN);
+  RET(upload_expT(h));
   h->hop_ok = true;
   return 0;
 }
@@ -1129,36 +1202,87 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
   if (!h || !v || chain < -1 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
   const int F = h->F, M = h->M, N = h->N;
   const size_t K = (size_t)F * M;
-  std::vector<int> site(K);
-  std::vector<zd> g(K), al(K), ee(K * 5);
-  std::vector<double> E(K);
+  std::vector<int> site(K), site2(K, -1);
+  std::vector<int8_t> nsite(K);
+  std::vector<zd> g(K), al(K), ee(K * 10);
+  std::vector<double> E(2 * K);
   std::vector<int8_t> ty(K);
+  std::vector<std::pair<int, int>> pairs;
+  double U[4] = {1.0, 0.0, 0.0, 1.0};
+  bool have_rot = false;
   for (size_t k = 0; k < K; ++k) {
-    if (v->op_n[k] != 1 || !v->op_diag[k]) return ALFGPU_ERROR_UNSUPPORTED;  // single-site diagonal only
+    const int n = v->op_n[k], nz = v->op_nz[k];
+    if (n < 1 || n > 2 || nz < 1 || nz > n) return ALFGPU_ERROR_UNSUPPORTED;
     if (v->op_type[k] != 1 && v->op_type[k] != 2) return ALFGPU_ERROR_UNSUPPORTED;
-    if (v->op_nz[k] != 1) return ALFGPU_ERROR_UNSUPPORTED;
-    int p = v->op_P[2 * k];
-    if (p < 0 || p >= N) return ALFGPU_ERROR_HAMILTONIAN;
-    site[k] = p;
+    for (int a = 0; a < n; ++a)
+      if (v->op_P[2 * k + a] < 0 || v->op_P[2 * k + a] >= N) return ALFGPU_ERROR_HAMILTONIAN;
+    if (!v->op_diag[k]) {  // non-diagonal: two sites, real eigenbasis shared by all such vertices
+      if (n != 2) return ALFGPU_ERROR_UNSUPPORTED;
+      double u[4];
+      for (int e = 0; e < 4; ++e) {
+        u[e] = v->op_U[(4 * k + e) * 2];
+        if (std::fabs(v->op_U[(4 * k + e) * 2 + 1]) > 1e-14) return ALFGPU_ERROR_UNSUPPORTED;
+      }
+      if (!have_rot) { memcpy(U, u, sizeof(U)); have_rot = true; }
+      for (int e = 0; e < 4; ++e)
+        if (std::fabs(u[e] - U[e]) > 1e-13) return ALFGPU_ERROR_UNSUPPORTED;
+      if (k < (size_t)M) pairs.emplace_back(v->op_P[2 * k], v->op_P[2 * k + 1]);
+    }
+    nsite[k] = (int8_t)nz;
+    site[k] = v->op_P[2 * k];
+    if (nz == 2) site2[k] = v->op_P[2 * k + 1];
     g[k] = zmk(v->op_g[2 * k], v->op_g[2 * k + 1]);
     al[k] = zmk(v->op_alpha[2 * k], v->op_alpha[2 * k + 1]);
-    E[k] = v->op_E[2 * k];
+    E[2 * k] = v->op_E[2 * k];
+    E[2 * k + 1] = v->op_E[2 * k + 1];
     ty[k] = (int8_t)v->op_type[k];
-    for (int s = 0; s < 5; ++s) ee[k * 5 + s] = zmk(v->op_Eexp[(k * 10 + s) * 2], v->op_Eexp[(k * 10 + s) * 2 + 1]);
+    for (int m = 0; m < 2; ++m)
+      for (int s = 0; s < 5; ++s)
+        ee[k * 10 + m * 5 + s] = zmk(v->op_Eexp[(k * 10 + m * 5 + s) * 2], v->op_Eexp[(k * 10 + m * 5 + s) * 2 + 1]);
     if (!std::isfinite(g[k].x) || !std::isfinite(g[k].y)) return ALFGPU_ERROR_HAMILTONIAN;
   }
-  // sites of one flavour must be distinct within every block of visits, and equal across flavours
+  // the vertices of every flavour act on the same sites
   for (int n = 0; n < M; ++n)
-    for (int f = 1; f < F; ++f)
-      if (site[(size_t)f * M + n] != site[n]) return ALFGPU_ERROR_UNSUPPORTED;
-  // a delayed-update block needs distinct sites; check the up-pass and down-pass blockings
+    for (int f = 1; f < F; ++f) {
+      const size_t k = (size_t)f * M + n;
+      if (site[k] != site[n] || site2[k] != site2[n] || v->op_diag[k] != v->op_diag[n]) return ALFGPU_ERROR_UNSUPPORTED;
+    }
+  // rotated pairs must be disjoint and untouched by any other vertex
+  if (have_rot) {
+    std::vector<int> cnt(N, 0), inpair(N, 0);
+    for (int n = 0; n < M; ++n) {
+      cnt[site[n]]++;
+      if (site2[n] >= 0) cnt[site2[n]]++;
+      if (!v->op_diag[n]) { inpair[site[n]] = 1; inpair[site2[n]] = 1; }
+    }
+    for (int i = 0; i < N; ++i)
+      if (inpair[i] && cnt[i] != 1) return ALFGPU_ERROR_UNSUPPORTED;
+    if (chain >= 0 && (!h->rot || h->rot_pairs != pairs)) {
+      if (h->vert_ok) return ALFGPU_ERROR_UNSUPPORTED;  // per-chain tables share one basis
+    }
+  }
+  // delayed-update blocks: up to kblk positions (one per non-zero eigenvalue), distinct sites
   for (int dir = 0; dir < 2; ++dir) {
+    std::vector<int>& st = h->blk_start[dir];
+    std::vector<int>& nc = h->blk_cnt[dir];
+    st.clear(); nc.clear();
     std::vector<int> seen(N, 0);
+    int npos = 0;
     for (int pos = 0; pos < M; ++pos) {
-      if (pos % h->kblk == 0) std::fill(seen.begin(), seen.end(), 0);
-      int s = site[dir == 0 ? pos : M - 1 - pos];
-      if (seen[s]) return ALFGPU_ERROR_UNSUPPORTED;
-      seen[s] = 1;
+      const int n = dir == 0 ? pos : M - 1 - pos;
+      const int s1 = site[n], s2 = site2[n], w = nsite[n];
+      const bool clash = seen[s1] || (s2 >= 0 && seen[s2]) || (s2 == s1);
+      if (st.empty() || npos + w > h->kblk || clash) {
+        if (!st.empty() && clash && npos == 0) return ALFGPU_ERROR_UNSUPPORTED;
+        st.push_back(pos); nc.push_back(0);
+        std::fill(seen.begin(), seen.end(), 0);
+        npos = 0;
+        if (s2 == s1) return ALFGPU_ERROR_UNSUPPORTED;
+      }
+      seen[s1] = 1;
+      if (s2 >= 0) seen[s2] = 1;
+      npos += w;
+      nc.back()++;
     }
   }
   // transition factors for every (vertex, old field, flip choice); type-1 fields flip sign
@@ -1169,37 +1293,68 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
       for (int ch = 0; ch < 3; ++ch) {
         const int sn = (t == 0) ? -so : h->ft.flip[so + 2][ch];
         UpdTab& e = tab[(k * 5 + so + 2) * 3 + ch];
-        if (sn < -2 || sn > 2) { e.myexp = zmk(1.0, 0.0); e.dlt = zmk(0.0, 0.0); e.expal = zmk(1.0, 0.0); continue; }
+        if (sn < -2 || sn > 2) {
+          for (int m = 0; m < 2; ++m) { e.myexp[m] = zmk(1.0, 0.0); e.dlt[m] = zmk(0.0, 0.0); }
+          e.expal = zmk(1.0, 0.0);
+          continue;
+        }
         const double dphi = h->ft.phi[t][sn + 2] - h->ft.phi[t][so + 2];
         const std::complex<double> Z1(g[k].x * dphi, g[k].y * dphi);
-        const std::complex<double> me = std::exp(Z1 * E[k]);
+        for (int m = 0; m < 2; ++m) {
+          const std::complex<double> me = std::exp(Z1 * E[2 * k + m]);
+          e.myexp[m] = zmk(me.real(), me.imag());
+          e.dlt[m] = zmk(me.real() - 1.0, me.imag());
+        }
         const std::complex<double> ea = std::exp(Z1 * std::complex<double>(al[k].x, al[k].y));
-        e.myexp = zmk(me.real(), me.imag());
-        e.dlt = zmk(me.real() - 1.0, me.imag());
         e.expal = zmk(ea.real(), ea.imag());
       }
   }
-  // vertices of each site, ascending, per flavour
-  std::vector<int> sptr((size_t)F * (N + 1), 0), slist(K);
+  // positions of each site, ascending (vertex n, eigen-index I) -> 2n + I, per flavour
+  std::vector<int> sptr((size_t)F * (N + 1), 0), slist((size_t)2 * K);
   for (int f = 0; f < F; ++f) {
     int* ptr = &sptr[(size_t)f * (N + 1)];
-    for (int n = 0; n < M; ++n) ptr[site[(size_t)f * M + n] + 1]++;
+    for (int n = 0; n < M; ++n) {
+      const size_t k = (size_t)f * M + n;
+      ptr[site[k] + 1]++;
+      if (site2[k] >= 0) ptr[site2[k] + 1]++;
+    }
     for (int i = 0; i < N; ++i) ptr[i + 1] += ptr[i];
     std::vector<int> fill(ptr, ptr + N);
-    for (int n = 0; n < M; ++n) slist[(size_t)f * M + fill[site[(size_t)f * M + n]]++] = n;
+    for (int n = 0; n < M; ++n) {
+      const size_t k = (size_t)f * M + n;
+      slist[(size_t)f * 2 * M + fill[site[k]]++] = 2 * n;
+      if (site2[k] >= 0) slist[(size_t)f * 2 * M + fill[site2[k]]++] = 2 * n + 1;
+    }
   }
   int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->C : chain + 1;
   for (int c = c0; c < c1; ++c) {
     CK(cudaMemcpy(h->v_tab + c * K * 15, tab.data(), K * 15 * sizeof(UpdTab), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_sptr + (size_t)c * F * (N + 1), sptr.data(), sptr.size() * sizeof(int), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->v_slist + (size_t)c * K, slist.data(), K * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_slist + (size_t)c * 2 * K, slist.data(), 2 * K * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_site + c * K, site.data(), K * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_site2 + c * K, site2.data(), K * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_nsite + c * K, nsite.data(), K, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_g + c * K, g.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_alpha + c * K, al.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->v_E + c * K, E.data(), K * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_type + c * K, ty.data(), K, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->v_Eexp + c * K * 5, ee.data(), K * 5 * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_Eexp + c * K * 10, ee.data(), K * 10 * sizeof(zd), cudaMemcpyHostToDevice));
   }
+  const bool rot_changed = have_rot != h->rot || (have_rot && (pairs != h->rot_pairs || memcmp(U, h->rot_U, sizeof(U))));
+  h->rot = have_rot;
+  h->rot_pairs = pairs;
+  memcpy(h->rot_U, U, sizeof(U));
+  if (have_rot) {
+    std::vector<int> pp(2 * pairs.size());
+    for (size_t i = 0; i < pairs.size(); ++i) { pp[2 * i] = pairs[i].first; pp[2 * i + 1] = pairs[i].second; }
+    if (!h->rot_dev) {
+      void* q = nullptr;
+      CK(cudaMalloc(&q, (size_t)N * sizeof(int)));
+      h->allocs.push_back(q);
+      h->rot_dev = (int*)q;
+    }
+    CK(cudaMemcpy(h->rot_dev, pp.data(), pp.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (rot_changed && h->hop_ok) RET(upload_expT(h));
   h->vert_ok = true;
   return 0;
 }
@@ -1353,8 +1508,14 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
 int alfgpu_get_green(alfgpu_t* h, int32_t chain, double* G) {
   if (!h || !G || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
   const size_t n = (size_t)h->F * h->N * h->N;
+  const zd* src = h->G + chain * n;
+  if (h->rot) {
+    RET(copy_mats(h, h->T1, src, n));
+    RET(rotate_out(h, h->T1, h->F));
+    src = h->T1;
+  }
   CK(cudaStreamSynchronize(h->st));
-  CK(cudaMemcpy(G, h->G + chain * n, n * sizeof(zd), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(G, src, n * sizeof(zd), cudaMemcpyDeviceToHost));
   return 0;
 }
 

@@ -7,22 +7,22 @@
 //   S(i) = prod_{n: P(n)=i} E_exp(1, s(n,nt1)),  Sinv(i) = prod E_exp(1, -s(n,nt1)).
 // This is Op_mmultR / Op_Wrapup for diagonal operators (Operator_mod.F90:686-693,
 // 776-781) for every vertex of the slice at once.  grid (B), block 256.
-// sptr/slist: per (chain, flavour) the vertices of each site in ascending order
-// (CSR, built at upload).
+// sptr/slist: per (chain, flavour) the positions (vertex n, eigen-index I) of each site
+// in ascending order, coded 2n + I (CSR, built at upload); Eexp: [k][I][s+2].
 __global__ void k_slice_scale(const int8_t* fields, int L, int M, int N, int F, int nt1, const int* sptr,
                               const int* slist, const zd* Eexp, zd* S, zd* Sinv) {
   const int b = blockIdx.x, c = b / F, f = b % F;
   const int8_t* fl = fields + (long long)c * L * M + (long long)(nt1 - 1) * M;
   const int* ptr = sptr + (long long)b * (N + 1);
-  const int* lst = slist + (long long)b * M;
-  const zd* ee = Eexp + ((long long)c * F * M + (long long)f * M) * 5;
+  const int* lst = slist + (long long)b * 2 * M;
+  const zd* ee = Eexp + ((long long)c * F * M + (long long)f * M) * 10;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     zd s = zmk(1.0, 0.0), si = zmk(1.0, 0.0);
     for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
-      const int n = lst[e];
+      const int code = lst[e], n = code >> 1, I = code & 1;
       const int sp = fl[n];
-      s = zmul(s, ee[(long long)n * 5 + sp + 2]);
-      si = zmul(si, ee[(long long)n * 5 - sp + 2]);
+      s = zmul(s, ee[(long long)(2 * n + I) * 5 + sp + 2]);
+      si = zmul(si, ee[(long long)(2 * n + I) * 5 - sp + 2]);
     }
     S[(long long)b * N + i] = s;
     Sinv[(long long)b * N + i] = si;
@@ -225,4 +225,32 @@ __global__ void k_expand_m(const int* m, int* out, int C, int F) {
 __global__ void k_count_sweep(double* stat, int C) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < C) stat[8 * c + 7] += 1.0;
+}
+
+// G <- W G W^T for the block-diagonal real orthogonal W with the 2x2 block U (column-major)
+// on every site pair: the rotated-basis G of two-site vertices back to the original basis.
+// Rows: grid (ceil(N*npairs/256), B); columns: the same grid.
+__global__ void k_rot_rows(zd* G, int N, const int* pairs, int npairs, double u00, double u10, double u01,
+                           double u11) {
+  const long long NN = (long long)N * N, b = blockIdx.y;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= (long long)N * npairs) return;
+  const int j = e % N, pr = e / N;
+  zd* g = G + b * NN + (long long)j * N;
+  const int a = pairs[2 * pr], c = pairs[2 * pr + 1];
+  const zd x = g[a], y = g[c];
+  g[a] = zadd(zscale(x, u00), zscale(y, u01));
+  g[c] = zadd(zscale(x, u10), zscale(y, u11));
+}
+__global__ void k_rot_cols(zd* G, int N, const int* pairs, int npairs, double u00, double u10, double u01,
+                           double u11) {
+  const long long NN = (long long)N * N, b = blockIdx.y;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= (long long)N * npairs) return;
+  const int i = e % N, pr = e / N;
+  zd* g = G + b * NN;
+  const int a = pairs[2 * pr], c = pairs[2 * pr + 1];
+  const zd x = g[i + (long long)a * N], y = g[i + (long long)c * N];
+  g[i + (long long)a * N] = zadd(zscale(x, u00), zscale(y, u01));
+  g[i + (long long)c * N] = zadd(zscale(x, u10), zscale(y, u11));
 }

@@ -36,7 +36,9 @@
 
 struct VertexDev {
   // per chain: K = F*M entries, index k = nf*M + n
-  const int* site;       // P(1), 0-based
+  const int* site;       // site of eigen-index 0 (P(1), 0-based)
+  const int* site2;      // site of eigen-index 1, or -1
+  const int8_t* nsite;   // positions of the vertex: its non-zero eigenvalues (1 or 2)
   const int8_t* type;    // 1 or 2
   long long sK;          // per-chain stride in entries (F*M)
 };
@@ -74,25 +76,31 @@ ALF_DEV int nranf3(double r) {
 }
 
 // Per-visit transition data, precomputed per (vertex k, old field s, flip choice):
-//   myexp = exp(Z E), dlt = myexp - 1, expal = exp(Z alpha),  Z = g (phi(s_new) - phi(s_old))
-// (Upgrade2's Mat(1,1) = myexp - dlt G(P,P), Hamiltonian_main_mod.F90 ratio factors).
+//   myexp_I = exp(Z E_I), dlt_I = myexp_I - 1, expal = exp(Z alpha),  Z = g (phi(s_new) - phi(s_old))
+// for the eigen-indices I = 0, 1 (Upgrade2's Mat(I,I) = myexp_I - dlt_I G(P_I,P_I),
+// upgrade_mod.F90:140-190).
 struct UpdTab {
-  zd myexp, dlt, expal;
+  zd myexp[2], dlt[2], expal;
 };
 
 // One CTA of UPD_THREADS threads per chain.  Dynamic shared memory:
-//   Gh[F][KMAX][KMAX+1]  the block Ghat, updated in place (arithmetic A)
+//   Gh[F][KMAX][KMAX+1]  the block Ghat over the block's positions, updated in place
 //   G0[F][KMAX][KMAX+1]  Ghat at block entry; reused as the ping-pong buffer of the
 //                        Gauss-Jordan inversion of Gamma.
+// A position is one non-zero eigenvalue of a vertex (its site in the diagonal basis);
+// single-site vertices have one, two-site vertices two consecutive positions whose
+// joint ratio is Upgrade2's 2x2 determinant, computed as D_a (1 + Delta_b (1 - G'_bb))
+// with G' after the tentative Sherman-Morrison update of position a; an accepted
+// two-site vertex is applied as two rank-1 updates, the second decided with the first.
 // Warp 0 runs the sequential Metropolis chain (all lanes compute the same scalars;
-// lane a handles row a of a column).  While warps 1..7 apply the rank-1 update of
-// an accepted visit q to rows a > q and columns b > q+1, warp 0 updates column q+1
-// itself and already decides visit q+1 from its new diagonal: one block barrier
-// per visit.  At block end, W = Delta_S Gamma^-1 is formed by Gauss-Jordan
-// elimination without pivoting: the pivots in accept order are the accepted
-// visits' own 1 + Delta (1 - G_jj) factors (the Sherman-Morrison sequence is the LU
-// factorisation of Gamma in that order), non-zero because a zero factor gives
-// weight 0 and is rejected.
+// lane a handles row a of a column).  While warps 1..7 apply the rank-1 update of an
+// accepted position q to rows a > q and the columns beyond those warp 0 needs next,
+// warp 0 updates the next one or two columns itself and already decides the next
+// position from them: one block barrier per position.  At block end, W = Delta_S Gamma^-1
+// is formed by Gauss-Jordan elimination without pivoting: the pivots in accept order
+// are the accepted positions' own 1 + Delta (1 - G_jj) factors (the Sherman-Morrison
+// sequence is the LU factorisation of Gamma in that order), non-zero because a zero
+// factor gives weight 0 and is rejected.
 template <class A>
 __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   typedef typename A::Z Z;
@@ -103,58 +111,86 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   extern __shared__ __align__(16) unsigned char upd_raw[];
   Z* Gh = reinterpret_cast<Z*>(upd_raw);
   Z* G0 = Gh + 2 * KM * LD;
-  __shared__ Z s_mye[2][KM], s_dlt[2][KM], s_tcol[2][2][KM], s_K[KM], s_rowt[2][KM], s_piv[2][2];
+  // per position
+  __shared__ Z s_mye[2][KM], s_dlt[2][KM], s_tcol[2][2][KM], s_rowt[2][KM], s_piv[2][2];
   __shared__ zd s_dlt64[2][KM];
+  __shared__ int s_psite[KM], s_pvis[KM], s_pkind[KM], s_accq[KM], s_acc[2];
+  // per visit
+  __shared__ Z s_K[KM];
   __shared__ R s_u2[KM], s_gr[KM];
-  __shared__ int s_site[KM], s_vtx[KM], s_snew[KM], s_prop[KM], s_accq[KM], s_acc[2];
+  __shared__ int s_vtx[KM], s_snew[KM], s_prop[KM];
   __shared__ short s_ij[KM * KM];
-  __shared__ int s_m;
+  __shared__ int s_m, s_np;
 
   const double2* G = reinterpret_cast<const double2*>(p.G) + (long long)c * p.sG;
   const int* site = p.V.site + (long long)c * p.V.sK;
+  const int* site2 = p.V.site2 + (long long)c * p.V.sK;
+  const int8_t* nsite = p.V.nsite + (long long)c * p.V.sK;
   const int8_t* ty = p.V.type + (long long)c * p.V.sK;
   const UpdTab* tab = p.tab + (long long)c * p.V.sK * 15;
   int8_t* fl = p.fields + (long long)c * p.L * M + (long long)(p.nt1 - 1) * M;
   const long long NN = (long long)N * N;
 
-  // Prologue: each vertex is visited once per block, so its old field is the field at
-  // block start and every visit's proposal, draws and transition factors are known.
-  if (tid < nq) {
-    const int q = tid, pos = p.q0 + q;
-    const int n = p.dir == 0 ? pos : M - 1 - pos;
-    s_vtx[q] = n;
-    s_site[q] = site[n];
-    const int v = p.visit_base + pos;
-    double u0, u1, uu2;
-    if (p.draws) {
-      const double* d = p.draws + (long long)c * p.sDraws + 3ll * v;
-      u0 = d[0]; u1 = d[1]; uu2 = d[2];
-    } else {
-      unsigned long long key = p.rngkey[c], ctr = p.rngctr[c] + 3ull * v;
-      u0 = alf_uniform(key, ctr); u1 = alf_uniform(key, ctr + 1); uu2 = alf_uniform(key, ctr + 2);
+  // Prologue (warp 0, lane q = visit): each vertex is visited once per block, so its old
+  // field is the field at block start and every visit's proposal, draws and transition
+  // factors are known; positions by an exclusive prefix sum of the vertex sizes.
+  if (warp == 0) {
+    const int q = lane;
+    int w = 0, n = 0;
+    if (q < nq) {
+      const int pos = p.q0 + q;
+      n = p.dir == 0 ? pos : M - 1 - pos;
+      w = nsite[n];
     }
-    const int so = fl[n], tp = ty[n];
-    const int ch = (tp == 1) ? 0 : nranf3(u0) - 1;
-    const int sn = (tp == 1) ? -so : (int)p.ft.flip[so + 2][ch];
-    s_snew[q] = sn;
-    s_prop[q] = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
-    s_u2[q] = A::mkr(uu2);
-    s_gr[q] = A::mkr(p.ft.grat[tp - 1][so + 2][sn + 2]);
-    zd K = zmk(1.0, 0.0);
-    for (int f = 0; f < F; ++f) {
-      const UpdTab e = tab[((long long)(f * M + n) * 5 + so + 2) * 3 + ch];
-      s_mye[f][q] = A::mk(e.myexp);
-      s_dlt[f][q] = A::mk(e.dlt);
-      s_dlt64[f][q] = e.dlt;
-      K = (f == 0) ? e.expal : zmul(K, e.expal);
+    int incl = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
     }
-    s_K[q] = A::mk(K);
+    const int p0 = incl - w;
+    if (lane == 31) s_np = incl;
+    if (q < nq) {
+      s_vtx[q] = n;
+      const int v = p.visit_base + p.q0 + q;
+      double u0, u1, uu2;
+      if (p.draws) {
+        const double* d = p.draws + (long long)c * p.sDraws + 3ll * v;
+        u0 = d[0]; u1 = d[1]; uu2 = d[2];
+      } else {
+        unsigned long long key = p.rngkey[c], ctr = p.rngctr[c] + 3ull * v;
+        u0 = alf_uniform(key, ctr); u1 = alf_uniform(key, ctr + 1); uu2 = alf_uniform(key, ctr + 2);
+      }
+      const int so = fl[n], tp = ty[n];
+      const int ch = (tp == 1) ? 0 : nranf3(u0) - 1;
+      const int sn = (tp == 1) ? -so : (int)p.ft.flip[so + 2][ch];
+      s_snew[q] = sn;
+      s_prop[q] = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
+      s_u2[q] = A::mkr(uu2);
+      s_gr[q] = A::mkr(p.ft.grat[tp - 1][so + 2][sn + 2]);
+      zd K = zmk(1.0, 0.0);
+      for (int f = 0; f < F; ++f) {
+        const UpdTab e = tab[((long long)(f * M + n) * 5 + so + 2) * 3 + ch];
+        for (int I = 0; I < w; ++I) {
+          s_mye[f][p0 + I] = A::mk(e.myexp[I]);
+          s_dlt[f][p0 + I] = A::mk(e.dlt[I]);
+          s_dlt64[f][p0 + I] = e.dlt[I];
+        }
+        K = (f == 0) ? e.expal : zmul(K, e.expal);
+      }
+      s_K[q] = A::mk(K);
+      for (int I = 0; I < w; ++I) {
+        s_psite[p0 + I] = I ? site2[n] : site[n];
+        s_pvis[p0 + I] = q;
+        s_pkind[p0 + I] = (w == 2) ? (I ? 2 : 1) : 0;  // 0 single, 1 first of a pair, 2 second
+      }
+    }
   }
   __syncthreads();
-  for (int a = warp; a < nq; a += NW)
-    if (lane < nq)
+  const int np = s_np;
+  for (int a = warp; a < np; a += NW)
+    if (lane < np)
       for (int f = 0; f < F; ++f) {
-        const Z v = A::mk(G[f * NN + s_site[a] + (long long)s_site[lane] * N]);
+        const Z v = A::mk(G[f * NN + s_psite[a] + (long long)s_psite[lane] * N]);
         Gh[(f * KM + a) * LD + lane] = v;
         G0[(f * KM + a) * LD + lane] = v;
       }
@@ -162,90 +198,131 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
 
   // warp-0 state (identical in all lanes)
   Z ph = A::mk(p.phase[c]);  // kept unnormalised (only its direction enters the weight)
-  int m = 0;
+  int m = 0, nacc = 0, pend = 0;
   long long n_prop = 0;
-  // Decide visit v from the current Ghat(v,v) (gd) and column Ghat(lane, v) (gc, lanes > v).
-  auto decide = [&](int v, const Z* gd, const Z* gc) {
+  auto accept_pos = [&](int v) {
+    if (lane == 0) {
+      s_accq[m] = v;
+      p.sites_out[(long long)c * KM + m] = s_psite[v];
+      for (int f = 0; f < F; ++f) p.delta_out[((long long)c * 2 + f) * KM + m] = s_dlt64[f][v];
+    }
+    m += 1;
+  };
+  // Decide position v from the current column v (gc, diagonal gd) and, for the first
+  // position of a pair, column v+1 (gc2).  Second positions follow their pair's decision.
+  auto decide = [&](int v, const Z* gd, const Z* gc, const Z* gc2) {
+    const int kind = s_pkind[v];
     int acc = 0;
-    Z Rt = A::zero();
-    if (s_prop[v]) {
-      Z D[2];
+    if (kind == 2) {  // second position of an accepted / rejected pair
+      acc = pend;
+      if (acc) {
 #pragma unroll
-      for (int f = 0; f < 2; ++f)  // Mat(1,1) = myexp - Delta G(P,P)
-        if (f < F) D[f] = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));
-      Rt = (F == 2) ? A::mul(D[0], D[1]) : D[0];
-      Rt = A::mul(Rt, s_K[v]);
+        for (int f = 0; f < 2; ++f)
+          if (f < F) {
+            const Z D = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));
+            const Z x = A::mul(s_dlt[f][v], A::rcp(D));
+            if (lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(x, gc[f]);
+          }
+        accept_pos(v);
+      }
+      if (lane == 0) s_acc[v & 1] = acc;
+      return;
+    }
+    const int q = s_pvis[v];
+    Z Rt = A::zero();
+    if (s_prop[q]) {
+      Z Rf[2], Df[2], x0[2];
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+        if (f < F) {
+          const Z D = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));  // Mat(1,1) = myexp - Delta G(P,P)
+          Rf[f] = D;
+          Df[f] = D;
+          if (kind == 1) {  // 2x2 determinant: D_a (myexp_b - Delta_b G'_bb)
+            x0[f] = A::mul(s_dlt[f][v], A::rcp(D));
+            const int w = v + 1;
+            const Z gww = A::shfl(gc2[f], w), gvw = A::shfl(gc2[f], v), gwv = A::shfl(gc[f], w);
+            const Z gp = A::mac(gww, A::mul(x0[f], gwv), gvw);
+            Rf[f] = A::mul(D, A::sub(s_mye[f][w], A::mul(s_dlt[f][w], gp)));
+          }
+        }
+      Rt = (F == 2) ? A::mul(Rf[0], Rf[1]) : Rf[0];
+      Rt = A::mul(Rt, s_K[q]);
       Z Rp = Rt;
       for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
-      Rt = A::scale(Rp, s_gr[v]);
+      Rt = A::scale(Rp, s_gr[q]);
       // weight = |Re(phase R) / Re(phase)| > u  (Wrapgr_mod.F90:141-143), division-free
       const R num = A::absr(A::re_mul(ph, Rt));
-      const R den = A::mulr(A::absr(A::re(ph)), s_u2[v]);
+      const R den = A::mulr(A::absr(A::re(ph)), s_u2[q]);
       acc = A::gt(num, den);
       if (acc) {
         ph = A::renorm(A::mul(ph, Rt));
 #pragma unroll
         for (int f = 0; f < 2; ++f)
           if (f < F) {
-            const Z x = A::mul(s_dlt[f][v], A::rcp(D[f]));  // Delta / Mat(1,1)
-            if (lane > v && lane < nq) s_tcol[v & 1][f][lane] = A::mul(x, gc[f]);
+            if (kind != 1) x0[f] = A::mul(s_dlt[f][v], A::rcp(Df[f]));  // Delta / Mat(1,1)
+            if (lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(x0[f], gc[f]);
           }
       }
     }
-    n_prop += s_prop[v];
+    n_prop += s_prop[q];
     if (lane == 0) {
       if (p.rec_acc) {
-        const long long r = (long long)c * p.sRec + p.visit_base + p.q0 + v;
+        const long long r = (long long)c * p.sRec + p.visit_base + p.q0 + q;
         p.rec_acc[r] = (int8_t)acc;
         p.rec_ratio[r] = A::wide(Rt);
       }
-      if (acc) {
-        s_accq[m] = v;
-        p.sites_out[(long long)c * KM + m] = s_site[v];
-        for (int f = 0; f < F; ++f) p.delta_out[((long long)c * 2 + f) * KM + m] = s_dlt64[f][v];
-        fl[s_vtx[v]] = (int8_t)s_snew[v];
-      }
+      if (acc) fl[s_vtx[q]] = (int8_t)s_snew[q];
       s_acc[v & 1] = acc;
     }
-    m += acc;
+    if (acc) { accept_pos(v); nacc += 1; }
+    pend = acc;
   };
 
   if (warp == 0) {
-    Z gd[2], gc[2];
+    Z gd[2], gc[2], gc2[2];
 #pragma unroll
     for (int f = 0; f < 2; ++f)
       if (f < F) {
-        gc[f] = (lane < nq) ? Gh[(f * KM + lane) * LD] : A::zero();
+        gc[f] = (lane < np) ? Gh[(f * KM + lane) * LD] : A::zero();
+        gc2[f] = (lane < np && np > 1) ? Gh[(f * KM + lane) * LD + 1] : A::zero();
         gd[f] = Gh[f * KM * LD];
       }
-    decide(0, gd, gc);
+    decide(0, gd, gc, gc2);
   }
   __syncthreads();
-  for (int q = 0; q < nq; ++q) {
+  for (int q = 0; q < np; ++q) {
     const int acc = s_acc[q & 1];
+    const int v = q + 1;
+    // columns warp 0 brings up to date for its next decision: v, and v+1 if v opens a pair
+    const int wc = (v < np && s_pkind[v] == 1) ? 2 : 1;
     if (warp == 0) {
-      if (q + 1 < nq) {
-        const int v = q + 1;
-        Z gd[2], gc[2];
+      if (v < np) {
+        Z gd[2], gc[2], gc2[2];
 #pragma unroll
         for (int f = 0; f < 2; ++f)
           if (f < F) {
-            Z col = (lane < nq) ? Gh[(f * KM + lane) * LD + v] : A::zero();
-            if (acc && lane > q && lane < nq) {  // column v of the rank-1 update of visit q
-              col = A::mac(col, s_tcol[q & 1][f][lane], Gh[(f * KM + q) * LD + v]);
-              Gh[(f * KM + lane) * LD + v] = col;
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+              if (t >= wc) continue;
+              const int col_i = v + t;
+              Z col = (lane < np) ? Gh[(f * KM + lane) * LD + col_i] : A::zero();
+              if (acc && lane > q && lane < np) {  // column col_i of the rank-1 update of position q
+                col = A::mac(col, s_tcol[q & 1][f][lane], Gh[(f * KM + q) * LD + col_i]);
+                Gh[(f * KM + lane) * LD + col_i] = col;
+              }
+              if (t == 0) gc[f] = col; else gc2[f] = col;
             }
-            gc[f] = col;
-            gd[f] = A::shfl(col, v);
+            gd[f] = A::shfl(gc[f], v);
           }
-        decide(v, gd, gc);
+        decide(v, gd, gc, gc2);
       }
     } else if (acc) {
-      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b), rows a > q, columns b > q+1
+      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b), rows a > q, columns b > q + wc
       const int b = lane;
-      if (b > q + 1 && b < nq)
+      if (b > q + wc && b < np)
         for (int f = 0; f < F; ++f)
-          for (int a = q + warp; a < nq; a += NW - 1) {
+          for (int a = q + warp; a < np; a += NW - 1) {
             Z* g = Gh + (f * KM + a) * LD + b;
             *g = A::mac(*g, s_tcol[q & 1][f][a], Gh[(f * KM + q) * LD + b]);
           }
@@ -304,7 +381,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
     for (int f = 0; f < F; ++f) p.m_out[p.nChains + c * F + f] = m;
     if (m > 0) p.phase[c] = A::unit(ph);
     long long* cn = p.cnt + 4ll * c;
-    cn[0] += n_prop; cn[1] += m; cn[2] += nq; cn[3] += m;
+    cn[0] += n_prop; cn[1] += nacc; cn[2] += nq; cn[3] += nacc;
   }
 }
 
