@@ -393,7 +393,7 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
       ap.V = Aout; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
       ap.C = Aout; ap.ldc = N; ap.sC = NN;
       ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0 + w; ap.conj_tau = 1; ap.init = 0;
-      k_bqr_apply<ArD><<<dim3(N - j0 - w, B), 128, 0, h->st>>>(ap);
+      bqr_apply<ArD>(ap, dim3(N - j0 - w, B), h->st);
       CKL();
     }
   }
@@ -419,8 +419,8 @@ static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
     ap.V = h->qr_df ? (const void*)h->QRdf : (const void*)F; ap.ldv = N; ap.sV = NN; ap.tau = h->tau; ap.sT = N;
     ap.C = Q; ap.ldc = N; ap.sC = NN;
     ap.N = N; ap.j0 = j0; ap.nb = w; ap.c0 = j0; ap.conj_tau = 0; ap.init = 1;
-    if (h->qr_df) k_bqr_apply<ArF><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
-    else k_bqr_apply<ArD><<<dim3(N - j0, B), 128, 0, h->st>>>(ap);
+    if (h->qr_df) bqr_apply<ArF>(ap, dim3(N - j0, B), h->st);
+    else bqr_apply<ArD>(ap, dim3(N - j0, B), h->st);
     CKL();
   }
   prof_end(h);
@@ -716,7 +716,7 @@ static int unmqr_n(alfgpu_s* h, const zd* F, const zd* tau, zd* Cm, int N2) {
     ap.V = F; ap.ldv = N2; ap.sV = NN2; ap.tau = tau; ap.sT = N2;
     ap.C = Cm; ap.ldc = N2; ap.sC = NN2;
     ap.N = N2; ap.j0 = j0; ap.nb = w; ap.c0 = 0; ap.conj_tau = 0; ap.init = 0;
-    k_bqr_apply<ArD><<<dim3(N2, h->B), 128, 0, h->st>>>(ap);
+    bqr_apply<ArD>(ap, dim3(N2, h->B), h->st);
     CKL();
   }
   return 0;

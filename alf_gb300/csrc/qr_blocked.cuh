@@ -233,9 +233,11 @@ struct BQRApply {
 // blocks above the reflector are skipped warp-uniformly; the four warp partials of
 // v^H x meet in shared memory (double-buffered: one barrier per reflector); the next
 // reflector is prefetched.  Arithmetic A: ArD or ArF.
-#define BQR_QW (BQR_LROWS / 4)
-template <class A>
+// QW: 32-row blocks per warp (4 * 32 * QW rows at most); launched with the smallest
+// QW that covers the matrix (bqr_apply below).
+template <class A, int QW>
 __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
+  constexpr int BQR_QW = QW;
   typedef typename A::Z Z;
   const int b = blockIdx.y, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int c = p.c0 + blockIdx.x;
@@ -305,6 +307,14 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
     const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
     if (blk < nblk && r < N) col[r] = A::wide(x[q]);
   }
+}
+
+template <class A>
+static inline void bqr_apply(const BQRApply& ap, dim3 grid, cudaStream_t st) {
+  const int rows = ap.N - ap.j0;
+  if (rows <= 256) k_bqr_apply<A, 2><<<grid, 128, 0, st>>>(ap);
+  else if (rows <= 512) k_bqr_apply<A, 4><<<grid, 128, 0, st>>>(ap);
+  else k_bqr_apply<A, BQR_LROWS / 4><<<grid, 128, 0, st>>>(ap);
 }
 
 // R(i, j) /= D(i) for j >= i (QDRP row normalisation); block x == 0 also forms

@@ -213,16 +213,16 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   auto decide = [&](int v, const Z* gd, const Z* gc, const Z* gc2) {
     const int kind = s_pkind[v];
     int acc = 0;
+    const int fo = (F == 2) ? (lane & 1) : 0;  // flavour of this lane's scalar work
     if (kind == 2) {  // second position of an accepted / rejected pair
       acc = pend;
       if (acc) {
+        const Z D = A::sub(s_mye[fo][v], A::mul(s_dlt[fo][v], fo ? gd[1] : gd[0]));
+        const Z xm = A::mul(s_dlt[fo][v], A::rcp(D));
+        const Z x[2] = {A::shfl(xm, 0), A::shfl(xm, 1)};
 #pragma unroll
         for (int f = 0; f < 2; ++f)
-          if (f < F) {
-            const Z D = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));
-            const Z x = A::mul(s_dlt[f][v], A::rcp(D));
-            if (lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(x, gc[f]);
-          }
+          if (f < F && lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(x[f], gc[f]);
         accept_pos(v);
       }
       if (lane == 0) s_acc[v & 1] = acc;
@@ -231,22 +231,19 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
     const int q = s_pvis[v];
     Z Rt = A::zero();
     if (s_prop[q]) {
-      Z Rf[2], Df[2], x0[2];
-#pragma unroll
-      for (int f = 0; f < 2; ++f)
-        if (f < F) {
-          const Z D = A::sub(s_mye[f][v], A::mul(s_dlt[f][v], gd[f]));  // Mat(1,1) = myexp - Delta G(P,P)
-          Rf[f] = D;
-          Df[f] = D;
-          if (kind == 1) {  // 2x2 determinant: D_a (myexp_b - Delta_b G'_bb)
-            x0[f] = A::mul(s_dlt[f][v], A::rcp(D));
-            const int w = v + 1;
-            const Z gww = A::shfl(gc2[f], w), gvw = A::shfl(gc2[f], v), gwv = A::shfl(gc[f], w);
-            const Z gp = A::mac(gww, A::mul(x0[f], gwv), gvw);
-            Rf[f] = A::mul(D, A::sub(s_mye[f][w], A::mul(s_dlt[f][w], gp)));
-          }
-        }
-      Rt = (F == 2) ? A::mul(Rf[0], Rf[1]) : Rf[0];
+      // lane parity carries flavour fo: Mat(1,1) = myexp - Delta G(P,P), and for the first
+      // position of a pair the 2x2 determinant D_a (myexp_b - Delta_b G'_bb)
+      const Z D = A::sub(s_mye[fo][v], A::mul(s_dlt[fo][v], fo ? gd[1] : gd[0]));
+      Z Rm = D, xm = A::zero();
+      if (kind == 1) {
+        xm = A::mul(s_dlt[fo][v], A::rcp(D));
+        const int w = v + 1;
+        const Z c2 = fo ? gc2[1] : gc2[0], c1 = fo ? gc[1] : gc[0];
+        const Z gww = A::shfl(c2, w), gvw = A::shfl(c2, v), gwv = A::shfl(c1, w);
+        const Z gp = A::mac(gww, A::mul(xm, gwv), gvw);
+        Rm = A::mul(D, A::sub(s_mye[fo][w], A::mul(s_dlt[fo][w], gp)));
+      }
+      Rt = (F == 2) ? A::mul(A::shfl(Rm, 0), A::shfl(Rm, 1)) : Rm;
       Rt = A::mul(Rt, s_K[q]);
       Z Rp = Rt;
       for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
@@ -257,12 +254,11 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       acc = A::gt(num, den);
       if (acc) {
         ph = A::renorm(A::mul(ph, Rt));
+        if (kind != 1) xm = A::mul(s_dlt[fo][v], A::rcp(D));  // Delta / Mat(1,1)
+        const Z x[2] = {A::shfl(xm, 0), A::shfl(xm, 1)};
 #pragma unroll
         for (int f = 0; f < 2; ++f)
-          if (f < F) {
-            if (kind != 1) x0[f] = A::mul(s_dlt[f][v], A::rcp(Df[f]));  // Delta / Mat(1,1)
-            if (lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(x0[f], gc[f]);
-          }
+          if (f < F && lane > v && lane < np) s_tcol[v & 1][f][lane] = A::mul(F == 2 ? x[f] : xm, gc[f]);
       }
     }
     n_prop += s_prop[q];
@@ -317,12 +313,14 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
           }
         decide(v, gd, gc, gc2);
       }
-    } else if (acc) {
-      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b), rows a > q, columns b > q + wc
+    } else if (acc && warp != 4) {
+      // Ghat(a,b) += x Ghat(a,q) Ghat(q,b), rows a > q, columns b > q + wc.  Warp 4 shares
+      // warp 0's SM sub-partition (FP64 unit) and stays idle so the chain is not delayed.
+      const int wk = warp < 4 ? warp : warp - 1;  // 1..6
       const int b = lane;
       if (b > q + wc && b < np)
         for (int f = 0; f < F; ++f)
-          for (int a = q + warp; a < np; a += NW - 1) {
+          for (int a = q + wk; a < np; a += NW - 2) {
             Z* g = Gh + (f * KM + a) * LD + b;
             *g = A::mac(*g, s_tcol[q & 1][f][a], Gh[(f * KM + q) * LD + b]);
           }

@@ -40,7 +40,7 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_DMMA_TFLOPS = 1.048
 # DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
 # the ncu capture summarised in profiles/k_zgemm_hop_hubbard16x16_fp64.md
-HOP_TRAFFIC_BYTES = None
+HOP_TRAFFIC_BYTES = 3.30e6
 
 
 def parse():
@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
     ap.add_argument("--pivoting", default="exact", choices=["norms", "exact", "exact-cgr", "exact-decompose"])
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--chains", type=int, default=1, help="independent chains per GPU (batched)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -131,15 +132,19 @@ def algorithmic_flops(m, phase: str, launches: int, n_acc: int) -> float:
 def run_ours(args, ws, rank, local):
     import torch
     from alf_gb300 import model as mdl, rng
+    from alf_gb300 import replicas
     from alf_gb300.sweep import Chains
 
     torch.cuda.set_device(local)
     m = mdl.config(args.config)
-    seed = args.seed + 1000 * rank
-    ch = Chains(m, n_chains=1, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags)
-    ch.set_fields(0, rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    C = args.chains
+    seed = replicas.replica_seed(args.seed, rank)
+    ch = Chains(m, n_chains=C, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags)
+    for c in range(C):
+        ch.set_fields(c, rng.initial_fields(replicas.replica_seed(args.seed, rank, c), c, m.n_op, m.ltrot))
     ch.init_state()
-    ch.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    for c in range(C):
+        ch.set_rng(c, replicas.replica_seed(args.seed, rank, c), rng.sweep_counter_base(m.n_op, m.ltrot, 0))
     stream = torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local)
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > 129 MB L2
 
@@ -167,7 +172,8 @@ def run_ours(args, ws, rank, local):
     st = ch.stats(0)
     n_acc = st.n_acc
     # e2e through the C ABI with host buffers
-    u_host = [rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 1000 + i)[None, :] for i in range(args.steps)]
+    u_host = [np.stack([rng.sweep_uniforms(replicas.replica_seed(args.seed, rank, c), c, m.n_op, m.ltrot, 1000 + i)
+                        for c in range(C)]) for i in range(args.steps)]
     G_host = np.zeros((m.n_fl, m.ndim, m.ndim), np.complex128)
     h2d = u_host[0].nbytes
     d2h = G_host.nbytes
@@ -185,10 +191,7 @@ def run_ours(args, ws, rank, local):
     prof = ch.profile()
     ch.set_profiling(False)
     # launch count per sweep from the profile pass
-    times = torch.tensor([ms / 1e3, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-    if ws > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    t_dev, t_e2e = float(times[0]), float(times[1])
+    t_dev, t_e2e = replicas.max_over_ranks([ms / 1e3, e2e_s], device=f"cuda:{local}")
     return dict(m=m, t_dev=t_dev, t_e2e=t_e2e, clocks=clk.summary(), prof=prof, n_acc=n_acc, h2d=h2d, d2h=d2h,
                 stats=st, chains=ch, launches=n_launch)
 
@@ -217,8 +220,9 @@ def main():
     m = mdl.config(args.config)
     workload = {"workload": f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
                             f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
-                            f"Nwrap={m.nwrap}, Mz four-valued fields, one chain per GPU",
-                "chains_per_gpu": 1, "precision": args.precision, "pivoting": args.pivoting, "flags": args.flags, "l2": "flushed between timed steps (256 MB write)",
+                            f"Nwrap={m.nwrap}, Mz four-valued fields, "
+                            + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"),
+                "chains_per_gpu": args.chains, "precision": args.precision, "pivoting": args.pivoting, "flags": args.flags, "l2": "flushed between timed steps (256 MB write)",
                 "draws": "device counter stream (value); host arrays through the C ABI (e2e)"}
     if args.impl == "reference":
         if rank != 0:
@@ -247,9 +251,9 @@ def main():
     if rank != 0:
         return
     m = r["m"]
-    total_sweeps = args.steps * ws
-    value = total_sweeps / r["t_dev"]
-    e2e = total_sweeps / r["t_e2e"]
+    from alf_gb300 import replicas
+    value = replicas.whole_job_rate(ws, args.chains, args.steps, r["t_dev"])
+    e2e = replicas.whole_job_rate(ws, args.chains, args.steps, r["t_e2e"])
     prof = r["prof"]
     # Roofline of the dominant kernel: the complex GEMM (k_zgemm on FP64 DMMA; k_dfgemm in
     # the mixed form) carries the largest share of the launch list, and its largest
