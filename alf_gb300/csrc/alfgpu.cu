@@ -45,6 +45,10 @@ struct alfgpu_s {
   int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
   // time-displaced Green functions (ltau = 1)
   int ltau = 0;
+  // CUDA graphs of the sweep: [0] device draws, [1] host draws (copied before the launch)
+  int use_graph = 1;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  long long glaunches[2] = {0, 0};
   zd *GT0 = nullptr, *G0T = nullptr, *G00 = nullptr, *GTT = nullptr, *Hn[4] = {nullptr, nullptr, nullptr, nullptr};
   UDVSet udvr_tau;
   zd *HB1 = nullptr, *HB2 = nullptr, *HLP = nullptr, *tau2 = nullptr, *V1I = nullptr, *Qt = nullptr;
@@ -285,6 +289,11 @@ static GemmParams gsq(alfgpu_s* h, int batch) {  // N x N x N square product, ba
   return p;
 }
 
+static void drop_graphs(alfgpu_s* h) {
+  for (int g = 0; g < 2; ++g)
+    if (h->gexec[g]) { cudaGraphExecDestroy(h->gexec[g]); h->gexec[g] = nullptr; }
+}
+
 static int copy_mats(alfgpu_s* h, zd* dst, const zd* src, size_t count) {
   CK(cudaMemcpyAsync(dst, src, count * sizeof(zd), cudaMemcpyDeviceToDevice, h->st));
   return 0;
@@ -474,7 +483,7 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   }
   p.C = h->Vtmp;
   RET(gemm_s(h, p));
-  std::swap(s.V, h->Vtmp);
+  RET(copy_mats(h, s.V, h->Vtmp, (size_t)B * N * N));  // buffer roles stay fixed (graph replay)
   CK(cudaMemcpyAsync(s.D, h->DUP, (size_t)B * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   RET(orgqr_any(h, h->QRw, s.U));
   k_scale_col0<<<B, 256, 0, h->st>>>(s.U, N, h->dphase);
@@ -566,7 +575,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
     prof_end(h);
     CKL();
     // G = U_L * P RHS (ZLAPMR backward folded into the B load)
@@ -584,7 +593,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 1;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
     prof_end(h);
     CKL();
     // G = (RHS P) U_R^H (ZLAPMT backward folded into the A load)
@@ -738,7 +747,7 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
     t.T = h->QRw; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, N * sizeof(zd), h->st>>>(t);
+    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
     prof_end(h);
     CKL();
   }
@@ -759,7 +768,7 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
     t.N = N2; t.nvec = N2; t.lower = 1; t.conj_io = 0; t.trans = 1;
     t.oscale = nullptr;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N2, B), 256, N2 * sizeof(zd), h->st>>>(t);
+    k_trsv<<<dim3(N2, B), 256, 3 * N2 * sizeof(zd), h->st>>>(t);
     prof_end(h);
     CKL();
   }
@@ -999,6 +1008,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->exact_cgr = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_CGR)) ? 1 : 0;
   h->df_stab = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_GEMM);
   h->df_qr = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_QR);
+  h->use_graph = !(d.reserved[0] & ALFGPU_FLAG_NO_GRAPH);
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
@@ -1121,6 +1131,7 @@ void alfgpu_destroy(alfgpu_t* h) {
   if (!h) return;
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
+  drop_graphs(h);
   for (void* p : h->allocs) cudaFree(p);
   if (h->obs_host) cudaFreeHost(h->obs_host);
   if (h->tau_host) cudaFreeHost(h->tau_host);
@@ -1355,6 +1366,7 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
     CK(cudaMemcpy(h->rot_dev, pp.data(), pp.size() * sizeof(int), cudaMemcpyHostToDevice));
   }
   if (rot_changed && h->hop_ok) RET(upload_expT(h));
+  drop_graphs(h);  // block partition and basis may have changed
   h->vert_ok = true;
   return 0;
 }
@@ -1429,19 +1441,10 @@ int alfgpu_init_state(alfgpu_t* h, double* phase_out) {
   return 0;
 }
 
-int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
-  if (!h) return ALFGPU_ERROR_ARGUMENT;
-  if (!h->state_ok) return ALFGPU_ERROR_ARGUMENT;
-  CK(cudaSetDevice(h->dev));
+// The sweep proper (main.F90:714-887): everything between the host copies of the draws and
+// the error check, so that it can be captured once into a CUDA graph and replayed.
+static int sweep_body(alfgpu_s* h, const double* dr, alfgpu_obs_cb cb, void* ctx) {
   const int L = h->L, M = h->M, Nstm = h->Nstm;
-  const double* dr = nullptr;
-  if (uniforms) {
-    CK(cudaMemcpyAsync(h->draws, uniforms, (size_t)h->C * 6 * M * L * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    dr = h->draws;
-  } else {
-    CK(cudaMemcpyAsync(h->rngkey, h->h_key.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->rngctr, h->h_ctr.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
-  }
   h->rec_stab = 0;
   // up pass (main.F90:717-774)
   RET(udv_reset(h, h->udvr));
@@ -1493,12 +1496,55 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
   RET(stabilise(h, 1, 1));
   RET(udv_reset(h, h->udvst[Nstm - 1]));
   if (h->ltau) RET(tau_m(h, cb, ctx));  // main.F90:879-881
+  k_count_sweep<<<(h->C + 127) / 128, 128, 0, h->st>>>(h->stat, h->C);
+  CKL();
+  return 0;
+}
+
+int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  if (!h->state_ok) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  const int L = h->L, M = h->M;
+  const double* dr = nullptr;
+  if (uniforms) {
+    CK(cudaMemcpyAsync(h->draws, uniforms, (size_t)h->C * 6 * M * L * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    dr = h->draws;
+  } else {
+    CK(cudaMemcpyAsync(h->rngkey, h->h_key.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->rngctr, h->h_ctr.data(), h->C * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st));
+  }
+  // the launch sequence is fixed for a handle, so the sweep is captured once into a graph
+  // (per draw source) and replayed; callbacks, recording, profiling and TAU_M's buffer
+  // rotation run the stream path
+  const int gi = uniforms ? 1 : 0;
+  if (h->use_graph && !cb && !h->profiling && !h->recording && !h->ltau) {
+    if (!h->gexec[gi]) {
+      const long long l0 = h->launches;
+      CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+      const int rc = sweep_body(h, dr, nullptr, nullptr);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
+      if (rc || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        h->launches = l0;
+        if (rc) return rc;
+        h->last_cuda = ce;
+        return ALFGPU_ERROR_CUDA;
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&h->gexec[gi], graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) { h->gexec[gi] = nullptr; h->last_cuda = ie; return ALFGPU_ERROR_CUDA; }
+      h->glaunches[gi] = h->launches - l0;
+      h->launches = l0;
+    }
+    CK(cudaGraphLaunch(h->gexec[gi], h->st));
+    h->launches += h->glaunches[gi];
+  } else {
+    RET(sweep_body(h, dr, cb, ctx));
+  }
   if (!uniforms)
     for (int c = 0; c < h->C; ++c) h->h_ctr[c] += 6ull * M * L;
-  {
-    k_count_sweep<<<(h->C + 127) / 128, 128, 0, h->st>>>(h->stat, h->C);
-    CKL();
-  }
   int rc = check_err(h);
   prof_collect(h);
   return rc;

@@ -274,39 +274,43 @@ struct TrsvParams {
   const double* oscale;  // optional: x_i *= oscale[i] after the solve (per batch, stride N)
 };
 
+// Dynamic shared memory: 3 N complex values (right-hand side, solution, diagonal
+// reciprocals).  Every thread forms x_i itself from the finished right-hand side entry,
+// so a row costs one barrier and no serial division.
 __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
   const int b = blockIdx.y, v = blockIdx.x, N = p.N;
   if (v >= p.nvec) return;
   const zd* T = p.T + b * p.sT;
   zd* x = p.B + b * p.sB + (long long)v * p.vstride;
   extern __shared__ zd xs[];
+  zd* xo = xs + N;
+  zd* dinv = xo + N;
   auto Tij = [&](int i, int j) -> zd {
     return p.trans ? zconj(T[j + (long long)i * p.ldt]) : T[i + (long long)j * p.ldt];
   };
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     zd t = x[(long long)i * p.estride];
     xs[i] = p.conj_io ? zconj(t) : t;
+    dinv[i] = zinv(Tij(i, i));
   }
   __syncthreads();
   if (!p.lower) {
     for (int i = N - 1; i >= 0; --i) {
-      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], Tij(i, i));
-      __syncthreads();
-      const zd xi = xs[i];
+      const zd xi = zmul(xs[i], dinv[i]);
+      if (threadIdx.x == 0) xo[i] = xi;
       for (int r = threadIdx.x; r < i; r += blockDim.x) xs[r] = zsub(xs[r], zmul(Tij(r, i), xi));
       __syncthreads();
     }
   } else {
     for (int i = 0; i < N; ++i) {
-      if (threadIdx.x == 0) xs[i] = zdiv(xs[i], Tij(i, i));
-      __syncthreads();
-      const zd xi = xs[i];
+      const zd xi = zmul(xs[i], dinv[i]);
+      if (threadIdx.x == 0) xo[i] = xi;
       for (int r = i + 1 + threadIdx.x; r < N; r += blockDim.x) xs[r] = zsub(xs[r], zmul(Tij(r, i), xi));
       __syncthreads();
     }
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    zd t = xs[i];
+    zd t = xo[i];
     if (p.oscale) t = zscale(t, p.oscale[(long long)b * N + i]);
     x[(long long)i * p.estride] = p.conj_io ? zconj(t) : t;
   }

@@ -31,6 +31,7 @@ FLAG_EXACT_QRP_DECOMPOSE = 8
 FLAG_DF_STAB_QR = 16
 FLAG_DF_STAB_GEMM = 32
 FLAG_DF_STAB = 48
+FLAG_NO_GRAPH = 64
 PIVOTING = {"norms": 0, "exact": FLAG_EXACT_QRP, "exact-cgr": FLAG_EXACT_QRP_CGR,
             "exact-decompose": FLAG_EXACT_QRP_DECOMPOSE}
 

@@ -78,6 +78,10 @@ enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_EXACT_QRP_CGR = 4, ALFGPU_FLAG_EXA
  * rises from 2.5e-6 (FP64) to 7.9e-6 (_QR) and 2.1e-5 (both): double-float keeps 48
  * of FP64's 53 mantissa bits, and the UDV products amplify rounding. */
 enum { ALFGPU_FLAG_DF_STAB_QR = 16, ALFGPU_FLAG_DF_STAB_GEMM = 32, ALFGPU_FLAG_DF_STAB = 48 };
+/* alfgpu_sweep captures its launch sequence into a CUDA graph on first use (one per
+ * draw source) and replays it; sweeps with a callback, recording, profiling or TAU_M
+ * use the stream path.  ALFGPU_FLAG_NO_GRAPH always uses the stream path. */
+enum { ALFGPU_FLAG_NO_GRAPH = 64 };
 
 typedef struct alfgpu_s alfgpu_t;
 

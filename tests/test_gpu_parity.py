@@ -204,3 +204,24 @@ def test_batched_chains_match_single_chains():
         o.sweep(u[c])
         np.testing.assert_array_equal(g.fields(c), o.fields())
         assert _relmax(g.green(c), o.green()) < RTOL
+
+
+def test_graph_replay_matches_stream_path():
+    # alfgpu_sweep replays a captured CUDA graph; the stream path must give identical state
+    from alf_gb300.sweep import FLAG_NO_GRAPH
+    m = mdl.hubbard("square", 6, 6, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    seed = 31
+    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+    out = []
+    for flags in (0, FLAG_NO_GRAPH):
+        g = Chains(m, flags=flags)
+        g.set_fields(0, f0)
+        g.init_state()
+        g.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+        for s in range(3):
+            g.sweep(None)
+        g.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 7)[None, :])
+        out.append((g.fields(0), g.green(0), g.phase()[0], g.stats(0).n_acc))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert _relmax(out[0][1], out[1][1]) == 0.0
+    assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
