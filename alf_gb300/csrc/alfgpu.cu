@@ -93,6 +93,8 @@ struct alfgpu_s {
   // stabilisation work
   zd *TP = nullptr, *Qb = nullptr, *RHS = nullptr, *tau = nullptr, *Vtmp = nullptr, *dphase = nullptr;
   zd* QRw = nullptr;         // factored matrix (R above, reflectors below) of the last QR
+  zd* gws = nullptr;         // split-K partial products of k_zgemm
+  long long gws_elems = 0;
   double* qkeys = nullptr;   // column keys of the pre-pivoting
   int *jpvt = nullptr, *perm = nullptr, *iperm = nullptr;
   double *DUP = nullptr, *vn = nullptr, *cmp = nullptr, *opang = nullptr;
@@ -259,8 +261,9 @@ static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
 
 
 static int gemm(alfgpu_s* h, const GemmParams& p) {
-  h->launches++;
-  CK(launch_zgemm(p, h->st));
+  int nl = 1;
+  CK(launch_zgemm(p, h->st, h->gws, h->gws_elems, &nl));
+  h->launches += nl;
   return 0;
 }
 
@@ -1093,6 +1096,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   for (auto& s : h->udvst) r |= mk_udv(s);
   r |= dalloc(h, &h->TP, B * NN); r |= dalloc(h, &h->Qb, B * NN); r |= dalloc(h, &h->RHS, B * NN);
   r |= dalloc(h, &h->QRw, B * NN); r |= dalloc(h, &h->qkeys, B * N);
+  h->gws_elems = 4ll * B * NN;
+  r |= dalloc(h, &h->gws, (size_t)h->gws_elems);
   h->ltau = d.ltau;
   if (h->ltau) {
     const size_t N2 = 2 * N, NN2 = N2 * N2;

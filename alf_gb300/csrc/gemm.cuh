@@ -28,6 +28,8 @@ struct GemmParams {
   const int* kdyn;  // per-batch K (<= k) or null
   int batch;
   int modA, modB;   // if > 0, operand batch index = b % mod (an operand shared across chains)
+  int ksplit;       // > 1: K split over ksplit CTAs per tile, partials into ws, summed by k_zgemm_reduce
+  zd* ws;           // [ksplit][batch][m][n] partial products (column-major per matrix)
 };
 
 static inline GemmParams gemm_defaults() {
@@ -36,6 +38,7 @@ static inline GemmParams gemm_defaults() {
   p.alpha = zmk(1.0, 0.0);
   p.beta = zmk(0.0, 0.0);
   p.batch = 1;
+  p.ksplit = 1;
   return p;
 }
 
@@ -73,13 +76,18 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
   __shared__ double As[2][GEMM_BK][SA];  // [re/im][k][m]
   __shared__ double Bs[2][GEMM_BK][SB];  // [re/im][k][n]
 
-  const int b = blockIdx.z;
+  const int ksplit = p.ksplit > 1 ? p.ksplit : 1;
+  const int b = blockIdx.z / ksplit, sidx = blockIdx.z % ksplit;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp % WARPS_M) * WM, wn = (warp / WARPS_M) * WN;
   const int g = lane >> 2, t = lane & 3;
 
-  const int K = p.kdyn ? min(p.kdyn[b], p.k) : p.k;
+  const int Kall = p.kdyn ? min(p.kdyn[b], p.k) : p.k;
+  // this CTA's K range (split-K): chunks of whole k-tiles
+  const int kchunk = ((p.k + ksplit - 1) / ksplit + GEMM_BK - 1) / GEMM_BK * GEMM_BK;
+  const int kbeg = sidx * kchunk;
+  const int K = min(Kall, kbeg + kchunk);
   const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
   const void* A = p.realA ? (const void*)((const double*)p.A + bA * p.sA) : (const void*)((const zd*)p.A + bA * p.sA);
   const void* B = p.realB ? (const void*)((const double*)p.B + bB * p.sB) : (const void*)((const zd*)p.B + bB * p.sB);
@@ -104,7 +112,7 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
     for (int r = 0; r < AE; ++r) {
       int e = tid + r * NT, i, kk;
       if (p.opA == OP_N) { i = e % BM; kk = e / BM; } else { kk = e % GEMM_BK; i = e / GEMM_BK; }
-      zd v = gemm_ld(A, p.lda, p.opA, p.realA, p.triA, pA, m0 + i, k0 + kk, p.m, K);
+      zd v = gemm_ld(A, p.lda, p.opA, p.realA, p.triA, pA, m0 + i, k0 + kk, p.m, K);  // K: end of this range
       if (ks && p.ksOnA && k0 + kk < K) {
         zd s = ks[k0 + kk];
         if (p.ksConj) s.y = -s.y;
@@ -158,13 +166,13 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
     }
   };
 
-  const int nk = (K + GEMM_BK - 1) / GEMM_BK;
-  if (nk > 0) load_tile(0);
+  const int nk = K > kbeg ? (K - kbeg + GEMM_BK - 1) / GEMM_BK : 0;
+  if (nk > 0) load_tile(kbeg);
   for (int kt = 0; kt < nk; ++kt) {
     __syncthreads();
     store_tile();
     __syncthreads();
-    if (kt + 1 < nk) load_tile((kt + 1) * GEMM_BK);
+    if (kt + 1 < nk) load_tile(kbeg + (kt + 1) * GEMM_BK);
 #pragma unroll
     for (int k4 = 0; k4 < GEMM_BK; k4 += 4) {
       double ar[MI], ai[MI], br[NI], bi[NI];
@@ -178,15 +186,30 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
         br[j] = Bs[0][k4 + t][wn + j * 8 + g];
         bi[j] = Bs[1][k4 + t][wn + j * 8 + g];
       }
+      // the four real products of a complex tile, interleaved over the warp's tiles so that
+      // consecutive MMAs never update the same accumulator
 #pragma unroll
       for (int i = 0; i < MI; ++i)
 #pragma unroll
-        for (int j = 0; j < NI; ++j) {
-          dmma(acc[i][j][0][0], acc[i][j][0][1], ar[i], br[j]);
-          if (!p.realB) dmma(acc[i][j][1][0], acc[i][j][1][1], ar[i], bi[j]);
-          if (!p.realA) dmma(acc[i][j][1][0], acc[i][j][1][1], ai[i], br[j]);
-          if (cplx) dmma(acc[i][j][0][0], acc[i][j][0][1], -ai[i], bi[j]);
-        }
+        for (int j = 0; j < NI; ++j) dmma(acc[i][j][0][0], acc[i][j][0][1], ar[i], br[j]);
+      if (!p.realB) {
+#pragma unroll
+        for (int i = 0; i < MI; ++i)
+#pragma unroll
+          for (int j = 0; j < NI; ++j) dmma(acc[i][j][1][0], acc[i][j][1][1], ar[i], bi[j]);
+      }
+      if (!p.realA) {
+#pragma unroll
+        for (int i = 0; i < MI; ++i)
+#pragma unroll
+          for (int j = 0; j < NI; ++j) dmma(acc[i][j][1][0], acc[i][j][1][1], ai[i], br[j]);
+      }
+      if (cplx) {
+#pragma unroll
+        for (int i = 0; i < MI; ++i)
+#pragma unroll
+          for (int j = 0; j < NI; ++j) dmma(acc[i][j][0][0], acc[i][j][0][1], -ai[i], bi[j]);
+      }
     }
   }
 
@@ -202,6 +225,10 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
         int row = m0 + wm + i * 8 + g, col = n0 + wn + j * 8 + 2 * t + h;
         if (row < p.m && col < p.n) {
           zd v = zmk(acc[i][j][0][h], acc[i][j][1][h]);
+          if (ksplit > 1) {  // raw partial; scalings and beta in k_zgemm_reduce
+            p.ws[((long long)sidx * p.batch + b) * p.m * p.n + row + (long long)col * p.m] = v;
+            continue;
+          }
           if (rs) v = p.rsInv ? zdiv(v, rs[row]) : zmul(rs[row], v);
           if (cs) v = p.csInv ? zdiv(v, cs[col]) : zmul(v, cs[col]);
           v = zmul(p.alpha, v);
@@ -212,16 +239,56 @@ __global__ void __launch_bounds__((BM / WM) * (BN / 16) * 32) k_zgemm(GemmParams
       }
 }
 
-// Host launcher: picks the tile so that a single N=256 product still spreads over the SMs.
-static inline cudaError_t launch_zgemm(const GemmParams& p, cudaStream_t st) {
+// C = alpha op(rs) (sum_s partial_s) op(cs) + beta C, partials summed in split order (deterministic).
+// grid (ceil(m*n/256), batch)
+__global__ void k_zgemm_reduce(GemmParams p) {
+  const int b = blockIdx.y;
+  const long long mn = (long long)p.m * p.n;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= mn) return;
+  const int row = e % p.m, col = e / p.m;
+  zd v = p.ws[(long long)b * mn + e];
+  for (int s = 1; s < p.ksplit; ++s) v = zadd(v, p.ws[((long long)s * p.batch + b) * mn + e]);
+  const zd* rs = p.rs ? p.rs + b * p.sRS : nullptr;
+  const zd* cs = p.cs ? p.cs + b * p.sCS : nullptr;
+  if (rs) v = p.rsInv ? zdiv(v, rs[row]) : zmul(rs[row], v);
+  if (cs) v = p.csInv ? zdiv(v, cs[col]) : zmul(v, cs[col]);
+  v = zmul(p.alpha, v);
+  zd* cp = p.C + b * p.sC + row + (long long)col * p.ldc;
+  if (p.beta.x != 0.0 || p.beta.y != 0.0) v = zadd(v, zmul(p.beta, *cp));
+  *cp = v;
+}
+
+// Host launcher: 64 x 64 tiles when there are enough of them; otherwise 32 x 32 tiles, and
+// when even those leave SMs idle and K is long, K is split (workspace permitting) so that
+// several CTAs per SM hide the latency between dependent FP64 MMAs.
+static inline cudaError_t launch_zgemm(const GemmParams& p0, cudaStream_t st, zd* ws = nullptr,
+                                       long long ws_elems = 0, int* nlaunch = nullptr) {
+  GemmParams p = p0;
+  p.ksplit = 1;
+  if (nlaunch) *nlaunch = 1;
   if (p.m <= 0 || p.n <= 0 || p.batch <= 0) return cudaSuccess;
   long long tiles64 = (long long)((p.m + 63) / 64) * ((p.n + 63) / 64) * p.batch;
   if (tiles64 >= 256) {
     dim3 grid((p.n + 63) / 64, (p.m + 63) / 64, p.batch);
     k_zgemm<64, 64, 32><<<grid, 256, 0, st>>>(p);
-  } else {
-    dim3 grid((p.n + 31) / 32, (p.m + 31) / 32, p.batch);
-    k_zgemm<32, 32, 16><<<grid, 128, 0, st>>>(p);
+    return cudaGetLastError();
+  }
+  const long long tiles32 = (long long)((p.n + 31) / 32) * ((p.m + 31) / 32) * p.batch;
+  int ks = 1;
+  while (ks < 4 && tiles32 * ks < 3 * 152 && p.k / (2 * ks) >= 64) ks *= 2;
+  if (ks > 1 && ws && (long long)ks * p.batch * p.m * p.n <= ws_elems) {
+    p.ksplit = ks;
+    p.ws = ws;
+  }
+  dim3 grid((p.n + 31) / 32, (p.m + 31) / 32, p.batch * p.ksplit);
+  k_zgemm<32, 32, 16><<<grid, 128, 0, st>>>(p);
+  if (p.ksplit > 1) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 rg((unsigned)(((long long)p.m * p.n + 255) / 256), p.batch);
+    k_zgemm_reduce<<<rg, 256, 0, st>>>(p);
+    if (nlaunch) *nlaunch = 2;
   }
   return cudaGetLastError();
 }

@@ -233,10 +233,11 @@ struct BQRApply {
 // blocks above the reflector are skipped warp-uniformly; the four warp partials of
 // v^H x meet in shared memory (double-buffered: one barrier per reflector); the next
 // reflector is prefetched.  Arithmetic A: ArD or ArF.
-// QW: 32-row blocks per warp (4 * 32 * QW rows at most); launched with the smallest
-// QW that covers the matrix (bqr_apply below).
-template <class A, int QW>
-__global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
+// WPC warps per column (4: latency, one per sub-partition; 1: throughput, when the
+// columns of the launch already fill the GPU), QW 32-row blocks per warp (WPC * 32 * QW
+// rows at most); launched with the smallest QW that covers the matrix (bqr_apply below).
+template <class A, int QW, int WPC>
+__global__ void __launch_bounds__(32 * WPC) k_bqr_apply(BQRApply p) {
   constexpr int BQR_QW = QW;
   typedef typename A::Z Z;
   const int b = blockIdx.y, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -245,6 +246,7 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
   const int N = p.N, j0 = p.j0, nb = p.nb;
   const int nblk = (N - j0 + 31) >> 5;  // 32-row blocks
   const Z* V = reinterpret_cast<const Z*>(p.V) + b * p.sV;
+  constexpr int NWc = WPC;
   const zd* tau = p.tau + b * p.sT;
   zd* col = p.C + b * p.sC + (long long)c * p.ldc;
   const bool fresh = p.init && c < j0 + nb;
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
   Z x[BQR_QW], vn[BQR_QW];
 #pragma unroll
   for (int q = 0; q < BQR_QW; ++q) {
-    const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
+    const int blk = w + NWc * q, r = j0 + lane + 32 * blk;
     x[q] = A::zero();
     vn[q] = A::zero();
     if (blk < nblk && r < N) x[q] = fresh ? (r == c ? A::one() : A::zero()) : A::mk(col[r]);
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
     const Z* v = V + (long long)kc * p.ldv;
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
-      const int blk = w + 4 * q;
+      const int blk = w + NWc * q;
       if (blk < blo || blk >= nblk) continue;
       const int r = j0 + lane + 32 * blk;
       vn[q] = (r < kc || r >= N) ? A::zero() : (r == kc ? A::one() : v[r]);
@@ -283,38 +285,49 @@ __global__ void __launch_bounds__(128) k_bqr_apply(BQRApply p) {
     Z s = A::zero();
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
-      const int blk = w + 4 * q;
+      const int blk = w + NWc * q;
       if (blk < blo || blk >= nblk) continue;
       s = A::mac(s, A::conj(vr[q]), x[q]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s = A::add(s, A::shfl_xor(s, o));
-    if (lane == 0) red[par][w] = s;
-    __syncthreads();
-    const Z f = A::neg(A::mul(A::mk(t), A::add(A::add(red[par][0], red[par][1]), A::add(red[par][2], red[par][3]))));
-    par ^= 1;
+    Z tot = s;
+    if (NWc > 1) {
+      if (lane == 0) red[par][w] = s;
+      __syncthreads();
+      tot = A::add(A::add(red[par][0], red[par][1]), A::add(red[par][2], red[par][3]));
+      par ^= 1;
+    }
+    const Z f = A::neg(A::mul(A::mk(t), tot));
 #pragma unroll
     for (int q = 0; q < BQR_QW; ++q) {
-      const int blk = w + 4 * q;
+      const int blk = w + NWc * q;
       if (blk < blo || blk >= nblk) continue;
       x[q] = A::mac(x[q], vr[q], f);
     }
   }
   if (fresh)
-    for (int r = threadIdx.x; r < j0; r += 128) col[r] = zmk(0.0, 0.0);
+    for (int r = threadIdx.x; r < j0; r += 32 * NWc) col[r] = zmk(0.0, 0.0);
 #pragma unroll
   for (int q = 0; q < BQR_QW; ++q) {
-    const int blk = w + 4 * q, r = j0 + lane + 32 * blk;
+    const int blk = w + NWc * q, r = j0 + lane + 32 * blk;
     if (blk < nblk && r < N) col[r] = A::wide(x[q]);
   }
 }
 
+// Four warps per column while the launch's columns leave sub-partitions idle (latency),
+// one warp per column once they fill the GPU (fewer reduction instructions per flop).
 template <class A>
 static inline void bqr_apply(const BQRApply& ap, dim3 grid, cudaStream_t st) {
   const int rows = ap.N - ap.j0;
-  if (rows <= 256) k_bqr_apply<A, 2><<<grid, 128, 0, st>>>(ap);
-  else if (rows <= 512) k_bqr_apply<A, 4><<<grid, 128, 0, st>>>(ap);
-  else k_bqr_apply<A, BQR_LROWS / 4><<<grid, 128, 0, st>>>(ap);
+  const long long cols = (long long)grid.x * grid.y;
+  if (cols >= 4 * 152 && rows <= 256) {  // (more rows per lane would spill)
+    k_bqr_apply<A, 8, 1><<<grid, 32, 0, st>>>(ap);
+  } else {
+    if (rows <= 256) k_bqr_apply<A, 2, 4><<<grid, 128, 0, st>>>(ap);
+    else if (rows <= 512) k_bqr_apply<A, 4, 4><<<grid, 128, 0, st>>>(ap);
+    else k_bqr_apply<A, BQR_LROWS / 4, 4><<<grid, 128, 0, st>>>(ap);
+  }
 }
 
 // R(i, j) /= D(i) for j >= i (QDRP row normalisation); block x == 0 also forms

@@ -260,11 +260,11 @@ def main():
     # consumer with a clean algorithmic count is the G wrap (2 real x complex N^3
     # products per flavour per slice, 2 L slices per sweep).
     hop_ms, hop_n = prof.get("hop", (0.0, 0))
-    flops = algorithmic_flops(m, "hop", hop_n, 0)
+    flops = algorithmic_flops(m, "hop", hop_n, 0) * args.chains
     roof = {"bound": "tensor", "kernel": "k_zgemm (G wraps)" if args.precision == "fp64" else "k_dfgemm (G wraps)",
             "achieved": None, "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
             "traffic": HOP_TRAFFIC_BYTES if args.precision == "fp64" and m.ndim == 256 else None,
-            "algorithmic_flops_per_launch": 2 * m.n_fl * 4.0 * m.ndim ** 3 / 2,
+            "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
             "peak_source": "FP64 mma.sync m8n8k4 throughput measured on this pool "
                            "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
     if flops and hop_ms > 0:
