@@ -80,6 +80,9 @@ def lib(build_if_missing: bool = True):
         "alfgpu_set_rng": ([vp, C.c_int32, C.c_uint64, C.c_uint64], C.c_int),
         "alfgpu_init_state": ([vp, vp], C.c_int),
         "alfgpu_sweep": ([vp, vp, OBS_CB, vp], C.c_int),
+        "alfgpu_set_delay": ([vp, C.c_int32], C.c_int),
+        "alfgpu_get_delay": ([vp, C.POINTER(C.c_int32)], C.c_int),
+        "alfgpu_tune_delay": ([vp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
         "alfgpu_get_green": ([vp, C.c_int32, vp], C.c_int),
         "alfgpu_get_phase": ([vp, vp], C.c_int),
         "alfgpu_get_stats": ([vp, C.c_int32, C.POINTER(Stats)], C.c_int),

@@ -76,6 +76,8 @@ struct alfgpu_s {
   int* v_site2 = nullptr;   // [chain][F*M] site of the second eigen-index (two-site vertices) or -1
   int8_t* v_nsite = nullptr;  // [chain][F*M] positions (non-zero eigenvalues) of each vertex
   std::vector<int> blk_start[2], blk_cnt[2];  // delayed-update blocks of the up / down pass (visit positions)
+  std::vector<int> hv_site, hv_site2;          // flavour-0 vertex sites (host), for re-blocking
+  std::vector<int8_t> hv_nsite;
   std::vector<double> h_expT, h_expTinv;      // hopping exponentials as uploaded (original basis)
   bool rot = false;                           // two-site vertices: the sweep runs in the rotated basis
   std::vector<std::pair<int, int>> rot_pairs;
@@ -1214,6 +1216,35 @@ int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv
   return 0;
 }
 
+// Delayed-update blocks of both passes: consecutive visits with at most kblk positions
+// (one per non-zero eigenvalue) on distinct sites.
+static int make_blocks(alfgpu_s* h) {
+  const int M = h->M, N = h->N;
+  for (int dir = 0; dir < 2; ++dir) {
+    std::vector<int>& st = h->blk_start[dir];
+    std::vector<int>& nc = h->blk_cnt[dir];
+    st.clear(); nc.clear();
+    std::vector<int> seen(N, 0);
+    int npos = 0;
+    for (int pos = 0; pos < M; ++pos) {
+      const int n = dir == 0 ? pos : M - 1 - pos;
+      const int s1 = h->hv_site[n], s2 = h->hv_site2[n], w = h->hv_nsite[n];
+      if (s2 == s1) return ALFGPU_ERROR_UNSUPPORTED;
+      const bool clash = seen[s1] || (s2 >= 0 && seen[s2]);
+      if (st.empty() || npos + w > h->kblk || clash) {
+        st.push_back(pos); nc.push_back(0);
+        std::fill(seen.begin(), seen.end(), 0);
+        npos = 0;
+      }
+      seen[s1] = 1;
+      if (s2 >= 0) seen[s2] = 1;
+      npos += w;
+      nc.back()++;
+    }
+  }
+  return 0;
+}
+
 int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v) {
   if (!h || !v || chain < -1 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
   const int F = h->F, M = h->M, N = h->N;
@@ -1277,30 +1308,10 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
       if (h->vert_ok) return ALFGPU_ERROR_UNSUPPORTED;  // per-chain tables share one basis
     }
   }
-  // delayed-update blocks: up to kblk positions (one per non-zero eigenvalue), distinct sites
-  for (int dir = 0; dir < 2; ++dir) {
-    std::vector<int>& st = h->blk_start[dir];
-    std::vector<int>& nc = h->blk_cnt[dir];
-    st.clear(); nc.clear();
-    std::vector<int> seen(N, 0);
-    int npos = 0;
-    for (int pos = 0; pos < M; ++pos) {
-      const int n = dir == 0 ? pos : M - 1 - pos;
-      const int s1 = site[n], s2 = site2[n], w = nsite[n];
-      const bool clash = seen[s1] || (s2 >= 0 && seen[s2]) || (s2 == s1);
-      if (st.empty() || npos + w > h->kblk || clash) {
-        if (!st.empty() && clash && npos == 0) return ALFGPU_ERROR_UNSUPPORTED;
-        st.push_back(pos); nc.push_back(0);
-        std::fill(seen.begin(), seen.end(), 0);
-        npos = 0;
-        if (s2 == s1) return ALFGPU_ERROR_UNSUPPORTED;
-      }
-      seen[s1] = 1;
-      if (s2 >= 0) seen[s2] = 1;
-      npos += w;
-      nc.back()++;
-    }
-  }
+  h->hv_site.assign(site.begin(), site.begin() + M);
+  h->hv_site2.assign(site2.begin(), site2.begin() + M);
+  h->hv_nsite.assign(nsite.begin(), nsite.begin() + M);
+  RET(make_blocks(h));
   // transition factors for every (vertex, old field, flip choice); type-1 fields flip sign
   std::vector<UpdTab> tab(K * 15);
   for (size_t k = 0; k < K; ++k) {
@@ -1555,6 +1566,42 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
   return rc;
 }
 
+
+int alfgpu_set_delay(alfgpu_t* h, int32_t k) {
+  if (!h || k < 2 || k > UPD_KMAX) return ALFGPU_ERROR_ARGUMENT;
+  h->kblk = k;
+  if (h->vert_ok) RET(make_blocks(h));
+  drop_graphs(h);
+  return 0;
+}
+
+int alfgpu_get_delay(alfgpu_t* h, int32_t* k) {
+  if (!h || !k) return ALFGPU_ERROR_ARGUMENT;
+  *k = h->kblk;
+  return 0;
+}
+
+int alfgpu_tune_delay(alfgpu_t* h, int32_t nsweeps, int32_t* k_out) {
+  if (!h || nsweeps < 1) return ALFGPU_ERROR_ARGUMENT;
+  if (!h->state_ok || !h->vert_ok) return ALFGPU_ERROR_ARGUMENT;
+  const int cand[4] = {8, 16, 24, 32};
+  const int prof0 = h->profiling;
+  double best = 1e300;
+  int kbest = h->kblk;
+  for (int c = 0; c < 4; ++c) {
+    RET(alfgpu_set_delay(h, cand[c]));
+    h->profiling = 1;
+    for (int i = 0; i < ALFGPU_PROF_N; ++i) { h->prof_ms[i] = 0.0; h->prof_n[i] = 0; }
+    for (int s = 0; s < nsweeps; ++s) RET(alfgpu_sweep(h, nullptr, nullptr, nullptr));
+    const double t = h->prof_ms[ALFGPU_PROF_UPDATE] + h->prof_ms[ALFGPU_PROF_FLUSH];
+    if (t < best) { best = t; kbest = cand[c]; }
+  }
+  h->profiling = prof0;
+  for (int i = 0; i < ALFGPU_PROF_N; ++i) { h->prof_ms[i] = 0.0; h->prof_n[i] = 0; }
+  RET(alfgpu_set_delay(h, kbest));
+  if (k_out) *k_out = kbest;
+  return 0;
+}
 
 int alfgpu_get_green(alfgpu_t* h, int32_t chain, double* G) {
   if (!h || !G || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;

@@ -39,11 +39,9 @@ struct ArD {
     const double s = rcp_pos(a.x * a.x + a.y * a.y);
     return zmk(a.x * s, -a.y * s);
   }
-  // positive rescaling towards |a| ~ 1 (direction unchanged)
-  static ALF_DEV Z renorm(Z a) {
-    const float m2 = __double2float_rn(a.x * a.x + a.y * a.y);
-    return (m2 > 0.f && m2 < 3e38f) ? zscale(a, (double)rsqrtf(m2)) : a;
-  }
+  // FP64 range holds the unnormalised phase of a block (<= 32 ratio factors); it is
+  // normalised once at block end
+  static ALF_DEV Z renorm(Z a) { return a; }
   static ALF_DEV zd unit(Z a) { const double r = sqrt(a.x * a.x + a.y * a.y); return zmk(a.x / r, a.y / r); }
   static ALF_DEV Z shfl(Z a, int src) {
     return zmk(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));

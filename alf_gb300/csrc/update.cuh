@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
         }
         K = (f == 0) ? e.expal : zmul(K, e.expal);
       }
+      // [prod_f exp(Z1 alpha)]^N_SUN gamma'/gamma: with N_SUN = 1 the gamma ratio joins K
+      if (p.NSUN == 1) K = zscale(K, p.ft.grat[tp - 1][so + 2][sn + 2]);
       s_K[q] = A::mk(K);
       for (int I = 0; I < w; ++I) {
         s_psite[p0 + I] = I ? site2[n] : site[n];
@@ -244,10 +246,14 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
         Rm = A::mul(D, A::sub(s_mye[fo][w], A::mul(s_dlt[fo][w], gp)));
       }
       Rt = (F == 2) ? A::mul(A::shfl(Rm, 0), A::shfl(Rm, 1)) : Rm;
-      Rt = A::mul(Rt, s_K[q]);
-      Z Rp = Rt;
-      for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
-      Rt = A::scale(Rp, s_gr[q]);
+      if (p.NSUN == 1) {
+        Rt = A::mul(Rt, s_K[q]);  // K carries the gamma ratio (prologue)
+      } else {
+        Rt = A::mul(Rt, s_K[q]);
+        Z Rp = Rt;
+        for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
+        Rt = A::scale(Rp, s_gr[q]);
+      }
       // weight = |Re(phase R) / Re(phase)| > u  (Wrapgr_mod.F90:141-143), division-free
       const R num = A::absr(A::re_mul(ph, Rt));
       const R den = A::mulr(A::absr(A::re(ph)), s_u2[q]);

@@ -130,6 +130,22 @@ class Chains:
         _lib.check(rc, "alfgpu_sweep")
         return (eq, tau) if measure else None
 
+    # --- delay depth ---------------------------------------------------------------------------
+    def set_delay(self, k: int):
+        _lib.check(self.L.alfgpu_set_delay(self.h, k), "alfgpu_set_delay")
+
+    def delay(self) -> int:
+        k = C.c_int32()
+        _lib.check(self.L.alfgpu_get_delay(self.h, C.byref(k)), "alfgpu_get_delay")
+        return k.value
+
+    def tune_delay(self, nsweeps: int = 1) -> int:
+        """Autotune the delay depth on nsweeps device-stream sweeps per candidate (these
+        sweeps advance the chains: use them as thermalisation)."""
+        k = C.c_int32()
+        _lib.check(self.L.alfgpu_tune_delay(self.h, nsweeps, C.byref(k)), "alfgpu_tune_delay")
+        return k.value
+
     # --- readback --------------------------------------------------------------------------------
     def green(self, chain: int = 0) -> np.ndarray:
         G = np.zeros((self.F, self.N, self.N), np.complex128)

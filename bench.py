@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--pivoting", default="exact", choices=["norms", "exact", "exact-cgr", "exact-decompose"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--chains", type=int, default=1, help="independent chains per GPU (batched)")
+    ap.add_argument("--no-tune", dest="tune", action="store_false", help="keep the default delay depth")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -145,6 +146,7 @@ def run_ours(args, ws, rank, local):
     ch.init_state()
     for c in range(C):
         ch.set_rng(c, replicas.replica_seed(args.seed, rank, c), rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    delay = ch.tune_delay(1) if args.tune else ch.delay()  # untimed (thermalisation) sweeps
     stream = torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local)
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > 129 MB L2
 
@@ -193,7 +195,7 @@ def run_ours(args, ws, rank, local):
     # launch count per sweep from the profile pass
     t_dev, t_e2e = replicas.max_over_ranks([ms / 1e3, e2e_s], device=f"cuda:{local}")
     return dict(m=m, t_dev=t_dev, t_e2e=t_e2e, clocks=clk.summary(), prof=prof, n_acc=n_acc, h2d=h2d, d2h=d2h,
-                stats=st, chains=ch, launches=n_launch)
+                stats=st, chains=ch, launches=n_launch, delay=delay)
 
 
 def cpu_oracle_rate(m, seed: int, threads: int, slices: int):
@@ -287,7 +289,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "df64+c128",
         "data": "synthetic (seeded fields and draws)",
-        "config": dict(workload, parallelism=f"replicas x{ws}"),
+        "config": dict(workload, parallelism=f"replicas x{ws}", delay_depth=r["delay"],
+                       delay_depth_source="autotuned (alfgpu_tune_delay)" if args.tune else "default"),
         "e2e": {"value": e2e, "unit": "sweeps/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
         "roofline": roof, "cpu_baseline": cpu, "clocks": r["clocks"], "gpu_launches": launches,
         "phases": phases,

@@ -167,6 +167,16 @@ int alfgpu_init_state(alfgpu_t* h, double* phase_out);
  * device stream.  cb may be NULL (no measurements). */
 int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx);
 
+/* Delay depth k of the delayed (block submatrix) update: at most k positions per
+ * block before the rank-k flush (2..32; the default is dims.delay_k or 32).
+ * alfgpu_tune_delay is the autotuner: it runs nsweeps sweeps on the device draw stream
+ * (thermalisation sweeps: they advance the chains) with each k in {8, 16, 24, 32},
+ * times the update and flush phases, and keeps the fastest k.  No counterpart in the
+ * reference (ALF has no delayed update). */
+int alfgpu_set_delay(alfgpu_t* h, int32_t k);
+int alfgpu_get_delay(alfgpu_t* h, int32_t* k);
+int alfgpu_tune_delay(alfgpu_t* h, int32_t nsweeps, int32_t* k_out);
+
 /* State readback. */
 int alfgpu_get_green(alfgpu_t* h, int32_t chain, double* G);  /* Ndim x Ndim x N_FL */
 int alfgpu_get_phase(alfgpu_t* h, double* phase);             /* complex per chain */

@@ -225,3 +225,27 @@ def test_graph_replay_matches_stream_path():
     np.testing.assert_array_equal(out[0][0], out[1][0])
     assert _relmax(out[0][1], out[1][1]) == 0.0
     assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
+
+
+def test_delay_depth_changes_only_rounding_and_autotuner_picks_a_candidate():
+    # the delay depth regroups the same Sherman-Morrison sequence; results agree to rounding
+    m = mdl.hubbard("square", 6, 6, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    seed = 41
+    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)[None, :]
+    res = []
+    for k in (8, 32):
+        g = Chains(m)
+        g.set_delay(k)
+        assert g.delay() == k
+        g.set_fields(0, f0)
+        g.init_state()
+        g.sweep(u)
+        res.append((g.fields(0), g.green(0)))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    assert _relmax(res[0][1], res[1][1]) < RTOL
+    g = Chains(m)
+    g.set_fields(0, f0)
+    g.init_state()
+    g.set_rng(0, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    assert g.tune_delay(1) in (8, 16, 24, 32)
