@@ -1009,8 +1009,12 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   h->dev = d.device;
   h->mixed = d.precision == ALFGPU_PRECISION_MIXED;
   h->mixed_propagate = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_PROPAGATION);
-  h->exact_dec = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_DECOMPOSE)) ? 1 : 0;
-  h->exact_cgr = (d.reserved[0] & (ALFGPU_FLAG_EXACT_QRP | ALFGPU_FLAG_EXACT_QRP_CGR)) ? 1 : 0;
+  {
+    const int fl = d.reserved[0];
+    const bool force = fl & ALFGPU_FLAG_EXACT_QRP;
+    h->exact_dec = force || !(fl & ALFGPU_FLAG_NORM_PIVOT_DECOMPOSE);
+    h->exact_cgr = force || (!(fl & ALFGPU_FLAG_NORM_PIVOT_CGR) && d.precision != ALFGPU_PRECISION_MIXED);
+  }
   h->df_stab = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_GEMM);
   h->df_qr = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_QR);
   h->use_graph = !(d.reserved[0] & ALFGPU_FLAG_NO_GRAPH);

@@ -26,14 +26,16 @@ PRECISIONS = {"fp64": 0, "mixed": 1}
 # dims.reserved[0] flags (include/alfgpu.h)
 FLAG_DF_PROPAGATION = 1
 FLAG_EXACT_QRP = 2
-FLAG_EXACT_QRP_CGR = 4
-FLAG_EXACT_QRP_DECOMPOSE = 8
+FLAG_NORM_PIVOT_CGR = 4
+FLAG_NORM_PIVOT_DECOMPOSE = 8
+FLAG_NORM_PIVOT = 12
 FLAG_DF_STAB_QR = 16
 FLAG_DF_STAB_GEMM = 32
 FLAG_DF_STAB = 48
 FLAG_NO_GRAPH = 64
-PIVOTING = {"norms": 0, "exact": FLAG_EXACT_QRP, "exact-cgr": FLAG_EXACT_QRP_CGR,
-            "exact-decompose": FLAG_EXACT_QRP_DECOMPOSE}
+# "default": ZGEQP3 everywhere in the FP64 form; norm-pivoted CGR in the mixed form
+PIVOTING = {"default": 0, "exact": FLAG_EXACT_QRP, "norms": FLAG_NORM_PIVOT,
+            "norms-cgr": FLAG_NORM_PIVOT_CGR, "norms-decompose": FLAG_NORM_PIVOT_DECOMPOSE}
 
 
 def _p(a: np.ndarray):
@@ -43,10 +45,12 @@ def _p(a: np.ndarray):
 class Chains:
     def __init__(self, model: Model, n_chains: int = 1, precision: str = "fp64", delay_k: int = 0,
                  device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None,
-                 pivoting: str = "exact", flags: int = 0):
-        """``pivoting``: "norms" orders the columns of every stabilisation QR once by
-        their norms (ALF's STABLOG pivoting) and factors them with the blocked QR;
-        "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)."""
+                 pivoting: str = "default", flags: int = 0):
+        """``pivoting``: "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)
+        for every stabilisation QR; "norms" orders the columns once by their norms (ALF's
+        STABLOG pivoting) and factors them with the blocked QR; "norms-cgr" /
+        "norms-decompose" do so at one call site; "default" is "exact" in the FP64 form and
+        "norms-cgr" in the mixed form."""
         self.L = _lib.lib()
         self.model = model
         self.C = n_chains

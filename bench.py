@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--config", default="hubbard16x16")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
-    ap.add_argument("--pivoting", default="exact", choices=["norms", "exact", "exact-cgr", "exact-decompose"])
+    ap.add_argument("--pivoting", default="default", choices=["default", "exact", "norms", "norms-cgr", "norms-decompose"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--chains", type=int, default=1, help="independent chains per GPU (batched)")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="keep the default delay depth")

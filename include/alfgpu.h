@@ -62,15 +62,20 @@ enum {
  * (1e5-1e10 at beta = 10), so this is only usable for small beta / Nwrap. */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
 enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
-/* Column pivoting of the stabilisation QRs.  Default: the columns are ordered once by
- * their norms and factored by a blocked unpivoted Householder QR (the pivoting of
- * ALF's STABLOG branch, Prog/udv_state_mod.F90:503-542), whose trailing work runs on
- * all SMs.  ALFGPU_FLAG_EXACT_QRP in dims.reserved[0] selects ZGEQP3's dynamic
- * pivoting with norm downdates (Prog/QDRP_decompose_mod.F90:60-101, the default
- * branch), run on one thread-block cluster per matrix, for every QR; _CGR and
- * _DECOMPOSE select it for the QR of CGR (cgr1_mod.F90:223) or of
- * decompose_UDV_state only.  ZGEQP3 pivoting is always used for Ndim > 512. */
-enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_EXACT_QRP_CGR = 4, ALFGPU_FLAG_EXACT_QRP_DECOMPOSE = 8 };
+/* Column pivoting of the stabilisation QRs.  Default: ZGEQP3's dynamic pivoting with
+ * norm downdates (Prog/QDRP_decompose_mod.F90:60-101, the reference's default branch) on
+ * one thread-block cluster per matrix, for every QR; in the mixed form the QR of CGR
+ * (cgr1_mod.F90:223) instead orders the columns once by their norms and factors them
+ * with the blocked unpivoted QR (the pivoting of ALF's STABLOG branch,
+ * Prog/udv_state_mod.F90:503-542), whose trailing work runs on all SMs.
+ * ALFGPU_FLAG_NORM_PIVOT_CGR / _DECOMPOSE select norm pivoting for that call site;
+ * ALFGPU_FLAG_EXACT_QRP forces ZGEQP3 pivoting everywhere (also in the mixed form).
+ * Measured on the 16x16 beta = 10 Hubbard chain: norm pivoting in decompose raises
+ * Precision Green from ~7e-7 to 3e-4; in CGR only to ~1e-6, and G at every
+ * stabilisation point still agrees with the ZGEQP3 oracle to 1e-10.  ZGEQP3 pivoting is
+ * always used for Ndim > 512. */
+enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_NORM_PIVOT_CGR = 4, ALFGPU_FLAG_NORM_PIVOT_DECOMPOSE = 8,
+       ALFGPU_FLAG_NORM_PIVOT = 12 };
 /* Mixed form only, opt-in: run parts of the stabilisation in double-float instead of
  * FP64.  _QR: the pivoted QR and explicit Q of decompose_UDV_state (the columns are
  * factored unscaled, exact in exponent range); _GEMM: the UDV propagation, decompose
