@@ -132,6 +132,9 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
   __shared__ zd xs[2][BQR_NB];  // this CTA's column partial sums (read remotely)
   __shared__ zd xr[2][BQR_NB];  // the pivot row, published by its owner
   __shared__ zd tot[BQR_NB], prow[BQR_NB];
+  __shared__ double s_beta;
+  __shared__ zd s_t, s_scal, s_alpha;
+  __shared__ bool s_triv;
   for (int il = g; il < nr; il += 8)
     if (j < nb) P[il][j] = A[(r0 + il) + (long long)(j0 + j) * lda];
   __syncthreads();
@@ -166,19 +169,27 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
       const unsigned ar = dsmem_addr(&xr[par][j], owner);
       prow[j] = zmk(dsmem_ld_f64(ar), dsmem_ld_f64(ar + 8));
     }
-    __syncthreads();
-    // ZLARFG on (alpha, x), x = A(kc+1:N, kc)
-    const zd alpha = prow[k];
-    const double xn2 = tot[k].x;
-    const bool trivial = (xn2 == 0.0 && alpha.y == 0.0);
-    double beta = alpha.x;
-    zd t = zmk(0.0, 0.0), scal = zmk(0.0, 0.0);
-    if (!trivial) {
-      beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn2))), alpha.x);
-      const double ib = bqr_rcp(beta);
-      t = zmk((beta - alpha.x) * ib, -alpha.y * ib);
-      scal = bqr_zrcp(zmk(alpha.x - beta, alpha.y));
+    // ZLARFG on (alpha, x), x = A(kc+1:N, kc), by warp 0 only (every FP64 instruction costs
+    // its sub-partition ~76 cycles; eight redundant copies would cost eight times that)
+    if (g == 0) {
+      __syncwarp();  // tot / prow were written by other lanes of this warp
+      const zd alpha = prow[k];
+      const double xn2 = tot[k].x;
+      const bool triv = (xn2 == 0.0 && alpha.y == 0.0);
+      double be = alpha.x;
+      zd tt = zmk(0.0, 0.0), sc = zmk(0.0, 0.0);
+      if (!triv) {
+        be = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn2))), alpha.x);
+        const double ib = bqr_rcp(be);
+        tt = zmk((be - alpha.x) * ib, -alpha.y * ib);
+        sc = bqr_zrcp(zmk(alpha.x - be, alpha.y));
+      }
+      if (j == 0) { s_beta = be; s_t = tt; s_scal = sc; s_triv = triv; s_alpha = alpha; }
     }
+    __syncthreads();
+    const bool trivial = s_triv;
+    const double beta = s_beta;
+    const zd t = s_t, scal = s_scal, alpha = s_alpha;
     // H^H applied to the panel's later columns: a_j -= conj(tau) v (v^H a_j),
     // v^H a_j = a_kc,j + conj(scal) sum_{i>kc} conj(a_ik) a_ij
     // v_i = scal a_ik for the warp's rows, read before any lane overwrites column k
@@ -186,7 +197,8 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
 #pragma unroll
     for (int q = 0; q < BQR_ROWS / 8; ++q) {
       const int il = g + 8 * q;
-      vi[q] = (il < nr) ? zmul(scal, P[il][k]) : zmk(0.0, 0.0);
+      if (il >= nr) break;  // warp-uniform (il depends on the warp only)
+      vi[q] = zmul(scal, P[il][k]);
     }
     __syncwarp();
     if (!trivial && j >= k && j < nb) {
@@ -194,7 +206,7 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
 #pragma unroll
       for (int q = 0; q < BQR_ROWS / 8; ++q) {
         const int il = g + 8 * q;
-        if (il >= nr) continue;
+        if (il >= nr) break;
         const int i = r0 + il;
         if (i > kc) {
           if (j == k) P[il][k] = vi[q];
@@ -379,7 +391,8 @@ __global__ void __launch_bounds__(256) k_bqr_finish(zd* A, long long lda, long l
 // applies the reflector to its rows, and downdates its own copy of the column
 // norms (identical in all CTAs: same inputs, same summation order), so the pivot
 // search needs no exchange.  A column whose downdate loses accuracy (ZLAQP2's
-// tol3z test) gets its norm recomputed through one more exchange.
+// tol3z test) gets its norm recomputed through one more exchange.  Norms are kept
+// squared (the pivot order is the same, the downdate becomes a subtraction).
 // Outputs as k_qrp before normalisation: R above, reflectors below, tau, jpvt,
 // D = |R_jj|, info.psign; k_bqr_finish then normalises and forms the products.
 struct QRRowsParams {
@@ -408,6 +421,46 @@ ALF_DEV Z dsm_ld16(uint32_t addr) {  // 16-byte value from a peer CTA's shared m
   return z;
 }
 
+// Lanes ci, ci + cpw, ci + 2 cpw, ... (cpw = 32 >> lk): the 1 << lk threads that share one
+// column in the K-threads-per-column mappings of k_qrp_rows.
+ALF_DEV unsigned qrr_gmask(int lk, int ci) {
+  const int cpw = 32 >> lk;
+  unsigned m = 0;
+  for (int t = 0; t < (1 << lk); ++t) m |= 1u << (t * cpw);
+  return m << ci;
+}
+
+template <class Z>
+ALF_DEV Z qrr_shfl_xor(Z v, int o, unsigned m) {  // 16-byte value, xor shuffle among the lanes of m
+  static_assert(sizeof(Z) == 16, "16-byte values");
+  unsigned w[4];
+  memcpy(w, &v, 16);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) w[i] = __shfl_xor_sync(m, w[i], o);
+  memcpy(&v, w, 16);
+  return v;
+}
+
+// Sum over the peers q = s, s + K, ... < CL (K = 1 << lk) of the 16-byte values at `a` in
+// their shared memory, four loads in flight.
+template <class A>
+ALF_DEV typename A::Z qrr_peer_sum(const typename A::Z* a, int s, int lk, int CL) {
+  typedef typename A::Z Z;
+  Z a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
+  const int K = 1 << lk, nq = (CL - s + K - 1) >> lk;
+  int u = 0;
+  for (; u + 3 < nq; u += 4) {
+    const Z v0 = dsm_ld16<Z>(dsmem_addr(a, s + (u << lk)));
+    const Z v1 = dsm_ld16<Z>(dsmem_addr(a, s + ((u + 1) << lk)));
+    const Z v2 = dsm_ld16<Z>(dsmem_addr(a, s + ((u + 2) << lk)));
+    const Z v3 = dsm_ld16<Z>(dsmem_addr(a, s + ((u + 3) << lk)));
+    a0 = A::add(a0, v0); a1 = A::add(a1, v1);
+    a2 = A::add(a2, v2); a3 = A::add(a3, v3);
+  }
+  for (; u < nq; ++u) a0 = A::add(a0, dsm_ld16<Z>(dsmem_addr(a, s + (u << lk))));
+  return A::add(A::add(a0, a1), A::add(a2, a3));
+}
+
 template <class A>
 ALF_DEV void qrr_argmax(typename A::R& v, int& i) {  // warp argmax, first index on ties
   for (int o = 16; o > 0; o >>= 1) {
@@ -417,8 +470,8 @@ ALF_DEV void qrr_argmax(typename A::R& v, int& i) {  // warp argmax, first index
   }
 }
 
-// Arithmetic A: ArD (FP64) or ArF (double-float).  A norm of -1 marks a column whose
-// norm is recomputed in the extra exchange of the step.
+// Arithmetic A: ArD (FP64) or ArF (double-float).  A squared norm of -1 marks a column
+// whose norm is recomputed in the extra exchange of the step.
 // Column scales: FP64 multiplies A(:,c) by colscale_c on load, like QDRP's caller.
 // Double-float has FP32's exponent range, and the UDV scales reach far beyond it, so
 // ArF factors the unscaled columns instead: with the same pivots QR(U D) = Q (R_U D)
@@ -448,6 +501,8 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
   __shared__ R s_bv[8];
   __shared__ double s_bvd[8];
   __shared__ int s_bi[8], s_pv, s_cnt;
+  __shared__ Z s_zb, s_zt, s_zs;
+  __shared__ bool s_triv;
   const R tol3z = A::mkr(1.0536712127723509e-08);  // sqrt(dlamch('Epsilon'))
   const R mone = A::mkr(-1.0);
   zd* Aout = p.A + b * p.sA;
@@ -479,8 +534,8 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
 #pragma unroll
     for (int q = 0; q < 16; ++q)
       if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xs[c], q)));
-    const R nrm = A::rsqrt_(A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3]))));
-    vn1[c] = nrm; vn2[c] = nrm;
+    const R nrm2 = A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3])));
+    vn1[c] = nrm2; vn2[c] = nrm2;
   }
   int par = 1;
   __syncthreads();
@@ -492,7 +547,7 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
       double bv = -1.0;
       int bi = N;
       for (int c = j + tid; c < N; c += 256) {
-        const double v = A::rwide(vn1[c]) * cs[c];
+        const double v = sqrt(A::rwide(vn1[c])) * cs[c];
         if (v > bv) { bv = v; bi = c; }
       }
       qrr_argmax<ArD>(bv, bi);
@@ -504,6 +559,33 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
         for (int w = 1; w < 8; ++w)
           if (s_bvd[w] > v || (s_bvd[w] == v && s_bi[w] < i)) { v = s_bvd[w]; i = s_bi[w]; }
         s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
+      }
+    } else if (!sep) {
+      // FP64 norms are >= 0: they order like their IEEE bit patterns, compared on the integer
+      // pipes (NaN maps below every norm, so it is never chosen)
+      long long bv = -1;
+      int bi = N;
+      for (int c = j + tid; c < N; c += 256) {
+        long long v = __double_as_longlong(A::rwide(vn1[c]));
+        if ((v & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) v = -1;  // NaN
+        if (v == (long long)0x8000000000000000ull) v = 0;                  // -0 ranks as +0
+        if (v > bv) { bv = v; bi = c; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (lane == 0) { s_bi[warp] = bi; s_bvd[warp] = __longlong_as_double(bv); }
+      __syncthreads();
+      if (tid == 0) {
+        long long v = __double_as_longlong(s_bvd[0]);
+        int i = s_bi[0];
+        for (int w = 1; w < 8; ++w) {
+          const long long u = __double_as_longlong(s_bvd[w]);
+          if (u > v || (u == v && s_bi[w] < i)) { v = u; i = s_bi[w]; }
+        }
+        s_pv = (i >= j && i < N) ? i : j;
       }
     } else {
       R bv = mone;
@@ -538,79 +620,111 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
       }
       __syncthreads();
     }
-    // partials over own rows i > j; the owner of row j publishes it
+    // partials over own rows i > j; the owner of row j publishes it.  With few columns
+    // left, K = 1 << lk threads share a column (rows interleaved, xor-shuffle sum), so the
+    // FP64 work spreads over all four sub-partitions.
     const unsigned owner = (unsigned)(j % (int)CL);
     const int ilj = j / (int)CL;
     const int il0 = (j >= (int)rank) ? (j - (int)rank) / (int)CL + 1 : 0;  // first own row > j
     Z* xsp = xs + par * N;
     Z* xrp = xr + par * N;
-    for (int c = j + tid; c < N; c += 256) {
-      Z s0 = A::zero(), s1 = s0;
-      int il = il0;
-      for (; il + 1 < nmine; il += 2) {
-        s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
-        s1 = A::mac(s1, A::conj(Ar[(size_t)(il + 1) * N + j]), Ar[(size_t)(il + 1) * N + c]);
+    const int ncol = N - j;
+    int lk = 0;
+    while (lk < 4 && (ncol << (lk + 1)) <= 256 && (1 << lk) < nmine - il0) ++lk;
+    {
+      const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
+      const unsigned gm = qrr_gmask(lk, ci);
+      for (int c = j + warp * cpw + ci; c < N; c += 8 * cpw) {
+        Z s0 = A::zero(), s1 = s0;
+        int il = il0 + s;
+        for (; il + K < nmine; il += 2 * K) {
+          s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
+          s1 = A::mac(s1, A::conj(Ar[(size_t)(il + K) * N + j]), Ar[(size_t)(il + K) * N + c]);
+        }
+        if (il < nmine) s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
+        Z acc = A::add(s0, s1);
+        for (int o = cpw; o < 32; o <<= 1) acc = A::add(acc, qrr_shfl_xor(acc, o, gm));
+        if (s == 0) {
+          xsp[c] = acc;
+          if (rank == owner) xrp[c] = Ar[(size_t)ilj * N + c];
+        }
       }
-      if (il < nmine) s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j]), Ar[(size_t)il * N + c]);
-      xsp[c] = A::add(s0, s1);
-      if (rank == owner) xrp[c] = Ar[(size_t)ilj * N + c];
     }
     cluster_sync();
-    for (int c = j + tid; c < N; c += 256) {
-      Z s[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
-#pragma unroll
-      for (int q = 0; q < 16; ++q)
-        if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xsp[c], q)));
-      tot[c] = A::add(A::add(s[0], s[1]), A::add(s[2], s[3]));
-      prow[c] = dsm_ld16<Z>(dsmem_addr(&xrp[c], owner));
+    {
+      int l4 = 0;
+      while (l4 < 4 && (ncol << (l4 + 1)) <= 256) ++l4;
+      const int cpw = 32 >> l4, s = lane / cpw, ci = lane % cpw;
+      const unsigned gm = qrr_gmask(l4, ci);
+      for (int c = j + warp * cpw + ci; c < N; c += 8 * cpw) {
+        Z acc = qrr_peer_sum<A>(&xsp[c], s, l4, (int)CL);
+        for (int o = cpw; o < 32; o <<= 1) acc = A::add(acc, qrr_shfl_xor(acc, o, gm));
+        if (s == 0) {
+          tot[c] = acc;
+          prow[c] = dsm_ld16<Z>(dsmem_addr(&xrp[c], owner));
+        }
+      }
     }
     par ^= 1;
     __syncthreads();
-    // ZLARFG on (alpha, x), x = A(j+1:N, j)
-    const Z alpha = prow[j];
-    const R xn2 = A::re(tot[j]);
-    const bool trivial = A::rzero_p(xn2) && A::rzero_p(A::im(alpha));
-    R beta = A::re(alpha);
-    Z t = A::zero(), scal = A::zero();
-    if (!trivial) {
-      beta = A::rneg(A::rcopysign(A::rsqrt_(A::radd(A::abs2(alpha), xn2)), A::re(alpha)));
-      const R ib = A::rrcp(beta);
-      t = A::mkz(A::mulr(A::rsub(beta, A::re(alpha)), ib), A::rneg(A::mulr(A::im(alpha), ib)));
-      scal = A::rcp(A::mkz(A::rsub(A::re(alpha), beta), A::im(alpha)));
+    // ZLARFG on (alpha, x), x = A(j+1:N, j), and v = scal x over own rows, by warp 0 only
+    // (each FP64 instruction occupies its sub-partition ~76 cycles; redundant copies in
+    // every warp would multiply that)
+    if (warp == 0) {
+      const Z alpha = prow[j];
+      const R xn2 = A::re(tot[j]);
+      const bool triv = A::rzero_p(xn2) && A::rzero_p(A::im(alpha));
+      R be = A::re(alpha);
+      Z tt = A::zero(), sc = A::zero();
+      if (!triv) {
+        be = A::rneg(A::rcopysign(A::rsqrt_(A::radd(A::abs2(alpha), xn2)), A::re(alpha)));
+        const R ib = A::rrcp(be);
+        tt = A::mkz(A::mulr(A::rsub(be, A::re(alpha)), ib), A::rneg(A::mulr(A::im(alpha), ib)));
+        sc = A::rcp(A::mkz(A::rsub(A::re(alpha), be), A::im(alpha)));
+      }
+      for (int il = il0 + lane; il < nmine; il += 32) vsh[il] = A::mul(sc, Ar[(size_t)il * N + j]);
+      if (lane == 0) { s_zb = A::mkz(be, A::rzero()); s_zt = tt; s_zs = sc; s_triv = triv; }
     }
-    for (int il = il0 + tid; il < nmine; il += 256) vsh[il] = A::mul(scal, Ar[(size_t)il * N + j]);
     __syncthreads();
-    // H^H on columns c > j (a_c -= conj(tau) v (v^H a_c)), reflector into column j,
-    // and the norm downdate with the updated pivot-row entry
+    const Z alpha = prow[j];
+    const bool trivial = s_triv;
+    const R beta = A::re(s_zb);
+    const Z t = s_zt, scal = s_zs;
+    // H^H on columns c > j (a_c -= conj(tau) v (v^H a_c)), reflector into column j, and the
+    // norm downdate with the updated pivot-row entry.  The norms are kept squared, so
+    // ZGEQP3's downdate vn1 *= sqrt(max(0, 1 - (|a|/vn1)^2)) and its recompute test
+    // (vn1/vn2)^2 max(0, 1 - (|a|/vn1)^2) <= tol3z need no division or square root.
     int need = 0;
-    for (int c = j + tid; c < N; c += 256) {
-      if (c == j) {
-        if (!trivial) {
-          for (int il = il0; il < nmine; ++il) Ar[(size_t)il * N + j] = vsh[il];
-          if (rank == owner) Ar[(size_t)ilj * N + j] = A::mkz(beta, A::rzero());
+    {
+      const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
+      for (int c = j + warp * cpw + ci; c < N; c += 8 * cpw) {
+        if (c == j) {
+          if (!trivial) {
+            for (int il = il0 + s; il < nmine; il += K) Ar[(size_t)il * N + j] = vsh[il];
+            if (rank == owner && s == 0) Ar[(size_t)ilj * N + j] = A::mkz(beta, A::rzero());
+          }
+          continue;
         }
-        continue;
-      }
-      Z anew = prow[c];
-      if (!trivial) {
-        const Z f = A::mul(A::conj(t), A::mac(prow[c], A::conj(scal), tot[c]));
-        const Z nf = A::neg(f);
-        for (int il = il0; il < nmine; ++il)
-          Ar[(size_t)il * N + c] = A::mac(Ar[(size_t)il * N + c], vsh[il], nf);
-        anew = A::sub(anew, f);
-        if (rank == owner) Ar[(size_t)ilj * N + c] = anew;
-      }
-      const R v1 = vn1[c];
-      if (!A::rzero_p(v1)) {
-        const R iv = A::rrcp(v1);
-        const R temp = A::rmax0(A::rsub(A::mkr(1.0), A::mulr(A::abs2(anew), A::mulr(iv, iv))));
-        const R q = A::mulr(v1, A::rrcp(vn2[c]));
-        const R temp2 = A::mulr(temp, A::mulr(q, q));
-        if (!A::gt(temp2, tol3z)) {
-          if (j < N - 1) { need = 1; vn1[c] = mone; }  // recomputed below
-          else { vn1[c] = A::rzero(); vn2[c] = A::rzero(); }
-        } else {
-          vn1[c] = A::mulr(v1, A::rsqrt_(temp));
+        Z anew = prow[c];
+        if (!trivial) {
+          const Z f = A::mul(A::conj(t), A::mac(prow[c], A::conj(scal), tot[c]));
+          const Z nf = A::neg(f);
+          for (int il = il0 + s; il < nmine; il += K)
+            Ar[(size_t)il * N + c] = A::mac(Ar[(size_t)il * N + c], vsh[il], nf);
+          anew = A::sub(anew, f);
+          if (rank == owner && s == 0) Ar[(size_t)ilj * N + c] = anew;
+        }
+        if (s == 0) {
+          const R v1 = vn1[c];
+          if (!A::rzero_p(v1)) {
+            const R rest = A::rmax0(A::rsub(v1, A::abs2(anew)));
+            if (!A::gt(rest, A::mulr(tol3z, vn2[c]))) {
+              if (j < N - 1) { need = 1; vn1[c] = mone; }  // recomputed below
+              else { vn1[c] = A::rzero(); vn2[c] = A::rzero(); }
+            } else {
+              vn1[c] = rest;
+            }
+          }
         }
       }
     }
@@ -634,8 +748,8 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
 #pragma unroll
         for (int q = 0; q < 16; ++q)
           if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xq[c], q)));
-        const R nrm = A::rsqrt_(A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3]))));
-        vn1[c] = nrm; vn2[c] = nrm;
+        const R nrm2 = A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3])));
+        vn1[c] = nrm2; vn2[c] = nrm2;
       }
       par ^= 1;
       __syncthreads();
