@@ -23,6 +23,7 @@
 #include "linalg.cuh"
 #include "update.cuh"
 #include "tau.cuh"
+#include "ozaki.cuh"
 
 namespace {
 
@@ -40,6 +41,16 @@ struct alfgpu_s {
   int N, F, M, L, C, B, Nstm, NSUN, CL, kblk, dev;
   int mixed = 0;           // double-float G wraps and flush GEMMs on the FP32 pipes, FP64 elsewhere
   int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products in double-float too
+  // mixed form: G wraps and delayed-update flushes as digit-sliced BF16 tensor-core GEMMs
+  // (ozaki.cuh); otherwise double-float GEMMs on the FP32 pipes
+  int oz = 0, eexp_complex = 0;
+  int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
+  int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
+  unsigned short* ozE[4] = {nullptr, nullptr, nullptr, nullptr};  // expT, expTinv as A; expT, expTinv as B
+  int* ozEe[4] = {nullptr, nullptr, nullptr, nullptr};
+  unsigned short *ozGA = nullptr, *ozGB = nullptr, *ozXA = nullptr, *ozYB = nullptr;
+  int *ozGAe = nullptr, *ozGBe = nullptr, *ozXAe = nullptr, *ozYBe = nullptr;
+  CUtensorMap tmE[4], tmGA, tmGB, tmXA, tmYB;
   int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
   int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
   int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
@@ -274,6 +285,56 @@ static int gemm32(alfgpu_s* h, const GemmParams& g, int tA, int tB, int tC) {
   P.g = g; P.tA = tA; P.tB = tB; P.tC = tC;
   h->launches++;
   CK(launch_dfgemm(P, h->st));
+  return 0;
+}
+
+// Digit slices of one operand for k_oz_gemm (see ozaki.cuh for the modes).
+static int oz_slice(alfgpu_s* h, const void* src, int mode, long long sr, long long sk, long long sb, int modb,
+                    const zd* ks, long long sks, int srows, int Kc, const int* kdyn, int S, int bits, int Rpad,
+                    int Kpad, unsigned short* out, int* expo, int batch) {
+  OzSliceParams p;
+  memset(&p, 0, sizeof(p));
+  p.src = src; p.mode = mode; p.sr = sr; p.sk = sk; p.sb = sb; p.modb = modb;
+  p.ks = ks; p.sks = sks; p.srows = srows; p.Kc = Kc; p.kdyn = kdyn;
+  p.S = S; p.bits = bits; p.Rpad = Rpad; p.Kpad = Kpad; p.out = out; p.expo = expo; p.err = h->err;
+  h->launches++;
+  CK(oz_launch_slice(p, batch, h->st));
+  return 0;
+}
+
+// C (M x Nn logical) = A B from two slice buffers; omode / osub as in OzGemmParams.
+static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int Nn, int Kpad, int S,
+                   int bits, int bn, int nst, int RpadA, int RpadB, int modA, int modB, const int* expA,
+                   const int* expB, int omode, int osub, void* out, long long ldr, long long ldc, long long sout,
+                   int batch) {
+  OzGemmParams p;
+  memset(&p, 0, sizeof(p));
+  p.M = M; p.N = Nn; p.nkc = Kpad / OZ_KC; p.S = S; p.bits = bits; p.nst = nst; p.nd = S + 1;
+  p.L = oz_shift(Kpad, bits, S, p.nd);
+  p.RpadA = RpadA; p.RpadB = RpadB; p.modA = modA; p.modB = modB; p.expA = expA; p.expB = expB;
+  p.omode = omode; p.osub = osub; p.out = out; p.ldr = ldr; p.ldc = ldc; p.sout = sout; p.err = h->err;
+  const dim3 grid((Nn + bn - 1) / bn, (M + OZ_BM - 1) / OZ_BM, batch);
+  const size_t sm = oz_smem_bytes(bn, S, p.nkc, nst);
+  if (bn == 32) k_oz_gemm<32><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  else k_oz_gemm<16><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  h->launches++;
+  CKL();
+  return 0;
+}
+
+// Slices of expT / expTinv (real, per flavour) as the M-side (rows i, K = columns) and
+// N-side operand (rows j = output columns, K = rows).
+static int oz_slice_expT(alfgpu_s* h) {
+  if (!h->oz) return 0;
+  const int N = h->N;
+  const long long NN = (long long)N * N;
+  const double* src[2] = {h->expT, h->expTinv};
+  for (int a = 0; a < 2; ++a) {
+    RET(oz_slice(h, src[a], OZ_REAL, 1, N, NN, 0, nullptr, 0, N, N, nullptr, h->oz_S, h->oz_bits, h->oz_RpN,
+                 h->oz_Kpad, h->ozE[a], h->ozEe[a], h->F));
+    RET(oz_slice(h, src[a], OZ_REAL, N, 1, NN, 0, nullptr, 0, N, N, nullptr, h->oz_S, h->oz_bits, h->oz_RpN,
+                 h->oz_Kpad, h->ozE[2 + a], h->ozEe[2 + a], h->F));
+  }
   return 0;
 }
 
@@ -861,6 +922,31 @@ static int hop(alfgpu_s* h, int up, int with_scale) {
 }
 static int hop_impl(alfgpu_s* h, int up, int with_scale) {
   const int N = h->N, F = h->F, B = h->B;
+  if (h->mixed && h->oz && !(with_scale && h->eexp_complex)) {
+    // up:   T1 = expT diag(S) G (row-major), G = T1 diag(Sinv) expTinv
+    // down: T1 = G diag(S) expT (column-major), G = expTinv diag(Sinv) T1
+    const long long NN = (long long)N * N;
+    const int S = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
+    const int bn = h->oz_bn, nst = h->oz_nst;
+    const zd* s1 = with_scale ? h->S : nullptr;
+    const zd* s2 = with_scale ? h->Sinv : nullptr;
+    if (up) {
+      RET(oz_slice(h, h->G, OZ_CROWS, N, 1, NN, 0, s1, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGB, h->ozGBe, B));
+      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, Kp, S, bits, bn, nst, RpN, Rp2, F, 0, h->ozEe[0], h->ozGBe,
+                  OZ_OUT_COLS, 0, h->T1, N, 1, NN, B));
+      RET(oz_slice(h, h->T1, OZ_CROWS, N, 1, NN, 0, s2, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGA, h->ozGAe, B));
+      RET(oz_gemm(h, h->tmGA, h->tmE[3], 2 * N, N, Kp, S, bits, bn, nst, Rp2, RpN, 0, F, h->ozGAe, h->ozEe[3],
+                  OZ_OUT_ROWS, 0, h->G, 1, N, NN, B));
+    } else {
+      RET(oz_slice(h, h->G, OZ_CROWS, 1, N, NN, 0, s1, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGA, h->ozGAe, B));
+      RET(oz_gemm(h, h->tmGA, h->tmE[2], 2 * N, N, Kp, S, bits, bn, nst, Rp2, RpN, 0, F, h->ozGAe, h->ozEe[2],
+                  OZ_OUT_ROWS, 0, h->T1, 1, N, NN, B));
+      RET(oz_slice(h, h->T1, OZ_CROWS, N, 1, NN, 0, s2, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGB, h->ozGBe, B));
+      RET(oz_gemm(h, h->tmE[1], h->tmGB, N, 2 * N, Kp, S, bits, bn, nst, RpN, Rp2, F, 0, h->ozEe[1], h->ozGBe,
+                  OZ_OUT_COLS, 0, h->G, 1, N, NN, B));
+    }
+    return 0;
+  }
   if (h->mixed) {
     const double* E1 = up ? h->expT : h->expTinv;
     const double* E2 = up ? h->expTinv : h->expT;
@@ -956,7 +1042,16 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
     p.kdyn = h->m + h->C;  // per-(chain, flavour) rank, written by k_update
-    if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
+    if (h->mixed && h->oz) {
+      // G -= X Y as one real product: [Re X | Im X] times the K-doubled complex rows of Y
+      const int Kf = 2 * UPD_KMAX;
+      RET(oz_slice(h, h->X, OZ_CKA, 1, N, p.sA, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,
+                   h->oz_RpN, Kf, h->ozXA, h->ozXAe, h->B));
+      RET(oz_slice(h, h->Y, OZ_CKB, UPD_KMAX, 1, p.sB, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,
+                   h->oz_Rp2N, Kf, h->ozYB, h->ozYBe, h->B));
+      RET(oz_gemm(h, h->tmXA, h->tmYB, N, 2 * N, Kf, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN,
+                  h->oz_Rp2N, 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, h->G, 1, N, NN, h->B));
+    } else if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
     else RET(gemm(h, p));
     prof_end(h);
   }
@@ -983,6 +1078,53 @@ const char* alfgpu_error_string(int code) {
     case ALFGPU_ERROR_SIZE: return "Ndim exceeds the static scratch of the no-allocation entry point";
     default: return "unknown error";
   }
+}
+
+// Buffers, tensor maps and tile shapes of the tensor-core GEMMs of the mixed form; leaves
+// h->oz = 0 (double-float GEMMs) when a size does not fit.
+static int oz_setup(alfgpu_s* h) {
+  const int N = h->N;
+  const size_t B = h->B, F = h->F;
+  h->oz = 0;
+  h->oz_Kpad = oz_round(N, OZ_KC);
+  h->oz_RpN = oz_round(N, OZ_BM);
+  h->oz_Rp2N = oz_round(2 * N, OZ_BM);
+  if (oz_pick(h->oz_Kpad, &h->oz_bits, &h->oz_S) || oz_pick(2 * UPD_KMAX, &h->ozf_bits, &h->ozf_S)) return 0;
+  // CTAs of one wrap product at BN = 32; fewer than two per SM: the narrow tile
+  int nsm = 152;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);
+  const long long tiles = (long long)((N + OZ_BM - 1) / OZ_BM) * ((2 * N + 31) / 32) * (long long)B;
+  const int narrow = tiles < 2ll * nsm;
+  if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
+      oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
+    return 0;
+  if (!oz_encoder()) return 0;
+  const size_t S = h->oz_S, Sf = h->ozf_S, Kp = h->oz_Kpad, Kf = 2 * UPD_KMAX, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
+  int r = 0;
+  for (int a = 0; a < 4; ++a) { r |= dalloc(h, &h->ozE[a], F * S * RpN * Kp); r |= dalloc(h, &h->ozEe[a], F * RpN); }
+  r |= dalloc(h, &h->ozGA, B * S * Rp2 * Kp); r |= dalloc(h, &h->ozGAe, B * Rp2);
+  r |= dalloc(h, &h->ozGB, B * S * Rp2 * Kp); r |= dalloc(h, &h->ozGBe, B * Rp2);
+  r |= dalloc(h, &h->ozXA, B * Sf * RpN * Kf); r |= dalloc(h, &h->ozXAe, B * RpN);
+  r |= dalloc(h, &h->ozYB, B * Sf * Rp2 * Kf); r |= dalloc(h, &h->ozYBe, B * Rp2);
+  if (r) return ALFGPU_ERROR_CUDA;
+  int t = 0;
+  for (int a = 0; a < 4; ++a)
+    t |= oz_tmap(&h->tmE[a], h->ozE[a], (int)Kp, (long long)(F * S * RpN), a < 2 ? OZ_BM : h->oz_bn);
+  t |= oz_tmap(&h->tmGA, h->ozGA, (int)Kp, (long long)(B * S * Rp2), OZ_BM);
+  t |= oz_tmap(&h->tmGB, h->ozGB, (int)Kp, (long long)(B * S * Rp2), h->oz_bn);
+  t |= oz_tmap(&h->tmXA, h->ozXA, (int)Kf, (long long)(B * Sf * RpN), OZ_BM);
+  t |= oz_tmap(&h->tmYB, h->ozYB, (int)Kf, (long long)(B * Sf * Rp2), h->ozf_bn);
+  if (t) return 0;
+  const size_t sm1 = oz_smem_bytes(h->oz_bn, h->oz_S, h->oz_Kpad / OZ_KC, h->oz_nst);
+  const size_t sm2 = oz_smem_bytes(h->ozf_bn, h->ozf_S, 1, h->ozf_nst);
+  const int sm32 = (int)std::max(h->oz_bn == 32 ? sm1 : 0, h->ozf_bn == 32 ? sm2 : 0);
+  const int sm16 = (int)std::max(h->oz_bn == 16 ? sm1 : 0, h->ozf_bn == 16 ? sm2 : 0);
+  if (sm32 && cudaFuncSetAttribute(k_oz_gemm<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32) != cudaSuccess)
+    return ALFGPU_ERROR_CUDA;
+  if (sm16 && cudaFuncSetAttribute(k_oz_gemm<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm16) != cudaSuccess)
+    return ALFGPU_ERROR_CUDA;
+  h->oz = 1;
+  return 0;
 }
 
 int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
@@ -1132,6 +1274,10 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->draws, C * 6 * M * L);
   r |= dalloc(h, &h->rngkey, C); r |= dalloc(h, &h->rngctr, C);
   if (r) return fail(ALFGPU_ERROR_CUDA);
+  if (h->mixed && !(d.reserved[0] & ALFGPU_FLAG_NO_TENSOR_GEMM)) {
+    const int e = oz_setup(h);
+    if (e) return fail(e);
+  }
   h->h_key.assign(C, 0); h->h_ctr.assign(C, 0);
   for (size_t c = 0; c < C; ++c) { h->h_key[c] = alf_chain_key(0, c); h->h_ctr[c] = M * L; }
   *out = h;
@@ -1205,6 +1351,8 @@ static int upload_expT(alfgpu_t* h) {
     }
   CK(cudaMemcpy(h->expT, a.data(), h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->expTinv, b.data(), h->F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  RET(oz_slice_expT(h));
+  CK(cudaStreamSynchronize(h->st));
   return 0;
 }
 
@@ -1290,6 +1438,8 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
     for (int m = 0; m < 2; ++m)
       for (int s = 0; s < 5; ++s)
         ee[k * 10 + m * 5 + s] = zmk(v->op_Eexp[(k * 10 + m * 5 + s) * 2], v->op_Eexp[(k * 10 + m * 5 + s) * 2 + 1]);
+    for (int s = 0; s < 10; ++s)
+      if (ee[k * 10 + s].y != 0.0) h->eexp_complex = 1;
     if (!std::isfinite(g[k].x) || !std::isfinite(g[k].y)) return ALFGPU_ERROR_HAMILTONIAN;
   }
   // the vertices of every flavour act on the same sites
@@ -1437,6 +1587,7 @@ static int check_err(alfgpu_s* h) {
     CK(cudaMemset(h->err, 0, sizeof(int)));
     if (e & 1) return ALFGPU_ERROR_NAN;
     if (e & 2) return ALFGPU_ERROR_UNSTABLE_MATRIX;
+    if (e & 4) return ALFGPU_ERROR_TIMEOUT;
     return ALFGPU_ERROR_GENERIC;
   }
   return 0;
@@ -1826,5 +1977,50 @@ extern "C" int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, doub
   u.detU = detU ? reinterpret_cast<zd*>(detU) : &s->detU;
   const int rc = decompose(&ctx, u, (side == 'l' || side == 'L') ? 1 : 0);
   ctx.st = nullptr;  // the caller owns the stream
+  return rc;
+}
+
+int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t lda, const double* B, int32_t ldb,
+                    double* C, int32_t ldc, int32_t device) {
+  if (m < 1 || n < 1 || k < 1 || !A || !B || !C || lda < m || ldb < k || ldc < m) return ALFGPU_ERROR_ARGUMENT;
+  const int Kp = oz_round(k, OZ_KC);
+  int bits = 0, S = 0, bn = 0, nst = 0;
+  if (oz_pick(Kp, &bits, &S) || oz_pick_tile(S, Kp / OZ_KC, &bn, &nst)) return ALFGPU_ERROR_SIZE;
+  if (!oz_encoder()) return ALFGPU_ERROR_CUDA;
+  alfgpu_s* h = new alfgpu_s();
+  h->dev = device;
+  int rc = 0;
+  auto run = [&]() -> int {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    const int RpA = oz_round(m, OZ_BM), RpB = oz_round(n, OZ_BM);
+    double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    unsigned short *sa = nullptr, *sb = nullptr;
+    int *ea = nullptr, *eb = nullptr;
+    int r = 0;
+    r |= dalloc(h, &dA, (size_t)m * k); r |= dalloc(h, &dB, (size_t)k * n); r |= dalloc(h, &dC, (size_t)m * n);
+    r |= dalloc(h, &sa, (size_t)S * RpA * Kp); r |= dalloc(h, &sb, (size_t)S * RpB * Kp);
+    r |= dalloc(h, &ea, (size_t)RpA); r |= dalloc(h, &eb, (size_t)RpB); r |= dalloc(h, &h->err, 1);
+    if (r) return ALFGPU_ERROR_CUDA;
+    CK(cudaMemcpy2D(dA, (size_t)m * sizeof(double), A, (size_t)lda * sizeof(double), (size_t)m * sizeof(double), k,
+                    cudaMemcpyHostToDevice));
+    CK(cudaMemcpy2D(dB, (size_t)k * sizeof(double), B, (size_t)ldb * sizeof(double), (size_t)k * sizeof(double), n,
+                    cudaMemcpyHostToDevice));
+    CUtensorMap ta, tb;
+    if (oz_tmap(&ta, sa, Kp, (long long)S * RpA, OZ_BM) || oz_tmap(&tb, sb, Kp, (long long)S * RpB, bn))
+      return ALFGPU_ERROR_CUDA;
+    const size_t sm = oz_smem_bytes(bn, S, Kp / OZ_KC, nst);
+    if (bn == 32) CK(cudaFuncSetAttribute(k_oz_gemm<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    else CK(cudaFuncSetAttribute(k_oz_gemm<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    RET(oz_slice(h, dA, OZ_REAL, 1, m, 0, 0, nullptr, 0, m, k, nullptr, S, bits, RpA, Kp, sa, ea, 1));
+    RET(oz_slice(h, dB, OZ_REAL, k, 1, 0, 0, nullptr, 0, n, k, nullptr, S, bits, RpB, Kp, sb, eb, 1));
+    RET(oz_gemm(h, ta, tb, m, n, Kp, S, bits, bn, nst, RpA, RpB, 0, 0, ea, eb, OZ_OUT_REAL, 0, dC, 1, m, 0, 1));
+    RET(check_err(h));
+    CK(cudaMemcpy2D(C, (size_t)ldc * sizeof(double), dC, (size_t)m * sizeof(double), (size_t)m * sizeof(double), n,
+                    cudaMemcpyDeviceToHost));
+    return 0;
+  };
+  rc = run();
+  alfgpu_destroy(h);
   return rc;
 }

@@ -87,6 +87,10 @@ enum { ALFGPU_FLAG_DF_STAB_QR = 16, ALFGPU_FLAG_DF_STAB_GEMM = 32, ALFGPU_FLAG_D
  * draw source) and replays it; sweeps with a callback, recording, profiling or TAU_M
  * use the stream path.  ALFGPU_FLAG_NO_GRAPH always uses the stream path. */
 enum { ALFGPU_FLAG_NO_GRAPH = 64 };
+/* Mixed form: the G wraps and delayed-update flushes run as digit-sliced BF16 products on
+ * the tensor cores (tcgen05), exact to ~2^-54 like FP64 (N_dim <= 448); this flag selects
+ * the double-float GEMMs on the FP32 pipes instead. */
+enum { ALFGPU_FLAG_NO_TENSOR_GEMM = 128 };
 
 typedef struct alfgpu_s alfgpu_t;
 
@@ -244,6 +248,15 @@ int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V);
  * stream-ordered: results are ready when the stream reaches them. */
 #define ALFGPU_NOALLOC_MAX_NDIM 256
 int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, double* V, double* detU, void* stream);
+
+/* C = A B for real column-major host matrices (m x k, k x n, m x n with leading
+ * dimensions lda, ldb, ldc) on the tensor-core GEMM of the mixed form (k_oz_gemm,
+ * digit-sliced BF16 with exact FP32 accumulation, ~2^-54 relative to the row and column
+ * scales of A and B; k <= 512, else ALFGPU_ERROR_SIZE).  The kernel the G wraps use, exposed for testing and
+ * for callers that want FP64-accurate products on the tensor cores.  Synchronous;
+ * allocates and frees its own device buffers. */
+int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t lda, const double* B, int32_t ldb,
+                    double* C, int32_t ldc, int32_t device);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,7 @@
-"""Mixed-precision form (double-float G wraps, delayed-update flush GEMMs and
-per-visit Metropolis arithmetic on the FP32 pipes; complex128 storage; FP64 UDV
-propagation, pivoted QR and CGR) against the FP64 CPU oracle on the same fields
-and draws.
+"""Mixed-precision form (G wraps and delayed-update flushes as digit-sliced BF16
+tensor-core products, per-visit Metropolis arithmetic in double-float on the FP32
+pipes; complex128 storage; FP64 UDV propagation, pivoted QR and CGR) against the FP64
+CPU oracle on the same fields and draws.
 
 Acceptance bound: max |G_mixed - G_fp64| <= 1e-5 at every stabilisation point
 (the freshly computed CGR result) while the accept/reject sequences agree, and
@@ -84,4 +84,12 @@ def test_mixed_double_float_stabilisation_small():
     from alf_gb300.sweep import FLAG_DF_STAB
     w = _compare(mdl.hubbard("square", 8, 8, U=4.0, beta=4.0, dtau=0.1, nwrap=10), seed=2, sweeps=1,
                  flags=FLAG_DF_STAB)
+    assert w < BOUND
+
+
+def test_mixed_double_float_wraps_small():
+    # the double-float G wraps and flushes on the FP32 pipes (instead of the tensor-core GEMM)
+    from alf_gb300.sweep import FLAG_NO_TENSOR_GEMM
+    w = _compare(mdl.hubbard("square", 8, 8, U=4.0, beta=4.0, dtau=0.1, nwrap=10), seed=2, sweeps=1,
+                 flags=FLAG_NO_TENSOR_GEMM)
     assert w < BOUND
