@@ -44,6 +44,7 @@ struct alfgpu_s {
   // mixed form: G wraps and delayed-update flushes as digit-sliced BF16 tensor-core GEMMs
   // (ozaki.cuh); otherwise double-float GEMMs on the FP32 pipes
   int oz = 0, eexp_complex = 0;
+  int oz_narrow = 0;  // small grids: BN = 16 tiles; the flush keeps the double-float GEMM (measured faster there)
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
   unsigned short* ozE[4] = {nullptr, nullptr, nullptr, nullptr};  // expT, expTinv as A; expT, expTinv as B
@@ -306,13 +307,14 @@ static int oz_slice(alfgpu_s* h, const void* src, int mode, long long sr, long l
 static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int Nn, int Kpad, int S,
                    int bits, int bn, int nst, int RpadA, int RpadB, int modA, int modB, const int* expA,
                    const int* expB, int omode, int osub, void* out, long long ldr, long long ldc, long long sout,
-                   int batch) {
+                   int batch, const zd* rsc = nullptr, long long srsc = 0) {
   OzGemmParams p;
   memset(&p, 0, sizeof(p));
   p.M = M; p.N = Nn; p.nkc = Kpad / OZ_KC; p.S = S; p.bits = bits; p.nst = nst; p.nd = S + 1;
   p.L = oz_shift(Kpad, bits, S, p.nd);
   p.RpadA = RpadA; p.RpadB = RpadB; p.modA = modA; p.modB = modB; p.expA = expA; p.expB = expB;
   p.omode = omode; p.osub = osub; p.out = out; p.ldr = ldr; p.ldc = ldc; p.sout = sout; p.err = h->err;
+  p.rsc = rsc; p.srsc = srsc;
   const dim3 grid((Nn + bn - 1) / bn, (M + OZ_BM - 1) / OZ_BM, batch);
   const size_t sm = oz_smem_bytes(bn, S, p.nkc, nst);
   if (bn == 32) k_oz_gemm<32><<<grid, 256, sm, h->st>>>(ta, tb, p);
@@ -337,6 +339,10 @@ static int oz_slice_expT(alfgpu_s* h) {
   }
   return 0;
 }
+
+// The mixed form's UDV propagation runs on the tensor-core GEMM (FP64-accurate) when the
+// slice scales are real.
+static bool oz_propagate(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_complex && !h->mixed_propagate; }
 
 // Stabilisation products (UDV propagation, decompose, CGR): double-float in the mixed
 // form, FP64 otherwise.
@@ -563,6 +569,14 @@ static int wrapur_u(alfgpu_s* h, UDVSet& u, int ntau, int ntau1) {
   prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
     RET(slice_scale(h, nt));
+    if (oz_propagate(h)) {  // U <- diag(S) expT U on the tensor cores, in place (U is sliced first)
+      RET(oz_slice(h, u.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->oz_S, h->oz_bits,
+                   h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
+      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->oz_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+                  h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, u.U, 1, N, (long long)N * N, B, h->S,
+                  N));
+      continue;
+    }
     GemmParams p = gsq(h, B);
     p.A = h->expT; p.realA = 1; p.modA = h->F;
     p.B = u.U; p.C = h->T1;
@@ -582,6 +596,13 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
   prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau1; nt >= ntau + 1; --nt) {
     RET(slice_scale(h, nt));
+    if (oz_propagate(h)) {  // U <- expT diag(conj S) U on the tensor cores (S real), in place
+      RET(oz_slice(h, h->udvl.U, OZ_CROWS, N, 1, (long long)N * N, 0, h->S, N, N, N, nullptr, h->oz_S, h->oz_bits,
+                   h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
+      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->oz_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+                  h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, h->udvl.U, 1, N, (long long)N * N, B));
+      continue;
+    }
     GemmParams q = gsq(h, B);
     q.A = h->expT; q.realA = 1; q.modA = h->F;
     q.B = h->udvl.U; q.C = h->T1;
@@ -1042,7 +1063,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
     p.kdyn = h->m + h->C;  // per-(chain, flavour) rank, written by k_update
-    if (h->mixed && h->oz) {
+    if (h->mixed && h->oz && !h->oz_narrow) {
       // G -= X Y as one real product: [Re X | Im X] times the K-doubled complex rows of Y
       const int Kf = 2 * UPD_KMAX;
       RET(oz_slice(h, h->X, OZ_CKA, 1, N, p.sA, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,
@@ -1095,6 +1116,7 @@ static int oz_setup(alfgpu_s* h) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);
   const long long tiles = (long long)((N + OZ_BM - 1) / OZ_BM) * ((2 * N + 31) / 32) * (long long)B;
   const int narrow = tiles < 2ll * nsm;
+  h->oz_narrow = narrow;
   if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
     return 0;

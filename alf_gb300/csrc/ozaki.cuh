@@ -375,6 +375,7 @@ struct OzGemmParams {
   int omode, osub;           // OZ_OUT_*, 1: out -= A B
   void* out; long long ldr, ldc, sout;  // element strides (complex128 for _COLS/_ROWS, float64 for _REAL)
   int* err;                  // bit 2: a bounded wait gave up
+  const zd* rsc; long long srsc;  // optional real scale of output row m (real part used), per batch
 };
 
 static inline size_t oz_smem_bytes(int bn, int S, int nkc, int nst) {
@@ -515,6 +516,11 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
       const int n = n0 + c0 + j;
       const int eb = (n < p.N) ? p.expB[(size_t)bB * p.RpadB + n] : 0;
       v[j] = oz_i64_to_f64(Z[j], ea + eb - L);
+    }
+    if (p.rsc && m < p.M) {
+      const double s = p.rsc[(size_t)b * p.srsc + m].x;
+#pragma unroll
+      for (int j = 0; j < HB; ++j) v[j] *= s;
     }
     if (p.omode == OZ_OUT_REAL) {
       double* o = (double*)p.out + (size_t)b * p.sout;
