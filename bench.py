@@ -8,6 +8,8 @@ sequential sweep (up pass, down pass, 2*Nstm stabilisations).
 
 value: sweeps/s with all state resident on the device, timed with CUDA events
        on the library's stream (device draw stream, no host traffic).
+mixed: (FP64 runs, one GPU) the same measurements for the mixed form on the same
+       workload, and max |G_mixed - G_fp64| after one sweep on identical fields and draws.
 e2e:   the same metric through the C ABI with host buffers: each step copies
        the host draws in (6*M*Ltrot doubles) and reads G back (N^2*N_FL complex),
        both inside the timed region.
@@ -43,6 +45,14 @@ FP64_DMMA_TFLOPS = 1.048
 HOP_TRAFFIC_BYTES = 3.30e6
 
 
+def measured_bf16_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)"
+    except Exception:
+        return 1900.0, "fallback 1.9 PFLOP/s bf16 burst"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -57,6 +67,8 @@ def parse():
     ap.add_argument("--chains", type=int, default=1, help="independent chains per GPU (batched)")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="keep the default delay depth")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="FP64 runs: skip the mixed-form measurement reported beside the headline")
     return ap.parse_args()
 
 
@@ -130,6 +142,42 @@ def algorithmic_flops(m, phase: str, launches: int, n_acc: int) -> float:
     return None
 
 
+def roofline(args, m, prof):
+    """Roofline object of the G-wrap GEMM, the largest consumer of the complex products with a
+    clean algorithmic count (2 real x complex N^3 products per flavour per slice, 2 L slices
+    per sweep).  FP64 form: k_zgemm against the measured FP64 MMA rate.  Mixed form:
+    k_oz_slice + k_oz_gemm (digit-sliced BF16 on tcgen05) against the measured BF16 peak; the
+    algorithmic count is the same as FP64's, the BF16 products actually executed are
+    reported beside it (tensor_op_tflops)."""
+    hop_ms, hop_n = prof.get("hop", (0.0, 0))
+    flops = algorithmic_flops(m, "hop", hop_n, 0) * args.chains
+    if args.precision == "fp64":
+        roof = {"bound": "tensor", "kernel": "k_zgemm (G wraps, FP64 mma.sync)", "achieved": None,
+                "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
+                "traffic": HOP_TRAFFIC_BYTES if m.ndim == 256 else None,
+                "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
+                "peak_source": "FP64 mma.sync m8n8k4 throughput measured on this pool "
+                               "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
+    else:
+        peak, src = measured_bf16_peak()
+        N, F = m.ndim, m.n_fl
+        kpad = (N + 63) // 64 * 64
+        bits, S = next((b, (54 + b - 1) // b) for b in range(7, 3, -1)
+                       if ((54 + b - 1) // b) * kpad * ((1 << b) - 1) ** 2 < 2 ** 24)
+        pairs = S * (S + 1) // 2 + (S - 1)  # digit pairs of the S + 1 accumulated diagonals
+        roof = {"bound": "tensor", "kernel": "k_oz_slice + k_oz_gemm (G wraps, digit-sliced BF16 on tcgen05)",
+                "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": None,
+                "algorithmic_flops_per_launch": args.chains * F * 4.0 * N ** 3,
+                "bf16_products_per_algorithmic_product": pairs,
+                "peak_source": src + "; of measured"}
+    if flops and hop_ms > 0:
+        roof["achieved"] = flops / (hop_ms / 1e3) / 1e12
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        if args.precision != "fp64":
+            roof["tensor_op_tflops"] = roof["achieved"] * roof["bf16_products_per_algorithmic_product"]
+    return roof
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from alf_gb300 import model as mdl, rng
@@ -198,6 +246,27 @@ def run_ours(args, ws, rank, local):
                 stats=st, chains=ch, launches=n_launch, delay=delay)
 
 
+def mixed_vs_fp64(m, seed: int, local: int, flags: int):
+    """max |G_mixed - G_fp64| over both flavours after one sweep from the same fields and
+    the same host draws (the accept sequences agree unless a draw falls within rounding of
+    its Metropolis weight), and the mixed form's own Precision Green of that sweep."""
+    from alf_gb300 import rng
+    from alf_gb300.sweep import Chains
+    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)[None, :]
+    gs = []
+    for prec in ("fp64", "mixed"):
+        ch = Chains(m, n_chains=1, precision=prec, device=local, flags=flags)
+        ch.set_fields(0, f0)
+        ch.init_state()
+        ch.sweep(u)
+        gs.append((ch.green(0), ch.fields(0), ch.stats(0).xmaxG))
+        ch.close()
+    same = bool(np.array_equal(gs[0][1], gs[1][1]))
+    return {"max_abs_dG_vs_fp64": float(np.max(np.abs(gs[1][0] - gs[0][0]))), "same_fields": same,
+            "xmaxG_mixed": gs[1][2], "xmaxG_fp64": gs[0][2], "sweeps": 1}
+
+
 def cpu_oracle_rate(m, seed: int, threads: int, slices: int):
     """Sweeps/s of the CPU restatement on a bounded sample (slices time slices incl. stabilisations)."""
     import oracle
@@ -261,17 +330,7 @@ def main():
     # the mixed form) carries the largest share of the launch list, and its largest
     # consumer with a clean algorithmic count is the G wrap (2 real x complex N^3
     # products per flavour per slice, 2 L slices per sweep).
-    hop_ms, hop_n = prof.get("hop", (0.0, 0))
-    flops = algorithmic_flops(m, "hop", hop_n, 0) * args.chains
-    roof = {"bound": "tensor", "kernel": "k_zgemm (G wraps)" if args.precision == "fp64" else "k_dfgemm (G wraps)",
-            "achieved": None, "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
-            "traffic": HOP_TRAFFIC_BYTES if args.precision == "fp64" and m.ndim == 256 else None,
-            "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
-            "peak_source": "FP64 mma.sync m8n8k4 throughput measured on this pool "
-                           "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
-    if flops and hop_ms > 0:
-        roof["achieved"] = flops / (hop_ms / 1e3) / 1e12
-        roof["frac"] = roof["achieved"] / FP64_DMMA_TFLOPS
+    roof = roofline(args, m, prof)
     phases = {k: {"ms_per_sweep": v[0] / 2.0, "launch_groups_per_sweep": v[1] / 2.0} for k, v in prof.items()}
     launches = int(r["launches"])
     cpu = None
@@ -284,10 +343,34 @@ def main():
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
     st = r["stats"]
+    mixed = None
+    if args.precision == "fp64" and args.compare and ws == 1:
+        import copy
+        a2 = copy.copy(args)
+        a2.precision = "mixed"
+        r2 = run_ours(a2, ws, rank, local)
+        st2 = r2["stats"]
+        mixed = {"value": replicas.whole_job_rate(ws, args.chains, args.steps, r2["t_dev"]), "unit": "sweeps/s",
+                 "e2e": replicas.whole_job_rate(ws, args.chains, args.steps, r2["t_e2e"]),
+                 "ms_per_step": 1e3 * r2["t_dev"] / args.steps, "gpu_launches": int(r2["launches"]),
+                 "delay_depth": r2["delay"], "clocks": r2["clocks"],
+                 "phases": {k: {"ms_per_sweep": v[0] / 2.0} for k, v in r2["prof"].items()},
+                 "precision_green": {"xmaxG": st2.xmaxG, "xmeanG": st2.xmeanG_sum / max(st2.ncg, 1),
+                                     "xmaxP": st2.xmaxP},
+                 "roofline": roofline(a2, m, r2["prof"]),
+                 "dtype": "c128 state; G wraps and UDV propagation (and the flushes of batched grids) as "
+                          "FP64-accurate digit-sliced BF16 tensor-core products; per-visit arithmetic and "
+                          "single-chain flushes in double-float; QR / CGR in FP64"}
+        r2["chains"].close()
+        try:
+            mixed["vs_fp64"] = mixed_vs_fp64(m, args.seed, local, args.flags)
+        except Exception as e:
+            mixed["vs_fp64"] = {"failed": str(e)}
     line = {
         "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "df64+c128",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products, df64 visits",
         "data": "synthetic (seeded fields and draws)",
         "config": dict(workload, parallelism=f"replicas x{ws}", delay_depth=r["delay"],
                        delay_depth_source="autotuned (alfgpu_tune_delay)" if args.tune else "default"),
@@ -297,6 +380,8 @@ def main():
         "precision_green": {"xmaxG": st.xmaxG, "xmeanG": st.xmeanG_sum / max(st.ncg, 1), "xmaxP": st.xmaxP},
         "acceptance": st.n_acc / max(st.n_prop, 1),
     }
+    if mixed is not None:
+        line["mixed"] = mixed
     print(json.dumps(line))
     r["chains"].close()
 
