@@ -96,6 +96,7 @@ def lib(build_if_missing: bool = True):
         "alfgpu_cgr": ([C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "alfgpu_decompose": ([C.c_int32, C.c_char, vp, vp, vp], C.c_int),
         "alfgpu_decompose_noalloc": ([C.c_int32, C.c_char, vp, vp, vp, vp, vp], C.c_int),
+        "alfgpu_last_error": ([vp], C.c_char_p),
         "alfgpu_oz_dgemm": ([C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, C.c_int32,
                              C.c_int32], C.c_int),
     }

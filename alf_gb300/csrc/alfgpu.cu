@@ -25,6 +25,10 @@
 #include "tau.cuh"
 #include "ozaki.cuh"
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace {
 
 struct UDVSet {  // one UDV state for all B = C*F (chain, flavour) pairs
@@ -79,6 +83,8 @@ struct alfgpu_s {
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda = cudaSuccess;
+  int last_line = 0;        // source line of the CUDA call that failed
+  char last_msg[160] = {0};
   bool hop_ok = false, vert_ok = false, fields_ok = false, state_ok = false;
   // model
   double *expT = nullptr, *expTinv = nullptr;
@@ -175,6 +181,7 @@ static void prof_collect(alfgpu_s* h) {
     cudaError_t e_ = (x);                       \
     if (e_ != cudaSuccess) {                    \
       h->last_cuda = e_;                        \
+      h->last_line = __LINE__;                  \
       return ALFGPU_ERROR_CUDA;                 \
     }                                           \
   } while (0)
@@ -188,6 +195,24 @@ static void prof_collect(alfgpu_s* h) {
     int r_ = (x);             \
     if (r_) return r_;        \
   } while (0)
+
+// A kernel's dynamic shared-memory limit is one setting per process and device, shared by
+// every handle: it is only ever raised, so a handle created later with smaller needs does
+// not invalidate the launches of an earlier one.
+template <typename K>
+static cudaError_t raise_smem_limit(K* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[std::make_pair((const void*)kernel, dev)];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
 
 template <typename T>
 static int dalloc(alfgpu_s* h, T** p, size_t count) {
@@ -1141,9 +1166,9 @@ static int oz_setup(alfgpu_s* h) {
   const size_t sm2 = oz_smem_bytes(h->ozf_bn, h->ozf_S, 1, h->ozf_nst);
   const int sm32 = (int)std::max(h->oz_bn == 32 ? sm1 : 0, h->ozf_bn == 32 ? sm2 : 0);
   const int sm16 = (int)std::max(h->oz_bn == 16 ? sm1 : 0, h->ozf_bn == 16 ? sm2 : 0);
-  if (sm32 && cudaFuncSetAttribute(k_oz_gemm<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32) != cudaSuccess)
+  if (sm32 && raise_smem_limit(k_oz_gemm<32>, (size_t)sm32) != cudaSuccess)
     return ALFGPU_ERROR_CUDA;
-  if (sm16 && cudaFuncSetAttribute(k_oz_gemm<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm16) != cudaSuccess)
+  if (sm16 && raise_smem_limit(k_oz_gemm<16>, (size_t)sm16) != cudaSuccess)
     return ALFGPU_ERROR_CUDA;
   h->oz = 1;
   return 0;
@@ -1192,10 +1217,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
         cudaFuncSetAttribute(k_bqr_panel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
       return fail(ALFGPU_ERROR_CUDA);
   }
-  if (cudaFuncSetAttribute(k_update<ArD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes()) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_update<ArF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes()) !=
-          cudaSuccess)
+  if (raise_smem_limit(k_update<ArD>, upd_smem_bytes()) != cudaSuccess ||
+      raise_smem_limit(k_update<ArF>, upd_smem_bytes()) != cudaSuccess)
     return fail(ALFGPU_ERROR_CUDA);
   // shrink the QR cluster until at least one cluster fits on the device
   while (h->CL > 1) {
@@ -1223,8 +1246,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   {
     const size_t sm = qrr_smem_bytes(h->N, h->CL);
     if (sm <= 227 * 1024 &&
-        cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
-        cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
+        raise_smem_limit(k_qrp_rows<ArD>, sm) == cudaSuccess && raise_smem_limit(k_qrp_rows<ArF>, sm) == cudaSuccess &&
         (h->CL <= 8 ||
          (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
           cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess))) {
@@ -1723,11 +1745,17 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
         h->launches = l0;
         if (rc) return rc;
         h->last_cuda = ce;
+        h->last_line = __LINE__;
         return ALFGPU_ERROR_CUDA;
       }
       const cudaError_t ie = cudaGraphInstantiate(&h->gexec[gi], graph, 0);
       cudaGraphDestroy(graph);
-      if (ie != cudaSuccess) { h->gexec[gi] = nullptr; h->last_cuda = ie; return ALFGPU_ERROR_CUDA; }
+      if (ie != cudaSuccess) {
+        h->gexec[gi] = nullptr;
+        h->last_cuda = ie;
+        h->last_line = __LINE__;
+        return ALFGPU_ERROR_CUDA;
+      }
       h->glaunches[gi] = h->launches - l0;
       h->launches = l0;
     }
@@ -2032,8 +2060,8 @@ int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t ld
     if (oz_tmap(&ta, sa, Kp, (long long)S * RpA, OZ_BM) || oz_tmap(&tb, sb, Kp, (long long)S * RpB, bn))
       return ALFGPU_ERROR_CUDA;
     const size_t sm = oz_smem_bytes(bn, S, Kp / OZ_KC, nst);
-    if (bn == 32) CK(cudaFuncSetAttribute(k_oz_gemm<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    else CK(cudaFuncSetAttribute(k_oz_gemm<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (bn == 32) CK(raise_smem_limit(k_oz_gemm<32>, sm));
+    else CK(raise_smem_limit(k_oz_gemm<16>, sm));
     RET(oz_slice(h, dA, OZ_REAL, 1, m, 0, 0, nullptr, 0, m, k, nullptr, S, bits, RpA, Kp, sa, ea, 1));
     RET(oz_slice(h, dB, OZ_REAL, k, 1, 0, 0, nullptr, 0, n, k, nullptr, S, bits, RpB, Kp, sb, eb, 1));
     RET(oz_gemm(h, ta, tb, m, n, Kp, S, bits, bn, nst, RpA, RpB, 0, 0, ea, eb, OZ_OUT_REAL, 0, dC, 1, m, 0, 1));
@@ -2045,4 +2073,10 @@ int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t ld
   rc = run();
   alfgpu_destroy(h);
   return rc;
+}
+
+const char* alfgpu_last_error(alfgpu_t* h) {
+  if (!h) return "null handle";
+  snprintf(h->last_msg, sizeof(h->last_msg), "alfgpu.cu:%d: %s", h->last_line, cudaGetErrorString(h->last_cuda));
+  return h->last_msg;
 }

@@ -132,7 +132,7 @@ class Chains:
             rc = self.L.alfgpu_sweep(self.h, _p(u), cb, None)
         else:
             rc = self.L.alfgpu_sweep(self.h, None, cb, None)
-        _lib.check(rc, "alfgpu_sweep")
+        _lib.check(rc, "alfgpu_sweep" + (f" ({self.L.alfgpu_last_error(self.h).decode()})" if rc == 100 else ""))
         return (eq, tau) if measure else None
 
     # --- delay depth ---------------------------------------------------------------------------

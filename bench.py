@@ -59,7 +59,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hubbard16x16")
+    ap.add_argument("--config", default="hubbard16x16",
+                    choices=["hubbard4x4", "hubbard16x16", "honeycomb12x12", "kondo12x12", "batch128"],
+                    help="hubbard16x16: one 16x16 chain; honeycomb12x12: 12x12 honeycomb, beta 20, TAU_M every "
+                         "sweep; kondo12x12: Kondo bilayer (ham_Uf = 0), TAU_M every sweep; batch128: 128 Hubbard "
+                         "chains with per-chain L, beta, U, one handle per (N_dim, Ltrot) group")
+    ap.add_argument("--ltau", type=int, default=-1, help="TAU_M every sweep (default: the config's)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
     ap.add_argument("--pivoting", default="default", choices=["default", "exact", "norms", "norms-cgr", "norms-decompose"])
@@ -178,6 +183,97 @@ def roofline(args, m, prof):
     return roof
 
 
+def workload_model(name: str):
+    """(model, ltau) of a named workload.  Kondo: the library runs the J_K vertices in their
+    shared eigenbasis and rejects U_f vertices, so ham_Uf = 0."""
+    from alf_gb300 import model as mdl
+    if name == "kondo12x12":
+        return mdl.kondo(12, 12, JK=1.5, Uf=0.0, beta=10.0, dtau=0.1, nwrap=10), 1
+    if name == "honeycomb12x12":
+        return mdl.config(name), 1
+    if name == "batch128":
+        return mdl.config("hubbard16x16"), 0
+    return mdl.config(name), 0
+
+
+def batch128_groups(seed: int, n: int = 128):
+    """Per chain, from its own seed: L in {6,8,10,12,14,16}, beta in {4,6,8,10} (dtau 0.1), U in
+    [2, 8]; grouped by (L, beta), i.e. by (N_dim, Ltrot)."""
+    groups = {}
+    for c in range(n):
+        r = np.random.default_rng([seed, c])
+        L = int(r.choice([6, 8, 10, 12, 14, 16]))
+        beta = float(r.choice([4.0, 6.0, 8.0, 10.0]))
+        U = float(r.uniform(2.0, 8.0))
+        groups.setdefault((L, beta), []).append((c, U))
+    return groups
+
+
+def run_batch(args, ws, rank, local):
+    """Config batch128: one handle per (N_dim, Ltrot) group with per-chain U; a step is one
+    sweep of every chain (groups one after the other on the GPU)."""
+    import torch
+    from alf_gb300 import model as mdl, rng, replicas
+    from alf_gb300.sweep import Chains
+    torch.cuda.set_device(local)
+    groups = batch128_groups(replicas.replica_seed(args.seed, rank))
+    hs = []
+    for (L, beta), members in sorted(groups.items()):
+        models = [mdl.hubbard("square", L, L, U=U, beta=beta, dtau=0.1, nwrap=10) for _, U in members]
+        ch = Chains(models[0], n_chains=len(members), precision=args.precision, device=local,
+                    pivoting=args.pivoting, flags=args.flags, models=models)
+        for k, (c, _) in enumerate(members):
+            s = replicas.replica_seed(args.seed, rank, c)
+            ch.set_fields(k, rng.initial_fields(s, k, models[0].n_op, models[0].ltrot))
+        ch.init_state()
+        for k, (c, _) in enumerate(members):
+            ch.set_rng(k, replicas.replica_seed(args.seed, rank, c), rng.sweep_counter_base(models[0].n_op, models[0].ltrot, 0))
+        hs.append((ch, models[0], members))
+    nchains = sum(len(x[2]) for x in hs)
+    streams = [torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local) for ch, _, _ in hs]
+    for _ in range(args.warmup):
+        for ch, m, mem in hs:
+            try:
+                ch.sweep(None)
+            except Exception as e:
+                raise RuntimeError(f"group L={m.params.get('L1')} Ltrot={m.ltrot} chains={len(mem)}: {e}") from e
+    for ch, _, _ in hs:
+        ch.reset_stats()
+    torch.cuda.synchronize()
+    n0 = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs)
+    ms = 0.0
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            for (ch, _, _), st in zip(hs, streams):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                ch.sweep(None)
+                e1.record(st)
+                e1.synchronize()
+                ms += e0.elapsed_time(e1)
+    n_launch = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs) - n0
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for ch, m, members in hs:
+            u = np.stack([rng.sweep_uniforms(replicas.replica_seed(args.seed, rank, c), k, m.n_op, m.ltrot, 1000 + i)
+                          for k, (c, _) in enumerate(members)])
+            ch.sweep(u)
+            g = ch.green(0)
+            if i == 0:
+                h2d += u.nbytes
+                d2h += g.nbytes
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    xmax = max(ch.stats(k).xmaxG for ch, _, mem in hs for k in range(len(mem)))
+    out = dict(t_dev=ms / 1e3, t_e2e=e2e_s, clocks=clk.summary(), launches=n_launch, h2d=h2d, d2h=d2h,
+               nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem)}
+                                       for _, m, mem in hs], xmaxG=xmax)
+    for ch, _, _ in hs:
+        ch.close()
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from alf_gb300 import model as mdl, rng
@@ -185,10 +281,13 @@ def run_ours(args, ws, rank, local):
     from alf_gb300.sweep import Chains
 
     torch.cuda.set_device(local)
-    m = mdl.config(args.config)
+    m, ltau = workload_model(args.config)
+    if args.ltau >= 0:
+        ltau = args.ltau
     C = args.chains
     seed = replicas.replica_seed(args.seed, rank)
-    ch = Chains(m, n_chains=C, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags)
+    ch = Chains(m, n_chains=C, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags,
+                ltau=ltau)
     for c in range(C):
         ch.set_fields(c, rng.initial_fields(replicas.replica_seed(args.seed, rank, c), c, m.n_op, m.ltrot))
     ch.init_state()
@@ -243,7 +342,7 @@ def run_ours(args, ws, rank, local):
     # launch count per sweep from the profile pass
     t_dev, t_e2e = replicas.max_over_ranks([ms / 1e3, e2e_s], device=f"cuda:{local}")
     return dict(m=m, t_dev=t_dev, t_e2e=t_e2e, clocks=clk.summary(), prof=prof, n_acc=n_acc, h2d=h2d, d2h=d2h,
-                stats=st, chains=ch, launches=n_launch, delay=delay)
+                stats=st, chains=ch, launches=n_launch, delay=delay, ltau=ltau)
 
 
 def mixed_vs_fp64(m, seed: int, local: int, flags: int):
@@ -267,11 +366,11 @@ def mixed_vs_fp64(m, seed: int, local: int, flags: int):
             "xmaxG_mixed": gs[1][2], "xmaxG_fp64": gs[0][2], "sweeps": 1}
 
 
-def cpu_oracle_rate(m, seed: int, threads: int, slices: int):
+def cpu_oracle_rate(m, seed: int, threads: int, slices: int, ltau: int = 0):
     """Sweeps/s of the CPU restatement on a bounded sample (slices time slices incl. stabilisations)."""
     import oracle
     from alf_gb300 import rng
-    o = oracle.Oracle(m, threads=threads)
+    o = oracle.Oracle(m, ltau=ltau, threads=threads)
     o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
     o.init_state()
     u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
@@ -287,12 +386,23 @@ def main():
     if ws > 1:
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    from alf_gb300 import model as mdl
-    m = mdl.config(args.config)
-    workload = {"workload": f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
-                            f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
-                            f"Nwrap={m.nwrap}, Mz four-valued fields, "
-                            + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"),
+    m, ltau0 = workload_model(args.config)
+    ltau = ltau0 if args.ltau < 0 else args.ltau
+    if args.config == "batch128":
+        desc = ("batch128: 128 Hubbard chains on square L x L lattices, per chain from its own seed L in "
+                "{6,...,16}, beta in {4,6,8,10}, dtau 0.1, U in [2,8], Nwrap 10, Mz fields; one handle per "
+                "(N_dim, Ltrot) group")
+    elif args.config == "kondo12x12":
+        desc = (f"kondo12x12: Kondo bilayer square 12x12, N_dim={m.ndim}, J_K=1.5, ham_Uf=0, beta={m.beta}, "
+                f"dtau={m.dtau}, Ltrot={m.ltrot}, Nwrap={m.nwrap}, N_SUN=2, N_FL=1, four-valued fields, "
+                f"TAU_M every sweep: {bool(ltau)}, "
+                + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"))
+    else:
+        desc = (f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
+                f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
+                f"Nwrap={m.nwrap}, Mz four-valued fields, TAU_M every sweep: {bool(ltau)}, "
+                + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"))
+    workload = {"workload": desc,
                 "chains_per_gpu": args.chains, "precision": args.precision, "pivoting": args.pivoting, "flags": args.flags, "l2": "flushed between timed steps (256 MB write)",
                 "draws": "device counter stream (value); host arrays through the C ABI (e2e)"}
     if args.impl == "reference":
@@ -302,7 +412,7 @@ def main():
         slices = 20 if m.ndim >= 200 else 2 * m.ltrot
         rates = []
         for i in range(args.warmup + args.steps):
-            r, dt = cpu_oracle_rate(m, args.seed, cores, slices)
+            r, dt = cpu_oracle_rate(m, args.seed, cores, slices, ltau)
             if i >= args.warmup:
                 rates.append(r)
         v = float(np.mean(rates))
@@ -311,10 +421,33 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded fields and draws)",
                 "config": dict(workload, chains_per_gpu=1, parallelism="host cores"),
                 "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{slices} time slices of one sweep (with their stabilisations) per step, "
+                                 "sample": f"{slices} time slices of one sweep (with their stabilisations"
+                          + ("; TAU_M, which runs after the down pass, is outside the sample" if ltau else "")
+                          + ") per step, "
                                            f"CPU restatement of ALF's default-STAB sweep calling OpenBLAS LAPACK "
                                            f"with {cores} threads; the Fortran reference has no compiler here"},
                 "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if args.config == "batch128":
+        rb = run_batch(args, ws, rank, local)
+        if rank != 0:
+            return
+        from alf_gb300 import replicas
+        t_dev, t_e2e = rb["t_dev"], rb["t_e2e"]
+        value = ws * rb["nchains"] * args.steps / t_dev
+        line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products, df64 visits",
+                "data": "synthetic (seeded fields and draws)",
+                "config": dict(workload, chains_per_gpu=rb["nchains"], groups=rb["groups"],
+                               parallelism=f"replicas x{ws}", delay_depth="default"),
+                "e2e": {"value": ws * rb["nchains"] * args.steps / t_e2e, "unit": "sweeps/s",
+                        "h2d_bytes_per_step": rb["h2d"], "d2h_bytes_per_step": rb["d2h"]},
+                "roofline": None, "cpu_baseline": None, "clocks": rb["clocks"], "gpu_launches": int(rb["launches"]),
+                "precision_green": {"xmaxG": rb["xmaxG"]}}
         print(json.dumps(line))
         return
 

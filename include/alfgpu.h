@@ -255,6 +255,10 @@ int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, doub
  * scales of A and B; k <= 512, else ALFGPU_ERROR_SIZE).  The kernel the G wraps use, exposed for testing and
  * for callers that want FP64-accurate products on the tensor cores.  Synchronous;
  * allocates and frees its own device buffers. */
+/* The CUDA call behind the last ALFGPU_ERROR_CUDA of this handle ("file:line: CUDA error
+ * string"); the pointer stays valid until the next call on the handle. */
+const char* alfgpu_last_error(alfgpu_t* h);
+
 int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t lda, const double* B, int32_t ldb,
                     double* C, int32_t ldc, int32_t device);
 
