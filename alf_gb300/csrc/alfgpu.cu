@@ -133,6 +133,7 @@ struct alfgpu_s {
   // recording
   int recording = 0, rec_stab = 0;
   int8_t* rec_acc = nullptr;
+  int rec_nstm = 0;  // stabilisation points the recording buffers hold
   zd *rec_ratio = nullptr, *rec_G = nullptr, *rec_Gw = nullptr, *rec_phase = nullptr;
   FieldTables ft;
   std::vector<void*> allocs;
@@ -1780,6 +1781,49 @@ int alfgpu_set_delay(alfgpu_t* h, int32_t k) {
   return 0;
 }
 
+// Stabilisation interval (control of the stabilisation drift): re-plans the stabilisation
+// points (Stab_nt of main.F90:446-457 with the new Nwrap) and grows the UDV stack as needed.
+// G and the stack belong to the old points afterwards, so alfgpu_init_state must run before
+// the next sweep.
+int alfgpu_set_nwrap(alfgpu_t* h, int32_t nwrap) {
+  if (!h || nwrap < 1 || nwrap > h->L) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  const int L = h->L;
+  const int nstm = (L % nwrap == 0) ? L / nwrap : L / nwrap + 1;
+  const size_t N = h->N, NN = N * N, B = h->B;
+  while ((int)h->udvst.size() < nstm) {
+    UDVSet s;
+    int q = 0;
+    q |= dalloc(h, &s.U, B * NN); q |= dalloc(h, &s.V, B * NN); q |= dalloc(h, &s.D, B * N); q |= dalloc(h, &s.detU, B);
+    if (q) return ALFGPU_ERROR_CUDA;
+    h->udvst.push_back(s);
+  }
+  if (h->rec_acc && nstm > h->rec_nstm) {
+    const size_t P = 2 * (size_t)nstm;
+    int r = 0;
+    r |= dalloc(h, &h->rec_G, P * B * NN);
+    r |= dalloc(h, &h->rec_Gw, P * B * NN);
+    r |= dalloc(h, &h->rec_phase, P * h->C);
+    if (r) return ALFGPU_ERROR_CUDA;
+    h->rec_nstm = nstm;
+  }
+  h->Nstm = nstm;
+  h->d.nwrap = nwrap;
+  h->stab_nt.assign(nstm + 1, 0);
+  for (int n = 1; n < nstm; ++n) h->stab_nt[n] = nwrap * n;
+  h->stab_nt[nstm] = L;
+  drop_graphs(h);
+  h->state_ok = false;
+  return 0;
+}
+
+int alfgpu_get_nwrap(alfgpu_t* h, int32_t* nwrap) {
+  if (!h || !nwrap) return ALFGPU_ERROR_ARGUMENT;
+  *nwrap = h->d.nwrap;
+  return 0;
+}
+
 int alfgpu_get_delay(alfgpu_t* h, int32_t* k) {
   if (!h || !k) return ALFGPU_ERROR_ARGUMENT;
   *k = h->kblk;
@@ -1862,6 +1906,7 @@ int alfgpu_set_recording(alfgpu_t* h, int32_t enable) {
     r |= dalloc(h, &h->rec_Gw, P * h->B * NN);
     r |= dalloc(h, &h->rec_phase, P * h->C);
     if (r) return ALFGPU_ERROR_CUDA;
+    h->rec_nstm = h->Nstm;
   }
   h->recording = enable ? 1 : 0;
   return 0;

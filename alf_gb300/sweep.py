@@ -151,6 +151,38 @@ class Chains:
         _lib.check(self.L.alfgpu_tune_delay(self.h, nsweeps, C.byref(k)), "alfgpu_tune_delay")
         return k.value
 
+    # --- stabilisation interval --------------------------------------------------------------
+    def set_nwrap(self, nwrap: int):
+        """New stabilisation interval; call init_state before the next sweep."""
+        _lib.check(self.L.alfgpu_set_nwrap(self.h, nwrap), "alfgpu_set_nwrap")
+
+    def nwrap(self) -> int:
+        k = C.c_int32()
+        _lib.check(self.L.alfgpu_get_nwrap(self.h, C.byref(k)), "alfgpu_get_nwrap")
+        return k.value
+
+    def adapt_nwrap(self, bound: float = 1e-5, sweeps: int = 1):
+        """Shorten Nwrap while the drift is too large: run `sweeps` device-draw sweeps, and if
+        any chain's Precision Green (max |G_wrapped - G_fresh|) exceeds `bound` (or the sweep
+        stops with ALF's ERROR_UNSTABLE_MATRIX), halve Nwrap, rebuild G and the UDV stack from
+        the current fields and try again.  The sweeps advance the chains (use them as
+        thermalisation).  Returns (nwrap, worst Precision Green)."""
+        while True:
+            self.reset_stats()
+            try:
+                for _ in range(sweeps):
+                    self.sweep(None)
+                worst = max(self.stats(c).xmaxG for c in range(self.C))
+            except _lib.AlfGpuError as e:
+                if e.code != 3:  # ERROR_UNSTABLE_MATRIX: ALF's abort at Precision Green > 10
+                    raise
+                worst = float("inf")
+            nw = self.nwrap()
+            if worst <= bound or nw == 1:
+                return nw, worst
+            self.set_nwrap(max(1, nw // 2))
+            self.init_state()
+
     # --- readback --------------------------------------------------------------------------------
     def green(self, chain: int = 0) -> np.ndarray:
         G = np.zeros((self.F, self.N, self.N), np.complex128)
@@ -186,7 +218,8 @@ class Chains:
 
     def record(self, chain: int = 0) -> dict:
         V = 2 * self.M * self.Lt
-        P = 2 * self.model.nstm
+        nw = self.nwrap()  # the handle's current interval (alfgpu_set_nwrap may have changed it)
+        P = 2 * ((self.Lt + nw - 1) // nw)
         acc = np.zeros(V, np.int8)
         ratio = np.zeros(V, np.complex128)
         G = np.zeros((P, self.F, self.N, self.N), np.complex128)

@@ -65,6 +65,8 @@ def parse():
                          "sweep; kondo12x12: Kondo bilayer (ham_Uf = 0), TAU_M every sweep; batch128: 128 Hubbard "
                          "chains with per-chain L, beta, U, one handle per (N_dim, Ltrot) group")
     ap.add_argument("--ltau", type=int, default=-1, help="TAU_M every sweep (default: the config's)")
+    ap.add_argument("--drift-bound", type=float, default=1e-5,
+                    help="batch128: Nwrap of a group is halved until its Precision Green is below this")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
     ap.add_argument("--pivoting", default="default", choices=["default", "exact", "norms", "norms-cgr", "norms-decompose"])
@@ -237,6 +239,11 @@ def run_batch(args, ws, rank, local):
                 ch.sweep(None)
             except Exception as e:
                 raise RuntimeError(f"group L={m.params.get('L1')} Ltrot={m.ltrot} chains={len(mem)}: {e}") from e
+    # drift control: per group, halve Nwrap until Precision Green <= the bound (untimed sweeps)
+    nwraps = []
+    for ch, m, mem in hs:
+        nw, worst = ch.adapt_nwrap(bound=args.drift_bound)
+        nwraps.append((nw, worst))
     for ch, _, _ in hs:
         ch.reset_stats()
     torch.cuda.synchronize()
@@ -267,8 +274,9 @@ def run_batch(args, ws, rank, local):
     e2e_s = time.perf_counter() - t0
     xmax = max(ch.stats(k).xmaxG for ch, _, mem in hs for k in range(len(mem)))
     out = dict(t_dev=ms / 1e3, t_e2e=e2e_s, clocks=clk.summary(), launches=n_launch, h2d=h2d, d2h=d2h,
-               nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem)}
-                                       for _, m, mem in hs], xmaxG=xmax)
+               nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem),
+                                        "nwrap": nw, "xmaxG_at_adapt": worst}
+                                       for (_, m, mem), (nw, worst) in zip(hs, nwraps)], xmaxG=xmax)
     for ch, _, _ in hs:
         ch.close()
     return out
@@ -390,8 +398,8 @@ def main():
     ltau = ltau0 if args.ltau < 0 else args.ltau
     if args.config == "batch128":
         desc = ("batch128: 128 Hubbard chains on square L x L lattices, per chain from its own seed L in "
-                "{6,...,16}, beta in {4,6,8,10}, dtau 0.1, U in [2,8], Nwrap 10, Mz fields; one handle per "
-                "(N_dim, Ltrot) group")
+                "{6,...,16}, beta in {4,6,8,10}, dtau 0.1, U in [2,8], Nwrap 10 (halved per group until Precision "
+                f"Green <= {args.drift_bound:g}), Mz fields; one handle per (N_dim, Ltrot) group")
     elif args.config == "kondo12x12":
         desc = (f"kondo12x12: Kondo bilayer square 12x12, N_dim={m.ndim}, J_K=1.5, ham_Uf=0, beta={m.beta}, "
                 f"dtau={m.dtau}, Ltrot={m.ltrot}, Nwrap={m.nwrap}, N_SUN=2, N_FL=1, four-valued fields, "

@@ -176,6 +176,13 @@ int alfgpu_init_state(alfgpu_t* h, double* phase_out);
  * device stream.  cb may be NULL (no measurements). */
 int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx);
 
+/* Stabilisation interval Nwrap (the reference's fixed Nwrap, main.F90:446-457): re-plans the
+ * stabilisation points and grows the UDV stack as needed; G and the stack must then be
+ * rebuilt from the current fields with alfgpu_init_state before the next sweep.  A driver
+ * shortens Nwrap when Precision Green (alfgpu_get_stats) exceeds its bound. */
+int alfgpu_set_nwrap(alfgpu_t* h, int32_t nwrap);
+int alfgpu_get_nwrap(alfgpu_t* h, int32_t* nwrap);
+
 /* Delay depth k of the delayed (block submatrix) update: at most k positions per
  * block before the rank-k flush (2..32; the default is dims.delay_k or 32).
  * alfgpu_tune_delay is the autotuner: it runs nsweeps sweeps on the device draw stream
@@ -195,7 +202,9 @@ int alfgpu_reset_stats(alfgpu_t* h);
 /* Parity recording (diagnostics): while enabled, every vertex visit's ratio and
  * accept bit, and G and the phase at every stabilisation point are kept on the
  * device for the next sweep; alfgpu_get_record copies them out for one chain.
- * Sizes per sweep: visits = 2*n_op*Ltrot, points = 2*Nstm. */
+ * Sizes per sweep: visits = 2*n_op*Ltrot, points = 2*Nstm with Nstm = ceil(Ltrot / Nwrap)
+ * for the handle's CURRENT Nwrap (alfgpu_get_nwrap; alfgpu_set_nwrap changes it): the
+ * caller's buffers must hold that many points. */
 int alfgpu_set_recording(alfgpu_t* h, int32_t enable);
 int alfgpu_get_record(alfgpu_t* h, int32_t chain, int8_t* acc, double* ratio, double* G_fresh,
                       double* G_wrapped, double* phase);

@@ -256,3 +256,51 @@ def test_sweep_hubbard_16x16_beta10_parity(pivoting):
     # the benchmark configuration itself (N_dim = 256, Ltrot = 100, 20 stabilisation points):
     # fresh G at every stabilisation point and every ratio against the oracle on one sweep
     _run_pair(mdl.config("hubbard16x16"), seed=3, sweeps=1, pivoting=pivoting)
+
+
+def test_set_nwrap_matches_oracle_with_that_nwrap():
+    # a handle built with Nwrap = 10, switched to Nwrap = 3 (ragged: Ltrot = 40 -> 14 points)
+    # and re-initialised from its fields, sweeps like the oracle built with Nwrap = 3
+    m10 = mdl.config("hubbard4x4")
+    m3 = mdl.hubbard("square", 4, 4, U=4.0, beta=4.0, dtau=0.1, nwrap=3)
+    seed = 31
+    f0 = rng.initial_fields(seed, 0, m10.n_op, m10.ltrot)
+    g = Chains(m10, n_chains=1)
+    g.set_fields(0, f0)
+    g.init_state()
+    g.set_nwrap(3)
+    assert g.nwrap() == 3
+    g.init_state()
+    o = oracle.Oracle(m3)
+    o.set_fields(f0)
+    o.init_state()
+    assert _relmax(g.green(0), o.green()) < RTOL
+    g.set_recording(True)
+    for s in range(2):
+        u = rng.sweep_uniforms(seed, 0, m3.n_op, m3.ltrot, s)
+        o.record(1)
+        o.sweep(u)
+        ro = o.recorded()
+        g.sweep(u[None, :])
+        rg = g.record(0)
+        np.testing.assert_array_equal(rg["acc"], ro["acc"])
+        assert rg["G"].shape[0] == ro["G"].shape[0] == 2 * 14
+        for p in range(ro["G"].shape[0]):
+            assert _relmax(rg["G"][p], ro["G"][p]) < RTOL, (s, p)
+    np.testing.assert_array_equal(g.fields(0), o.fields())
+
+
+def test_adapt_nwrap_shortens_until_the_drift_bound_holds():
+    # U = 8 at beta = 4 with Nwrap = 20: the wrap drift is far above 1e-12; halving Nwrap
+    # until Precision Green <= 1e-12 ends at a shorter interval that meets it (or at 1)
+    m = mdl.hubbard("square", 4, 4, U=8.0, beta=4.0, dtau=0.1, nwrap=20)
+    g = Chains(m, n_chains=2)
+    for c in range(2):
+        g.set_fields(c, rng.initial_fields(40 + c, c, m.n_op, m.ltrot))
+    g.init_state()
+    for c in range(2):
+        g.set_rng(c, 40 + c, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    nw, worst = g.adapt_nwrap(bound=1e-12)
+    assert nw < 20 and (worst <= 1e-12 or nw == 1)
+    g.sweep(None)
+    assert max(g.stats(c).xmaxG for c in range(2)) < 1e-9
