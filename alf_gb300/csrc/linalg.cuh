@@ -27,6 +27,20 @@ struct QRParams {
   QRInfo* info;
 };
 
+// Squared 2-norm of a complex vector segment, computed by one warp: the plain sum of
+// squares (FP64 products only); the scaled form below when that sum over- or underflows.
+ALF_DEV double warp_znrm2(const zd* x, int n);
+ALF_DEV double warp_znrm2sq(const zd* x, int n) {
+  double s = 0.0;
+  for (int i = threadIdx.x & 31; i < n; i += 32) s = fma(x[i].x, x[i].x, fma(x[i].y, x[i].y, s));
+  s = warp_sum(s);
+  if (!(s < 1e300) || (s != 0.0 && s < 1e-290)) {
+    const double r = warp_znrm2(x, n);
+    s = r * r;
+  }
+  return s;
+}
+
 // Scaled 2-norm of a strided complex vector segment, computed by one warp.
 ALF_DEV double warp_znrm2(const zd* x, int n) {
   double mx = 0.0;
@@ -69,8 +83,8 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
       for (int r = lane; r < N; r += 32) col[r] = zscale(col[r], s);
       __syncwarp();
     }
-    double nrm = warp_znrm2(col, N);
-    if (lane == 0) { vn1[c] = nrm; vn2[c] = nrm; jpvt[c] = c + 1; }
+    const double nrm2 = warp_znrm2sq(col, N);  // squared norms throughout (same pivot order)
+    if (lane == 0) { vn1[c] = nrm2; vn2[c] = nrm2; jpvt[c] = c + 1; }
   }
   cluster_sync();
 
@@ -122,15 +136,18 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
       // ZLARFG on A(j:N, j)
       if (warp == 0) {
         const int nx = N - j - 1;
-        double xnorm = warp_znrm2(cj + j + 1, nx);
+        const double xn2 = warp_znrm2sq(cj + j + 1, nx);
         zd alpha = cj[j];
         zd t = zmk(0.0, 0.0), scal = zmk(0.0, 0.0);
         double beta = 0.0;
-        bool trivial = (xnorm == 0.0 && alpha.y == 0.0);
+        bool trivial = (xn2 == 0.0 && alpha.y == 0.0);
         if (!trivial) {
           double ar = alpha.x, ai = alpha.y;
-          double w = fmax(fabs(ar), fmax(fabs(ai), xnorm));
-          double l3 = w * sqrt((ar / w) * (ar / w) + (ai / w) * (ai / w) + (xnorm / w) * (xnorm / w));
+          double l3 = sqrt(fma(ar, ar, fma(ai, ai, xn2)));
+          if (!(l3 < 1e150)) {  // the scaled form of ZLAPY3 where the squares could overflow
+            const double xnorm = sqrt(xn2), w = fmax(fabs(ar), fmax(fabs(ai), xnorm));
+            l3 = w * sqrt((ar / w) * (ar / w) + (ai / w) * (ai / w) + (xnorm / w) * (xnorm / w));
+          }
           beta = -copysign(l3, ar);
           t = zmk((beta - ar) / beta, -ai / beta);
           scal = zdiv(zmk(1.0, 0.0), zsub(alpha, zmk(beta, 0.0)));
@@ -163,19 +180,16 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
         for (int r = j + lane; r < N; r += 32) col[r] = zsub(col[r], zmul(vsh[r], f));
         __syncwarp();
       }
-      // norm downdate (ZLAQP2)
-      double v1 = vn1[c];
+      // norm downdate (ZLAQP2) on squared norms: vn1^2 (1 - (|a|/vn1)^2) = vn1^2 - |a|^2, and the
+      // recompute test (vn1/vn2)^2 max(0, 1 - (|a|/vn1)^2) <= tol3z needs no division
+      const double v1 = vn1[c];
       if (v1 != 0.0) {
         const zd a = col[j];
-        double tmp = fmax(1.0 - (a.x * a.x + a.y * a.y) / (v1 * v1), 0.0);
-        double r2 = v1 / vn2[c];
-        double tmp2 = tmp * r2 * r2;
-        double nv1, nv2 = vn2[c];
-        if (tmp2 <= tol3z) {
-          if (j < N - 1) { nv1 = warp_znrm2(col + j + 1, N - j - 1); nv2 = nv1; }
+        const double rest = fmax(v1 - fma(a.x, a.x, a.y * a.y), 0.0);
+        double nv1 = rest, nv2 = vn2[c];
+        if (rest <= tol3z * nv2) {
+          if (j < N - 1) { nv1 = warp_znrm2sq(col + j + 1, N - j - 1); nv2 = nv1; }
           else { nv1 = 0.0; nv2 = 0.0; }
-        } else {
-          nv1 = v1 * sqrt(tmp);
         }
         if (lane == 0) { vn1[c] = nv1; vn2[c] = nv2; }
       }
