@@ -1,0 +1,66 @@
+"""Bin analysis of Monte Carlo observables: ALF's jackknife with the sign.
+
+Restates the published algorithm of Libraries/Modules/errors_mod.F90 (ERRCALC :98-126,
+ERRCALC_JS :290-327, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
+Analysis/ana_mod.F90 (ERRCALCJ calls, e.g. :1380, :1587, :1783) applies to the per-bin
+averages of <O s> and <s> written by the observables module:
+
+* rebin: consecutive groups of ``nrebin`` bins are averaged (a trailing remainder is
+  dropped, like the reference's integer division);
+* jackknife: leave-one-out ratios x_n = (sum_b O_b - O_n) / (sum_b s_b - s_n), optionally
+  mapped by f;
+* mean and error: the mean of the x_n, and sqrt(sum_n (x_n - mean)^2) (the reference's
+  ERRCALC standard error times the number of bins, without the (n - 1)/n factor of the
+  textbook jackknife).
+
+Complex observables are analysed part by part (ERRCALC_C): real and imaginary errors.
+"""
+from __future__ import annotations
+
+from typing import Callable, Optional, Tuple
+
+import numpy as np
+
+
+def errcalc(en) -> Tuple[float, float]:
+    """Mean and standard error of the mean of the samples (ERRCALC)."""
+    en = np.asarray(en, dtype=np.float64)
+    n = en.size
+    xm = en.sum() / n
+    xsq = ((en - xm) ** 2).sum() / n
+    xerr = xsq / n
+    return float(xm), float(np.sqrt(xerr)) if xerr > 0 else 0.0
+
+
+def rebin(x, nrebin: int) -> np.ndarray:
+    """Averages of consecutive groups of nrebin bins (the remainder is dropped)."""
+    x = np.asarray(x)
+    n = x.shape[0] // nrebin
+    return x[: n * nrebin].reshape((n, nrebin) + x.shape[1:]).mean(axis=1)
+
+
+def _js_real(en, si, f):
+    en = np.asarray(en, dtype=np.float64)
+    si = np.asarray(si, dtype=np.float64)
+    if en.shape != si.shape:
+        raise ValueError("jackknife: observable and sign bins differ in number")
+    x = (en.sum() - en) / (si.sum() - si)
+    if f is not None:
+        x = np.array([f(v) for v in x], dtype=np.float64)
+    xm, xerr = errcalc(x)
+    return xm, xerr * en.size
+
+
+def jackknife(en, si=None, nrebin: int = 1, f: Optional[Callable[[float], float]] = None):
+    """Sign-weighted jackknife of per-bin averages ``en`` (of O s) and ``si`` (of s):
+    mean and error of <O s>/<s> (or of f of it).  si = None: no sign (all ones).  Complex
+    en: (mean, error) with real and imaginary parts analysed separately."""
+    en = np.asarray(en)
+    si = np.ones(en.shape[0]) if si is None else np.asarray(si, dtype=np.float64)
+    if nrebin > 1:
+        en, si = rebin(en, nrebin), rebin(si, nrebin)
+    if np.iscomplexobj(en):
+        mr, er = _js_real(en.real, si, f)
+        mi, ei = _js_real(en.imag, si, f)
+        return complex(mr, mi), complex(er, ei)
+    return _js_real(en, si, f)

@@ -1617,6 +1617,20 @@ int alfgpu_get_fields(alfgpu_t* h, int32_t chain, int8_t* f) {
   return 0;
 }
 
+int alfgpu_get_rng_state(alfgpu_t* h, int32_t chain, uint64_t* key, uint64_t* counter) {
+  if (!h || chain < 0 || chain >= h->C || !key || !counter) return ALFGPU_ERROR_ARGUMENT;
+  *key = h->h_key[chain];
+  *counter = h->h_ctr[chain];
+  return 0;
+}
+
+int alfgpu_set_rng_state(alfgpu_t* h, int32_t chain, uint64_t key, uint64_t counter) {
+  if (!h || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
+  h->h_key[chain] = key;
+  h->h_ctr[chain] = counter;
+  return 0;
+}
+
 int alfgpu_set_rng(alfgpu_t* h, int32_t chain, uint64_t seed, uint64_t counter) {
   if (!h || chain < 0 || chain >= h->C) return ALFGPU_ERROR_ARGUMENT;
   h->h_key[chain] = alf_chain_key(seed, (uint64_t)chain);

@@ -151,6 +151,35 @@ class Chains:
         _lib.check(self.L.alfgpu_tune_delay(self.h, nsweeps, C.byref(k)), "alfgpu_tune_delay")
         return k.value
 
+    # --- checkpoint / resume (the reference's confout files) ------------------------------------
+    def checkpoint(self, path: str):
+        """Write every chain's fields and draw-stream state, the stabilisation interval and the
+        delay depth to an .npz file."""
+        keys = np.zeros(self.C, np.uint64)
+        ctrs = np.zeros(self.C, np.uint64)
+        for c in range(self.C):
+            k, n = C.c_uint64(), C.c_uint64()
+            _lib.check(self.L.alfgpu_get_rng_state(self.h, c, C.byref(k), C.byref(n)), "alfgpu_get_rng_state")
+            keys[c], ctrs[c] = k.value, n.value
+        np.savez(path, fields=np.stack([self.fields(c) for c in range(self.C)]), keys=keys, counters=ctrs,
+                 nwrap=self.nwrap(), delay=self.delay(), ndim=self.N, ltrot=self.Lt, n_op=self.M)
+
+    def restore(self, path: str) -> np.ndarray:
+        """Resume from checkpoint(): fields, draw streams, Nwrap and delay depth; G and the UDV
+        stack are rebuilt from the fields (init_state), as the reference does on restart."""
+        z = np.load(path)
+        if (int(z["ndim"]), int(z["ltrot"]), int(z["n_op"])) != (self.N, self.Lt, self.M) or \
+                z["fields"].shape[0] != self.C:
+            raise ValueError("checkpoint does not match this handle's sizes")
+        for c in range(self.C):
+            self.set_fields(c, z["fields"][c])
+            _lib.check(self.L.alfgpu_set_rng_state(self.h, c, int(z["keys"][c]), int(z["counters"][c])),
+                       "alfgpu_set_rng_state")
+        if int(z["nwrap"]) != self.nwrap():
+            self.set_nwrap(int(z["nwrap"]))
+        self.set_delay(int(z["delay"]))
+        return self.init_state()
+
     # --- stabilisation interval --------------------------------------------------------------
     def set_nwrap(self, nwrap: int):
         """New stabilisation interval; call init_state before the next sweep."""

@@ -166,6 +166,13 @@ int alfgpu_get_fields(alfgpu_t* h, int32_t chain, int8_t* f);
 
 /* Per-chain draw stream used when alfgpu_sweep gets uniforms = NULL. */
 int alfgpu_set_rng(alfgpu_t* h, int32_t chain, uint64_t seed, uint64_t counter);
+/* Checkpoint / resume of a chain (the reference writes the fields and its generator state to
+ * confout_<rank>, Fields_mod.F90:474-506, and reads them back, :750-778): the draw stream's
+ * key and next counter.  With alfgpu_get_fields / alfgpu_set_fields and alfgpu_init_state
+ * (G is rebuilt from the fields, as on the reference's restart) a chain resumes on the same
+ * draws. */
+int alfgpu_get_rng_state(alfgpu_t* h, int32_t chain, uint64_t* key, uint64_t* counter);
+int alfgpu_set_rng_state(alfgpu_t* h, int32_t chain, uint64_t key, uint64_t counter);
 
 /* Initial UDV stack and G (main.F90:589-631); phase_out: complex per chain (may be NULL). */
 int alfgpu_init_state(alfgpu_t* h, double* phase_out);

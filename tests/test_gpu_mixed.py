@@ -93,3 +93,54 @@ def test_mixed_double_float_wraps_small():
     w = _compare(mdl.hubbard("square", 8, 8, U=4.0, beta=4.0, dtau=0.1, nwrap=10), seed=2, sweeps=1,
                  flags=FLAG_NO_TENSOR_GEMM)
     assert w < BOUND
+
+
+def test_mixed_kondo_bilayer_vs_fp64_oracle():
+    # two-site J_K vertices in their shared eigenbasis, tensor-core wraps in that basis
+    m = mdl.kondo(4, 4, JK=1.5, Uf=0.0, beta=2.0, dtau=0.1, nwrap=10)
+    w = _compare(m, seed=8, sweeps=1)
+    assert w < BOUND
+
+
+def test_mixed_tau_m_quartets_vs_fp64_oracle():
+    # TAU_M propagation in the mixed form (tensor-core hopping products): every quartet
+    # [GT0, G0T, G00, GTT] within 1e-5 of the FP64 oracle's
+    m = mdl.hubbard("honeycomb", 3, 3, U=5.0, beta=1.0, dtau=0.05, nwrap=5)
+    seed = 3
+    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
+    o = oracle.Oracle(m, ltau=1)
+    o.set_fields(f0)
+    o.init_state()
+    _, tau_o = o.collect_measurements()
+    o.sweep(u)
+    g = Chains(m, precision="mixed", ltau=1)
+    g.set_fields(0, f0)
+    g.init_state()
+    _, tau_g = g.sweep(u[None, :], measure=True)
+    if not np.array_equal(g.fields(0), o.fields()):
+        pytest.skip("accept sequences parted at a draw within rounding of its weight")
+    assert len(tau_g) == len(tau_o) == m.ltrot + 1
+    for (c, nt, qg, _), (nt_o, qo, _) in zip(tau_g, tau_o):
+        for k in range(4):
+            assert np.max(np.abs(qg[k] - qo[k])) <= BOUND, (nt, k)
+
+
+def test_mixed_batched_chains_with_own_couplings_vs_oracle():
+    # one handle, two chains with different U (per-chain vertex tables): each within 1e-5 of
+    # its own FP64 oracle run
+    ms = [mdl.hubbard("square", 6, 6, U=U, beta=2.0, dtau=0.1, nwrap=10) for U in (3.0, 7.0)]
+    seeds = (12, 13)
+    g = Chains(ms[0], n_chains=2, precision="mixed", models=ms)
+    for c in range(2):
+        g.set_fields(c, rng.initial_fields(seeds[c], c, ms[c].n_op, ms[c].ltrot))
+    g.init_state()
+    us = np.stack([rng.sweep_uniforms(seeds[c], c, ms[c].n_op, ms[c].ltrot, 0) for c in range(2)])
+    g.sweep(us)
+    for c in range(2):
+        o = oracle.Oracle(ms[c])
+        o.set_fields(rng.initial_fields(seeds[c], c, ms[c].n_op, ms[c].ltrot))
+        o.init_state()
+        o.sweep(us[c])
+        if np.array_equal(g.fields(c), o.fields()):
+            assert np.max(np.abs(g.green(c) - o.green())) < BOUND, c

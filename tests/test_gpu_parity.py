@@ -304,3 +304,30 @@ def test_adapt_nwrap_shortens_until_the_drift_bound_holds():
     assert nw < 20 and (worst <= 1e-12 or nw == 1)
     g.sweep(None)
     assert max(g.stats(c).xmaxG for c in range(2)) < 1e-9
+
+
+def test_checkpoint_resume_continues_on_the_same_draws(tmp_path):
+    # confout-style restart: fields + draw-stream state (+ Nwrap, delay depth) written after two
+    # sweeps; a new handle restored from it and the original both run two more sweeps
+    m = mdl.config("hubbard4x4")
+    g = Chains(m, n_chains=2)
+    for c in range(2):
+        g.set_fields(c, rng.initial_fields(50 + c, c, m.n_op, m.ltrot))
+        g.set_rng(c, 50 + c, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    g.init_state()
+    g.set_nwrap(5)
+    g.init_state()
+    for _ in range(2):
+        g.sweep(None)
+    path = str(tmp_path / "confout.npz")
+    g.checkpoint(path)
+    for _ in range(2):
+        g.sweep(None)
+    h = Chains(m, n_chains=2)
+    h.restore(path)
+    assert h.nwrap() == 5
+    for _ in range(2):
+        h.sweep(None)
+    for c in range(2):
+        np.testing.assert_array_equal(h.fields(c), g.fields(c))
+        assert _relmax(h.green(c), g.green(c)) < 1e-8
