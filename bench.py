@@ -477,10 +477,11 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            rate, dt = cpu_oracle_rate(m, args.seed, 1, 20 if m.ndim >= 200 else 2 * m.ltrot)
+            ns = 2 * m.ltrot if m.ndim <= 256 else 40  # one full sweep (~6 s for 16x16 on one core)
+            rate, dt = cpu_oracle_rate(m, args.seed, 1, ns, r.get("ltau", 0))
             cpu = {"value": rate, "unit": "sweeps/s", "cores": 1, "kind": "port",
-                   "sample": f"{20 if m.ndim >= 200 else 2 * m.ltrot} time slices with their stabilisations "
-                             f"({dt:.1f} s), CPU restatement of ALF's sweep with single-threaded OpenBLAS"}
+                   "sample": f"{ns} time slices with their stabilisations ({dt:.1f} s), CPU restatement of ALF's "
+                             f"sweep with single-threaded OpenBLAS"}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
     st = r["stats"]
