@@ -98,6 +98,9 @@ def lib(build_if_missing: bool = True):
         "alfgpu_decompose_noalloc": ([C.c_int32, C.c_char, vp, vp, vp, vp, vp], C.c_int),
         "alfgpu_last_error": ([vp], C.c_char_p),
         "alfgpu_set_nwrap": ([vp, C.c_int32], C.c_int),
+        "alfgpu_set_scalar_obs": ([vp, vp, vp], C.c_int),
+        "alfgpu_get_scalar_obs": ([vp, C.c_int32, vp], C.c_int),
+        "alfgpu_reset_scalar_obs": ([vp], C.c_int),
         "alfgpu_get_rng_state": ([vp, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
         "alfgpu_set_rng_state": ([vp, C.c_int32, C.c_uint64, C.c_uint64], C.c_int),
         "alfgpu_get_nwrap": ([vp, C.POINTER(C.c_int32)], C.c_int),

@@ -47,6 +47,9 @@ struct alfgpu_s {
   int mixed_propagate = 0; // mixed form, opt-in: UDV propagation products in double-float too
   // mixed form: G wraps and delayed-update flushes as digit-sliced BF16 tensor-core GEMMs
   // (ozaki.cuh); otherwise double-float GEMMs on the FP32 pipes
+  // device-side equal-time scalar observables (alfgpu_set_scalar_obs)
+  int obs_scal = 0, obs_nsun = 1;
+  double *obs_HT = nullptr, *obs_trH = nullptr, *obs_U = nullptr, *obs_acc = nullptr;
   int oz = 0, eexp_complex = 0;
   int oz_narrow = 0;  // small grids: BN = 16 tiles; the flush keeps the double-float GEMM (measured faster there)
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
@@ -767,8 +770,7 @@ static int ensure_obs_host(alfgpu_s* h) {
 // ham%Obser(GR, PHASE, ntau1) for every chain (main.F90:757-772, 788-803).  With a pending
 // vertex scaling (up pass), G in ALF's frame is S G Sinv, formed into the work matrix Gw.
 static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pending) {
-  if (!cb) return 0;
-  RET(ensure_obs_host(h));
+  if (!cb && !h->obs_scal) return 0;
   const long long NN = (long long)h->N * h->N;
   const zd* src = h->G;
   if (pending || h->rot) {
@@ -781,6 +783,13 @@ static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pendi
     RET(rotate_out(h, h->Gw, h->B));
     src = h->Gw;
   }
+  if (h->obs_scal) {
+    k_obs_scal<<<h->C, 256, 0, h->st>>>(src, h->phase, h->obs_HT, h->obs_trH, h->obs_U, h->N, h->F, h->obs_nsun,
+                                        h->obs_acc);
+    CKL();
+  }
+  if (!cb) return 0;
+  RET(ensure_obs_host(h));
   CK(cudaMemcpyAsync(h->obs_host, src, (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->phase_host, h->phase, (size_t)h->C * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -2138,4 +2147,58 @@ const char* alfgpu_last_error(alfgpu_t* h) {
   if (!h) return "null handle";
   snprintf(h->last_msg, sizeof(h->last_msg), "alfgpu.cu:%d: %s", h->last_line, cudaGetErrorString(h->last_cuda));
   return h->last_msg;
+}
+
+int alfgpu_set_scalar_obs(alfgpu_t* h, const double* H, const double* U) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  if (!H || !U) {  // off
+    h->obs_scal = 0;
+    drop_graphs(h);
+    return 0;
+  }
+  const size_t N = h->N, NN = N * N, F = h->F;
+  if (!h->obs_HT) {
+    int r = 0;
+    r |= dalloc(h, &h->obs_HT, F * NN); r |= dalloc(h, &h->obs_trH, F); r |= dalloc(h, &h->obs_U, N);
+    r |= dalloc(h, &h->obs_acc, 10 * (size_t)h->C);
+    if (r) return ALFGPU_ERROR_CUDA;
+  }
+  std::vector<double> ht(F * NN), tr(F, 0.0);
+  for (size_t f = 0; f < F; ++f)
+    for (size_t i = 0; i < N; ++i) {
+      tr[f] += H[f * NN + i + i * N];
+      for (size_t j = 0; j < N; ++j) {
+        const double v = H[f * NN + i + j * N];  // H_f(i, j)
+        if (!std::isfinite(v)) return ALFGPU_ERROR_ARGUMENT;
+        ht[f * NN + j + i * N] = v;
+      }
+    }
+  for (size_t i = 0; i < N; ++i)
+    if (!std::isfinite(U[i])) return ALFGPU_ERROR_ARGUMENT;
+  if (h->rot) return ALFGPU_ERROR_UNSUPPORTED;  // two-site vertices: measure through the callback
+  CK(cudaMemcpy(h->obs_HT, ht.data(), F * NN * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->obs_trH, tr.data(), F * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->obs_U, U, N * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(h->obs_acc, 0, 10 * (size_t)h->C * sizeof(double)));
+  h->obs_nsun = h->NSUN;
+  h->obs_scal = 1;
+  drop_graphs(h);
+  return 0;
+}
+
+int alfgpu_get_scalar_obs(alfgpu_t* h, int32_t chain, double* sums) {
+  if (!h || !sums || chain < 0 || chain >= h->C || !h->obs_acc) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(sums, h->obs_acc + 10ll * chain, 10 * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int alfgpu_reset_scalar_obs(alfgpu_t* h) {
+  if (!h || !h->obs_acc) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemsetAsync(h->obs_acc, 0, 10 * (size_t)h->C * sizeof(double), h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
 }

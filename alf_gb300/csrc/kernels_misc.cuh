@@ -254,3 +254,78 @@ __global__ void k_rot_cols(zd* G, int N, const int* pairs, int npairs, double u0
   g[i + (long long)a * N] = zadd(zscale(x, u00), zscale(y, u01));
   g[i + (long long)c * N] = zadd(zscale(x, u10), zscale(y, u11));
 }
+
+
+// Equal-time scalar observables of the Hubbard-type models at one ham%Obser call site
+// (Hamiltonian_Hubbard_smod.F90:695-801; kinetic term as Predefined_Hoppings_Compute_Kin,
+// Predefined_Hop_mod.F90:1905-1959), accumulated per chain:
+//   GRC(i,j) = delta_ij - G(j,i),  ZP = Phase / Re(Phase),  ZS = sign(Re(Phase))
+//   Kin  = N_SUN sum_f sum_ij H_f(i,j) GRC_f(i,j) = N_SUN sum_f [tr H_f - sum_ij H_f(i,j) G_f(j,i)]
+//   Pot  = sum_i U_i GRC_1(i,i) GRC_dec(i,i)   (dec = 2 for two flavours, else 1)
+//   Part = N_SUN sum_f sum_i GRC_f(i,i),  Ener = Kin + Pot
+// acc[c] += {ZP ZS Kin, ZP ZS Pot, ZP ZS Part, ZP ZS Ener} (complex), ZS, 1.
+// HT holds H_f transposed (HT_f[j + i N] = H_f(i,j)), so sum_ij H(i,j) G(j,i) is the
+// elementwise sum over the two column-major arrays.  One CTA (256 threads) per chain, fixed
+// summation order.
+__global__ void __launch_bounds__(256) k_obs_scal(const zd* G, const zd* phase, const double* HT, const double* trH,
+                                                  const double* U, int N, int F, int nsun, double* acc) {
+  const int c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long NN = (long long)N * N;
+  double kr = 0.0, ki = 0.0, pr = 0.0, pi = 0.0;
+  for (int f = 0; f < F; ++f) {
+    const zd* g = G + ((long long)c * F + f) * NN;
+    const double* ht = HT + (long long)f * NN;
+    for (long long e = tid; e < NN; e += 256) {
+      const zd v = g[e];
+      kr = fma(ht[e], v.x, kr);
+      ki = fma(ht[e], v.y, ki);
+    }
+  }
+  // Pot and Part need the diagonals of both flavours at the same site
+  double rr = 0.0, ri = 0.0;
+  for (int i = tid; i < N; i += 256) {
+    const zd g1 = G[((long long)c * F) * NN + i + (long long)i * N];
+    const zd a = zmk(1.0 - g1.x, -g1.y);  // GRC_1(i,i)
+    zd b = a;
+    if (F == 2) {
+      const zd g2 = G[((long long)c * F + 1) * NN + i + (long long)i * N];
+      b = zmk(1.0 - g2.x, -g2.y);
+      rr += b.x; ri += b.y;
+    }
+    rr += a.x; ri += a.y;
+    const zd ab = zmul(a, b);
+    pr = fma(U[i], ab.x, pr);
+    pi = fma(U[i], ab.y, pi);
+  }
+  double v[6] = {kr, ki, pr, pi, rr, ri};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) v[q] = warp_sum(v[q]);
+  __shared__ double wsum[6][8];
+  if (lane == 0)
+    for (int q = 0; q < 6; ++q) wsum[q][warp] = v[q];
+  __syncthreads();
+  if (tid == 0) {
+    double s[6];
+    for (int q = 0; q < 6; ++q) {
+      s[q] = 0.0;
+      for (int w = 0; w < 8; ++w) s[q] += wsum[q][w];
+    }
+    double trh = 0.0;
+    for (int f = 0; f < F; ++f) trh += trH[f];
+    const zd kin = zmk(nsun * (trh - s[0]), -nsun * s[1]);
+    const zd pot = zmk(s[2], s[3]);
+    const zd part = zmk(nsun * s[4], nsun * s[5]);  // s[4], s[5]: sum_f sum_i GRC_f(i,i)
+    const zd ph = phase[c];
+    const double zs = ph.x > 0.0 ? 1.0 : (ph.x < 0.0 ? -1.0 : 0.0);
+    const zd zpzs = ph.x != 0.0 ? zscale(zmk(1.0, ph.y / ph.x), zs) : zmk(0.0, 0.0);
+    const zd o[4] = {kin, pot, part, zadd(kin, pot)};
+    double* a = acc + 10ll * c;
+    for (int q = 0; q < 4; ++q) {
+      const zd w = zmul(o[q], zpzs);
+      a[2 * q] += w.x;
+      a[2 * q + 1] += w.y;
+    }
+    a[8] += zs;
+    a[9] += 1.0;
+  }
+}

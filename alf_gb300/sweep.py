@@ -151,6 +151,30 @@ class Chains:
         _lib.check(self.L.alfgpu_tune_delay(self.h, nsweeps, C.byref(k)), "alfgpu_tune_delay")
         return k.value
 
+    # --- device-side scalar observables ----------------------------------------------------------
+    def set_scalar_obs(self, H: Optional[np.ndarray] = None, U: Optional[np.ndarray] = None):
+        """Accumulate Kin, Pot, Part, Ener on the device at every ham%Obser point (see
+        alfgpu_set_scalar_obs).  H: [n_fl][N][N] real hopping Hamiltonian (row index first);
+        U: [N].  No arguments: off."""
+        if H is None:
+            _lib.check(self.L.alfgpu_set_scalar_obs(self.h, None, None), "alfgpu_set_scalar_obs")
+            return
+        Hc = np.ascontiguousarray(np.transpose(np.asarray(H, np.float64).reshape(self.F, self.N, self.N),
+                                               (0, 2, 1)))  # column-major per flavour
+        Uc = np.ascontiguousarray(np.asarray(U, np.float64).reshape(self.N))
+        self._keep.append((Hc, Uc))
+        _lib.check(self.L.alfgpu_set_scalar_obs(self.h, _p(Hc), _p(Uc)), "alfgpu_set_scalar_obs")
+
+    def scalar_obs(self, chain: int = 0) -> dict:
+        """Accumulators of one chain: sums of ZP ZS {kin, pot, part, ener}, sum of ZS (sign), count."""
+        a = np.zeros(10, np.float64)
+        _lib.check(self.L.alfgpu_get_scalar_obs(self.h, chain, _p(a)), "alfgpu_get_scalar_obs")
+        return {"kin": complex(a[0], a[1]), "pot": complex(a[2], a[3]), "part": complex(a[4], a[5]),
+                "ener": complex(a[6], a[7]), "sign": a[8], "count": int(a[9])}
+
+    def reset_scalar_obs(self):
+        _lib.check(self.L.alfgpu_reset_scalar_obs(self.h), "alfgpu_reset_scalar_obs")
+
     # --- checkpoint / resume (the reference's confout files) ------------------------------------
     def checkpoint(self, path: str):
         """Write every chain's fields and draw-stream state, the stabilisation interval and the

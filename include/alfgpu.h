@@ -271,6 +271,23 @@ int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, doub
  * scales of A and B; k <= 512, else ALFGPU_ERROR_SIZE).  The kernel the G wraps use, exposed for testing and
  * for callers that want FP64-accurate products on the tensor cores.  Synchronous;
  * allocates and frees its own device buffers. */
+/* Device-side equal-time scalar observables of the Hubbard-type models (the Obs_scal part of
+ * ham%Obser, Hamiltonian_Hubbard_smod.F90:695-801; kinetic term as
+ * Predefined_Hoppings_Compute_Kin, Prog/Predefined_Hop_mod.F90:1905-1959).  At every
+ * ham%Obser call site of the sweep (after every slice of both passes) the library adds, per
+ * chain, ZP*ZS*{Kin, Pot, Part, Ener} (complex), ZS and 1 to its accumulators, with
+ * GRC(i,j) = delta_ij - G(j,i), ZP = Phase/Re(Phase), ZS = sign(Re(Phase)),
+ * Kin = N_SUN sum_f sum_ij H_f(i,j) GRC_f(i,j), Pot = sum_i U_i GRC_1(i,i) GRC_dec(i,i)
+ * (dec = 2 for two flavours, else 1), Part = N_SUN sum_f sum_i GRC_f(i,i), Ener = Kin + Pot.
+ * H: n_fl x Ndim x Ndim real column-major (the hopping Hamiltonian Op_T%O, chemical
+ * potential included), U: Ndim on-site couplings (ham_U).  H = U = NULL switches it off.
+ * Not for two-site (rotated-basis) vertices (ALFGPU_ERROR_UNSUPPORTED).
+ * alfgpu_get_scalar_obs: 10 doubles: Kin, Pot, Part, Ener as (re, im), sum of ZS, count;
+ * a bin is the accumulators between two alfgpu_reset_scalar_obs calls. */
+int alfgpu_set_scalar_obs(alfgpu_t* h, const double* H, const double* U);
+int alfgpu_get_scalar_obs(alfgpu_t* h, int32_t chain, double* sums);
+int alfgpu_reset_scalar_obs(alfgpu_t* h);
+
 /* The CUDA call behind the last ALFGPU_ERROR_CUDA of this handle ("file:line: CUDA error
  * string"); the pointer stays valid until the next call on the handle. */
 const char* alfgpu_last_error(alfgpu_t* h);
