@@ -52,6 +52,7 @@ struct alfgpu_s {
   double *obs_HT = nullptr, *obs_trH = nullptr, *obs_U = nullptr, *obs_acc = nullptr;
   int oz = 0, eexp_complex = 0;
   int oz_narrow = 0;  // small grids: BN = 16 tiles; the flush keeps the double-float GEMM (measured faster there)
+  int oz_stab = 0;    // the stabilisation's complex products on the tensor-core GEMM too
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
   unsigned short* ozE[4] = {nullptr, nullptr, nullptr, nullptr};  // expT, expTinv as A; expT, expTinv as B
@@ -369,6 +370,45 @@ static int oz_slice_expT(alfgpu_s* h) {
   return 0;
 }
 
+// Complex products of the stabilisation (CGR's U_R^H U_L, D_R V_R V_L D_L + RHS, the Q / U
+// products with 1/DUP scales and pivot permutations; decompose's R P V) on the tensor-core
+// GEMM in the mixed form: both operands as interleaved real / imaginary rows, the output
+// row / column scales folded into the digit exponents of A's rows / B's rows, the four real
+// products combined in the epilogue.  The real parts of rs / cs are used (the call sites pass
+// real singular values); alpha = 1, beta in {0, 1}, square N x N x N only.
+static bool oz_stab_ok(alfgpu_s* h, const GemmParams& g) {
+  return h->mixed && h->oz && h->oz_stab && !g.realA && !g.realB && !g.ks && !g.kdyn && g.modA == 0 &&
+         g.modB == 0 && g.alpha.x == 1.0 && g.alpha.y == 0.0 && g.beta.y == 0.0 &&
+         (g.beta.x == 0.0 || g.beta.x == 1.0) && g.m == h->N && g.n == h->N && g.k == h->N && g.opA != OP_T &&
+         g.opB != OP_T && g.batch == h->B;
+}
+
+static int oz_zgemm(alfgpu_s* h, const GemmParams& g) {
+  const int N = h->N;
+  OzSliceParams a;
+  memset(&a, 0, sizeof(a));
+  a.src = g.A; a.mode = OZ_CROWS; a.sb = g.sA; a.srows = N; a.Kc = N;
+  if (g.opA == OP_N) { a.sr = 1; a.sk = g.lda; a.trans = 0; }
+  else { a.sr = g.lda; a.sk = 1; a.trans = 1; a.conj = 1; }  // op(A)(i, k) = conj(A(k, i))
+  a.perm = g.permA; a.sperm = g.sPA; a.tri = g.triA;
+  a.rsc = g.rs; a.srsc = g.sRS; a.rinv = g.rsInv;
+  a.S = h->oz_S; a.bits = h->oz_bits; a.Rpad = h->oz_Rp2N; a.Kpad = h->oz_Kpad;
+  a.out = h->ozGA; a.expo = h->ozGAe; a.err = h->err;
+  OzSliceParams bq = a;
+  bq.src = g.B; bq.sb = g.sB;
+  if (g.opB == OP_N) { bq.sr = g.ldb; bq.sk = 1; bq.trans = 1; bq.conj = 0; }  // op(B)(k, j) = B(k, j)
+  else { bq.sr = 1; bq.sk = g.ldb; bq.trans = 0; bq.conj = 1; }              // op(B)(k, j) = conj(B(j, k))
+  bq.perm = g.permB; bq.sperm = g.sPB; bq.tri = g.triB;
+  bq.rsc = g.cs; bq.srsc = g.sCS; bq.rinv = g.csInv;
+  bq.out = h->ozGB; bq.expo = h->ozGBe;
+  h->launches += 2;
+  CK(oz_launch_slice(a, h->B, h->st));
+  CK(oz_launch_slice(bq, h->B, h->st));
+  return oz_gemm(h, h->tmGA, h->tmGB, 2 * N, 2 * N, h->oz_Kpad, h->oz_S, h->oz_bits, h->oz_bn, h->oz_nst,
+                 h->oz_Rp2N, h->oz_Rp2N, 0, 0, h->ozGAe, h->ozGBe, OZ_OUT_CPLX, g.beta.x == 1.0 ? -1 : 0, g.C, 1,
+                 g.ldc, g.sC, h->B);
+}
+
 // The mixed form's UDV propagation runs on the tensor-core GEMM (FP64-accurate) when the
 // slice scales are real.
 static bool oz_propagate(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_complex && !h->mixed_propagate; }
@@ -376,6 +416,7 @@ static bool oz_propagate(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_com
 // Stabilisation products (UDV propagation, decompose, CGR): double-float in the mixed
 // form, FP64 otherwise.
 static int gemm_s(alfgpu_s* h, const GemmParams& g) {
+  if (oz_stab_ok(h, g)) return oz_zgemm(h, g);
   if (!h->df_stab) return gemm(h, g);
   return gemm32(h, g, g.realA ? ST_R64 : ST_C128, g.realB ? ST_R64 : ST_C128, ST_C128);
 }
@@ -1331,6 +1372,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   if (h->mixed && !(d.reserved[0] & ALFGPU_FLAG_NO_TENSOR_GEMM)) {
     const int e = oz_setup(h);
     if (e) return fail(e);
+    h->oz_stab = h->oz && !(d.reserved[0] & ALFGPU_FLAG_FP64_STAB_GEMM) && !h->df_stab;
   }
   h->h_key.assign(C, 0); h->h_ctr.assign(C, 0);
   for (size_t c = 0; c < C; ++c) { h->h_key[c] = alf_chain_key(0, c); h->h_ctr[c] = M * L; }

@@ -38,7 +38,7 @@
 #include "common.cuh"
 
 enum { OZ_REAL = 0, OZ_CROWS = 1, OZ_CKA = 2, OZ_CKB = 3 };
-enum { OZ_OUT_COLS = 0, OZ_OUT_ROWS = 1, OZ_OUT_REAL = 2 };
+enum { OZ_OUT_COLS = 0, OZ_OUT_ROWS = 1, OZ_OUT_REAL = 2, OZ_OUT_CPLX = 3 };
 #define OZ_KC 64          // K chunk of one TMA box (128 bytes of BF16)
 #define OZ_BM 128         // MMA M
 #define OZ_TARGET_BITS 54
@@ -56,6 +56,10 @@ struct OzSliceParams {
   int srows;                // source rows (complex rows for OZ_C*)
   int Kc;                   // source K extent (complex k for OZ_C*)
   const int* kdyn;          // optional per-batch valid source K (entries beyond are zero)
+  const int* perm; long long sperm;  // optional K remap (OZ_CROWS): element (i, k) is source (i, perm[k])
+  int tri, trans;           // tri: zero the strictly lower triangle of the source in storage
+                            // coordinates (row, col) = trans ? (k', i) : (i, k'), k' the remapped k
+  const zd* rsc; long long srsc; int rinv;  // optional real per-row scale (real part), or its inverse
   int S, bits;
   int Rpad, Kpad;
   unsigned short* out;      // BF16 bits, [batch][S][Rpad][Kpad]
@@ -173,6 +177,12 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
   const int kd = p.kdyn ? min(p.kdyn[b], p.Kc) : p.Kc;
   double x0[2] = {0.0, 0.0}, x1[2] = {0.0, 0.0}, sc[2] = {1.0, 1.0};
   const int k0 = 2 * tid;
+  double rs_row = 1.0;  // per-row scale (an output row / column scale of the product)
+  if (p.rsc) {
+    rs_row = p.rsc[(size_t)b * p.srsc + i].x;
+    if (p.rinv) rs_row = 1.0 / rs_row;
+  }
+  const bool scaled = ks != nullptr || p.rsc != nullptr;
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     const int k = k0 + u;
@@ -183,7 +193,9 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
         break;
       case OZ_CROWS:
         if (k < kd) {
-          const zd z = srz[i * p.sr + k * p.sk];
+          const int kq = p.perm ? p.perm[(size_t)b * p.sperm + k] : k;
+          if (p.tri && (p.trans ? kq > i : i > kq)) break;  // below the diagonal of an upper triangle
+          const zd z = srz[i * p.sr + kq * p.sk];
           x0[u] = z.x; x1[u] = p.conj ? -z.y : z.y;
         }
         break;
@@ -201,9 +213,11 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
       } break;
     }
     if (ks) sc[u] = ks[k].x;
+    if (p.rsc) sc[u] = rs_row;
   }
-  int e0 = max(oz_ebound(x0[0], ks ? &sc[0] : nullptr), oz_ebound(x0[1], ks ? &sc[1] : nullptr));
-  int e1 = two ? max(oz_ebound(x1[0], ks ? &sc[0] : nullptr), oz_ebound(x1[1], ks ? &sc[1] : nullptr)) : -100000;
+  int e0 = max(oz_ebound(x0[0], scaled ? &sc[0] : nullptr), oz_ebound(x0[1], scaled ? &sc[1] : nullptr));
+  int e1 = two ? max(oz_ebound(x1[0], scaled ? &sc[0] : nullptr), oz_ebound(x1[1], scaled ? &sc[1] : nullptr))
+               : -100000;
   e0 = __reduce_max_sync(0xffffffffu, e0);
   e1 = __reduce_max_sync(0xffffffffu, e1);
   if (lane == 0) { red[0][warp] = e0; red[1][warp] = e1; }
@@ -220,8 +234,9 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
   if (k0 >= Kl) return;
   int bad = 0;
   unsigned* o = reinterpret_cast<unsigned*>(p.out + ((size_t)b * p.S * p.Rpad + r0) * p.Kpad + k0);
-  oz_write_pair(p, o, x0[0], x0[1], ks ? &sc[0] : nullptr, ks ? &sc[1] : nullptr, e0, &bad);
-  if (two) oz_write_pair(p, o + p.Kpad / 2, x1[0], x1[1], ks ? &sc[0] : nullptr, ks ? &sc[1] : nullptr, e1, &bad);
+  oz_write_pair(p, o, x0[0], x0[1], scaled ? &sc[0] : nullptr, scaled ? &sc[1] : nullptr, e0, &bad);
+  if (two)
+    oz_write_pair(p, o + p.Kpad / 2, x1[0], x1[1], scaled ? &sc[0] : nullptr, scaled ? &sc[1] : nullptr, e1, &bad);
   if (bad && p.err) atomicOr(p.err, 1);
 }
 
@@ -372,7 +387,7 @@ struct OzGemmParams {
   int RpadA, RpadB;
   int modA, modB;            // operand batch = b % mod when > 0
   const int* expA; const int* expB;
-  int omode, osub;           // OZ_OUT_*, 1: out -= A B
+  int omode, osub;           // OZ_OUT_*; osub 1: out -= A B, -1: out += A B (OZ_OUT_CPLX)
   void* out; long long ldr, ldc, sout;  // element strides (complex128 for _COLS/_ROWS, float64 for _REAL)
   int* err;                  // bit 2: a bounded wait gave up
   const zd* rsc; long long srsc;  // optional real scale of output row m (real part used), per batch
@@ -541,6 +556,39 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
             zd* w = o + m * p.ldr + jc * p.ldc;
             zd x = zmk(v[2 * j], v[2 * j + 1]);
             if (p.osub) { const zd g = *w; x = zmk(g.x - x.x, g.y - x.y); }
+            *w = x;
+          }
+        }
+    } else if (p.omode == OZ_OUT_CPLX) {
+      // complex x complex: rows 2i / 2i+1 hold Re / Im of A's row i, columns 2j / 2j+1 Re / Im
+      // of op(B)'s column j; C(i, j) = (ReA ReB - ImA ImB) + i (ReA ImB + ImA ReB).  The lane
+      // pair of rows 2i, 2i+1 exchanges halves: even lanes finish the first HQ complex columns
+      // of the thread's HB real columns, odd lanes the other HQ.
+      zd* o = (zd*)p.out + (size_t)b * p.sout;
+      const int i = m >> 1, c = m & 1;
+      constexpr int HQ = HB / 4;
+      double mine[HB / 2], got[HB / 2];
+#pragma unroll
+      for (int q2 = 0; q2 < HQ; ++q2) {
+        // static register indices: select the value, not the index
+        const double lo0 = v[2 * q2], lo1 = v[2 * q2 + 1], hi0 = v[2 * (HQ + q2)], hi1 = v[2 * (HQ + q2) + 1];
+        got[2 * q2] = __shfl_xor_sync(0xffffffffu, c ? lo0 : hi0, 1);  // what the partner finishes
+        got[2 * q2 + 1] = __shfl_xor_sync(0xffffffffu, c ? lo1 : hi1, 1);
+        mine[2 * q2] = c ? hi0 : lo0;
+        mine[2 * q2 + 1] = c ? hi1 : lo1;
+      }
+      if (2 * i < p.M)
+#pragma unroll
+        for (int q2 = 0; q2 < HQ; ++q2) {
+          const int jc = (n0 + c0) / 2 + (c ? HQ + q2 : q2);
+          if (2 * jc < p.N) {
+            // even lane: mine = (ReA ReB, ReA ImB), got = (ImA ReB, ImA ImB); odd lane the reverse
+            const double rr = c ? got[2 * q2] : mine[2 * q2], ri = c ? got[2 * q2 + 1] : mine[2 * q2 + 1];
+            const double ir = c ? mine[2 * q2] : got[2 * q2], ii = c ? mine[2 * q2 + 1] : got[2 * q2 + 1];
+            zd x = zmk(rr - ii, ri + ir);
+            zd* w = o + i * p.ldr + jc * p.ldc;
+            if (p.osub > 0) { const zd g = *w; x = zmk(g.x - x.x, g.y - x.y); }
+            else if (p.osub < 0) { const zd g = *w; x = zmk(g.x + x.x, g.y + x.y); }
             *w = x;
           }
         }

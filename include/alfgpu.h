@@ -91,6 +91,11 @@ enum { ALFGPU_FLAG_NO_GRAPH = 64 };
  * the tensor cores (tcgen05), exact to ~2^-54 like FP64 (N_dim <= 448); this flag selects
  * the double-float GEMMs on the FP32 pipes instead. */
 enum { ALFGPU_FLAG_NO_TENSOR_GEMM = 128 };
+/* Mixed form: the complex products inside the stabilisation (CGR's U_R^H U_L and
+ * D_R V_R V_L D_L, the products with Q and the pivot permutations, decompose's R P V) run on
+ * the same FP64-accurate tensor-core GEMM by default; this flag keeps them on the FP64 GEMM
+ * (the pivoted QR, triangular solves and phases are FP64 arithmetic either way). */
+enum { ALFGPU_FLAG_FP64_STAB_GEMM = 256 };
 
 typedef struct alfgpu_s alfgpu_t;
 
