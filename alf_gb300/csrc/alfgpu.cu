@@ -1122,8 +1122,12 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     prof_end(h);
     CKL();
     prof_begin(h, ALFGPU_PROF_FLUSH);
-    k_flush_xy<<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W, h->X,
-                                                                  h->Y);
+    if (h->mixed)
+      k_flush_xy<ArF><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
+                                                                         h->X, h->Y);
+    else
+      k_flush_xy<ArD><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
+                                                                         h->X, h->Y);
     CKL();
     void* Gst = h->G;
     void* Xst = h->X;

@@ -391,23 +391,26 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
 
 constexpr size_t upd_smem_bytes() { return 2ull * 2 * UPD_KMAX * (UPD_KMAX + 1) * 16; }  // Z is 16 bytes
 
-// Flush operands for G = G0 - X Y (one launch, spread over the GPU):
+// Flush operands for G = G0 - X Y (one launch, spread over the GPU; the m x m x N product of
+// Y in the precision form's arithmetic, double-float in the mixed form):
 //   X(:, l) = G0(:, s_l)
 //   Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :))
 // block 32 x 8 threads = (l, column / row); grid (ceil(N/8), chains*flavours).
 // X: [chain][2][N][KMAX] col-major (ld N); Y: [chain][2][KMAX][N] col-major (ld KMAX).
+template <class A>
 __global__ void k_flush_xy(const zd* Gv, long long sG, int N, int F, const int* m_in, const int* sites, const zd* W,
                            zd* X, zd* Y) {
+  typedef typename A::Z Z;
   const int b = blockIdx.y, c = b / F, f = b % F;
   const int m = m_in[c];
   if (m == 0) return;
-  __shared__ zd Ws[UPD_KMAX][UPD_KMAX + 1];
-  __shared__ zd gb[8][UPD_KMAX];
+  __shared__ Z Ws[UPD_KMAX][UPD_KMAX + 1];
+  __shared__ Z gb[8][UPD_KMAX];
   __shared__ int st[UPD_KMAX];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   for (int l = tid; l < m; l += 256) st[l] = sites[(long long)c * UPD_KMAX + l];
   for (int e = tid; e < m * m; e += 256)
-    Ws[e / m][e % m] = W[(((long long)c * 2 + f) * UPD_KMAX + e / m) * UPD_KMAX + e % m];
+    Ws[e / m][e % m] = A::mk(W[(((long long)c * 2 + f) * UPD_KMAX + e / m) * UPD_KMAX + e % m]);
   __syncthreads();
   const int col = blockIdx.x * 8 + ty;
   const zd* Gf = Gv + (long long)c * sG + (long long)f * N * N;
@@ -415,13 +418,13 @@ __global__ void k_flush_xy(const zd* Gv, long long sG, int N, int F, const int* 
   if (col < N && tx < m) {
     const int s = st[tx];
     X[xy + col + (long long)tx * N] = Gf[col + (long long)s * N];  // row `col` of X
-    gb[ty][tx] = zsub(zmk(s == col ? 1.0 : 0.0, 0.0), Gf[s + (long long)col * N]);
+    gb[ty][tx] = A::mk(zsub(zmk(s == col ? 1.0 : 0.0, 0.0), Gf[s + (long long)col * N]));
   }
   __syncthreads();
   if (col < N && tx < m) {
-    zd y = zmk(0.0, 0.0);
-    for (int l2 = 0; l2 < m; ++l2) y = zadd(y, zmul(Ws[tx][l2], gb[ty][l2]));
-    Y[xy + tx + (long long)col * UPD_KMAX] = y;
+    Z y = A::zero();
+    for (int l2 = 0; l2 < m; ++l2) y = A::mac(y, Ws[tx][l2], gb[ty][l2]);
+    Y[xy + tx + (long long)col * UPD_KMAX] = A::wide(y);
   }
 }
 
