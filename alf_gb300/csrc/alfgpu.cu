@@ -53,6 +53,7 @@ struct alfgpu_s {
   int oz = 0, eexp_complex = 0;
   int oz_narrow = 0;  // small grids: BN = 16 tiles; the flush keeps the double-float GEMM (measured faster there)
   int oz_stab = 0;    // the stabilisation's complex products on the tensor-core GEMM too
+  zd *ozGm = nullptr, *ozTm = nullptr, *ozWm = nullptr, *ozXm = nullptr;  // compact-WY explicit Q work
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
   unsigned short* ozE[4] = {nullptr, nullptr, nullptr, nullptr};  // expT, expTinv as A; expT, expTinv as B
@@ -556,9 +557,67 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
 }
 
 // Explicit Q (first N columns of H_1 ... H_N) of the factored matrix F into Q (Q != F).
+// Explicit Q (ZUNGQR) in compact-WY form on the tensor-core GEMM (mixed form): per panel of
+// w <= 32 reflectors at column j0, from the last panel to the first, the Gram matrix
+// V^H V and W = V^H Q[:, j0:] as digit-sliced products, T by ZLARFT's recursion, X = V T,
+// and Q[:, j0:] -= X W as a digit-sliced rank-w product.  Q starts as the identity; the
+// columns of a panel are still e_c when it is applied, as in ZUNGQR.
+static int orgqr_wy(alfgpu_s* h, const zd* F, zd* Q) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  prof_begin(h, ALFGPU_PROF_ORGQR);
+  k_bqr_eye<<<dim3((unsigned)((NN + 255) / 256), B), 256, 0, h->st>>>(Q, N, NN);
+  CKL();
+  const int S = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, Rp2 = h->oz_Rp2N, bn = h->oz_bn, nst = h->oz_nst;
+  for (int j0 = ((N - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
+    const int w = (N - j0 < 32) ? N - j0 : 32, nc = N - j0;
+    OzSliceParams a;
+    memset(&a, 0, sizeof(a));
+    a.src = F + (long long)j0 * N; a.mode = OZ_CROWS; a.sb = NN; a.srows = w; a.Kc = N;
+    a.sr = N; a.sk = 1; a.trans = 1; a.conj = 1; a.unitlow = 1; a.doff = j0;  // op C of V
+    a.S = S; a.bits = bits; a.Rpad = Rp2; a.Kpad = Kp; a.out = h->ozGA; a.expo = h->ozGAe; a.err = h->err;
+    OzSliceParams v = a;
+    v.conj = 0; v.out = h->ozGB; v.expo = h->ozGBe;  // V itself as the N-side operand
+    h->launches += 2;
+    CK(oz_launch_slice(a, B, h->st));
+    CK(oz_launch_slice(v, B, h->st));
+    RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * w, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
+                OZ_OUT_CPLX, 0, h->ozGm, 1, 32, 1024, B));
+    k_bqr_larft<<<B, 32, 0, h->st>>>(h->ozGm, h->tau, N, j0, w, h->ozTm);
+    CKL();
+    OzSliceParams qs = a;  // Q[:, j0:] as the N-side operand: row j = column j0 + j, K = rows
+    qs.src = Q + (long long)j0 * N; qs.srows = nc; qs.conj = 0; qs.unitlow = 0; qs.out = h->ozGB;
+    qs.expo = h->ozGBe;
+    h->launches++;
+    CK(oz_launch_slice(qs, B, h->st));
+    RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * nc, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
+                OZ_OUT_CPLX, 0, h->ozWm, 1, 32, 32ll * N, B));
+    k_bqr_vt<<<dim3((N + 7) / 8, B), dim3(32, 8), 0, h->st>>>(F, N, NN, h->ozTm, N, j0, w, h->ozXm, 32ll * N);
+    CKL();
+    // Q[:, j0:] -= X W: [Re X | Im X] times the K-doubled rows of W (the flush's product)
+    OzSliceParams xa;
+    memset(&xa, 0, sizeof(xa));
+    xa.src = h->ozXm; xa.mode = OZ_CKA; xa.sr = 1; xa.sk = N; xa.sb = 32ll * N; xa.srows = N; xa.Kc = 32;
+    xa.kvalid = w; xa.S = h->ozf_S; xa.bits = h->ozf_bits; xa.Rpad = h->oz_RpN; xa.Kpad = 64; xa.out = h->ozXA;
+    xa.expo = h->ozXAe; xa.err = h->err;
+    OzSliceParams yb = xa;
+    yb.src = h->ozWm; yb.mode = OZ_CKB; yb.sr = 32; yb.sk = 1; yb.srows = nc; yb.Rpad = Rp2; yb.out = h->ozYB;
+    yb.expo = h->ozYBe;
+    h->launches += 2;
+    CK(oz_launch_slice(xa, B, h->st));
+    CK(oz_launch_slice(yb, B, h->st));
+    RET(oz_gemm(h, h->tmXA, h->tmYB, N, 2 * nc, 64, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN, Rp2, 0,
+                0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, Q + (long long)j0 * N, 1, N, NN, B));
+  }
+  prof_end(h);
+  return 0;
+}
+
 static int orgqr_any(alfgpu_s* h, const zd* F, zd* Q) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
+  // compact WY pays on batched grids; one chain's grid is too small for its launch chain
+  if (h->oz_stab && !h->oz_narrow && !h->qr_df && N <= 32 * BQR_LROWS) return orgqr_wy(h, F, Q);
   if (N > 32 * BQR_LROWS) {  // beyond the rows a lane of k_bqr_apply holds
     RET(copy_mats(h, Q, F, (size_t)B * NN));
     return launch_orgqr(h, Q, B);
@@ -1208,6 +1267,8 @@ static int oz_setup(alfgpu_s* h) {
   r |= dalloc(h, &h->ozGB, B * S * Rp2 * Kp); r |= dalloc(h, &h->ozGBe, B * Rp2);
   r |= dalloc(h, &h->ozXA, B * Sf * RpN * Kf); r |= dalloc(h, &h->ozXAe, B * RpN);
   r |= dalloc(h, &h->ozYB, B * Sf * Rp2 * Kf); r |= dalloc(h, &h->ozYBe, B * Rp2);
+  r |= dalloc(h, &h->ozGm, B * 1024); r |= dalloc(h, &h->ozTm, B * 1024);
+  r |= dalloc(h, &h->ozWm, B * 32 * (size_t)N); r |= dalloc(h, &h->ozXm, B * 32 * (size_t)N);
   if (r) return ALFGPU_ERROR_CUDA;
   int t = 0;
   for (int a = 0; a < 4; ++a)

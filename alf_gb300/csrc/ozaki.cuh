@@ -60,6 +60,9 @@ struct OzSliceParams {
   int tri, trans;           // tri: zero the strictly lower triangle of the source in storage
                             // coordinates (row, col) = trans ? (k', i) : (i, k'), k' the remapped k
   const zd* rsc; long long srsc; int rinv;  // optional real per-row scale (real part), or its inverse
+  int kvalid;               // > 0: source k >= kvalid are zero (with kdyn: the smaller bound)
+  int unitlow, doff;        // OZ_CROWS: the source is a unit lower trapezoid (Householder vectors of a
+                            // QR panel): storage (r, c) is 0 for r < c + doff, 1 for r == c + doff
   int S, bits;
   int Rpad, Kpad;
   unsigned short* out;      // BF16 bits, [batch][S][Rpad][Kpad]
@@ -174,7 +177,8 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
   const double* srd = (const double*)p.src + (size_t)bs * p.sb;
   const zd* srz = (const zd*)p.src + (size_t)bs * p.sb;
   const zd* ks = p.ks ? p.ks + (size_t)b * p.sks : nullptr;
-  const int kd = p.kdyn ? min(p.kdyn[b], p.Kc) : p.Kc;
+  int kd = p.kdyn ? min(p.kdyn[b], p.Kc) : p.Kc;
+  if (p.kvalid > 0) kd = min(kd, p.kvalid);
   double x0[2] = {0.0, 0.0}, x1[2] = {0.0, 0.0}, sc[2] = {1.0, 1.0};
   const int k0 = 2 * tid;
   double rs_row = 1.0;  // per-row scale (an output row / column scale of the product)
@@ -195,6 +199,11 @@ __global__ void __launch_bounds__(256) k_oz_slice(OzSliceParams p) {
         if (k < kd) {
           const int kq = p.perm ? p.perm[(size_t)b * p.sperm + k] : k;
           if (p.tri && (p.trans ? kq > i : i > kq)) break;  // below the diagonal of an upper triangle
+          if (p.unitlow) {
+            const int r = p.trans ? kq : i, cc = (p.trans ? i : kq) + p.doff;
+            if (r < cc) break;
+            if (r == cc) { x0[u] = 1.0; break; }
+          }
           const zd z = srz[i * p.sr + kq * p.sk];
           x0[u] = z.x; x1[u] = p.conj ? -z.y : z.y;
         }

@@ -779,3 +779,65 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
   }
   cluster_sync();  // no CTA leaves while its shared memory may still be read
 }
+
+
+// ---------------------------------------------------------------------------------------
+// Explicit Q in compact-WY form (the mixed form's ZUNGQR on the tensor-core GEMM).  Panel
+// of w <= 32 reflectors starting at column j0: H_j0 ... H_{j0+w-1} = I - V T V^H
+// (ZLARFT forward / columnwise), Q[:, j0:] <- Q[:, j0:] - (V T) (V^H Q[:, j0:]).
+// ---------------------------------------------------------------------------------------
+
+// Q = I for every matrix.  grid (ceil(NN/256), B)
+__global__ void k_bqr_eye(zd* Q, int N, long long sQ) {
+  const long long NN = (long long)N * N, e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= NN) return;
+  Q[blockIdx.y * sQ + e] = zmk((e % N) == (e / N) ? 1.0 : 0.0, 0.0);
+}
+
+// T (w x w, upper triangular, ld 32) of one panel from its Gram matrix Gm = V^H V (ld 32) and
+// tau: T(i,i) = tau_i; T(0:i, i) = T(0:i, 0:i) (-tau_i Gm(0:i, i)).  One warp per matrix.
+__global__ void k_bqr_larft(const zd* Gm, const zd* tau, long long sT, int j0, int w, zd* T) {
+  const int b = blockIdx.x, lane = threadIdx.x;
+  const zd* g = Gm + (long long)b * 32 * 32;
+  zd* t = T + (long long)b * 32 * 32;
+  const zd* tb = tau + b * sT + j0;
+  for (int i = 0; i < w; ++i) {
+    const zd ti = tb[i];
+    // z(l) = -tau_i Gm(l, i) for l < i (lane l)
+    const zd z = lane < i ? zneg(zmul(ti, g[lane + i * 32])) : zmk(0.0, 0.0);
+    // T(l, i) = sum_{l' >= l, l' < i} T(l, l') z(l')
+    zd acc = zmk(0.0, 0.0);
+    for (int l2 = 0; l2 < i; ++l2) {
+      const zd zl = zmk(__shfl_sync(0xffffffffu, z.x, l2), __shfl_sync(0xffffffffu, z.y, l2));
+      if (lane <= l2) acc = zadd(acc, zmul(t[lane + l2 * 32], zl));
+    }
+    __syncwarp();
+    if (lane < i) t[lane + i * 32] = acc;
+    if (lane == i) t[i + i * 32] = ti;
+    if (lane > i && lane < 32) t[lane + i * 32] = zmk(0.0, 0.0);
+    __syncwarp();
+  }
+}
+
+// X = V T (N x w, stored column-major with ld N in the flush layout [matrix][N][32]), V the
+// unit lower trapezoid of the panel (column i: 1 at row j0 + i, F(r, j0 + i) below).
+// grid (ceil(N / 8), B), block (32, 8): lane = column i, ty = row.
+__global__ void k_bqr_vt(const zd* F, long long ldf, long long sF, const zd* T, int N, int j0, int w, zd* X,
+                         long long sX) {
+  __shared__ zd ts[32][33];
+  const int b = blockIdx.y, i = threadIdx.x, ty = threadIdx.y;
+  for (int e = ty * 32 + i; e < 32 * 32; e += 256) ts[e % 32][e / 32] = T[(long long)b * 1024 + e];
+  __syncthreads();
+  const int r = blockIdx.x * 8 + ty;
+  if (r >= N || i >= w) return;
+  const zd* f = F + b * sF;
+  zd acc = zmk(0.0, 0.0);
+  for (int l = 0; l <= i; ++l) {  // T upper triangular: l <= i
+    const int c = j0 + l;
+    zd v;
+    if (r < c) continue;
+    v = (r == c) ? zmk(1.0, 0.0) : f[r + c * ldf];
+    acc = zadd(acc, zmul(v, ts[l][i]));
+  }
+  X[b * sX + r + (long long)i * N] = acc;
+}
