@@ -483,6 +483,8 @@ static int slice_scale(alfgpu_s* h, int nt1) {
 // decompose_UDV_state (udv_state_mod.F90:466-578) on all B pairs; s.U holds the propagated A.
 // QR of Ain * diag(colscale) into Aout (Aout != Ain): R above the diagonal (rows
 // normalised by D = DUP), reflectors below, tau, jpvt, info.
+static int wy_apply(alfgpu_s* h, const zd* F, int j0, int w, zd* C, int ncol, int adj);
+
 static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, int exact, int df = 0) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
@@ -557,57 +559,67 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
 }
 
 // Explicit Q (first N columns of H_1 ... H_N) of the factored matrix F into Q (Q != F).
-// Explicit Q (ZUNGQR) in compact-WY form on the tensor-core GEMM (mixed form): per panel of
-// w <= 32 reflectors at column j0, from the last panel to the first, the Gram matrix
-// V^H V and W = V^H Q[:, j0:] as digit-sliced products, T by ZLARFT's recursion, X = V T,
-// and Q[:, j0:] -= X W as a digit-sliced rank-w product.  Q starts as the identity; the
-// columns of a panel are still e_c when it is applied, as in ZUNGQR.
+// One panel of w <= 32 Householder reflectors (columns j0 .. j0+w-1 of F: unit lower
+// trapezoid V, tau) applied in compact-WY form to the ncol columns starting at C (ld N):
+// C <- (I - V T V^H) C (adj = 0, ZUNGQR's H_j0 ... H_{j0+w-1}) or (I - V T^H V^H) C
+// (adj = 1, the QR trailing update with H^H).  The Gram matrix V^H V and W = V^H C are
+// digit-sliced tensor-core products, T follows ZLARFT's forward columnwise recursion,
+// X = V T (or V T^H) is formed directly, and C -= X W is the flush's digit-sliced rank-w
+// product.
+static int wy_apply(alfgpu_s* h, const zd* F, int j0, int w, zd* C, int ncol, int adj) {
+  const int N = h->N, B = h->B;
+  const long long NN = (long long)N * N;
+  const int S = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, Rp2 = h->oz_Rp2N, bn = h->oz_bn, nst = h->oz_nst;
+  OzSliceParams a;
+  memset(&a, 0, sizeof(a));
+  a.src = F + (long long)j0 * N; a.mode = OZ_CROWS; a.sb = NN; a.srows = w; a.Kc = N;
+  a.sr = N; a.sk = 1; a.trans = 1; a.conj = 1; a.unitlow = 1; a.doff = j0;  // op C of V
+  a.S = S; a.bits = bits; a.Rpad = Rp2; a.Kpad = Kp; a.out = h->ozGA; a.expo = h->ozGAe; a.err = h->err;
+  OzSliceParams v = a;
+  v.conj = 0; v.out = h->ozGB; v.expo = h->ozGBe;  // V itself as the N-side operand
+  h->launches += 2;
+  CK(oz_launch_slice(a, B, h->st));
+  CK(oz_launch_slice(v, B, h->st));
+  RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * w, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
+              OZ_OUT_CPLX, 0, h->ozGm, 1, 32, 1024, B));
+  k_bqr_larft<<<B, 32, 0, h->st>>>(h->ozGm, h->tau, N, j0, w, h->ozTm);
+  CKL();
+  OzSliceParams cs = a;  // C as the N-side operand: row j = column j of C, K = rows
+  cs.src = C; cs.srows = ncol; cs.conj = 0; cs.unitlow = 0; cs.out = h->ozGB; cs.expo = h->ozGBe;
+  h->launches++;
+  CK(oz_launch_slice(cs, B, h->st));
+  RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * ncol, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
+              OZ_OUT_CPLX, 0, h->ozWm, 1, 32, 32ll * N, B));
+  k_bqr_vt<<<dim3((N + 7) / 8, B), dim3(32, 8), 0, h->st>>>(F, N, NN, h->ozTm, N, j0, w, h->ozXm, 32ll * N, adj);
+  CKL();
+  // C -= X W: [Re X | Im X] times the K-doubled rows of W (the flush's product)
+  OzSliceParams xa;
+  memset(&xa, 0, sizeof(xa));
+  xa.src = h->ozXm; xa.mode = OZ_CKA; xa.sr = 1; xa.sk = N; xa.sb = 32ll * N; xa.srows = N; xa.Kc = 32;
+  xa.kvalid = w; xa.S = h->ozf_S; xa.bits = h->ozf_bits; xa.Rpad = h->oz_RpN; xa.Kpad = 64; xa.out = h->ozXA;
+  xa.expo = h->ozXAe; xa.err = h->err;
+  OzSliceParams yb = xa;
+  yb.src = h->ozWm; yb.mode = OZ_CKB; yb.sr = 32; yb.sk = 1; yb.srows = ncol; yb.Rpad = Rp2; yb.out = h->ozYB;
+  yb.expo = h->ozYBe;
+  h->launches += 2;
+  CK(oz_launch_slice(xa, B, h->st));
+  CK(oz_launch_slice(yb, B, h->st));
+  return oz_gemm(h, h->tmXA, h->tmYB, N, 2 * ncol, 64, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN, Rp2,
+                 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, C, 1, N, NN, B);
+}
+
+// Explicit Q (ZUNGQR) in compact-WY form on the tensor-core GEMM (mixed form, batched
+// grids): Q starts as the identity and the panels are applied from the last to the first
+// to the columns from their first one on (the columns of a panel are still e_c then).
 static int orgqr_wy(alfgpu_s* h, const zd* F, zd* Q) {
   const int N = h->N, B = h->B;
   const long long NN = (long long)N * N;
   prof_begin(h, ALFGPU_PROF_ORGQR);
   k_bqr_eye<<<dim3((unsigned)((NN + 255) / 256), B), 256, 0, h->st>>>(Q, N, NN);
   CKL();
-  const int S = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, Rp2 = h->oz_Rp2N, bn = h->oz_bn, nst = h->oz_nst;
   for (int j0 = ((N - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
-    const int w = (N - j0 < 32) ? N - j0 : 32, nc = N - j0;
-    OzSliceParams a;
-    memset(&a, 0, sizeof(a));
-    a.src = F + (long long)j0 * N; a.mode = OZ_CROWS; a.sb = NN; a.srows = w; a.Kc = N;
-    a.sr = N; a.sk = 1; a.trans = 1; a.conj = 1; a.unitlow = 1; a.doff = j0;  // op C of V
-    a.S = S; a.bits = bits; a.Rpad = Rp2; a.Kpad = Kp; a.out = h->ozGA; a.expo = h->ozGAe; a.err = h->err;
-    OzSliceParams v = a;
-    v.conj = 0; v.out = h->ozGB; v.expo = h->ozGBe;  // V itself as the N-side operand
-    h->launches += 2;
-    CK(oz_launch_slice(a, B, h->st));
-    CK(oz_launch_slice(v, B, h->st));
-    RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * w, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
-                OZ_OUT_CPLX, 0, h->ozGm, 1, 32, 1024, B));
-    k_bqr_larft<<<B, 32, 0, h->st>>>(h->ozGm, h->tau, N, j0, w, h->ozTm);
-    CKL();
-    OzSliceParams qs = a;  // Q[:, j0:] as the N-side operand: row j = column j0 + j, K = rows
-    qs.src = Q + (long long)j0 * N; qs.srows = nc; qs.conj = 0; qs.unitlow = 0; qs.out = h->ozGB;
-    qs.expo = h->ozGBe;
-    h->launches++;
-    CK(oz_launch_slice(qs, B, h->st));
-    RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * nc, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
-                OZ_OUT_CPLX, 0, h->ozWm, 1, 32, 32ll * N, B));
-    k_bqr_vt<<<dim3((N + 7) / 8, B), dim3(32, 8), 0, h->st>>>(F, N, NN, h->ozTm, N, j0, w, h->ozXm, 32ll * N);
-    CKL();
-    // Q[:, j0:] -= X W: [Re X | Im X] times the K-doubled rows of W (the flush's product)
-    OzSliceParams xa;
-    memset(&xa, 0, sizeof(xa));
-    xa.src = h->ozXm; xa.mode = OZ_CKA; xa.sr = 1; xa.sk = N; xa.sb = 32ll * N; xa.srows = N; xa.Kc = 32;
-    xa.kvalid = w; xa.S = h->ozf_S; xa.bits = h->ozf_bits; xa.Rpad = h->oz_RpN; xa.Kpad = 64; xa.out = h->ozXA;
-    xa.expo = h->ozXAe; xa.err = h->err;
-    OzSliceParams yb = xa;
-    yb.src = h->ozWm; yb.mode = OZ_CKB; yb.sr = 32; yb.sk = 1; yb.srows = nc; yb.Rpad = Rp2; yb.out = h->ozYB;
-    yb.expo = h->ozYBe;
-    h->launches += 2;
-    CK(oz_launch_slice(xa, B, h->st));
-    CK(oz_launch_slice(yb, B, h->st));
-    RET(oz_gemm(h, h->tmXA, h->tmYB, N, 2 * nc, 64, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN, Rp2, 0,
-                0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, Q + (long long)j0 * N, 1, N, NN, B));
+    const int w = (N - j0 < 32) ? N - j0 : 32;
+    RET(wy_apply(h, F, j0, w, Q + (long long)j0 * N, N - j0, 0));
   }
   prof_end(h);
   return 0;
@@ -1254,7 +1266,7 @@ static int oz_setup(alfgpu_s* h) {
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);
   const long long tiles = (long long)((N + OZ_BM - 1) / OZ_BM) * ((2 * N + 31) / 32) * (long long)B;
-  const int narrow = tiles < 2ll * nsm;
+  const int narrow = tiles < 2ll * nsm && !(h->d.reserved[0] & ALFGPU_FLAG_TENSOR_WIDE);
   h->oz_narrow = narrow;
   if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))

@@ -819,11 +819,11 @@ __global__ void k_bqr_larft(const zd* Gm, const zd* tau, long long sT, int j0, i
   }
 }
 
-// X = V T (N x w, stored column-major with ld N in the flush layout [matrix][N][32]), V the
-// unit lower trapezoid of the panel (column i: 1 at row j0 + i, F(r, j0 + i) below).
+// X = V T or V T^H (N x w, stored column-major with ld N in the flush layout [matrix][N][32]),
+// V the unit lower trapezoid of the panel (column i: 1 at row j0 + i, F(r, j0 + i) below).
 // grid (ceil(N / 8), B), block (32, 8): lane = column i, ty = row.
 __global__ void k_bqr_vt(const zd* F, long long ldf, long long sF, const zd* T, int N, int j0, int w, zd* X,
-                         long long sX) {
+                         long long sX, int adj) {
   __shared__ zd ts[32][33];
   const int b = blockIdx.y, i = threadIdx.x, ty = threadIdx.y;
   for (int e = ty * 32 + i; e < 32 * 32; e += 256) ts[e % 32][e / 32] = T[(long long)b * 1024 + e];
@@ -832,12 +832,13 @@ __global__ void k_bqr_vt(const zd* F, long long ldf, long long sF, const zd* T, 
   if (r >= N || i >= w) return;
   const zd* f = F + b * sF;
   zd acc = zmk(0.0, 0.0);
-  for (int l = 0; l <= i; ++l) {  // T upper triangular: l <= i
+  // adj = 0: X = V T (T upper: l <= i); adj = 1: X = V T^H (T^H lower: l >= i, conj(T(i, l)))
+  const int l0 = adj ? i : 0, l1 = adj ? w - 1 : i;
+  for (int l = l0; l <= l1; ++l) {
     const int c = j0 + l;
-    zd v;
     if (r < c) continue;
-    v = (r == c) ? zmk(1.0, 0.0) : f[r + c * ldf];
-    acc = zadd(acc, zmul(v, ts[l][i]));
+    const zd v = (r == c) ? zmk(1.0, 0.0) : f[r + c * ldf];
+    acc = zadd(acc, zmul(v, adj ? zconj(ts[i][l]) : ts[l][i]));
   }
   X[b * sX + r + (long long)i * N] = acc;
 }

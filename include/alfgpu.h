@@ -96,6 +96,11 @@ enum { ALFGPU_FLAG_NO_TENSOR_GEMM = 128 };
  * the same FP64-accurate tensor-core GEMM by default; this flag keeps them on the FP64 GEMM
  * (the pivoted QR, triangular solves and phases are FP64 arithmetic either way). */
 enum { ALFGPU_FLAG_FP64_STAB_GEMM = 256 };
+/* Mixed form: the tensor-core choices made for batched grids (32-wide tiles, the flush and
+ * the explicit Q on the tensor cores) also for a grid that does not fill the GPU (by
+ * default one chain keeps 16-wide tiles and the double-float flush / FP64 explicit Q,
+ * measured faster there). */
+enum { ALFGPU_FLAG_TENSOR_WIDE = 512 };
 
 typedef struct alfgpu_s alfgpu_t;
 

@@ -144,3 +144,14 @@ def test_mixed_batched_chains_with_own_couplings_vs_oracle():
         o.sweep(us[c])
         if np.array_equal(g.fields(c), o.fields()):
             assert np.max(np.abs(g.green(c) - o.green())) < BOUND, c
+
+
+def test_mixed_wide_grid_paths_vs_fp64_oracle():
+    # the batched-grid choices on one chain: 32-wide tiles, the flush on the tensor cores and
+    # the explicit Q in compact-WY form (Gram matrix, ZLARFT, rank-32 digit-sliced updates)
+    from alf_gb300.sweep import FLAG_TENSOR_WIDE
+    w = _compare(mdl.hubbard("square", 8, 8, U=4.0, beta=4.0, dtau=0.1, nwrap=10), seed=2, sweeps=2,
+                 flags=FLAG_TENSOR_WIDE)
+    assert w < BOUND
+    w = _compare(mdl.config("hubbard16x16"), seed=1, sweeps=1, flags=FLAG_TENSOR_WIDE)
+    assert w < BOUND
