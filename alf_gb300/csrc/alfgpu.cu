@@ -582,7 +582,7 @@ static int wy_apply(alfgpu_s* h, const zd* F, int j0, int w, zd* C, int ncol, in
   CK(oz_launch_slice(v, B, h->st));
   RET(oz_gemm(h, h->tmGA, h->tmGB, 2 * w, 2 * w, Kp, S, bits, bn, nst, Rp2, Rp2, 0, 0, h->ozGAe, h->ozGBe,
               OZ_OUT_CPLX, 0, h->ozGm, 1, 32, 1024, B));
-  k_bqr_larft<<<B, 32, 0, h->st>>>(h->ozGm, h->tau, N, j0, w, h->ozTm);
+  k_bqr_larft<<<B, 256, 0, h->st>>>(h->ozGm, h->tau, N, j0, w, h->ozTm);
   CKL();
   OzSliceParams cs = a;  // C as the N-side operand: row j = column j of C, K = rows
   cs.src = C; cs.srows = ncol; cs.conj = 0; cs.unitlow = 0; cs.out = h->ozGB; cs.expo = h->ozGBe;

@@ -795,28 +795,39 @@ __global__ void k_bqr_eye(zd* Q, int N, long long sQ) {
 }
 
 // T (w x w, upper triangular, ld 32) of one panel from its Gram matrix Gm = V^H V (ld 32) and
-// tau: T(i,i) = tau_i; T(0:i, i) = T(0:i, 0:i) (-tau_i Gm(0:i, i)).  One warp per matrix.
-__global__ void k_bqr_larft(const zd* Gm, const zd* tau, long long sT, int j0, int w, zd* T) {
-  const int b = blockIdx.x, lane = threadIdx.x;
+// tau: T(i,i) = tau_i; T(0:i, i) = T(0:i, 0:i) (-tau_i Gm(0:i, i)).  One CTA of 256 threads
+// per matrix, T in shared memory: warps 1..7 split the triangular mat-vec of each step by
+// columns, warp 0 forms z and sums the partials (an FP64 instruction occupies a warp ~64
+// cycles, so the serial chain is kept short).
+__global__ void __launch_bounds__(256) k_bqr_larft(const zd* Gm, const zd* tau, long long sT, int j0, int w, zd* T) {
+  __shared__ zd ts[32][33];  // ts[l][i] = T(l, i)
+  __shared__ zd zs[32];
+  __shared__ zd part[8][32];
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const zd* g = Gm + (long long)b * 32 * 32;
-  zd* t = T + (long long)b * 32 * 32;
   const zd* tb = tau + b * sT + j0;
+  for (int e = tid; e < 32 * 32; e += 256) ts[e % 32][e / 32] = zmk(0.0, 0.0);
+  __syncthreads();
   for (int i = 0; i < w; ++i) {
     const zd ti = tb[i];
-    // z(l) = -tau_i Gm(l, i) for l < i (lane l)
-    const zd z = lane < i ? zneg(zmul(ti, g[lane + i * 32])) : zmk(0.0, 0.0);
-    // T(l, i) = sum_{l' >= l, l' < i} T(l, l') z(l')
-    zd acc = zmk(0.0, 0.0);
-    for (int l2 = 0; l2 < i; ++l2) {
-      const zd zl = zmk(__shfl_sync(0xffffffffu, z.x, l2), __shfl_sync(0xffffffffu, z.y, l2));
-      if (lane <= l2) acc = zadd(acc, zmul(t[lane + l2 * 32], zl));
+    if (warp == 0 && lane < i) zs[lane] = zneg(zmul(ti, g[lane + i * 32]));
+    __syncthreads();
+    if (warp > 0) {
+      zd acc = zmk(0.0, 0.0);
+      for (int l2 = warp - 1; l2 < i; l2 += 7)
+        if (lane <= l2) acc = zadd(acc, zmul(ts[lane][l2], zs[l2]));
+      part[warp][lane] = acc;
     }
-    __syncwarp();
-    if (lane < i) t[lane + i * 32] = acc;
-    if (lane == i) t[i + i * 32] = ti;
-    if (lane > i && lane < 32) t[lane + i * 32] = zmk(0.0, 0.0);
-    __syncwarp();
+    __syncthreads();
+    if (warp == 0) {
+      zd s = zmk(0.0, 0.0);
+#pragma unroll
+      for (int q = 1; q < 8; ++q) s = zadd(s, part[q][lane]);
+      ts[lane][i] = lane < i ? s : (lane == i ? ti : zmk(0.0, 0.0));
+    }
+    __syncthreads();
   }
+  for (int e = tid; e < 32 * 32; e += 256) T[(long long)b * 1024 + e] = ts[e % 32][e / 32];
 }
 
 // X = V T or V T^H (N x w, stored column-major with ld N in the flush layout [matrix][N][32]),
