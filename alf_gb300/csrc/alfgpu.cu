@@ -64,6 +64,7 @@ struct alfgpu_s {
   int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
   int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
   int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
+  int CLr = 1;                       // k_qrp_rows cluster size (CL, or CL / 2 on batched grids)
   // time-displaced Green functions (ltau = 1)
   int ltau = 0;
   // CUDA graphs of the sweep: [0] device draws, [1] host draws (copied before the launch)
@@ -250,6 +251,39 @@ static int cluster_size(int N) {
   if (N >= 64) return 4;
   if (N >= 32) return 2;
   return 1;
+}
+
+// Factorisation time of one matrix on a cluster of CL / 2 CTAs relative to CL CTAs, times 4
+// (measured 1.85 at N_dim = 256: 16 chains of the 16x16 Hubbard model, 4 waves -> 2).
+#define QRR_HALF_RATIO_X4 7
+
+// Resident clusters of CL CTAs for k_qrp_rows on an N x N matrix (0: it does not fit).  The
+// shared-memory limits it raises are process-global and only ever raised.
+static int qrr_clusters(int N, int CL) {
+  const size_t sm = qrr_smem_bytes(N, CL);
+  if (sm > 227 * 1024) return 0;
+  if (raise_smem_limit(k_qrp_rows<ArD>, sm) != cudaSuccess || raise_smem_limit(k_qrp_rows<ArF>, sm) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (CL > 8 && (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+                 cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(CL, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = sm;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_qrp_rows<ArD>, &cfg) != cudaSuccess) n = 0;
+  cudaGetLastError();
+  return n;
 }
 
 // ---------------------------------------------------------------------------
@@ -504,13 +538,13 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
     q.tau = h->tau; q.sT = N; q.jpvt = h->jpvt; q.sP = N; q.D = h->DUP; q.sD = N; q.info = h->info;
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3(h->CL, B, 1);
+    cfg.gridDim = dim3(h->CLr, B, 1);
     cfg.blockDim = dim3(256, 1, 1);
-    cfg.dynamicSmemBytes = qrr_smem_bytes(N, h->CL);
+    cfg.dynamicSmemBytes = qrr_smem_bytes(N, h->CLr);
     cfg.stream = h->st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    at[0].val.clusterDim.x = h->CLr; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
     cfg.attrs = at; cfg.numAttrs = 1;
     h->launches++;
     if (df) CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArF>, q));
@@ -1370,27 +1404,20 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     cudaGetLastError();
     h->CL /= 2;
   }
-  // exact pivoting on the row-distributed cluster kernel when its row block fits in shared memory
+  // exact pivoting on the row-distributed cluster kernel when its row block fits in shared memory.
+  // A launch over B matrices runs in ceil(B / resident clusters) waves: a batched grid may take
+  // clusters of CL / 2 CTAs (twice the rows per CTA, twice the clusters resident) when that
+  // saves enough waves to pay for the longer factorisation of each matrix.
   {
-    const size_t sm = qrr_smem_bytes(h->N, h->CL);
-    if (sm <= 227 * 1024 &&
-        raise_smem_limit(k_qrp_rows<ArD>, sm) == cudaSuccess && raise_smem_limit(k_qrp_rows<ArF>, sm) == cudaSuccess &&
-        (h->CL <= 8 ||
-         (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-          cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess))) {
-      cudaLaunchConfig_t cfg;
-      memset(&cfg, 0, sizeof(cfg));
-      cfg.gridDim = dim3(h->CL, 1, 1);
-      cfg.blockDim = dim3(256, 1, 1);
-      cfg.dynamicSmemBytes = sm;
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = h->CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-      cfg.attrs = at; cfg.numAttrs = 1;
-      int n = 0;
-      h->qrr_ok = cudaOccupancyMaxActiveClusters(&n, k_qrp_rows<ArD>, &cfg) == cudaSuccess && n > 0;
+    const int n1 = qrr_clusters(h->N, h->CL);
+    h->qrr_ok = n1 > 0;
+    h->CLr = h->CL;
+    if (h->qrr_ok && h->CL >= 4) {
+      const int fl = d.reserved[0];
+      const int n2 = (fl & ALFGPU_FLAG_QR_FULL_CLUSTER) ? 0 : qrr_clusters(h->N, h->CL / 2);
+      const long long w1 = (h->B + n1 - 1) / n1, w2 = n2 > 0 ? (h->B + n2 - 1) / n2 : 0;
+      if (n2 > 0 && ((fl & ALFGPU_FLAG_QR_HALF_CLUSTER) || QRR_HALF_RATIO_X4 * w2 < 4 * w1)) h->CLr = h->CL / 2;
     }
-    cudaGetLastError();
   }
   // the blocked QR keeps at most BQR_ROWS panel rows per CTA and BQR_LROWS rows per lane
   if (h->N > 32 * BQR_LROWS || (h->N + h->CL - 1) / h->CL > BQR_ROWS) h->exact_dec = h->exact_cgr = 1;

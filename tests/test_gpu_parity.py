@@ -20,7 +20,7 @@ import pytest
 
 import oracle
 from alf_gb300 import model as mdl, rng
-from alf_gb300.sweep import Chains, cgr as gpu_cgr, decompose as gpu_decompose
+from alf_gb300.sweep import FLAG_QR_HALF_CLUSTER, Chains, cgr as gpu_cgr, decompose as gpu_decompose
 
 pytestmark = pytest.mark.gpu
 
@@ -98,13 +98,13 @@ def _variant_ratios(m, f0, seed, sweeps, chain):
         oracle.set_variant(0)
 
 
-def _run_pair(m, seed=5, sweeps=1, chain=0, pivoting="default"):
+def _run_pair(m, seed=5, sweeps=1, chain=0, pivoting="default", flags=0):
     f0 = rng.initial_fields(seed, chain, m.n_op, m.ltrot)
     var = _variant_ratios(m, f0, seed, sweeps, chain)
     o = oracle.Oracle(m)
     o.set_fields(f0)
     ph_o = o.init_state()
-    g = Chains(m, n_chains=1, pivoting=pivoting)
+    g = Chains(m, n_chains=1, pivoting=pivoting, flags=flags)
     g.set_fields(0, f0)
     ph_g = g.init_state()[0]
     assert abs(ph_g - ph_o) < 1e-10
@@ -152,6 +152,13 @@ def test_sweep_hubbard_8x8_parity(pivoting):
     # blocked QR (two panels)
     m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
     _run_pair(m, seed=4, sweeps=1, pivoting=pivoting)
+
+
+def test_sweep_hubbard_8x8_half_cluster_qr_parity():
+    # the exact pivoted QR on clusters of half the default size (2 CTAs of 32 rows each at
+    # N_dim = 64), the shape batched grids take when it saves waves
+    m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    _run_pair(m, seed=4, sweeps=1, flags=FLAG_QR_HALF_CLUSTER)
 
 
 def test_sweep_hubbard_odd_sizes_parity():
