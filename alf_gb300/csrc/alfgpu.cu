@@ -253,10 +253,6 @@ static int cluster_size(int N) {
   return 1;
 }
 
-// Factorisation time of one matrix on a cluster of CL / 2 CTAs relative to CL CTAs, times 4
-// (measured 1.85 at N_dim = 256: 16 chains of the 16x16 Hubbard model, 4 waves -> 2).
-#define QRR_HALF_RATIO_X4 7
-
 // Resident clusters of CL CTAs for k_qrp_rows on an N x N matrix (0: it does not fit).  The
 // shared-memory limits it raises are process-global and only ever raised.
 static int qrr_clusters(int N, int CL) {
@@ -1405,18 +1401,21 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     h->CL /= 2;
   }
   // exact pivoting on the row-distributed cluster kernel when its row block fits in shared memory.
-  // A launch over B matrices runs in ceil(B / resident clusters) waves: a batched grid may take
-  // clusters of CL / 2 CTAs (twice the rows per CTA, twice the clusters resident) when that
-  // saves enough waves to pay for the longer factorisation of each matrix.
+  // A launch over B matrices whose full-size clusters would put more than two CTAs on every SM
+  // takes clusters of CL / 2 CTAs: the same FP64 work in half as many CTAs, each pivot step's
+  // cluster exchange and barriers shared by half as many (16 chains of the 16x16 Hubbard model:
+  // 512 -> 256 CTAs on 152 SMs, QR time per sweep 501 -> 478 ms).  A grid that fits keeps CL.
   {
-    const int n1 = qrr_clusters(h->N, h->CL);
-    h->qrr_ok = n1 > 0;
+    h->qrr_ok = qrr_clusters(h->N, h->CL) > 0;
     h->CLr = h->CL;
     if (h->qrr_ok && h->CL >= 4) {
       const int fl = d.reserved[0];
-      const int n2 = (fl & ALFGPU_FLAG_QR_FULL_CLUSTER) ? 0 : qrr_clusters(h->N, h->CL / 2);
-      const long long w1 = (h->B + n1 - 1) / n1, w2 = n2 > 0 ? (h->B + n2 - 1) / n2 : 0;
-      if (n2 > 0 && ((fl & ALFGPU_FLAG_QR_HALF_CLUSTER) || QRR_HALF_RATIO_X4 * w2 < 4 * w1)) h->CLr = h->CL / 2;
+      int nsm = 152;
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);
+      cudaGetLastError();
+      const bool want = (fl & ALFGPU_FLAG_QR_HALF_CLUSTER) ||
+                        (!(fl & ALFGPU_FLAG_QR_FULL_CLUSTER) && (long long)h->B * h->CL > 2ll * nsm);
+      if (want && qrr_clusters(h->N, h->CL / 2) > 0) h->CLr = h->CL / 2;
     }
   }
   // the blocked QR keeps at most BQR_ROWS panel rows per CTA and BQR_LROWS rows per lane

@@ -102,9 +102,8 @@ enum { ALFGPU_FLAG_FP64_STAB_GEMM = 256 };
  * measured faster there). */
 enum { ALFGPU_FLAG_TENSOR_WIDE = 512 };
 /* The exact pivoted QR (ZGEQP3 on one thread-block cluster per matrix) takes clusters of half
- * the default size when a batched launch then needs enough fewer waves to make up for the
- * longer factorisation of each matrix; these flags force the half-size or the full-size
- * cluster. */
+ * the default size when the full-size clusters of a batched launch would put more than two
+ * CTAs on every SM; these flags force the half-size or the full-size cluster. */
 enum { ALFGPU_FLAG_QR_HALF_CLUSTER = 1024, ALFGPU_FLAG_QR_FULL_CLUSTER = 2048 };
 
 typedef struct alfgpu_s alfgpu_t;
