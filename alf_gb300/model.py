@@ -166,6 +166,15 @@ def hopping_matrix(lattice: str, L1: int, L2: int, t: float = 1.0, chem: float =
         bonds = [(0, 0, 1, 0, -t), (0, 0, 0, 1, -t), (1, 1, 1, 0, -t2), (1, 1, 0, 1, -t2),
                  (0, 1, 0, 0, -tperp)]
         tloc = [-chem, -chem]
+    elif lat == "N_LEG_LADDER":
+        # Predefined_Latt_mod.F90:133-146 and Predefined_Hop_mod.F90:631-812: L1 cells along
+        # the legs (periodic), the L2 legs are the orbitals of one cell (open across legs)
+        if L1 != 1 and L1 % 2 != 0:
+            raise ValueError("the N_leg_ladder hopping needs L1 = 1 or L1 even")
+        norb = L2
+        bonds = [(n, n, 1, 0, -t) for n in range(L2)] + [(n, n + 1, 0, 0, -tperp) for n in range(L2 - 1)]
+        tloc = [-chem] * L2
+        L2 = 1
     else:
         raise ValueError(f"lattice {lattice!r} not supported")
     ncell = L1 * L2
@@ -289,7 +298,7 @@ def _mz_pair(site: int, dtau: float, U: float):
 
 def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U: float = 4.0,
             chem: float = 0.0, beta: float = 4.0, dtau: float = 0.1, nwrap: int = 10,
-            n_sun_input: int = 2) -> Model:
+            n_sun_input: int = 2, tperp: float = 0.0) -> Model:
     """Mz Hubbard model with dense hopping, as ``Ham_Set`` builds it.
 
     ``N_FL = 2`` and ``N_SUN`` is halved (Hamiltonian_Hubbard_smod.F90:264-266);
@@ -298,7 +307,7 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
     """
     ltrot = int(round(beta / dtau))
     n_sun = n_sun_input // 2
-    O = hopping_matrix(lattice, L1, L2, t=t, chem=chem)
+    O = hopping_matrix(lattice, L1, L2, t=t, chem=chem, tperp=tperp)
     N = O.shape[0]
     mat, inv = exp_hopping(O, dtau)
     up, do = [], []
@@ -310,7 +319,7 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
     return Model(name=f"hubbard_{lattice.lower()}_{L1}x{L2}", ndim=N, n_fl=2, n_sun=n_sun,
                  ltrot=ltrot, nwrap=nwrap, dtau=dtau, beta=beta, expT=[mat, mat.copy()],
                  expTinv=[inv, inv.copy()], vertices=[up, do],
-                 params=dict(lattice=lattice, L1=L1, L2=L2, t=t, U=U, chem=chem))
+                 params=dict(lattice=lattice, L1=L1, L2=L2, t=t, U=U, chem=chem, tperp=tperp))
 
 
 def kondo(L1: int = 12, L2: int = 12, t: float = 1.0, JK: float = 1.5, Uf: float = 2.0,

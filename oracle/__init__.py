@@ -72,6 +72,8 @@ def lib():
     L.oracle_set_variant.argtypes = [_c.c_int]
     L.oracle_set_eq_callback.argtypes = [_p, EQ_CB, _p]
     L.oracle_set_tau_callback.argtypes = [_p, TAU_CB, _p]
+    L.oracle_set_scalar_obs.argtypes = [_p, _p, _p]
+    L.oracle_get_scalar_obs.argtypes = [_p, _p, _c.c_int]
     _lib = L
     return L
 
@@ -204,6 +206,25 @@ class Oracle:
         lib().oracle_set_eq_callback(self.h, self._cbs[0], None)
         lib().oracle_set_tau_callback(self.h, self._cbs[1], None)
         return eq, tau
+
+    def set_scalar_obs(self, H=None, U=None):
+        """Accumulate ZP ZS {Kin, Pot, Part, Ener}, ZS and the count at every ham%Obser point
+        (the Hubbard Obs_scal, the same sums alfgpu_set_scalar_obs forms on the device).
+        H: [n_fl][N][N] real hopping Hamiltonian (row index first); U: [N].  No arguments: off."""
+        if H is None:
+            lib().oracle_set_scalar_obs(self.h, None, None)
+            return
+        self._obs = (np.ascontiguousarray(np.transpose(np.asarray(H, np.float64).reshape(self.F, self.N, self.N),
+                                                       (0, 2, 1))),
+                     np.ascontiguousarray(np.asarray(U, np.float64).reshape(self.N)))
+        lib().oracle_set_scalar_obs(self.h, _ptr(self._obs[0]), _ptr(self._obs[1]))
+
+    def scalar_obs(self, reset: bool = False) -> dict:
+        """Accumulators since the last reset: sums of ZP ZS {kin, pot, part, ener}, sum of ZS, count."""
+        a = np.zeros(10, np.float64)
+        lib().oracle_get_scalar_obs(self.h, _ptr(a), int(reset))
+        return {"kin": complex(a[0], a[1]), "pot": complex(a[2], a[3]), "part": complex(a[4], a[5]),
+                "ener": complex(a[6], a[7]), "sign": a[8], "count": int(a[9])}
 
     def green(self) -> np.ndarray:
         G = np.zeros((self.F, self.N, self.N), np.complex128)  # [nf][col][row] memory = col-major per flavour

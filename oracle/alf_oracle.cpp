@@ -23,6 +23,7 @@
 //   Prog/Fields_mod.F90:112-217                   phi / gamma / flip
 //   Libraries/Modules/random_wrap_mod.F90:159-168 nranf
 //   Libraries/Modules/mymats_mod.F90:683-704, 1334-1366  COMPARE_C, DET_C
+//   Prog/Hamiltonians/Hamiltonian_Hubbard_smod.F90:695-801  Obs_scal of ham%Obser (Kin, Pot, Part, Ener)
 //
 // Storage: column-major complex128 (Fortran layout).  Indices are 0-based.
 #include <complex>
@@ -179,10 +180,49 @@ struct Oracle {
   // equal-time measurements (ham%Obser, main.F90:757-772 and 788-803): G of all flavours
   void (*eq_cb)(void*, int, const zc*, zc) = nullptr;
   void* eq_ctx = nullptr;
+  // scalar observables of ham%Obser (Hubbard): H F x N x N column-major, U per site
+  vector<double> obsH, obsU;
+  zc obs_sum[4] = {0.0, 0.0, 0.0, 0.0};  // Kin, Pot, Part, Ener, each times ZP ZS
+  double obs_sign = 0.0;
+  int64_t obs_count = 0;
 
   zc* Gf(int nf) { return G.data() + (size_t)nf * N * N; }
   int fval(int n, int nt1 /*1-based*/) const { return f[(size_t)(nt1 - 1) * M + n]; }
 };
+
+// Obs_scal part of the Hubbard ham%Obser (Prog/Hamiltonians/Hamiltonian_Hubbard_smod.F90:695-801,
+// kinetic term as Predefined_Hoppings_Compute_Kin for a dense hopping matrix):
+// GRC(i,j) = delta_ij - G(j,i); ZP = Phase / Re(Phase); ZS = sign(Re(Phase));
+// Kin = N_SUN sum_f sum_ij H_f(i,j) GRC_f(i,j); Pot = sum_i U_i GRC_1(i,i) GRC_dec(i,i);
+// Part = N_SUN sum_f sum_i GRC_f(i,i); Ener = Kin + Pot.
+static void obs_scal(Oracle& o) {
+  if (o.obsH.empty()) return;
+  const int N = o.N;
+  const size_t NN = (size_t)N * N;
+  const double re = o.phase.real();
+  const zc zp = o.phase / re;
+  const double zs = re > 0 ? 1.0 : (re < 0 ? -1.0 : 0.0);
+  zc kin = 0.0, pot = 0.0, part = 0.0;
+  for (int nf = 0; nf < o.F; ++nf) {
+    const zc* G = o.Gf(nf);
+    const double* H = o.obsH.data() + nf * NN;
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const zc grc = (i == j ? 1.0 : 0.0) - G[j + (size_t)i * N];
+        kin += H[i + (size_t)j * N] * grc;
+      }
+    for (int i = 0; i < N; ++i) part += 1.0 - G[i + (size_t)i * N];
+  }
+  const int dec = o.F == 2 ? 1 : 0;
+  for (int i = 0; i < N; ++i)
+    pot += o.obsU[i] * (1.0 - o.Gf(0)[i + (size_t)i * N]) * (1.0 - o.Gf(dec)[i + (size_t)i * N]);
+  kin *= (double)o.NSUN;
+  part *= (double)o.NSUN;
+  const zc w = zp * zs;
+  o.obs_sum[0] += kin * w; o.obs_sum[1] += pot * w; o.obs_sum[2] += part * w; o.obs_sum[3] += (kin + pot) * w;
+  o.obs_sign += zs;
+  o.obs_count++;
+}
 
 // ---------------------------------------------------------------------------
 // Hop_mod (dense real Op_T; ZDSLSYMM dense branch uses ZLARCM / ZLACRM)
@@ -958,6 +998,7 @@ int oracle_sweep_chunk(void* h, const double* u, int nslices) {
         cur.NST++;
       }
       if (o.eq_cb) o.eq_cb(o.eq_ctx, ntau1, o.G.data(), o.phase);  // LOBS_ST = 1, LOBS_EN = Ltrot
+      obs_scal(o);
       cur.ntau++;
       if (cur.ntau == o.L) {
         for (int nf = 0; nf < o.F; ++nf) o.udvl[nf].reset(o.N, 'l');
@@ -967,6 +1008,7 @@ int oracle_sweep_chunk(void* h, const double* u, int nslices) {
       const int ntau = cur.ntau, ntau1 = ntau - 1;
       wrapgrdo(o, ntau, u + (size_t)o.L * per_slice + (size_t)(o.L - ntau) * per_slice);
       if (o.eq_cb && ntau1 >= 1) o.eq_cb(o.eq_ctx, ntau1, o.G.data(), o.phase);
+      if (ntau1 >= 1) obs_scal(o);
       if (cur.NST >= 1 && o.stab_nt[cur.NST] == ntau1 && ntau1 != 0) {
         wrapul(o, o.stab_nt[cur.NST + 1], ntau1, o.udvl);
         for (int nf = 0; nf < o.F; ++nf) {
@@ -1033,6 +1075,22 @@ void oracle_set_tau_callback(void* h, void (*cb)(void*, int, const zc*, const zc
 void oracle_set_eq_callback(void* h, void (*cb)(void*, int, const zc*, zc), void* ctx) {
   Oracle& o = *(Oracle*)h;
   o.eq_cb = cb; o.eq_ctx = ctx;
+}
+// H: F x N x N real column-major (NULL: off), U: N.  Accumulators are cleared.
+void oracle_set_scalar_obs(void* h, const double* H, const double* U) {
+  Oracle& o = *(Oracle*)h;
+  const size_t NN = (size_t)o.N * o.N;
+  if (H) { o.obsH.assign(H, H + o.F * NN); o.obsU.assign(U, U + o.N); }
+  else { o.obsH.clear(); o.obsU.clear(); }
+  for (auto& z : o.obs_sum) z = 0.0;
+  o.obs_sign = 0.0; o.obs_count = 0;
+}
+// out: Kin, Pot, Part, Ener as (re, im), sum of ZS, count; then cleared when reset != 0.
+void oracle_get_scalar_obs(void* h, double* out, int reset) {
+  Oracle& o = *(Oracle*)h;
+  for (int k = 0; k < 4; ++k) { out[2 * k] = o.obs_sum[k].real(); out[2 * k + 1] = o.obs_sum[k].imag(); }
+  out[8] = o.obs_sign; out[9] = (double)o.obs_count;
+  if (reset) { for (auto& z : o.obs_sum) z = 0.0; o.obs_sign = 0.0; o.obs_count = 0; }
 }
 
 }  // extern "C"

@@ -1,0 +1,150 @@
+"""Physics known answer for the sweep: the energy of the 4-site Hubbard ring.
+
+The reference's test suite checks ALF's finite-temperature sweep against exact
+diagonalisation on the N_leg_ladder lattice with L1 = 4, L2 = 1 (a periodic 4-site
+chain), t = 1, U = 4, beta = 2, Mz decoupling and dense hopping, with
+E_ED = -1.47261997 (testsuite/test_vs_ed/test_specs.yaml:25-47; Ener_scal0 extrapolated
+in dtau^2 by testsuite/test_vs_ed/analysis.py). Here this is pinned in three layers:
+
+* Exact diagonalisation in the 256-state Fock space of the model this package builds
+  gives that number. The ensemble is the Mz form K - U/2 sum (n_up - n_do)^2. The
+  estimator is Ener = Kin + U sum <n_up n_do> (Hamiltonian_Hubbard_smod.F90:695-801).
+* The Trotterized ensemble, with the HS field summed out exactly per site and slice using
+  the package's vertices and four-point tables, is the exact expectation of the Monte
+  Carlo estimator at finite dtau. Its dtau -> 0 extrapolation gives the ED number.
+* The oracle's Monte Carlo at dtau = 0.1 agrees with that exact finite-dtau value within
+  its jackknife error bar. The oracle accumulates the Obs_scal part of ham%Obser at every
+  measurement point; bins are analysed with alf_gb300.analysis.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+import oracle
+from alf_gb300 import model as mdl, rng
+from alf_gb300.analysis import jackknife
+
+E_ED = -1.47261997  # testsuite/test_vs_ed/test_specs.yaml:25
+L_SITES, T_HOP, U_INT, BETA = 4, 1.0, 4.0, 2.0
+
+
+def _ring(dtau, nwrap):
+    return mdl.hubbard("n_leg_ladder", L_SITES, 1, t=T_HOP, U=U_INT, beta=BETA, dtau=dtau, nwrap=nwrap)
+
+
+class _Fock:
+    """Dense many-body operators of F flavours x N sites (Jordan-Wigner, orbital f*N + i)."""
+
+    def __init__(self, N, F=2):
+        self.N, self.F = N, F
+        no = N * F
+        self.dim = 1 << no
+        states = np.arange(self.dim)
+        self.occ = (states[:, None] >> np.arange(no)[None, :]) & 1
+        self.c = []
+        for k in range(no):
+            m = np.zeros((self.dim, self.dim))
+            src = states[self.occ[:, k] == 1]
+            below = self.occ[src, :k].sum(axis=1)
+            m[src ^ (1 << k), src] = np.where(below % 2 == 0, 1.0, -1.0)
+            self.c.append(m)
+
+    def n(self, f, i):
+        return np.diag(self.occ[:, f * self.N + i].astype(np.float64))
+
+    def one_body(self, H, f):
+        """sum_ij H(i,j) c+_{i,f} c_{j,f}"""
+        N = self.N
+        out = np.zeros((self.dim, self.dim))
+        for i in range(N):
+            for j in range(N):
+                if H[i, j] != 0.0:
+                    out += H[i, j] * self.c[f * N + i].T @ self.c[f * N + j]
+        return out
+
+
+def _operators(m):
+    fk = _Fock(m.ndim)
+    H = mdl.hopping_matrix("n_leg_ladder", L_SITES, 1, t=T_HOP).real
+    K = sum(m.n_sun * fk.one_body(H, f) for f in range(2))
+    D = sum(fk.n(0, i) @ fk.n(1, i) for i in range(m.ndim))
+    return fk, K, D, K + U_INT * D
+
+
+def _trotter_energy(dtau):
+    """Tr[O (W e^{-dtau K})^L] / Tr[(W e^{-dtau K})^L], W = prod_i sum_s gamma(s)
+    prod_f exp(g_f phi(s) (n_{i,f} - alpha_f)) from the model's own vertices: the
+    expectation of Ener over the HS fields, measured (as ham%Obser is) after a slice's
+    vertex exponentials."""
+    m = _ring(dtau, 10)
+    fk, K, _, O = _operators(m)
+    w = np.ones(fk.dim)
+    for i in range(m.ndim):
+        wi = np.zeros(fk.dim)
+        for s in (-2, -1, 1, 2):
+            e = np.zeros(fk.dim)
+            for f in range(2):
+                v = m.vertices[f][i]
+                assert v.P == [i] and v.op_type == 2
+                e = e + (v.g * mdl.phi(s, 2) * (fk.occ[:, f * m.ndim + i] - v.alpha)).real
+            wi += mdl.GAMA_TYPE2[s] * np.exp(e)
+        w *= wi
+    B = w[:, None] * sl.expm(-dtau * K)
+    B /= np.abs(B).max()
+    P = np.linalg.matrix_power(B, m.ltrot)
+    return float(np.trace(O @ P) / np.trace(P))
+
+
+def test_exact_diagonalisation_gives_the_reference_energy():
+    m = _ring(0.1, 10)
+    fk, K, D, O = _operators(m)
+    mz = sum((fk.n(0, i) - fk.n(1, i)) @ (fk.n(0, i) - fk.n(1, i)) for i in range(m.ndim))
+    w, V = np.linalg.eigh(K - 0.5 * U_INT * mz)
+    p = np.exp(-BETA * (w - w.min()))
+    p /= p.sum()
+    e = float(np.sum(p * np.einsum("ki,kl,li->i", V, O, V)))
+    assert abs(e - E_ED) < 5e-9, e
+
+
+def test_trotterized_energy_extrapolates_to_the_exact_diagonalisation():
+    dt = np.array([0.05, 0.1, 0.2])
+    e = np.array([_trotter_energy(x) for x in dt])
+    # finite dtau moves the energy by O(dtau^2); the HS sum is exact to higher order
+    A = np.stack([np.ones_like(dt), dt ** 2, dt ** 4], axis=1)
+    y0 = np.linalg.solve(A, e)[0]
+    assert abs(y0 - E_ED) < 2e-4, (y0, e)
+    assert abs(e[1] - E_ED) > 0.02  # the Trotter shift at dtau = 0.1 is far above the MC error below
+
+
+def test_oracle_monte_carlo_energy_matches_the_trotterized_value():
+    dtau, nwrap = 0.1, 15  # test_specs.yaml:42-43
+    m = _ring(dtau, nwrap)
+    seed = 790789
+    o = oracle.Oracle(m)
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    n_warm, n_bins, n_per_bin = 200, 40, 500
+    for s in range(n_warm):
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+    H = mdl.hopping_matrix("n_leg_ladder", L_SITES, 1, t=T_HOP).real
+    o.set_scalar_obs(np.stack([H, H]), np.full(m.ndim, U_INT))
+    en, si = [], []
+    sweep = n_warm
+    for b in range(n_bins):
+        for _ in range(n_per_bin):
+            o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, sweep))
+            sweep += 1
+        d = o.scalar_obs(reset=True)
+        assert d["count"] == n_per_bin * (2 * m.ltrot - 1)
+        en.append(d["ener"].real / d["count"])
+        si.append(d["sign"] / d["count"])
+    e_mc, err = jackknife(np.array(en), np.array(si))
+    e_ex = _trotter_energy(dtau)
+    assert err < 0.01, err
+    assert abs(e_mc - e_ex) < 3.5 * err, (e_mc, err, e_ex)
+
+
+@pytest.mark.parametrize("L1", [3, 5])
+def test_n_leg_ladder_needs_even_length(L1):
+    with pytest.raises(ValueError):
+        mdl.hopping_matrix("n_leg_ladder", L1, 1)
