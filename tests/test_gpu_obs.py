@@ -62,3 +62,41 @@ def test_device_scalar_observables_match_host_sums(precision):
     assert g.scalar_obs(0)["count"] == 0
     g.sweep(None)
     assert g.scalar_obs(0)["count"] == 2 * m.ltrot - 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_energy_of_the_four_site_ring_matches_the_trotterized_value(precision):
+    # the reference's exact-diagonalisation case (4-site Hubbard ring, U = 4, beta = 2) at
+    # dtau = 0.1: 64 batched chains on device draws, Ener accumulated on the device, ALF's
+    # jackknife over (chain, bin) against the exact Trotterized expectation of the estimator
+    from test_ed_energy import L_SITES, T_HOP, U_INT, _ring, _trotter_energy
+    from alf_gb300.analysis import jackknife
+
+    m = _ring(0.1, 15)
+    C, seed = 64, 452938
+    g = Chains(m, n_chains=C, precision=precision)
+    for c in range(C):
+        g.set_fields(c, rng.initial_fields(seed, c, m.n_op, m.ltrot))
+    g.init_state()
+    for c in range(C):
+        g.set_rng(c, seed, rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+    for _ in range(50):
+        g.sweep(None)
+    H = mdl.hopping_matrix("n_leg_ladder", L_SITES, 1, t=T_HOP).real
+    g.set_scalar_obs(np.stack([H, H]), np.full(m.ndim, U_INT))
+    en, si = [], []
+    for _ in range(8):
+        g.reset_scalar_obs()
+        for _ in range(50):
+            g.sweep(None)
+        for c in range(C):
+            d = g.scalar_obs(c)
+            assert d["count"] == 50 * (2 * m.ltrot - 1)
+            en.append(d["ener"].real / d["count"])
+            si.append(d["sign"] / d["count"])
+    g.close()
+    e, err = jackknife(np.array(en), np.array(si))
+    e_ex = _trotter_energy(0.1)
+    print(f"{precision}: E = {e:.4f} +- {err:.4f}, exact Trotterized {e_ex:.4f}")
+    assert err < 0.01, err
+    assert abs(e - e_ex) < 3.5 * err, (e, err, e_ex)
