@@ -1,7 +1,7 @@
 """Bin analysis of Monte Carlo observables: ALF's jackknife with the sign.
 
 Restates the published algorithm of Libraries/Modules/errors_mod.F90 (ERRCALC :98-126,
-ERRCALC_JS :290-327, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
+ERRCALC_J :160-190, ERRCALC_J_REBIN :257-287, ERRCALC_JS :290-327, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
 Analysis/ana_mod.F90 (ERRCALCJ calls, e.g. :1380, :1587, :1783) applies to the per-bin
 averages of <O s> and <s> written by the observables module:
 
@@ -64,3 +64,16 @@ def jackknife(en, si=None, nrebin: int = 1, f: Optional[Callable[[float], float]
         mi, ei = _js_real(en.imag, si, f)
         return complex(mr, mi), complex(er, ei)
     return _js_real(en, si, f)
+
+
+def jackknife_plain(en, nrebin: int = 1):
+    """Jackknife without a sign (ERRCALC_J, ERRCALC_J_REBIN): leave-one-out means
+    (sum - x_n) / (n - 1) of the (rebinned) samples; mean and ERRCALC error times n."""
+    en = np.asarray(en, dtype=np.float64)
+    if nrebin > 1:
+        en = rebin(en, nrebin)
+    n = en.size
+    if n < 2:
+        raise ValueError("jackknife: fewer than two bins")
+    xm, xerr = errcalc((en.sum() - en) / (n - 1))
+    return xm, xerr * n

@@ -179,6 +179,16 @@ class Chains:
     def reset_scalar_obs(self):
         _lib.check(self.L.alfgpu_reset_scalar_obs(self.h), "alfgpu_reset_scalar_obs")
 
+    def scalar_bin(self, reset: bool = True):
+        """One bin of the scalar observables: per chain Obs_vec / N and Ave_sign / N, averaged
+        over the handle's chains as ALF averages walkers (alf_gb300.bins); then, with reset,
+        the accumulators are cleared for the next bin.  Returns (Kin, Pot, Part, Ener), sign."""
+        from . import bins
+        b = bins.walker_mean(bins.bin_from_sums(self.scalar_obs(c)) for c in range(self.C))
+        if reset:
+            self.reset_scalar_obs()
+        return b
+
     # --- checkpoint / resume (the reference's confout files) ------------------------------------
     def checkpoint(self, path: str):
         """Write every chain's fields and draw-stream state, the stabilisation interval and the
