@@ -1341,6 +1341,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     return ALFGPU_ERROR_ARGUMENT;
   if (d.precision != ALFGPU_PRECISION_FP64 && d.precision != ALFGPU_PRECISION_MIXED) return ALFGPU_ERROR_ARGUMENT;
   if (d.ltau != 0 && d.ltau != 1) return ALFGPU_ERROR_ARGUMENT;
+  if ((d.reserved[0] & ALFGPU_FLAG_QR_HALF_CLUSTER) && (d.reserved[0] & ALFGPU_FLAG_QR_FULL_CLUSTER))
+    return ALFGPU_ERROR_ARGUMENT;
   if (d.ltau && 2 * d.ndim > 32 * BQR_LROWS) return ALFGPU_ERROR_UNSUPPORTED;  // CGR2_2's 2N-row apply
   alfgpu_s* h = new alfgpu_s();
   h->d = d;

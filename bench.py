@@ -41,7 +41,7 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # Measured on this machine's GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
 FP64_DMMA_TFLOPS = 1.048
 # DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
-# the ncu capture summarised in profiles/k_zgemm_hop_hubbard16x16_fp64.md
+# the ncu capture summarised in profiles/k_zgemm_hubbard16x16_fp64.md
 HOP_TRAFFIC_BYTES = 3.30e6
 
 
@@ -183,6 +183,47 @@ def roofline(args, m, prof):
         if args.precision != "fp64":
             roof["tensor_op_tflops"] = roof["achieved"] * roof["bf16_products_per_algorithmic_product"]
     return roof
+
+
+def sweep_flops(m, n_acc: float, ltau: int) -> dict:
+    """Algorithmic FLOPs of one sweep of one chain by phase (real-flop convention, LAPACK
+    counts): per flavour G wraps 16 L N^3, UDV propagation 8 L N^3, decompose_UDV_state
+    2 Nstm x 14.7 N^3, CGR 2 Nstm x 44 N^3, rank-1 updates 8 N^2 per accepted flip; with
+    TAU_M also its wraps 16 L N^3, WRAPUR 4 L N^3 and Nstm CGR2_2 on 2N (~161.7 N^3)."""
+    N, F, L = m.ndim, m.n_fl, m.ltrot
+    nstm = -(-L // m.nwrap)
+    n3 = float(N) ** 3
+    out = {"wraps": F * 16.0 * L * n3, "propagate": F * 8.0 * L * n3,
+           "decompose": F * 2.0 * nstm * 14.7 * n3, "cgr": F * 2.0 * nstm * 44.0 * n3,
+           "rank1": F * 8.0 * N * N * float(n_acc)}
+    if ltau:
+        out["tau_wraps"] = F * 20.0 * L * n3
+        out["tau_cgr2_2"] = F * nstm * (14.7 + 147.0) * n3
+    return out
+
+
+# phases whose products the mixed form runs on the tensor cores; the rest stay FP64
+_TENSOR_PHASES = ("wraps", "propagate", "rank1", "tau_wraps")
+
+
+def sweep_roofline(m, n_acc: float, ltau: int, chains: int, ms_per_step: float, precision: str,
+                   p_fp64: float, p_bf16: float) -> dict:
+    """Whole-sweep roofline: t_roof = sum over phases of FLOPs / peak for one step (one sweep of
+    every chain).  FP64 form: every phase at the FP64 rate.  Mixed form: the wraps,
+    propagation and rank-k flushes at the BF16 tensor peak, the QR / CGR phases at the FP64
+    rate.  frac = t_roof / measured step time."""
+    fl = {k: v * chains for k, v in sweep_flops(m, n_acc, ltau).items()}
+    t = 0.0
+    for k, v in fl.items():
+        peak = p_bf16 if (precision != "fp64" and k in _TENSOR_PHASES) else p_fp64
+        t += v / (peak * 1e12)
+    total = sum(fl.values())
+    return {"flops_per_step": total, "flops_by_phase": fl, "t_roof_ms": 1e3 * t, "ms_per_step": ms_per_step,
+            "frac": 1e3 * t / ms_per_step if ms_per_step > 0 else None,
+            "achieved_tflops": total / (ms_per_step / 1e3) / 1e12 if ms_per_step > 0 else None,
+            "peaks_tflops": {"fp64": p_fp64, "bf16": p_bf16},
+            "basis": "FP64 phases at the measured FP64 MMA rate" + (
+                "" if precision == "fp64" else "; wraps, propagation and flushes at the measured BF16 peak")}
 
 
 def workload_model(name: str):
@@ -500,6 +541,9 @@ def main():
                  "precision_green": {"xmaxG": st2.xmaxG, "xmeanG": st2.xmeanG_sum / max(st2.ncg, 1),
                                      "xmaxP": st2.xmaxP},
                  "roofline": roofline(a2, m, r2["prof"]),
+                 "sweep_roofline": sweep_roofline(m, st2.n_acc / max(args.steps, 1), r2.get("ltau", 0), args.chains,
+                                                  1e3 * r2["t_dev"] / args.steps, "mixed", FP64_DMMA_TFLOPS,
+                                                  measured_bf16_peak()[0]),
                  "dtype": "c128 state; G wraps and UDV propagation (and the flushes of batched grids) as "
                           "FP64-accurate digit-sliced BF16 tensor-core products; per-visit arithmetic and "
                           "single-chain flushes in double-float; QR / CGR in FP64"}
@@ -521,6 +565,9 @@ def main():
         "phases": phases,
         "precision_green": {"xmaxG": st.xmaxG, "xmeanG": st.xmeanG_sum / max(st.ncg, 1), "xmaxP": st.xmaxP},
         "acceptance": st.n_acc / max(st.n_prop, 1),
+        "sweep_roofline": sweep_roofline(m, st.n_acc / max(args.steps, 1), r.get("ltau", 0), args.chains,
+                                         1e3 * r["t_dev"] / args.steps, args.precision, FP64_DMMA_TFLOPS,
+                                         measured_bf16_peak()[0]),
     }
     if mixed is not None:
         line["mixed"] = mixed

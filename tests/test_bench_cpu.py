@@ -1,0 +1,28 @@
+"""The bench's whole-sweep roofline arithmetic (no GPU): per-sweep algorithmic FLOPs of the
+16x16 Hubbard workload (about 1.20e11 plus 8 N^2 per accepted flip and flavour) and the
+roofline time of each form."""
+import bench
+from alf_gb300 import model as mdl
+
+
+def test_sweep_flops_of_the_16x16_workload():
+    m = mdl.config("hubbard16x16")
+    f = bench.sweep_flops(m, 0, 0)
+    n3 = 256.0 ** 3
+    assert abs(sum(f.values()) - 2 * (24 * 100 + 2 * 10 * 58.7) * n3) < 1e-3 * sum(f.values())
+    assert abs(sum(f.values()) - 1.20e11) < 0.01e11
+    assert bench.sweep_flops(m, 1000, 0)["rank1"] == 2 * 8.0 * 256 * 256 * 1000
+    t = bench.sweep_flops(m, 0, 1)
+    assert t["tau_wraps"] == 2 * 20.0 * 100 * n3 and "tau_cgr2_2" in t
+
+
+def test_sweep_roofline_of_each_form():
+    m = mdl.config("hubbard16x16")
+    r64 = bench.sweep_roofline(m, 20000, 0, 16, 4000.0, "fp64", 1.0, 2000.0)
+    assert abs(r64["t_roof_ms"] - r64["flops_per_step"] / 1e12 * 1e3) < 1e-9 * r64["t_roof_ms"]
+    assert abs(r64["frac"] - r64["t_roof_ms"] / 4000.0) < 1e-15
+    rmx = bench.sweep_roofline(m, 20000, 0, 16, 4000.0, "mixed", 1.0, 2000.0)
+    fl = rmx["flops_by_phase"]
+    expect = (fl["decompose"] + fl["cgr"]) / 1e12 + (fl["wraps"] + fl["propagate"] + fl["rank1"]) / 2e15
+    assert abs(rmx["t_roof_ms"] - 1e3 * expect) < 1e-9 * rmx["t_roof_ms"]
+    assert rmx["t_roof_ms"] < r64["t_roof_ms"]
