@@ -15,6 +15,8 @@ in dtau^2 by testsuite/test_vs_ed/analysis.py). Here this is pinned in three lay
 * The oracle's Monte Carlo at dtau = 0.1 agrees with that exact finite-dtau value within
   its jackknife error bar. The oracle accumulates the Obs_scal part of ham%Obser at every
   measurement point; bins are analysed with alf_gb300.analysis.
+* With Ltau = 1, TAU_M's time-displaced Green functions agree at every tau with the exact
+  Trotterized <c(tau) c+(0)> of the same transfer matrix.
 """
 import numpy as np
 import pytest
@@ -71,11 +73,11 @@ def _operators(m):
     return fk, K, D, K + U_INT * D
 
 
-def _trotter_energy(dtau):
-    """Tr[O (W e^{-dtau K})^L] / Tr[(W e^{-dtau K})^L], W = prod_i sum_s gamma(s)
-    prod_f exp(g_f phi(s) (n_{i,f} - alpha_f)) from the model's own vertices: the
-    expectation of Ener over the HS fields, measured (as ham%Obser is) after a slice's
-    vertex exponentials."""
+def _transfer(dtau):
+    """(model, Fock space, energy operator, B) with B = W e^{-dtau K}: one slice of the
+    Trotterized ensemble with the HS field summed out, W = prod_i sum_s gamma(s) prod_f
+    exp(g_f phi(s) (n_{i,f} - alpha_f)) from the model's own vertices (as Upgrade2 weighs a
+    field: the vertex exponentials times gamma).  B is scaled to max |B| = 1."""
     m = _ring(dtau, 10)
     fk, K, _, O = _operators(m)
     w = np.ones(fk.dim)
@@ -90,9 +92,32 @@ def _trotter_energy(dtau):
             wi += mdl.GAMA_TYPE2[s] * np.exp(e)
         w *= wi
     B = w[:, None] * sl.expm(-dtau * K)
-    B /= np.abs(B).max()
+    return m, fk, O, B / np.abs(B).max()
+
+
+def _trotter_energy(dtau):
+    """Tr[O B^L] / Tr[B^L]: the expectation of Ener over the HS fields, measured (as
+    ham%Obser is) after a slice's vertex exponentials."""
+    m, _, O, B = _transfer(dtau)
     P = np.linalg.matrix_power(B, m.ltrot)
     return float(np.trace(O @ P) / np.trace(P))
+
+
+def _trotter_green(dtau):
+    """Time-displaced Green functions of the Trotterized ensemble at tau = 0..L (orbital 0
+    and its neighbour 1 of flavour 0): [<c_0(tau) c+_0>, <c_0(tau) c+_1>, -<c+_0(tau) c_0>]
+    with c(tau) = U(tau,0)^-1 c U(tau,0), U(tau,0) = B^tau, i.e. the expectations of TAU_M's
+    GT0(0,0), GT0(0,1) and G0T(0,0)."""
+    m, fk, _, B = _transfer(dtau)
+    L = m.ltrot
+    A = [np.eye(fk.dim)]
+    for _ in range(L):
+        A.append(B @ A[-1])
+    Z = np.trace(A[L])
+    c0, c1 = fk.c[0], fk.c[1]
+    return m, np.array([[np.trace(A[L - k] @ c0 @ A[k] @ c0.T) / Z for k in range(L + 1)],
+                        [np.trace(A[L - k] @ c0 @ A[k] @ c1.T) / Z for k in range(L + 1)],
+                        [-np.trace(A[L - k] @ c0.T @ A[k] @ c0) / Z for k in range(L + 1)]]).real
 
 
 def test_exact_diagonalisation_gives_the_reference_energy():
@@ -148,3 +173,41 @@ def test_oracle_monte_carlo_energy_matches_the_trotterized_value():
 def test_n_leg_ladder_needs_even_length(L1):
     with pytest.raises(ValueError):
         mdl.hopping_matrix("n_leg_ladder", L1, 1)
+
+
+def test_oracle_time_displaced_green_functions_match_the_trotterized_values():
+    # TAU_M (PROPR / PROPRM1 and the CGR2_2 refreshes) on the same ring, Ltau = 1: the site-
+    # and spin-averaged GT0(i,i), GT0(i,i+1) and G0T(i,i) at every tau against the exact
+    # Trotterized curves; at tau = 0 and beta particle-hole symmetry makes the local values
+    # exact per configuration (zero error bar)
+    m, ex = _trotter_green(0.1)
+    L = m.ltrot
+    o = oracle.Oracle(m, ltau=1)
+    seed = 1048
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    for s in range(100):
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+    _, tau = o.collect_measurements()
+    n_bins, n_per_bin = 20, 100
+    rows = []
+    for s in range(100, 100 + n_bins * n_per_bin):
+        tau.clear()
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+        row = np.zeros((3, L + 1))
+        for nt, (gt0, g0t, _, _), ph in tau:
+            assert ph.real > 0 and abs(ph.imag) < 1e-10  # Mz at half filling: no sign problem
+            nn = [0.5 * (gt0[f][i, (i + 1) % 4] + gt0[f][(i + 1) % 4, i]).real for f in range(2) for i in range(4)]
+            row[0, nt] = np.mean([gt0[f][i, i].real for f in range(2) for i in range(4)])
+            row[1, nt] = np.mean(nn)
+            row[2, nt] = np.mean([g0t[f][i, i].real for f in range(2) for i in range(4)])
+        rows.append(row)
+        assert len(tau) == L + 1
+    a = np.array(rows).reshape(n_bins, n_per_bin, 3, L + 1).mean(axis=1)
+    mean = a.mean(axis=0)
+    err = a.std(axis=0, ddof=1) / np.sqrt(n_bins)
+    dev = np.abs(mean - ex)
+    assert np.all(dev <= 4.0 * err + 1e-9), np.max(dev / (err + 1e-300))
+    z = (mean - ex)[:, 1:L] / err[:, 1:L]
+    assert np.mean(z ** 2) < 2.0, np.mean(z ** 2)
+    assert np.max(err[:, 1:L]) < 0.01
