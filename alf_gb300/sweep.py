@@ -72,7 +72,8 @@ class Chains:
         if models is None:
             self._upload_vertices(-1, pk)
         else:
-            assert len(models) == n_chains
+            if len(models) != n_chains:
+                raise ValueError(f"{len(models)} models for {n_chains} chains")
             for c, m in enumerate(models):
                 self._upload_vertices(c, m.pack())
 
@@ -94,7 +95,8 @@ class Chains:
     # --- fields and draws -------------------------------------------------------------------
     def set_fields(self, chain: int, f: np.ndarray):
         f = np.ascontiguousarray(f, dtype=np.int8)
-        assert f.shape == (self.Lt, self.M)
+        if f.shape != (self.Lt, self.M):
+            raise ValueError(f"fields of shape {f.shape}, expected {(self.Lt, self.M)}")
         _lib.check(self.L.alfgpu_set_fields(self.h, chain, _p(f)), "alfgpu_set_fields")
 
     def fields(self, chain: int) -> np.ndarray:
@@ -132,7 +134,8 @@ class Chains:
         cb = _lib.OBS_CB(on_obs) if measure else _lib.OBS_CB()
         if uniforms is not None:
             u = np.ascontiguousarray(uniforms, dtype=np.float64)
-            assert u.size == self.C * 6 * self.M * self.Lt
+            if u.size != self.C * 6 * self.M * self.Lt:
+                raise ValueError(f"{u.size} draws, expected {self.C * 6 * self.M * self.Lt} (chains x 6 M Ltrot)")
             rc = self.L.alfgpu_sweep(self.h, _p(u), cb, None)
         else:
             rc = self.L.alfgpu_sweep(self.h, None, cb, None)
