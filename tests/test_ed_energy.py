@@ -1,4 +1,4 @@
-"""Physics known answer for the sweep: the energy of the 4-site Hubbard ring.
+"""Physics known answers for the sweep: the 4-site Hubbard ring and a small Kondo bilayer.
 
 The reference's test suite checks ALF's finite-temperature sweep against exact
 diagonalisation on the N_leg_ladder lattice with L1 = 4, L2 = 1 (a periodic 4-site
@@ -17,6 +17,8 @@ in dtau^2 by testsuite/test_vs_ed/analysis.py). Here this is pinned in three lay
   measurement point; bins are analysed with alf_gb300.analysis.
 * With Ltau = 1, TAU_M's time-displaced Green functions agree at every tau with the exact
   Trotterized <c(tau) c+(0)> of the same transfer matrix.
+* The Kondo model's two-site vertices get the same exact Trotterized check, on one- and
+  two-body observables of a 2 x 1 bilayer.
 """
 import numpy as np
 import pytest
@@ -211,3 +213,71 @@ def test_oracle_time_displaced_green_functions_match_the_trotterized_values():
     z = (mean - ex)[:, 1:L] / err[:, 1:L]
     assert np.mean(z ** 2) < 2.0, np.mean(z ** 2)
     assert np.max(err[:, 1:L]) < 0.01
+
+
+def test_kondo_two_site_vertices_match_the_trotterized_values():
+    # config 5's vertex algebra (two-site V_SUN vertices, N_FL = 1, N_SUN = 2, ham_Uf = 0) on a
+    # bilayer of 2 x 1 cells (c0 f0 c1 f1): the c kinetic energy and the J_K correlator
+    # sum_i <D_i^2>, D_i = sum_sigma (c+_i f_i + f+_i c_i), from the oracle's ham%Obser G
+    # (Wick per configuration, two identical species) against Tr[O B^L] / Tr[B^L] with the
+    # HS field summed out per c-f pair
+    dtau = 0.1
+    m = mdl.kondo(2, 1, JK=1.5, Uf=0.0, beta=BETA, dtau=dtau, nwrap=10)
+    N = m.ndim
+    H = mdl.hopping_matrix("BILAYER_SQUARE", 2, 1, t=1.0).real
+    fk = _Fock(N, F=2)  # the two SU(2) species of the single flavour
+
+    def ob(A):
+        return sum(fk.one_body(A, sp) for sp in range(2))
+
+    pairs = [(2 * i, 2 * i + 1) for i in range(N // 2)]
+    W = np.eye(fk.dim)
+    for v in m.vertices[0]:
+        Ov = np.zeros((N, N))
+        for a, pa in enumerate(v.P):
+            for b, pb in enumerate(v.P):
+                Ov[pa, pb] = v.O[a, b].real
+        w, Z = np.linalg.eigh(ob(Ov))
+        W = sum(mdl.GAMA_TYPE2[s] * (Z * np.exp((v.g * mdl.phi(s, 2)).real * (w - m.n_sun * v.alpha.real))) @ Z.T
+                for s in (-2, -1, 1, 2)) @ W
+    B = W @ sl.expm(-dtau * ob(H))
+    P = np.linalg.matrix_power(B / np.abs(B).max(), m.ltrot)
+    DD = np.zeros((fk.dim, fk.dim))
+    for c, f in pairs:
+        Oi = np.zeros((N, N))
+        Oi[c, f] = Oi[f, c] = 1.0
+        Di = ob(Oi)
+        DD += Di @ Di
+    ex = np.array([np.trace(ob(H) @ P), np.trace(DD @ P)]) / np.trace(P)
+
+    o = oracle.Oracle(m)
+    seed = 2024
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    for s in range(100):
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+    eq, _ = o.collect_measurements()
+    n_bins, n_per_bin = 20, 100
+    vals = []
+    sel = np.zeros((N, N))
+    for c, f in pairs:
+        sel[c, f] = sel[f, c] = 1.0
+    for s in range(100, 100 + n_bins * n_per_bin):
+        eq.clear()
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+        kin = dd = 0.0
+        for _, G, ph in eq:
+            assert ph.real > 0 and abs(ph.imag) < 1e-10  # N_SUN = 2, real couplings: no sign problem
+            g = G[0]
+            grc = np.eye(N) - g.T  # <c+_a c_b>
+            kin += m.n_sun * np.sum(H * grc).real
+            for c, f in pairs:
+                idx = [(c, f), (f, c)]
+                d = sum(grc[a, b] for a, b in idx)
+                w2 = sum(grc[a, b] * grc[p, q] + grc[a, q] * g[b, p] for a, b in idx for p, q in idx)
+                dd += (2.0 * w2 + 2.0 * d * d).real
+        vals.append((kin / len(eq), dd / len(eq)))
+    a = np.array(vals).reshape(n_bins, n_per_bin, 2).mean(axis=1)
+    mean, err = a.mean(axis=0), a.std(axis=0, ddof=1) / np.sqrt(n_bins)
+    assert np.all(err < 0.05), err
+    assert np.all(np.abs(mean - ex) < 4.0 * err), (mean, err, ex)
