@@ -225,8 +225,8 @@ template <typename T>
 static int dalloc(alfgpu_s* h, T** p, size_t count) {
   void* q = nullptr;
   CK(cudaMalloc(&q, count * sizeof(T) + 16));
+  h->allocs.push_back(q);  // freed by alfgpu_destroy even if the clear below fails
   CK(cudaMemset(q, 0, count * sizeof(T) + 16));
-  h->allocs.push_back(q);
   *p = (T*)q;
   return 0;
 }
