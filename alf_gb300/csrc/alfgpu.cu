@@ -1757,10 +1757,9 @@ int alfgpu_set_fields_c128(alfgpu_t* h, int32_t chain, const double* f) {
   const size_t ML = (size_t)h->M * h->L;
   std::vector<int8_t> b(ML);
   for (size_t i = 0; i < ML; ++i) {
-    double x = f[2 * i];
-    long v = lround(x);
-    if ((double)v != x || f[2 * i + 1] != 0.0) return ALFGPU_ERROR_FIELDS;
-    b[i] = (int8_t)v;
+    const double x = f[2 * i];  // nsigma%f stores the discrete field values as complex numbers
+    if (!(x == 1.0 || x == -1.0 || x == 2.0 || x == -2.0) || f[2 * i + 1] != 0.0) return ALFGPU_ERROR_FIELDS;
+    b[i] = (int8_t)x;
   }
   return alfgpu_set_fields(h, chain, b.data());
 }
