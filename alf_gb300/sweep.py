@@ -99,6 +99,13 @@ class Chains:
             raise ValueError(f"fields of shape {f.shape}, expected {(self.Lt, self.M)}")
         _lib.check(self.L.alfgpu_set_fields(self.h, chain, _p(f)), "alfgpu_set_fields")
 
+    def set_fields_c128(self, chain: int, f: np.ndarray):
+        """The fields as ALF stores them (nsigma%f: complex, values +-1 / +-2), [Ltrot][M]."""
+        z = np.ascontiguousarray(f, dtype=np.complex128)
+        if z.shape != (self.Lt, self.M):
+            raise ValueError(f"fields of shape {z.shape}, expected {(self.Lt, self.M)}")
+        _lib.check(self.L.alfgpu_set_fields_c128(self.h, chain, _p(z)), "alfgpu_set_fields_c128")
+
     def fields(self, chain: int) -> np.ndarray:
         f = np.zeros((self.Lt, self.M), np.int8)
         _lib.check(self.L.alfgpu_get_fields(self.h, chain, _p(f)), "alfgpu_get_fields")

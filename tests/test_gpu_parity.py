@@ -161,6 +161,28 @@ def test_sweep_hubbard_8x8_half_cluster_qr_parity():
     _run_pair(m, seed=4, sweeps=1, flags=FLAG_QR_HALF_CLUSTER)
 
 
+def test_complex_fields_entry_matches_the_int8_entry():
+    # nsigma%f as the Fortran side holds it (complex) gives the same state as the int8 form;
+    # a value that is not a discrete field is rejected (ALFGPU_ERROR_FIELDS)
+    m = mdl.config("hubbard4x4")
+    f0 = rng.initial_fields(3, 0, m.n_op, m.ltrot)
+    u = rng.sweep_uniforms(3, 0, m.n_op, m.ltrot, 0)[None, :]
+    a, b = Chains(m), Chains(m)
+    a.set_fields(0, f0)
+    b.set_fields_c128(0, f0.astype(np.complex128))
+    for g in (a, b):
+        g.init_state()
+        g.sweep(u)
+    np.testing.assert_array_equal(a.fields(0), b.fields(0))
+    assert _relmax(a.green(0), b.green(0)) == 0.0
+    bad = f0.astype(np.complex128)
+    bad[0, 0] = 1.5
+    with pytest.raises(RuntimeError):
+        b.set_fields_c128(0, bad)
+    a.close()
+    b.close()
+
+
 def test_sweep_hubbard_odd_sizes_parity():
     # ragged blocks (M not a multiple of the delay block), odd Nwrap remainder
     m = mdl.hubbard("square", 6, 4, U=6.0, beta=1.3, dtau=0.1, nwrap=4)
