@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "AFQMC sweeps/s (per chain & aggregate), mixed vs FP64 GPU at max|dG|<=1e-5"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# Measured on this machine's GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
+# Measured on a GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
 FP64_DMMA_TFLOPS = 1.048
 # DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
 # the ncu capture summarised in profiles/k_zgemm_hubbard16x16_fp64.md
@@ -163,7 +163,7 @@ def roofline(args, m, prof):
                 "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
                 "traffic": HOP_TRAFFIC_BYTES if m.ndim == 256 else None,
                 "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
-                "peak_source": "FP64 mma.sync m8n8k4 throughput measured on this pool "
+                "peak_source": "FP64 mma.sync m8n8k4 throughput measured on a GB300 "
                                "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
     else:
         peak, src = measured_bf16_peak()

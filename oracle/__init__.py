@@ -4,7 +4,8 @@
 header for the reference file:line list) and calls the same LAPACK routines the
 Fortran calls, resolved at run time from the OpenBLAS that ships inside SciPy.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg use this package, and only as the checker / the reported CPU baseline.
+leg use this package: as the reference results are compared with, and as the
+reported CPU baseline.
 """
 from __future__ import annotations
 

@@ -3,9 +3,9 @@
 // This file restates ALF's default (no STAB flag) sequential sweep on the CPU,
 // calling the same LAPACK/BLAS routines the Fortran calls (ZGEQP3, ZUNGQR,
 // ZUNMQR, ZTRSM, ZTRMM, ZGETRF, ZLAPMR/ZLAPMT, ZLARCM/ZLACRM, ZGEMM), which are
-// resolved at run time from an OpenBLAS shared library (dlopen).  It is the
-// parity checker for the GPU library and the timed CPU baseline; the product
-// never links, loads or calls it.
+// resolved at run time from an OpenBLAS shared library (dlopen).  The GPU
+// library's results are compared with it, and it is the timed CPU baseline; the
+// product never links, loads or calls it.
 //
 // Reference files followed (paths inside the ALF tree):
 //   Prog/main.F90:446-457, 589-631, 714-887       init chain and sweep block
