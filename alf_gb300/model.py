@@ -144,14 +144,61 @@ def _cell(n1: int, n2: int, L1: int, L2: int) -> int:
     return (n1 % L1) + L1 * (n2 % L2)
 
 
+# primitive vectors a1, a2 of the unit cells (Predefined_Latt_mod.F90:100-265)
+_PRIMITIVE = {"SQUARE": ((1.0, 0.0), (0.0, 1.0)), "BILAYER_SQUARE": ((1.0, 0.0), (0.0, 1.0)),
+              "HONEYCOMB": ((1.0, 0.0), (0.5, math.sqrt(3.0) / 2.0)), "N_LEG_LADDER": ((1.0, 0.0), (0.0, 1.0))}
+
+
+def alf_cell_order(lattice: str, L1: int, L2: int) -> List[int]:
+    """The unit cells in the order of ALF's Make_lattice (lattices_v3_mod.F90:88-336), as
+    indices of this module's natural numbering (n1 fastest).
+
+    Make_lattice walks i1 (outer) and i2 (inner) over -L..L, L the largest
+    |BZ_i . L_j / 2 pi|, and keeps x = i1 a1 + i2 a2 when -|a|^2/2 < x . a <= |a|^2/2
+    (within Eps_small) for a in {L2, L1, L2 - L1, L2 + L1}: one representative per
+    periodic class, centred on the origin.  Here L1 = L1 a1 and L2 = L2 a2 (one cell
+    along a2 for the N_leg_ladder, whose legs are orbitals), so (i1, i2) is the cell
+    (i1 mod L1, i2 mod L2)."""
+    lat = lattice.upper()
+    a1, a2 = (np.array(v) for v in _PRIMITIVE[lat])
+    n2c = 1 if lat == "N_LEG_LADDER" else L2
+    L1p, L2p = L1 * a1, n2c * a2
+    Minv = np.linalg.inv(np.array([a1, a2]))
+    bz = [2.0 * math.pi * Minv[:, 0], 2.0 * math.pi * Minv[:, 1]]
+    L = max(abs(int(round(float(b @ v) / (2.0 * math.pi)))) for b in bz for v in (L1p, L2p))
+    tests = [L2p, L1p, L2p - L1p, L2p + L1p]
+    order = []
+    for i1 in range(-L, L + 1):
+        for i2 in range(-L, L + 1):
+            x = i1 * a1 + i2 * a2
+            if all(float(x @ a) <= float(a @ a) / 2.0 + EPS_SMALL and float(x @ a) >= -float(a @ a) / 2.0 + EPS_SMALL
+                   for a in tests):
+                order.append(_cell(i1, i2, L1, n2c))
+    if sorted(order) != list(range(L1 * n2c)):
+        raise ValueError(f"{lattice} {L1}x{L2}: the centred cell does not tile the lattice")
+    return order
+
+
+def _site_permutation(lattice: str, L1: int, L2: int, norb: int, site_order: str) -> Optional[np.ndarray]:
+    if site_order == "natural":
+        return None
+    if site_order != "alf":
+        raise ValueError(f"site_order {site_order!r}: 'natural' or 'alf'")
+    cells = alf_cell_order(lattice, L1, L2)
+    return np.array([I * norb + o for I in cells for o in range(norb)])
+
+
 def hopping_matrix(lattice: str, L1: int, L2: int, t: float = 1.0, chem: float = 0.0,
-                   t2: float = 0.0, tperp: float = 0.0) -> np.ndarray:
+                   t2: float = 0.0, tperp: float = 0.0, site_order: str = "natural") -> np.ndarray:
     """Dense Hermitian hopping ``Op_T(1,nf)%O`` (no flux, no checkerboard).
 
     Bond tables follow ``Set_Default_hopping_parameters_*``; the assembly
     ``O(I1,J1) = T; O(J1,I1) = conj(T); O(I1,I1) = T_loc`` follows
-    Prog/Predefined_Hop_mod.F90:1730-1761.
+    Prog/Predefined_Hop_mod.F90:1730-1761.  Sites are ``cell * norb + orbital``; cells
+    are numbered n1 fastest (``site_order="natural"``) or in Make_lattice's order
+    (``"alf"``, see alf_cell_order), which is ALF's Invlist and vertex order.
     """
+    lat0, L1_0, L2_0 = lattice, L1, L2
     lat = lattice.upper()
     if lat == "SQUARE":
         norb = 1
@@ -191,7 +238,8 @@ def hopping_matrix(lattice: str, L1: int, L2: int, t: float = 1.0, chem: float =
                 O[j1, i1] = np.conj(tb)
             for o in range(norb):
                 O[I * norb + o, I * norb + o] = tloc[o]
-    return O
+    p = _site_permutation(lat0, L1_0, L2_0, norb, site_order)
+    return O if p is None else O[np.ix_(p, p)]
 
 
 def exp_hopping(O: np.ndarray, dtau: float):
@@ -298,7 +346,7 @@ def _mz_pair(site: int, dtau: float, U: float):
 
 def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U: float = 4.0,
             chem: float = 0.0, beta: float = 4.0, dtau: float = 0.1, nwrap: int = 10,
-            n_sun_input: int = 2, tperp: float = 0.0) -> Model:
+            n_sun_input: int = 2, tperp: float = 0.0, site_order: str = "natural") -> Model:
     """Mz Hubbard model with dense hopping, as ``Ham_Set`` builds it.
 
     ``N_FL = 2`` and ``N_SUN`` is halved (Hamiltonian_Hubbard_smod.F90:264-266);
@@ -307,7 +355,7 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
     """
     ltrot = int(round(beta / dtau))
     n_sun = n_sun_input // 2
-    O = hopping_matrix(lattice, L1, L2, t=t, chem=chem, tperp=tperp)
+    O = hopping_matrix(lattice, L1, L2, t=t, chem=chem, tperp=tperp, site_order=site_order)
     N = O.shape[0]
     mat, inv = exp_hopping(O, dtau)
     up, do = [], []
@@ -319,12 +367,13 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
     return Model(name=f"hubbard_{lattice.lower()}_{L1}x{L2}", ndim=N, n_fl=2, n_sun=n_sun,
                  ltrot=ltrot, nwrap=nwrap, dtau=dtau, beta=beta, expT=[mat, mat.copy()],
                  expTinv=[inv, inv.copy()], vertices=[up, do],
-                 params=dict(lattice=lattice, L1=L1, L2=L2, t=t, U=U, chem=chem, tperp=tperp))
+                 params=dict(lattice=lattice, L1=L1, L2=L2, t=t, U=U, chem=chem, tperp=tperp,
+                             site_order=site_order))
 
 
 def kondo(L1: int = 12, L2: int = 12, t: float = 1.0, JK: float = 1.5, Uf: float = 2.0,
           chem: float = 0.0, beta: float = 10.0, dtau: float = 0.1, nwrap: int = 10,
-          n_sun: int = 2) -> Model:
+          n_sun: int = 2, site_order: str = "natural") -> Model:
     """SU(N) Kondo lattice on the bilayer square lattice (N_FL = 1).
 
     Vertex order follows Hamiltonian_Kondo_smod.F90:464-530: first the ``Uf``
@@ -332,7 +381,7 @@ def kondo(L1: int = 12, L2: int = 12, t: float = 1.0, JK: float = 1.5, Uf: float
     one ``V_SUN`` vertex per c-f pair with ``JK/2`` (N_SUN = 2 branch).
     """
     ltrot = int(round(beta / dtau))
-    O = hopping_matrix("BILAYER_SQUARE", L1, L2, t=t, chem=chem, t2=0.0, tperp=0.0)
+    O = hopping_matrix("BILAYER_SQUARE", L1, L2, t=t, chem=chem, t2=0.0, tperp=0.0, site_order=site_order)
     N = O.shape[0]
     mat, inv = exp_hopping(O, dtau)
     verts = []
@@ -352,7 +401,8 @@ def kondo(L1: int = 12, L2: int = 12, t: float = 1.0, JK: float = 1.5, Uf: float
             verts.append(op_set(Vertex(P=[c, f], O=Oj, g=g, alpha=0.0, op_type=2)))
     return Model(name=f"kondo_bilayer_{L1}x{L2}", ndim=N, n_fl=1, n_sun=n_sun, ltrot=ltrot,
                  nwrap=nwrap, dtau=dtau, beta=beta, expT=[mat], expTinv=[inv], vertices=[verts],
-                 params=dict(lattice="bilayer_square", L1=L1, L2=L2, t=t, JK=JK, Uf=Uf, chem=chem))
+                 params=dict(lattice="bilayer_square", L1=L1, L2=L2, t=t, JK=JK, Uf=Uf, chem=chem,
+                             site_order=site_order))
 
 
 # Named workloads (sizes as quoted in the project's benchmark configurations).
