@@ -468,7 +468,9 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded fields and draws)",
-                "config": dict(workload, chains_per_gpu=1, parallelism="host cores"),
+                "config": dict(workload, chains_per_gpu=1, parallelism="host cores",
+                               l2="not applicable (host run; the sample's working set is the chain's own state)",
+                               draws="host arrays of the same counter stream"),
                 "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
                                  "sample": f"{slices} time slices of one sweep (with their stabilisations"
                           + ("; TAU_M, which runs after the down pass, is outside the sample" if ltau else "")
