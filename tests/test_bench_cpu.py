@@ -26,3 +26,20 @@ def test_sweep_roofline_of_each_form():
     expect = (fl["decompose"] + fl["cgr"]) / 1e12 + (fl["wraps"] + fl["propagate"] + fl["rank1"]) / 2e15
     assert abs(rmx["t_roof_ms"] - 1e3 * expect) < 1e-9 * rmx["t_roof_ms"]
     assert rmx["t_roof_ms"] < r64["t_roof_ms"]
+
+
+def test_reference_arm_prints_one_contract_line():
+    # the host-core arm runs without a GPU: one JSON line with the reference markers
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--config",
+                          "hubbard4x4", "--steps", "2", "--warmup", "1"], capture_output=True, text=True,
+                         timeout=300, check=True).stdout.strip().splitlines()
+    d = json.loads(out[-1])
+    assert d["impl"] == "reference" and d["unit"] == "sweeps/s" and d["value"] > 0
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["higher_is_better"] is True and d["steps"] == 2 and d["warmup"] == 1
