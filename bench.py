@@ -212,7 +212,16 @@ def sweep_roofline(m, n_acc: float, ltau: int, chains: int, ms_per_step: float, 
     every chain).  FP64 form: every phase at the FP64 rate.  Mixed form: the wraps,
     propagation and rank-k flushes at the BF16 tensor peak, the QR / CGR phases at the FP64
     rate.  frac = t_roof / measured step time."""
-    fl = {k: v * chains for k, v in sweep_flops(m, n_acc, ltau).items()}
+    return sweep_roofline_groups([(m, n_acc, ltau, chains)], ms_per_step, precision, p_fp64, p_bf16)
+
+
+def sweep_roofline_groups(groups, ms_per_step: float, precision: str, p_fp64: float, p_bf16: float) -> dict:
+    """The same over several handles run one after the other in a step: groups of
+    (model, accepted flips per chain and sweep, ltau, chains)."""
+    fl = {}
+    for m, n_acc, ltau, chains in groups:
+        for k, v in sweep_flops(m, n_acc, ltau).items():
+            fl[k] = fl.get(k, 0.0) + v * chains
     t = 0.0
     for k, v in fl.items():
         peak = p_bf16 if (precision != "fp64" and k in _TENSOR_PHASES) else p_fp64
@@ -300,6 +309,11 @@ def run_batch(args, ws, rank, local):
                 e1.synchronize()
                 ms += e0.elapsed_time(e1)
     n_launch = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs) - n0
+    # per group for the whole-sweep roofline: the adapted Nwrap, accepted flips per chain and sweep
+    import dataclasses
+    rgroups = [(dataclasses.replace(m, nwrap=ch.nwrap()),
+                sum(ch.stats(k).n_acc for k in range(len(mem))) / float(args.steps * len(mem)), 0, len(mem))
+               for ch, m, mem in hs]
     h2d = d2h = 0
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -317,7 +331,8 @@ def run_batch(args, ws, rank, local):
     out = dict(t_dev=ms / 1e3, t_e2e=e2e_s, clocks=clk.summary(), launches=n_launch, h2d=h2d, d2h=d2h,
                nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem),
                                         "nwrap": nw, "xmaxG_at_adapt": worst}
-                                       for (_, m, mem), (nw, worst) in zip(hs, nwraps)], xmaxG=xmax)
+                                       for (_, m, mem), (nw, worst) in zip(hs, nwraps)], xmaxG=xmax,
+               rgroups=rgroups)
     for ch, _, _ in hs:
         ch.close()
     return out
@@ -429,6 +444,26 @@ def cpu_oracle_rate(m, seed: int, threads: int, slices: int, ltau: int = 0):
     return (slices / (2.0 * m.ltrot)) / dt, dt
 
 
+def batch_cpu_baseline(seed: int, slices: int = 10):
+    """One host core on the batch: per (L, beta) group a bounded oracle sample (``slices`` time
+    slices of one chain, by default Nwrap of them with the one stabilisation they end in, so
+    the sample holds the sweep's own mix; scaled to a sweep); a step costs the sum
+    over all chains, so the aggregate rate is chains / sum of per-chain sweep times."""
+    from alf_gb300 import model as mdl
+    groups = batch128_groups(seed)
+    t_step, t_sample, n = 0.0, 0.0, 0
+    for (L, beta), members in sorted(groups.items()):
+        m = mdl.hubbard("square", L, L, U=members[0][1], beta=beta, dtau=0.1, nwrap=10)
+        rate, dt = cpu_oracle_rate(m, seed, 1, min(slices, 2 * m.ltrot), 0)
+        t_step += len(members) / rate
+        t_sample += dt
+        n += len(members)
+    return {"value": n / t_step, "unit": "sweeps/s", "cores": 1, "kind": "port",
+            "sample": f"{slices} time slices (with their stabilisations) of one chain per (L, beta) group, "
+                      f"scaled to a sweep and summed over the {n} chains ({t_sample:.1f} s); CPU restatement "
+                      f"of ALF's sweep with single-threaded OpenBLAS"}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -487,6 +522,12 @@ def main():
             return
         from alf_gb300 import replicas
         t_dev, t_e2e = rb["t_dev"], rb["t_e2e"]
+        cpu = None
+        if not args.no_cpu_baseline:
+            try:
+                cpu = batch_cpu_baseline(replicas.replica_seed(args.seed, rank))
+            except Exception as e:  # the baseline is reported, never required
+                cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
         value = ws * rb["nchains"] * args.steps / t_dev
         line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
@@ -497,8 +538,10 @@ def main():
                                parallelism=f"replicas x{ws}", delay_depth="default"),
                 "e2e": {"value": ws * rb["nchains"] * args.steps / t_e2e, "unit": "sweeps/s",
                         "h2d_bytes_per_step": rb["h2d"], "d2h_bytes_per_step": rb["d2h"]},
-                "roofline": None, "cpu_baseline": None, "clocks": rb["clocks"], "gpu_launches": int(rb["launches"]),
-                "precision_green": {"xmaxG": rb["xmaxG"]}}
+                "roofline": None, "cpu_baseline": cpu, "clocks": rb["clocks"], "gpu_launches": int(rb["launches"]),
+                "precision_green": {"xmaxG": rb["xmaxG"]},
+                "sweep_roofline": sweep_roofline_groups(rb["rgroups"], 1e3 * t_dev / args.steps, args.precision,
+                                                        FP64_DMMA_TFLOPS, measured_bf16_peak()[0])}
         print(json.dumps(line))
         return
 

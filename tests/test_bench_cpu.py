@@ -43,3 +43,13 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"] == {"value": d["value"], "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["higher_is_better"] is True and d["steps"] == 2 and d["warmup"] == 1
+
+
+def test_grouped_roofline_sums_the_groups():
+    a = mdl.hubbard("square", 6, 6, beta=4.0)
+    b = mdl.config("hubbard16x16")
+    g = bench.sweep_roofline_groups([(a, 100.0, 0, 3), (b, 2000.0, 0, 2)], 1000.0, "mixed", 1.0, 2000.0)
+    one = bench.sweep_roofline(a, 100.0, 0, 3, 1000.0, "mixed", 1.0, 2000.0)
+    two = bench.sweep_roofline(b, 2000.0, 0, 2, 1000.0, "mixed", 1.0, 2000.0)
+    assert abs(g["t_roof_ms"] - one["t_roof_ms"] - two["t_roof_ms"]) < 1e-9 * g["t_roof_ms"]
+    assert abs(g["flops_per_step"] - one["flops_per_step"] - two["flops_per_step"]) < 1e-6 * g["flops_per_step"]
