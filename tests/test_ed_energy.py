@@ -281,3 +281,41 @@ def test_kondo_two_site_vertices_match_the_trotterized_values():
     mean, err = a.mean(axis=0), a.std(axis=0, ddof=1) / np.sqrt(n_bins)
     assert np.all(err < 0.05), err
     assert np.all(np.abs(mean - ex) < 4.0 * err), (mean, err, ex)
+
+
+def test_lattice_correlations_of_the_ring_match_the_trotterized_values():
+    # the SpinZ and Den lattice observables (Predefined_Obs measurements on the oracle's
+    # ham%Obser G, alf_gb300.lattice_obs) against N <m_r m_0> and N <n_r n_0> of the exact
+    # Trotterized ensemble, m = n_up - n_do, n = n_up + n_do, r over Make_lattice's list
+    from alf_gb300 import lattice_obs as lo
+
+    m, fk, _, B = _transfer(0.1)
+    P = np.linalg.matrix_power(B, m.ltrot)
+    Z = np.trace(P)
+    L = lo.Lattice("n_leg_ladder", L_SITES, 1)
+    mz = [fk.n(0, i) - fk.n(1, i) for i in range(L_SITES)]
+    nn = [fk.n(0, i) + fk.n(1, i) for i in range(L_SITES)]
+    ex = {"SpinZ": np.array([L_SITES * np.trace(mz[i1 % L_SITES] @ mz[0] @ P) / Z for i1, _ in L.list]).real,
+          "Den": np.array([L_SITES * np.trace(nn[i1 % L_SITES] @ nn[0] @ P) / Z for i1, _ in L.list]).real}
+    o = oracle.Oracle(m)
+    seed = 31
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    for s in range(100):
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+    eq, _ = o.collect_measurements()
+    obs = lo.EqualTimeObs(L, n_sun=m.n_sun)
+    bins = []
+    for b in range(20):
+        for s in range(100):
+            eq.clear()
+            o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 100 + 100 * b + s))
+            for _, G, ph in eq:
+                obs.measure(G, ph)
+        bins.append(obs.bin())
+    for k in ("SpinZ", "Den"):
+        a = np.array([bb[k]["latt"][:, 0, 0, 0].real for bb in bins])
+        mean, err = a.mean(axis=0), a.std(axis=0, ddof=1) / np.sqrt(len(bins))
+        assert np.all(np.abs(mean - ex[k]) < 4.0 * err + 1e-12), (k, mean, err, ex[k])
+    # backgrounds: <m> = 0 and <n> = 1 per site at half filling
+    assert abs(np.mean([bb["Den"]["latt0"][0].real for bb in bins]) - 1.0) < 1e-9

@@ -1,0 +1,125 @@
+"""Lattice-resolved equal-time observables on the host (alf_gb300.lattice_obs): Make_lattice's
+walks and imj, the R -> K transform, the Predefined_Obs measurements against plain per-site
+loops, the legacy ``*_eq`` files, and the spin and density correlations of the 4-site ring
+against the exact Trotterized values."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from alf_gb300 import lattice_obs as lo, model as mdl
+
+
+@pytest.mark.parametrize("lat,L1,L2", [("square", 4, 4), ("square", 6, 4), ("honeycomb", 6, 6),
+                                       ("bilayer_square", 4, 4), ("n_leg_ladder", 4, 2), ("n_leg_ladder", 4, 1)])
+def test_walks_tile_and_imj_is_the_folded_difference(lat, L1, L2):
+    L = lo.Lattice(lat, L1, L2)
+    A = np.array([L.L1p, L.L2p]).T  # columns: the periods
+    for i in range(L.N):
+        for j in range(L.N):
+            d = L.R[i] - L.R[j] - L.R[L.imj[i, j]]
+            n = np.linalg.solve(A, d)  # integer multiples of the periods
+            assert np.allclose(n, np.round(n), atol=1e-9), (i, j)
+    # the k points are distinct modulo the reciprocal periods
+    B = np.array([L.b1 * L.L1, L.b2 * L.n2]).T
+    fr = np.linalg.solve(B, L.K.T).T
+    keys = {tuple(np.round(np.mod(f, 1.0) * 1e6).astype(int) % 1000000) for f in fr}
+    assert len(keys) == L.N
+    # the list is the one model.alf_cell_order walks
+    assert [(i1 % L1) + L1 * (i2 % L.n2) for i1, i2 in L.list] == mdl.alf_cell_order(lat, L1, L2)
+
+
+def test_square_walk_order():
+    L = lo.Lattice("square", 4, 4)
+    assert L.list == [(i1, i2) for i1 in (-1, 0, 1, 2) for i2 in (-1, 0, 1, 2)]
+    np.testing.assert_allclose(L.b1, [math.pi / 2, 0.0], atol=1e-15)
+    np.testing.assert_allclose(L.b2, [0.0, math.pi / 2], atol=1e-15)
+
+
+def test_fourier_of_a_delta_and_of_a_plane_wave():
+    L = lo.Lattice("honeycomb", 3, 3)
+    x = np.zeros(L.N, complex)
+    x[L.list.index((0, 0))] = 1.0
+    np.testing.assert_allclose(L.fourier_r_to_k(x), np.full(L.N, 1.0 / L.N), atol=1e-15)
+    k0 = 4
+    wave = np.exp(1j * (L.R @ L.K[k0]))
+    xk = L.fourier_r_to_k(wave)
+    e = np.zeros(L.N)
+    e[k0] = 1.0
+    np.testing.assert_allclose(xk, e, atol=1e-12)
+
+
+def _loop_measure(L, G, phase, n_sun):
+    """Predefined_Obs_eq_{Green,SpinMz,Den}_measure written out per site pair."""
+    nd = G.shape[1]
+    GR = lambda i, j, f: G[f][i, j]
+    GRC = lambda i, j, f: (1.0 if i == j else 0.0) - G[f][j, i]
+    zp, zs = phase / phase.real, np.sign(phase.real)
+    no = L.norb
+    obs = {k: np.zeros((L.N, no, no), complex) for k in lo.EQ_NAMES}
+    obs0 = {k: np.zeros(no, complex) for k in lo.EQ_NAMES}
+    for i1 in range(nd):
+        I, oi = L.site_cell[i1], L.site_orb[i1]
+        zi = n_sun * (GRC(i1, i1, 0) + GRC(i1, i1, 1))
+        for j1 in range(nd):
+            J, oj = L.site_cell[j1], L.site_orb[j1]
+            r = L.imj[I, J]
+            obs["Green"][r, oi, oj] += n_sun * (GRC(i1, j1, 0) + GRC(i1, j1, 1)) * zp * zs
+            zxy = GRC(i1, j1, 0) * GR(i1, j1, 1) + GRC(i1, j1, 1) * GR(i1, j1, 0)
+            zz = (GRC(i1, j1, 0) * GR(i1, j1, 0) + GRC(i1, j1, 1) * GR(i1, j1, 1)
+                  + (GRC(i1, i1, 1) - GRC(i1, i1, 0)) * (GRC(j1, j1, 1) - GRC(j1, j1, 0)))
+            obs["SpinZ"][r, oi, oj] += zz * zp * zs
+            obs["SpinXY"][r, oi, oj] += zxy * zp * zs
+            obs["SpinT"][r, oi, oj] += (2 * zxy + zz) * zp * zs / 3.0
+            zj = n_sun * (GRC(j1, j1, 0) + GRC(j1, j1, 1))
+            z = n_sun * (GRC(i1, j1, 0) * GR(i1, j1, 0) + GRC(i1, j1, 1) * GR(i1, j1, 1))
+            obs["Den"][r, oi, oj] += (zi * zj + z) * zp * zs
+        dz = GRC(i1, i1, 1) - GRC(i1, i1, 0)
+        obs0["SpinZ"][oi] += dz * zp * zs
+        obs0["SpinT"][oi] += dz * zp * zs / math.sqrt(3.0)
+        obs0["Den"][oi] += zi * zp * zs
+    return obs, obs0
+
+
+@pytest.mark.parametrize("order", ["natural", "alf"])
+def test_measurements_equal_the_per_site_loops(order):
+    L = lo.Lattice("honeycomb", 2, 3, site_order=order)
+    nd = L.N * L.norb
+    r = np.random.default_rng(11)
+    G = r.standard_normal((2, nd, nd)) + 1j * r.standard_normal((2, nd, nd))
+    ph = complex(0.8, 0.3)
+    m = lo.EqualTimeObs(L, n_sun=1)
+    m.measure(G, ph)
+    m.measure(G, ph)
+    b = m.bin()
+    ref, ref0 = _loop_measure(L, G, ph, 1)
+    for k in lo.EQ_NAMES:
+        np.testing.assert_allclose(b[k]["latt"][:, 0], ref[k], rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(b[k]["latt0"], ref0[k] / L.N, rtol=1e-13, atol=1e-13)
+        assert b[k]["sign"] == 1.0
+    assert m.count == 0
+
+
+def test_eq_files_round_trip(tmp_path):
+    L = lo.Lattice("honeycomb", 2, 2)
+    nd = L.N * L.norb
+    r = np.random.default_rng(2)
+    m = lo.EqualTimeObs(L, n_sun=1)
+    bins = []
+    for _ in range(2):
+        G = r.standard_normal((2, nd, nd)) * 0.3 + 0.5 * np.eye(nd)[None]
+        m.measure(G.astype(complex), complex(1.0, 0.0))
+        bins.append(m.bin())
+        lo.write_eq_bin(str(tmp_path), "SpinZ", bins[-1]["SpinZ"], L, dtau=0.1)
+    back = lo.read_eq(str(tmp_path / "SpinZ_eq"))
+    assert len(back) == 2
+    for b, rd in zip(bins, back):
+        assert rd["sign"] == b["SpinZ"]["sign"]
+        np.testing.assert_array_equal(rd["latt0"], b["SpinZ"]["latt0"])
+        np.testing.assert_array_equal(rd["k"], L.K)
+        want = np.stack([L.fourier_r_to_k(b["SpinZ"]["latt"][:, 0, a, c]) for a in range(2) for c in range(2)], axis=1)
+        np.testing.assert_array_equal(rd["values"].reshape(L.N, 4), want)
+    info = open(tmp_path / "SpinZ_eq_info").read().splitlines()
+    assert info[0] == "          Observable: SpinZ_eq" and info[2].endswith(" 1") and "Bravais" in info[4]
+    assert os.path.getsize(tmp_path / "SpinZ_eq_info") > 0
