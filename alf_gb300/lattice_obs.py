@@ -1,4 +1,4 @@
-"""Lattice-resolved equal-time observables and their legacy ``*_eq`` bins, on the host.
+"""Lattice-resolved equal-time and time-displaced observables and their legacy bins, on the host.
 
 The sweep hands every equal-time Green function to ``ham%Obser`` (the library's observable
 callback).  For callers without ALF's Fortran driver, this module restates what the Hubbard
@@ -11,11 +11,14 @@ models do there with the lattice:
   Prog/Predefined_Latt_mod.F90:100-262;
 * the measurements Predefined_Obs_eq_Green_measure, _SpinMz_measure and _Den_measure
   (Prog/Predefined_Obs_mod.F90:137-330) as Hamiltonian_Hubbard_smod.F90:776-790 calls them
-  for N_FL = 2: Green, SpinZ, SpinXY, SpinT, Den;
+  for N_FL = 2: Green, SpinZ, SpinXY, SpinT, Den; and their time-displaced versions
+  Predefined_Obs_tau_*_measure (Predefined_Obs_mod.F90:330-600) on the TAU_M quartets, as
+  ham%ObserT calls them (Hamiltonian_Hubbard_smod.F90:847-850);
 * Print_bin_Latt's legacy output (Prog/observables_mod.F90:355-500): Obs_Latt / N,
   Obs_Latt0 / (N Ns Ntau), Ave_sign / N, the transform to k space
   X(k) = 1/Ns sum_R exp(-i k.R) X(R) (FT_R_to_K_C, lattices_v3_mod.F90:847-872), one
-  ``<name>_eq_info`` file and one block per bin appended to ``<name>_eq``.
+  ``<name>_eq_info`` (``_tau_info``) file and one block per bin appended to ``<name>_eq``
+  (``<name>_tau``).
 
 Sites are numbered as the model numbers them (``model.hopping_matrix``'s ``site_order``):
 site = cell * Norb + orbital, cells in natural order or in Make_lattice's order.
@@ -170,6 +173,71 @@ class EqualTimeObs:
         return out
 
 
+class TimeDisplacedObs:
+    """Obs_tau of the Hubbard models with N_FL = 2 on the quartets of ham%ObserT at
+    NT = 0..Ltrot: Obs_Latt(imj, NT + 1, no_I, no_J), Obs_Latt0(no); N and Ave_sign count
+    the NT = 0 calls."""
+
+    def __init__(self, latt: Lattice, n_sun: int, ntau: int):
+        self.latt, self.n_sun, self.ntau = latt, n_sun, ntau
+        self.reset()
+
+    def reset(self):
+        no, N = self.latt.norb, self.latt.N
+        self.obs = {k: np.zeros((N, self.ntau, no, no), np.complex128) for k in EQ_NAMES}
+        self.obs0 = {k: np.zeros(no, np.complex128) for k in EQ_NAMES}
+        self.count, self.sign = 0, 0.0
+
+    def measure(self, nt: int, GT0, G0T, G00, GTT, phase: complex):
+        """One ham%ObserT call: NT and the quartet, each [n_fl][row][col]."""
+        GT0, G0T, G00, GTT = (np.asarray(x) for x in (GT0, G0T, G00, GTT))
+        if GT0.shape[0] != 2:
+            raise ValueError("the N_FL = 2 observables need both flavours")
+        zp = phase / phase.real
+        zs = float(np.sign(phase.real))
+        w = zp * zs
+        if nt == 0:
+            self.count += 1
+            self.sign += zs
+        L = self.latt
+        nd = GT0.shape[1]
+        rows = L.imj[np.ix_(L.site_cell, L.site_cell)]
+        oi = np.broadcast_to(L.site_orb[:, None], (nd, nd))
+        oj = np.broadcast_to(L.site_orb[None, :], (nd, nd))
+        ns = self.n_sun
+        g0t = [G0T[f].T for f in range(2)]  # g0t[f][I1][J1] = G0T(J1, I1, f)
+
+        def add(name, val):
+            np.add.at(self.obs[name][:, nt], (rows, oi, oj), val * w)
+
+        add("Green", (GT0[0] + GT0[1]) / 2.0)
+        dtt = np.diag(GTT[0]) - np.diag(GTT[1])
+        d00 = np.diag(G00[0]) - np.diag(G00[1])
+        zz = dtt[:, None] * d00[None, :] - g0t[0] * GT0[0] - g0t[1] * GT0[1]
+        zxy = -g0t[0] * GT0[1] - g0t[1] * GT0[0]
+        add("SpinZ", zz)
+        add("SpinXY", zxy)
+        add("SpinT", (2.0 * zxy + zz) / 3.0)
+        np.add.at(self.obs0["SpinZ"], L.site_orb, -dtt * w)
+        np.add.at(self.obs0["SpinT"], L.site_orb, -dtt * w / math.sqrt(3.0))
+        zi = ns * ((1.0 - np.diag(GTT[0])) + (1.0 - np.diag(GTT[1])))
+        zj = ns * ((1.0 - np.diag(G00[0])) + (1.0 - np.diag(G00[1])))
+        z = -ns * (g0t[0] * GT0[0] + g0t[1] * GT0[1])
+        add("Den", zi[:, None] * zj[None, :] + z)
+        np.add.at(self.obs0["Den"], L.site_orb, zi * w)
+
+    def bin(self, reset: bool = True) -> Dict[str, dict]:
+        """Obs_Latt / N, Obs_Latt0 / (N Ns Ntau), Ave_sign / N."""
+        if self.count == 0:
+            raise ValueError("an empty bin")
+        n, ns = self.count, self.latt.N
+        out = {k: {"latt": self.obs[k] / n, "latt0": self.obs0[k] / (n * ns * self.ntau), "sign": self.sign / n}
+               for k in EQ_NAMES}
+        if reset:
+            self.reset()
+        return out
+
+
 def _a20(label: str) -> str:
     return label.rjust(20) + ": "
 
@@ -177,13 +245,21 @@ def _a20(label: str) -> str:
 def write_eq_bin(directory: str, name: str, b: dict, latt: Lattice, dtau: float, channel: str = "--") -> None:
     """Append one bin to ``<name>_eq`` (and write ``<name>_eq_info`` once), as the legacy
     branch of Print_bin_Latt does for Ntau = 1."""
+    write_latt_bin(directory, name, b, latt, dtau, channel)
+
+
+def write_latt_bin(directory: str, name: str, b: dict, latt: Lattice, dtau: float, channel: str = "--") -> None:
+    """Append one bin to ``<name>_eq`` (Ntau = 1) or ``<name>_tau`` (Ntau > 1, the time
+    slices taken from the bin) and write the ``_info`` file once (Print_bin_Latt)."""
+    ntau = b["latt"].shape[1]
+    suff = "_eq" if ntau == 1 else "_tau"
     os.makedirs(directory, exist_ok=True)
-    base = os.path.join(directory, f"{name}_eq")
+    base = os.path.join(directory, f"{name}{suff}")
     if not os.path.exists(base + "_info"):
         with open(base + "_info", "w") as f:
-            f.write(_a20("Observable") + f"{name}_eq\n")
+            f.write(_a20("Observable") + f"{name}{suff}\n")
             f.write(_a20("Channel") + f"{channel}\n")
-            f.write(_a20("Ntau") + f"{1:10d}\n")
+            f.write(_a20("Ntau") + f"{ntau:10d}\n")
             f.write(_a20("dtau") + fortran_e(dtau, 26, 17) + "\n")
             f.write("       ====== Bravais Lattice ======\n")
             f.write(_a20("Unit cells") + f"{latt.N:10d}\n")
@@ -195,15 +271,18 @@ def write_eq_bin(directory: str, name: str, b: dict, latt: Lattice, dtau: float,
             f.write(_a20("Ndim") + f"{len(latt.orb_pos[0]):10d}\n")
             for no, pos in enumerate(latt.orb_pos, start=1):
                 f.write(_a20(f"Orbital {no}") + "".join(fortran_e(x, 26, 17) for x in pos) + "\n")
-    xk = np.stack([latt.fourier_r_to_k(b["latt"][:, 0, no, no1]) for no in range(latt.norb)
-                   for no1 in range(latt.norb)], axis=1)  # [k][no * norb + no1]
+    xk = np.stack([latt.fourier_r_to_k(b["latt"][:, nt, no, no1]) for nt in range(ntau) for no in range(latt.norb)
+                   for no1 in range(latt.norb)], axis=1)  # [k][(nt * norb + no) * norb + no1]
 
     def cz(z):
         z = complex(z)
         return f"({fortran_e(z.real, 25, 17)},{fortran_e(z.imag, 25, 17)})"
 
     with open(base, "a") as f:
-        f.write(f"{fortran_e(b['sign'], 25, 17)}{latt.norb:11d}{latt.N:11d}\n")
+        if ntau == 1:
+            f.write(f"{fortran_e(b['sign'], 25, 17)}{latt.norb:11d}{latt.N:11d}\n")
+        else:
+            f.write(f"{fortran_e(b['sign'], 25, 17)}{latt.norb:11d}{latt.N:11d}{ntau:11d}{fortran_e(dtau, 26, 17)}\n")
         for no in range(latt.norb):
             f.write(cz(b["latt0"][no]) + "\n")
         for k in range(latt.N):
@@ -217,8 +296,9 @@ _CPLX = re.compile(r"^\(\s*(" + _NUM + r")\s*,\s*(" + _NUM + r")\s*\)$")
 
 
 def read_eq(path: str) -> List[dict]:
-    """All bins of a legacy ``<name>_eq`` file: per bin the sign, the background
-    [norb], the k points [Ns][2] and the k-space values [Ns][norb][norb]."""
+    """All bins of a legacy ``<name>_eq`` or ``<name>_tau`` file: per bin the sign, the
+    background [norb], the k points [Ns][2] and the k-space values [Ns][Ntau][norb][norb]
+    ([Ns][norb][norb] for ``_eq``)."""
     with open(path) as f:
         lines = [ln.strip() for ln in f if ln.strip()]
 
@@ -232,15 +312,17 @@ def read_eq(path: str) -> List[dict]:
     while p < len(lines):
         head = lines[p].split()
         sign, norb, ns = float(head[0]), int(head[1]), int(head[2])
+        ntau = int(head[3]) if len(head) > 3 else 1
         p += 1
         back = np.array([z(lines[p + i]) for i in range(norb)])
         p += norb
-        ks, vals = np.zeros((ns, 2)), np.zeros((ns, norb, norb), np.complex128)
+        ks, vals = np.zeros((ns, 2)), np.zeros((ns, ntau, norb, norb), np.complex128)
         for k in range(ns):
             ks[k] = [float(x) for x in lines[p].split()]
             p += 1
-            for i in range(norb * norb):
-                vals[k, i // norb, i % norb] = z(lines[p + i])
-            p += norb * norb
-        out.append({"sign": sign, "latt0": back, "k": ks, "values": vals})
+            for i in range(ntau * norb * norb):
+                vals[k, i // (norb * norb), (i // norb) % norb, i % norb] = z(lines[p + i])
+            p += ntau * norb * norb
+        out.append({"sign": sign, "latt0": back, "k": ks, "values": vals[:, 0] if len(head) <= 3 else vals,
+                    **({"dtau": float(head[4])} if len(head) > 4 else {})})
     return out

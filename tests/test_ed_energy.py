@@ -319,3 +319,43 @@ def test_lattice_correlations_of_the_ring_match_the_trotterized_values():
         assert np.all(np.abs(mean - ex[k]) < 4.0 * err + 1e-12), (k, mean, err, ex[k])
     # backgrounds: <m> = 0 and <n> = 1 per site at half filling
     assert abs(np.mean([bb["Den"]["latt0"][0].real for bb in bins]) - 1.0) < 1e-9
+
+
+def test_time_displaced_lattice_correlations_of_the_ring_match_the_trotterized_values():
+    # SpinZ(r, tau) and Den(r, tau) from the oracle's TAU_M quartets (Predefined_Obs_tau_*
+    # measurements, alf_gb300.lattice_obs) against N <O_r(tau) O_0(0)> of the exact
+    # Trotterized ensemble at every tau
+    from alf_gb300 import lattice_obs as lo
+
+    m, fk, _, B = _transfer(0.1)
+    Lt = m.ltrot
+    A = [np.eye(fk.dim)]
+    for _ in range(Lt):
+        A.append(B @ A[-1])
+    Z = np.trace(A[Lt])
+    L = lo.Lattice("n_leg_ladder", L_SITES, 1)
+    mz = [fk.n(0, i) - fk.n(1, i) for i in range(L_SITES)]
+    nn = [fk.n(0, i) + fk.n(1, i) for i in range(L_SITES)]
+    ex = {k: np.array([[L_SITES * np.trace(A[Lt - t] @ ops[i1 % L_SITES] @ A[t] @ ops[0]) / Z
+                        for t in range(Lt + 1)] for i1, _ in L.list]).real
+          for k, ops in (("SpinZ", mz), ("Den", nn))}
+    o = oracle.Oracle(m, ltau=1)
+    seed = 77
+    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+    o.init_state()
+    for s in range(100):
+        o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, s))
+    _, tau = o.collect_measurements()
+    obs = lo.TimeDisplacedObs(L, n_sun=m.n_sun, ntau=Lt + 1)
+    bins = []
+    for b in range(20):
+        for s in range(100):
+            tau.clear()
+            o.sweep(rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 100 + 100 * b + s))
+            for nt, (gt0, g0t, g00, gtt), ph in tau:
+                obs.measure(nt, gt0, g0t, g00, gtt, ph)
+        bins.append(obs.bin())
+    for k in ("SpinZ", "Den"):
+        a = np.array([bb[k]["latt"][:, :, 0, 0].real for bb in bins])
+        mean, err = a.mean(axis=0), a.std(axis=0, ddof=1) / np.sqrt(len(bins))
+        assert np.all(np.abs(mean - ex[k]) < 4.0 * err + 1e-9), (k, np.max(np.abs(mean - ex[k]) / (err + 1e-300)))

@@ -1,7 +1,8 @@
-"""Lattice-resolved equal-time observables on the host (alf_gb300.lattice_obs): Make_lattice's
-walks and imj, the R -> K transform, the Predefined_Obs measurements against plain per-site
-loops, the legacy ``*_eq`` files, and the spin and density correlations of the 4-site ring
-against the exact Trotterized values."""
+"""Lattice-resolved observables on the host (alf_gb300.lattice_obs): Make_lattice's walks and
+imj, the R -> K transform, the equal-time and time-displaced Predefined_Obs measurements
+against plain per-site loops, and the legacy ``*_eq`` / ``*_tau`` files.  Their physics (spin
+and density correlations of the 4-site ring against exact Trotterized values) is tested in
+test_ed_energy.py."""
 import math
 import os
 
@@ -123,3 +124,62 @@ def test_eq_files_round_trip(tmp_path):
     info = open(tmp_path / "SpinZ_eq_info").read().splitlines()
     assert info[0] == "          Observable: SpinZ_eq" and info[2].endswith(" 1") and "Bravais" in info[4]
     assert os.path.getsize(tmp_path / "SpinZ_eq_info") > 0
+
+
+def _loop_measure_tau(L, nt, GT0, G0T, G00, GTT, phase, n_sun):
+    """Predefined_Obs_tau_{Green,SpinMz,Den}_measure written out per site pair."""
+    nd = GT0.shape[1]
+    w = phase / phase.real * np.sign(phase.real)
+    no = L.norb
+    obs = {k: np.zeros((L.N, no, no), complex) for k in lo.EQ_NAMES}
+    obs0 = {k: np.zeros(no, complex) for k in lo.EQ_NAMES}
+    for i1 in range(nd):
+        I, oi = L.site_cell[i1], L.site_orb[i1]
+        zi = n_sun * sum(1.0 - GTT[f][i1, i1] for f in range(2))
+        for j1 in range(nd):
+            J, oj = L.site_cell[j1], L.site_orb[j1]
+            r = L.imj[I, J]
+            obs["Green"][r, oi, oj] += (GT0[0][i1, j1] + GT0[1][i1, j1]) / 2.0 * w
+            zz = ((GTT[0][i1, i1] - GTT[1][i1, i1]) * (G00[0][j1, j1] - G00[1][j1, j1])
+                  - G0T[0][j1, i1] * GT0[0][i1, j1] - G0T[1][j1, i1] * GT0[1][i1, j1])
+            zxy = -G0T[0][j1, i1] * GT0[1][i1, j1] - G0T[1][j1, i1] * GT0[0][i1, j1]
+            obs["SpinZ"][r, oi, oj] += zz * w
+            obs["SpinXY"][r, oi, oj] += zxy * w
+            obs["SpinT"][r, oi, oj] += (2 * zxy + zz) / 3.0 * w
+            zj = n_sun * sum(1.0 - G00[f][j1, j1] for f in range(2))
+            z = -n_sun * sum(G0T[f][j1, i1] * GT0[f][i1, j1] for f in range(2))
+            obs["Den"][r, oi, oj] += (zi * zj + z) * w
+        d = GTT[1][i1, i1] - GTT[0][i1, i1]
+        obs0["SpinZ"][oi] += d * w
+        obs0["SpinT"][oi] += d * w / math.sqrt(3.0)
+        obs0["Den"][oi] += zi * w
+    return obs, obs0
+
+
+def test_time_displaced_measurements_equal_the_per_site_loops_and_round_trip(tmp_path):
+    L = lo.Lattice("square", 2, 3, site_order="alf")
+    nd = L.N * L.norb
+    r = np.random.default_rng(4)
+    ntau = 3
+    m = lo.TimeDisplacedObs(L, n_sun=1, ntau=ntau)
+    ref = {k: np.zeros((L.N, ntau, 1, 1), complex) for k in lo.EQ_NAMES}
+    ref0 = {k: np.zeros(1, complex) for k in lo.EQ_NAMES}
+    ph = complex(-0.7, 0.2)
+    for nt in range(ntau):
+        q = [r.standard_normal((2, nd, nd)) + 1j * r.standard_normal((2, nd, nd)) for _ in range(4)]
+        m.measure(nt, *q, ph)
+        o, o0 = _loop_measure_tau(L, nt, *q, ph, 1)
+        for k in lo.EQ_NAMES:
+            ref[k][:, nt] += o[k]
+            ref0[k] += o0[k]
+    b = m.bin()
+    for k in lo.EQ_NAMES:
+        np.testing.assert_allclose(b[k]["latt"], ref[k], rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(b[k]["latt0"], ref0[k] / (L.N * ntau), rtol=1e-13, atol=1e-13)
+        assert b[k]["sign"] == -1.0
+    lo.write_latt_bin(str(tmp_path), "Den", b["Den"], L, dtau=0.05)
+    back = lo.read_eq(str(tmp_path / "Den_tau"))
+    assert len(back) == 1 and back[0]["dtau"] == 0.05 and back[0]["values"].shape == (L.N, ntau, 1, 1)
+    for nt in range(ntau):
+        np.testing.assert_array_equal(back[0]["values"][:, nt, 0, 0], L.fourier_r_to_k(b["Den"]["latt"][:, nt, 0, 0]))
+    assert open(tmp_path / "Den_tau_info").readline().rstrip() == "          Observable: Den_tau"
