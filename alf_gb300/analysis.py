@@ -1,7 +1,8 @@
 """Bin analysis of Monte Carlo observables: ALF's jackknife with the sign.
 
 Restates the published algorithm of Libraries/Modules/errors_mod.F90 (ERRCALC :98-126,
-ERRCALC_J :160-190, ERRCALC_J_REBIN :257-287, ERRCALC_JS :290-327, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
+ERRCALC_C :128-158, ERRCALC_J :160-190, ERRCALC_J_REBIN :257-287, ERRCALC_JS :290-327,
+ERRCALC_JS_C_F :432-476 / _REBIN_F :599-, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
 Analysis/ana_mod.F90 (ERRCALCJ calls, e.g. :1380, :1587, :1783) applies to the per-bin
 averages of <O s> and <s> written by the observables module:
 
@@ -77,3 +78,25 @@ def jackknife_plain(en, nrebin: int = 1):
         raise ValueError("jackknife: fewer than two bins")
     xm, xerr = errcalc((en.sum() - en) / (n - 1))
     return xm, xerr * n
+
+
+def jackknife_vec(en, si, f: Callable, nrebin: int = 1):
+    """ERRCALC_JS_C_F / ERRCALC_JS_C_REBIN_F: en [n_obs][n_bins] (complex) and the sign bins
+    si [n_bins]; f maps the leave-one-out ratio vector (sum_b en_b - en_n) / (sum_b si_b -
+    si_n) to a complex number.  Mean and error of the f values, real and imaginary parts
+    separately (ERRCALC_C), the error times the number of (rebinned) bins."""
+    en = np.asarray(en, dtype=np.complex128)
+    si = np.asarray(si, dtype=np.complex128)
+    if en.shape[1] != si.shape[0]:
+        raise ValueError("jackknife: observable and sign bins differ in number")
+    if nrebin > 1:
+        en = rebin(en.T, nrebin).T
+        si = rebin(si, nrebin)
+    n = si.size
+    if n < 2:
+        raise ValueError("jackknife: fewer than two bins")
+    X = (en.sum(axis=1)[:, None] - en) / (si.sum() - si)[None, :]
+    vals = np.array([complex(f(X[:, b])) for b in range(n)])
+    mr, er = errcalc(vals.real)
+    mi, ei = errcalc(vals.imag)
+    return complex(mr, mi), complex(er, ei) * n

@@ -107,6 +107,13 @@ class Lattice:
         ph = np.exp(-1j * (self.K @ self.R.T))  # [k][R]
         return np.tensordot(ph, np.asarray(x_r, dtype=np.complex128), axes=(1, 0)) / self.N
 
+    def fourier_k_to_r(self, x_k: np.ndarray) -> np.ndarray:
+        """X(R) = 1/Ns sum_k exp(i k.R) X(k) over the first axis (FT_K_to_R_Mat_C,
+        lattices_v3_mod.F90:672-709; with the 1/Ns of both directions a round trip divides
+        by Ns, so ana_eq's real-space results are per-site correlations)."""
+        ph = np.exp(1j * (self.R @ self.K.T))  # [R][k]
+        return np.tensordot(ph, np.asarray(x_k, dtype=np.complex128), axes=(1, 0)) / self.N
+
 
 class EqualTimeObs:
     """Obs_eq of the Hubbard models with N_FL = 2 (Green, SpinZ, SpinXY, SpinT, Den),
@@ -326,3 +333,52 @@ def read_eq(path: str) -> List[dict]:
         out.append({"sign": sign, "latt0": back, "k": ks, "values": vals[:, 0] if len(head) <= 3 else vals,
                     **({"dtau": float(head[4])} if len(head) > 4 else {})})
     return out
+
+
+EPS_CONVERGENCE = 1.0e-6  # Natural_Constants Eps_convergence: the k = 0 test of ana_eq
+
+
+def ana_eq(bins: Sequence[dict], latt: Lattice, n_skip: int = 1, n_rebin: int = 1):
+    """ana_eq (Analysis/ana_mod.F90:1427-1648, default zone) on the bins read_eq returns:
+    per k point and orbital pair the signed jackknife (analysis.jackknife_vec) of
+    f(X) = X1 - X2 X3 with X1 the bin's value, and at k = 0 only X2 = Ns <O_no>, X3 = <O_no1>
+    (the background), else 0; in real space (FT_K_to_R of the k-space bins) X2 = <O_no>,
+    X3 = <O_no1> at every R.  Returns (jk, jr): complex arrays [Ns][norb][norb][2] of
+    (mean, error)."""
+    from .analysis import jackknife_vec
+    b = list(bins)[n_skip:]
+    if len(b) // n_rebin < 2:
+        raise ValueError("effective number of bins smaller than 2")
+    sgn = np.array([x["sign"] for x in b], dtype=np.complex128)
+    vk = np.stack([x["values"] for x in b], axis=-1)  # [Ns][no][no1][nb]
+    bg = np.stack([x["latt0"] for x in b], axis=-1)   # [no][nb]
+    vr = np.stack([latt.fourier_k_to_r(x["values"]) for x in b], axis=-1)
+    f = lambda X: X[0] - X[1] * X[2]
+    ns, no = latt.N, latt.norb
+    jk = np.zeros((ns, no, no, 2), np.complex128)
+    jr = np.zeros((ns, no, no, 2), np.complex128)
+    zero = np.zeros(len(b), np.complex128)
+    for k in range(ns):
+        at0 = float(np.hypot(*latt.K[k])) < EPS_CONVERGENCE
+        for a in range(no):
+            for c in range(no):
+                V = np.stack([vk[k, a, c], bg[a] * ns if at0 else zero, bg[c] if at0 else zero])
+                jk[k, a, c] = jackknife_vec(V, sgn, f, n_rebin)
+                VR = np.stack([vr[k, a, c], bg[a], bg[c]])
+                jr[k, a, c] = jackknife_vec(VR, sgn, f, n_rebin)
+    return jk, jr
+
+
+def write_ana_eq(directory: str, name: str, jk: np.ndarray, jr: np.ndarray, latt: Lattice) -> None:
+    """``<name>JK`` and ``<name>JR`` as ana_eq writes them: per k point (R point) its
+    coordinates as ``2(E26.17E3)``, then per orbital pair ``(2(I11), 4(E26.17E3))`` no, no1,
+    Re mean, Re error, Im mean, Im error."""
+    for suffix, arr, pts in (("JK", jk, latt.K), ("JR", jr, latt.R)):
+        with open(os.path.join(directory, f"{name}{suffix}"), "w") as f:
+            for n in range(latt.N):
+                f.write(fortran_e(pts[n, 0], 26, 17) + fortran_e(pts[n, 1], 26, 17) + "\n")
+                for a in range(latt.norb):
+                    for c in range(latt.norb):
+                        m, e = arr[n, a, c]
+                        f.write(f"{a + 1:11d}{c + 1:11d}" + fortran_e(m.real, 26, 17) + fortran_e(e.real, 26, 17)
+                                + fortran_e(m.imag, 26, 17) + fortran_e(e.imag, 26, 17) + "\n")

@@ -42,3 +42,21 @@ def test_complex_observables_are_analysed_part_by_part():
     mr, er = analysis.jackknife(z.real)
     mi, ei = analysis.jackknife(z.imag)
     assert m == complex(mr, mi) and e == complex(er, ei)
+
+
+def test_vector_jackknife_reduces_to_the_signed_scalar_one():
+    from alf_gb300.analysis import jackknife, jackknife_vec
+    r = np.random.default_rng(8)
+    en = r.standard_normal(30)
+    si = 0.7 + 0.2 * r.random(30)
+    m, e = jackknife_vec(en[None, :], si, lambda X: X[0])
+    m2, e2 = jackknife(en, si)
+    assert abs(m.real - m2) < 1e-14 and abs(e.real - e2) < 1e-14 and m.imag == 0.0 and e.imag == 0.0
+    # with rebinning, and a non-linear function of two observables
+    en2 = np.stack([en + 1j * r.standard_normal(30), 1.0 + 0.1 * r.standard_normal(30)])
+    m3, e3 = jackknife_vec(en2, si, lambda X: X[0] / X[1], nrebin=3)
+    a, s = en2.reshape(2, 10, 3).mean(axis=2), si.reshape(10, 3).mean(axis=1)
+    x = [((a[0].sum() - a[0][n]) / (s.sum() - s[n])) / ((a[1].sum() - a[1][n]) / (s.sum() - s[n])) for n in range(10)]
+    x = np.array(x)
+    assert abs(m3 - x.mean()) < 1e-13
+    assert abs(e3.real - np.sqrt(np.sum((x.real - x.real.mean()) ** 2) / 10 / 10) * 10) < 1e-13

@@ -319,6 +319,18 @@ def test_lattice_correlations_of_the_ring_match_the_trotterized_values():
         assert np.all(np.abs(mean - ex[k]) < 4.0 * err + 1e-12), (k, mean, err, ex[k])
     # backgrounds: <m> = 0 and <n> = 1 per site at half filling
     assert abs(np.mean([bb["Den"]["latt0"][0].real for bb in bins]) - 1.0) < 1e-9
+    # the same bins through the legacy files and ana_eq: real-space results are the connected
+    # per-site correlations <O_r O_0> - <O>^2
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        for bb in bins:
+            for k in ("SpinZ", "Den"):
+                lo.write_eq_bin(d, k, bb[k], L, dtau=m.dtau)
+        for k, bgk in (("SpinZ", 0.0), ("Den", 1.0)):
+            _, jr = lo.ana_eq(lo.read_eq(f"{d}/{k}_eq"), L, n_skip=1)
+            mean, err = jr[:, 0, 0, 0].real, jr[:, 0, 0, 1].real
+            want = ex[k] / L_SITES - bgk ** 2
+            assert np.all(np.abs(mean - want) < 4.0 * err + 1e-9), (k, mean, err, want)
 
 
 def test_time_displaced_lattice_correlations_of_the_ring_match_the_trotterized_values():

@@ -183,3 +183,35 @@ def test_time_displaced_measurements_equal_the_per_site_loops_and_round_trip(tmp
     for nt in range(ntau):
         np.testing.assert_array_equal(back[0]["values"][:, nt, 0, 0], L.fourier_r_to_k(b["Den"]["latt"][:, nt, 0, 0]))
     assert open(tmp_path / "Den_tau_info").readline().rstrip() == "          Observable: Den_tau"
+
+
+def test_ana_eq_subtracts_the_background_at_k0_and_in_real_space(tmp_path):
+    from alf_gb300.analysis import jackknife_vec
+    L = lo.Lattice("square", 4, 2)
+    r = np.random.default_rng(6)
+    bins = []
+    for _ in range(9):
+        b = {"latt": (r.standard_normal((L.N, 1, 1, 1)) + 1j * r.standard_normal((L.N, 1, 1, 1))),
+             "latt0": np.array([0.3 + 0.1 * r.standard_normal()], complex), "sign": 0.9 + 0.05 * r.random()}
+        lo.write_eq_bin(str(tmp_path), "Den", b, L, dtau=0.1)
+    back = lo.read_eq(str(tmp_path / "Den_eq"))
+    jk, jr = lo.ana_eq(back, L, n_skip=1)
+    use = back[1:]
+    sg = np.array([x["sign"] for x in use])
+    bg = np.array([x["latt0"][0] for x in use])
+    k0 = int(np.argmin(np.hypot(L.K[:, 0], L.K[:, 1])))
+    for k in range(L.N):
+        v = np.array([x["values"][k, 0, 0] for x in use])
+        if k == k0:
+            want = jackknife_vec(np.stack([v, bg * L.N, bg]), sg, lambda X: X[0] - X[1] * X[2])
+        else:
+            want = jackknife_vec(v[None, :], sg, lambda X: X[0])
+        np.testing.assert_allclose(jk[k, 0, 0], want, rtol=1e-12, atol=1e-14)
+    vr = np.array([L.fourier_k_to_r(x["values"][:, 0, 0]) for x in use])  # [nb][R]
+    for R in range(L.N):
+        want = jackknife_vec(np.stack([vr[:, R], bg, bg]), sg, lambda X: X[0] - X[1] * X[2])
+        np.testing.assert_allclose(jr[R, 0, 0], want, rtol=1e-12, atol=1e-14)
+    lo.write_ana_eq(str(tmp_path), "Den", jk, jr, L)
+    lines = open(tmp_path / "DenJK").read().splitlines()
+    assert len(lines) == 2 * L.N and lines[1].split()[:2] == ["1", "1"]
+    assert float(lines[1].split()[2]) == float(jk[0, 0, 0, 0].real)  # 17 digits: the double itself
