@@ -2,7 +2,7 @@
 
 Restates the published algorithm of Libraries/Modules/errors_mod.F90 (ERRCALC :98-126,
 ERRCALC_C :128-158, ERRCALC_J :160-190, ERRCALC_J_REBIN :257-287, ERRCALC_JS :290-327,
-ERRCALC_JS_C_F :432-476 / _REBIN_F :599-, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
+ERRCALC_JS_C_F :432-476 / _REBIN_F :599-, and ana_mod.F90:862-933 jack, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
 Analysis/ana_mod.F90 (ERRCALCJ calls, e.g. :1380, :1587, :1783) applies to the per-bin
 averages of <O s> and <s> written by the observables module:
 
@@ -100,3 +100,20 @@ def jackknife_vec(en, si, f: Callable, nrebin: int = 1):
     mr, er = errcalc(vals.real)
     mi, ei = errcalc(vals.imag)
     return complex(mr, mi), complex(er, ei) * n
+
+
+def jack(func: Callable, data, n_skip: int = 0, n_rebin: int = 1):
+    """Analysis/ana_mod.F90:862-933 (jack): data [n_obs][n_bins]; bins after the first n_skip
+    are rebinned by n_rebin (remainder dropped), func maps each leave-one-out mean vector
+    (sum - x_n) / (n - 1) to a complex number; mean and error of those values, real and
+    imaginary parts separately, the error times n.  No sign weighting."""
+    data = np.asarray(data, dtype=np.complex128)[:, n_skip:]
+    nr = data.shape[1] // n_rebin
+    if nr < 2:
+        raise ValueError("jack: fewer than two rebinned bins")
+    d = data[:, : nr * n_rebin].reshape(data.shape[0], nr, n_rebin).mean(axis=2)
+    X = (d.sum(axis=1)[:, None] - d) / (nr - 1)
+    vals = np.array([complex(func(X[:, n])) for n in range(nr)])
+    mr, er = errcalc(vals.real)
+    mi, ei = errcalc(vals.imag)
+    return complex(mr, mi), complex(er, ei) * nr

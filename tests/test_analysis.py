@@ -60,3 +60,16 @@ def test_vector_jackknife_reduces_to_the_signed_scalar_one():
     x = np.array(x)
     assert abs(m3 - x.mean()) < 1e-13
     assert abs(e3.real - np.sqrt(np.sum((x.real - x.real.mean()) ** 2) / 10 / 10) * 10) < 1e-13
+
+
+def test_jack_is_the_unsigned_vector_jackknife_after_skip_and_rebin():
+    from alf_gb300.analysis import jack, jackknife_plain, jackknife_vec
+    r = np.random.default_rng(9)
+    d = r.standard_normal((2, 25)) + 1j * r.standard_normal((2, 25))
+    m, e = jack(lambda X: X[0] * X[1], d, n_skip=1, n_rebin=4)
+    # the same as the signed form with unit signs (leave-one-out sums over n - 1 bins)
+    m2, e2 = jackknife_vec(d[:, 1:], np.ones(24), lambda X: X[0] * X[1], nrebin=4)
+    assert abs(m - m2) < 1e-13 and abs(e - e2) < 1e-13
+    m3, e3 = jack(lambda X: X[0], d[:1].real, n_skip=0, n_rebin=1)
+    m4, e4 = jackknife_plain(d[0].real)
+    assert abs(m3.real - m4) < 1e-14 and abs(e3.real - e4) < 1e-14
