@@ -2,9 +2,10 @@
 
 Restates the published algorithm of Libraries/Modules/errors_mod.F90 (ERRCALC :98-126,
 ERRCALC_C :128-158, ERRCALC_J :160-190, ERRCALC_J_REBIN :257-287, ERRCALC_JS :290-327,
-ERRCALC_JS_C_F :432-476 / _REBIN_F :599-, and ana_mod.F90:862-933 jack, ERRCALC_JS_F :338-388, ERRCALC_JS_REBIN :481-516), which
-Analysis/ana_mod.F90 (ERRCALCJ calls, e.g. :1380, :1587, :1783) applies to the per-bin
-averages of <O s> and <s> written by the observables module:
+ERRCALC_JS_F :338-388, ERRCALC_JS_C_F :432-476, ERRCALC_JS_REBIN :481-516,
+ERRCALC_JS_C_REBIN_F :599-) and Analysis/ana_mod.F90:862-933 (jack).  ana_mod applies them
+(ERRCALCJ calls, e.g. :1380, :1587, :1783) to the per-bin averages of <O s> and <s> written
+by the observables module:
 
 * rebin: consecutive groups of ``nrebin`` bins are averaged (a trailing remainder is
   dropped, like the reference's integer division);
