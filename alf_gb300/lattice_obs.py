@@ -35,7 +35,13 @@ import numpy as np
 from . import model as mdl
 from .bins import fortran_e
 
-EQ_NAMES = ("Green", "SpinZ", "SpinXY", "SpinT", "Den")
+EQ_NAMES = ("Green", "SpinZ", "SpinXY", "SpinT", "Den")  # N_FL = 2 (Mz Hubbard)
+EQ_NAMES_SUN = ("Green", "SpinZ", "Den")                   # N_FL = 1 (SU(N) models, Kondo): SpinZ by SpinSUN
+
+
+def names_for(n_fl: int):
+    """The Obs_eq / Obs_tau files of the predefined measurements for N_FL flavours."""
+    return EQ_NAMES if n_fl == 2 else EQ_NAMES_SUN
 
 
 def _walk(v1: np.ndarray, v2: np.ndarray, tests: Sequence[np.ndarray], L: int) -> List[Tuple[int, int]]:
@@ -116,24 +122,30 @@ class Lattice:
 
 
 class EqualTimeObs:
-    """Obs_eq of the Hubbard models with N_FL = 2 (Green, SpinZ, SpinXY, SpinT, Den),
-    accumulated as Obs_Latt(imj, 1, no_I, no_J), Obs_Latt0(no), N and Ave_sign."""
+    """Obs_eq of the predefined measurements, accumulated as Obs_Latt(imj, 1, no_I, no_J),
+    Obs_Latt0(no), N and Ave_sign: for N_FL = 2 (Hubbard Mz) Green, SpinZ, SpinXY, SpinT,
+    Den; for N_FL = 1 (SU(N) Hubbard, Kondo) Green, SpinZ (SpinSUN), Den."""
 
-    def __init__(self, latt: Lattice, n_sun: int):
-        self.latt, self.n_sun = latt, n_sun
+    def __init__(self, latt: Lattice, n_sun: int, n_fl: int = 2):
+        if n_fl not in (1, 2):
+            raise ValueError("N_FL is 1 or 2")
+        self.latt, self.n_sun, self.n_fl = latt, n_sun, n_fl
+        self.names = names_for(n_fl)
         self.reset()
 
     def reset(self):
         no, N = self.latt.norb, self.latt.N
-        self.obs = {k: np.zeros((N, 1, no, no), np.complex128) for k in EQ_NAMES}
-        self.obs0 = {k: np.zeros(no, np.complex128) for k in EQ_NAMES}
+        self.obs = {k: np.zeros((N, 1, no, no), np.complex128) for k in self.names}
+        self.obs0 = {k: np.zeros(no, np.complex128) for k in self.names}
         self.count, self.sign = 0, 0.0
 
     def measure(self, G: np.ndarray, phase: complex):
         """One ham%Obser call: G [n_fl][row][col] (the callback's frame), phase."""
         G = np.asarray(G)
-        if G.shape[0] != 2:
-            raise ValueError("the N_FL = 2 observables need both flavours")
+        if G.shape[0] != self.n_fl:
+            raise ValueError(f"G has {G.shape[0]} flavours, expected {self.n_fl}")
+        if self.n_fl == 1:
+            return self._measure_sun(G, phase)
         zp = phase / phase.real
         zs = float(np.sign(phase.real))
         w = zp * zs
@@ -167,6 +179,29 @@ class EqualTimeObs:
         self.count += 1
         self.sign += zs
 
+    def _measure_sun(self, G: np.ndarray, phase: complex):
+        """N_FL = 1: Green and Den as above with one flavour, SpinZ by
+        Predefined_Obs_eq_SpinSUN_measure (N_SUN GRC(I,J) GR(I,J), no background)."""
+        w = phase / phase.real * float(np.sign(phase.real))
+        nd = G.shape[1]
+        GR, GRC = G[0], np.eye(nd) - G[0].T
+        L = self.latt
+        rows = L.imj[np.ix_(L.site_cell, L.site_cell)]
+        oi = np.broadcast_to(L.site_orb[:, None], (nd, nd))
+        oj = np.broadcast_to(L.site_orb[None, :], (nd, nd))
+        ns = self.n_sun
+
+        def add(name, val):
+            np.add.at(self.obs[name][:, 0], (rows, oi, oj), val * w)
+
+        add("Green", ns * GRC)
+        add("SpinZ", ns * GRC * GR)
+        zi = ns * np.diag(GRC)
+        add("Den", zi[:, None] * zi[None, :] + ns * GRC * GR)
+        np.add.at(self.obs0["Den"], L.site_orb, zi * w)
+        self.count += 1
+        self.sign += float(np.sign(phase.real))
+
     def bin(self, reset: bool = True) -> Dict[str, dict]:
         """Print_bin_Latt's normalisation: per observable Obs_Latt / N, Obs_Latt0 / (N Ns Ntau)
         and Ave_sign / N (Ntau = 1)."""
@@ -174,38 +209,43 @@ class EqualTimeObs:
             raise ValueError("an empty bin")
         n, ns = self.count, self.latt.N
         out = {k: {"latt": self.obs[k] / n, "latt0": self.obs0[k] / (n * ns), "sign": self.sign / n}
-               for k in EQ_NAMES}
+               for k in self.names}
         if reset:
             self.reset()
         return out
 
 
 class TimeDisplacedObs:
-    """Obs_tau of the Hubbard models with N_FL = 2 on the quartets of ham%ObserT at
-    NT = 0..Ltrot: Obs_Latt(imj, NT + 1, no_I, no_J), Obs_Latt0(no); N and Ave_sign count
-    the NT = 0 calls."""
+    """Obs_tau of the predefined measurements on the quartets of ham%ObserT at NT = 0..Ltrot:
+    Obs_Latt(imj, NT + 1, no_I, no_J), Obs_Latt0(no); N and Ave_sign count the NT = 0 calls.
+    Files as EqualTimeObs (N_FL = 1: SpinZ by Predefined_Obs_tau_SpinSUN_measure)."""
 
-    def __init__(self, latt: Lattice, n_sun: int, ntau: int):
-        self.latt, self.n_sun, self.ntau = latt, n_sun, ntau
+    def __init__(self, latt: Lattice, n_sun: int, ntau: int, n_fl: int = 2):
+        if n_fl not in (1, 2):
+            raise ValueError("N_FL is 1 or 2")
+        self.latt, self.n_sun, self.ntau, self.n_fl = latt, n_sun, ntau, n_fl
+        self.names = names_for(n_fl)
         self.reset()
 
     def reset(self):
         no, N = self.latt.norb, self.latt.N
-        self.obs = {k: np.zeros((N, self.ntau, no, no), np.complex128) for k in EQ_NAMES}
-        self.obs0 = {k: np.zeros(no, np.complex128) for k in EQ_NAMES}
+        self.obs = {k: np.zeros((N, self.ntau, no, no), np.complex128) for k in self.names}
+        self.obs0 = {k: np.zeros(no, np.complex128) for k in self.names}
         self.count, self.sign = 0, 0.0
 
     def measure(self, nt: int, GT0, G0T, G00, GTT, phase: complex):
         """One ham%ObserT call: NT and the quartet, each [n_fl][row][col]."""
         GT0, G0T, G00, GTT = (np.asarray(x) for x in (GT0, G0T, G00, GTT))
-        if GT0.shape[0] != 2:
-            raise ValueError("the N_FL = 2 observables need both flavours")
+        if GT0.shape[0] != self.n_fl:
+            raise ValueError(f"the quartet has {GT0.shape[0]} flavours, expected {self.n_fl}")
         zp = phase / phase.real
         zs = float(np.sign(phase.real))
         w = zp * zs
         if nt == 0:
             self.count += 1
             self.sign += zs
+        if self.n_fl == 1:
+            return self._measure_sun(nt, GT0[0], G0T[0], G00[0], GTT[0], w)
         L = self.latt
         nd = GT0.shape[1]
         rows = L.imj[np.ix_(L.site_cell, L.site_cell)]
@@ -233,13 +273,32 @@ class TimeDisplacedObs:
         add("Den", zi[:, None] * zj[None, :] + z)
         np.add.at(self.obs0["Den"], L.site_orb, zi * w)
 
+    def _measure_sun(self, nt, gt0, g0t, g00, gtt, w):
+        """N_FL = 1: Green (GT0 / N_FL), SpinZ (-N_SUN G0T(J,I) GT0(I,J)) and Den."""
+        L = self.latt
+        nd = gt0.shape[0]
+        rows = L.imj[np.ix_(L.site_cell, L.site_cell)]
+        oi = np.broadcast_to(L.site_orb[:, None], (nd, nd))
+        oj = np.broadcast_to(L.site_orb[None, :], (nd, nd))
+        ns = self.n_sun
+
+        def add(name, val):
+            np.add.at(self.obs[name][:, nt], (rows, oi, oj), val * w)
+
+        add("Green", gt0)
+        conn = g0t.T * gt0
+        add("SpinZ", -ns * conn)
+        zi, zj = ns * (1.0 - np.diag(gtt)), ns * (1.0 - np.diag(g00))
+        add("Den", zi[:, None] * zj[None, :] - ns * conn)
+        np.add.at(self.obs0["Den"], L.site_orb, zi * w)
+
     def bin(self, reset: bool = True) -> Dict[str, dict]:
         """Obs_Latt / N, Obs_Latt0 / (N Ns Ntau), Ave_sign / N."""
         if self.count == 0:
             raise ValueError("an empty bin")
         n, ns = self.count, self.latt.N
         out = {k: {"latt": self.obs[k] / n, "latt0": self.obs0[k] / (n * ns * self.ntau), "sign": self.sign / n}
-               for k in EQ_NAMES}
+               for k in self.names}
         if reset:
             self.reset()
         return out

@@ -249,6 +249,16 @@ def test_kondo_two_site_vertices_match_the_trotterized_values():
         Di = ob(Oi)
         DD += Di @ Di
     ex = np.array([np.trace(ob(H) @ P), np.trace(DD @ P)]) / np.trace(P)
+    # the lattice density correlation of the bilayer (N_FL = 1 Den, alf_gb300.lattice_obs):
+    # Den(r, no, no1) = sum over cell pairs with imj = r of <n_{I,no} n_{J,no1}>, both species
+    from alf_gb300 import lattice_obs as lo
+    latt = lo.Lattice("bilayer_square", 2, 1)
+    nop = [fk.n(0, i) + fk.n(1, i) for i in range(N)]
+    den_ex = np.zeros((latt.N, 2, 2))
+    for i1 in range(N):
+        for j1 in range(N):
+            rr = latt.imj[latt.site_cell[i1], latt.site_cell[j1]]
+            den_ex[rr, latt.site_orb[i1], latt.site_orb[j1]] += (np.trace(nop[i1] @ nop[j1] @ P) / np.trace(P)).real
 
     o = oracle.Oracle(m)
     seed = 2024
@@ -259,6 +269,8 @@ def test_kondo_two_site_vertices_match_the_trotterized_values():
     eq, _ = o.collect_measurements()
     n_bins, n_per_bin = 20, 100
     vals = []
+    den_obs = lo.EqualTimeObs(latt, n_sun=m.n_sun, n_fl=1)
+    den_bins = []
     sel = np.zeros((N, N))
     for c, f in pairs:
         sel[c, f] = sel[f, c] = 1.0
@@ -276,11 +288,17 @@ def test_kondo_two_site_vertices_match_the_trotterized_values():
                 d = sum(grc[a, b] for a, b in idx)
                 w2 = sum(grc[a, b] * grc[p, q] + grc[a, q] * g[b, p] for a, b in idx for p, q in idx)
                 dd += (2.0 * w2 + 2.0 * d * d).real
+            den_obs.measure(G, ph)
         vals.append((kin / len(eq), dd / len(eq)))
+        if (s - 99) % n_per_bin == 0:
+            den_bins.append(den_obs.bin()["Den"]["latt"][:, 0].real)
     a = np.array(vals).reshape(n_bins, n_per_bin, 2).mean(axis=1)
     mean, err = a.mean(axis=0), a.std(axis=0, ddof=1) / np.sqrt(n_bins)
     assert np.all(err < 0.05), err
     assert np.all(np.abs(mean - ex) < 4.0 * err), (mean, err, ex)
+    db = np.array(den_bins)
+    dm, de = db.mean(axis=0), db.std(axis=0, ddof=1) / np.sqrt(len(db))
+    assert len(db) == n_bins and np.all(np.abs(dm - den_ex) < 4.0 * de + 1e-9), (dm, de, den_ex)
 
 
 def test_lattice_correlations_of_the_ring_match_the_trotterized_values():

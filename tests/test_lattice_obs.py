@@ -215,3 +215,50 @@ def test_ana_eq_subtracts_the_background_at_k0_and_in_real_space(tmp_path):
     lines = open(tmp_path / "DenJK").read().splitlines()
     assert len(lines) == 2 * L.N and lines[1].split()[:2] == ["1", "1"]
     assert float(lines[1].split()[2]) == float(jk[0, 0, 0, 0].real)  # 17 digits: the double itself
+
+
+def test_single_flavour_measurements_equal_the_per_site_loops():
+    # N_FL = 1 (SU(N) models, Kondo): Green, SpinZ by SpinSUN, Den; equal time and tau
+    L = lo.Lattice("bilayer_square", 2, 2)
+    nd = L.N * L.norb
+    r = np.random.default_rng(13)
+    ns = 2
+    G = r.standard_normal((1, nd, nd)) + 1j * r.standard_normal((1, nd, nd))
+    ph = complex(1.2, -0.1)
+    w = ph / ph.real
+    m = lo.EqualTimeObs(L, n_sun=ns, n_fl=1)
+    m.measure(G, ph)
+    b = m.bin()
+    assert tuple(b) == lo.EQ_NAMES_SUN
+    GR = G[0]
+    GRC = np.eye(nd) - GR.T
+    ref = {k: np.zeros((L.N, 2, 2), complex) for k in lo.EQ_NAMES_SUN}
+    ref0 = np.zeros(2, complex)
+    for i1 in range(nd):
+        for j1 in range(nd):
+            rr, a, c = L.imj[L.site_cell[i1], L.site_cell[j1]], L.site_orb[i1], L.site_orb[j1]
+            ref["Green"][rr, a, c] += ns * GRC[i1, j1] * w
+            ref["SpinZ"][rr, a, c] += ns * GRC[i1, j1] * GR[i1, j1] * w
+            ref["Den"][rr, a, c] += (ns * GRC[i1, i1] * ns * GRC[j1, j1] + ns * GRC[i1, j1] * GR[i1, j1]) * w
+        ref0[L.site_orb[i1]] += ns * GRC[i1, i1] * w
+    for k in lo.EQ_NAMES_SUN:
+        np.testing.assert_allclose(b[k]["latt"][:, 0], ref[k], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(b["Den"]["latt0"], ref0 / L.N, rtol=1e-13)
+    t = lo.TimeDisplacedObs(L, n_sun=ns, ntau=2, n_fl=1)
+    q = [r.standard_normal((1, nd, nd)) + 1j * r.standard_normal((1, nd, nd)) for _ in range(4)]
+    t.measure(0, *q, ph)
+    t.measure(1, *q, ph)
+    bt = t.bin()
+    gt0, g0t, g00, gtt = (x[0] for x in q)
+    refs = np.zeros((L.N, 2, 2), complex)
+    refd = np.zeros((L.N, 2, 2), complex)
+    for i1 in range(nd):
+        for j1 in range(nd):
+            rr, a, c = L.imj[L.site_cell[i1], L.site_cell[j1]], L.site_orb[i1], L.site_orb[j1]
+            refs[rr, a, c] += -ns * g0t[j1, i1] * gt0[i1, j1] * w
+            refd[rr, a, c] += (ns * (1 - gtt[i1, i1]) * ns * (1 - g00[j1, j1]) - ns * g0t[j1, i1] * gt0[i1, j1]) * w
+    for nt in range(2):
+        np.testing.assert_allclose(bt["SpinZ"]["latt"][:, nt], refs, rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(bt["Den"]["latt"][:, nt], refd, rtol=1e-13, atol=1e-13)
+    with pytest.raises(ValueError):
+        m.measure(np.zeros((2, nd, nd)), ph)
