@@ -2,8 +2,6 @@
 every entry point declared in include/alfgpu.h.  No compute calls (no GPU here)."""
 import ctypes
 
-import pytest
-
 from alf_gb300 import _lib, build
 
 
