@@ -293,10 +293,15 @@ class Chains:
     def set_recording(self, enable: bool = True):
         _lib.check(self.L.alfgpu_set_recording(self.h, int(enable)), "alfgpu_set_recording")
 
+    def record_sizes(self) -> tuple:
+        """(visits, stabilisation points) of one sweep's record at the handle's current Nwrap
+        (alfgpu_set_nwrap may have changed it since the model was built): 2 M Ltrot visits and
+        2 Nstm points, Nstm = ceil(Ltrot / Nwrap)."""
+        nw = self.nwrap()
+        return 2 * self.M * self.Lt, 2 * ((self.Lt + nw - 1) // nw)
+
     def record(self, chain: int = 0) -> dict:
-        V = 2 * self.M * self.Lt
-        nw = self.nwrap()  # the handle's current interval (alfgpu_set_nwrap may have changed it)
-        P = 2 * ((self.Lt + nw - 1) // nw)
+        V, P = self.record_sizes()
         acc = np.zeros(V, np.int8)
         ratio = np.zeros(V, np.complex128)
         G = np.zeros((P, self.F, self.N, self.N), np.complex128)
