@@ -1,7 +1,8 @@
 """Host-side policies of the Python mirror (alf_gb300.sweep.Chains) on the CPU, driven by a
 stand-in for the C library: the drift-control loop (adapt_nwrap), the sizing of the record
-buffers from the handle's current Nwrap, and checkpoint / restore.  The library calls are the
-ones include/alfgpu.h declares; the stand-in keeps their state in Python."""
+buffers from the handle's current Nwrap, checkpoint / restore, the layouts of the observable
+callback and the scalar accumulators.  The library calls are the ones include/alfgpu.h
+declares; the stand-in keeps their state in Python."""
 import ctypes as C
 
 import numpy as np
@@ -166,3 +167,70 @@ def test_checkpoint_restore_round_trip_and_size_check(fake, tmp_path):
     with pytest.raises(ValueError):
         ch3.restore(p)
     ch3.close()
+
+
+class FakeObsLib(FakeLib):
+    """Adds the observable callback (ham%Obser G and ham%ObserT quartets in the library's
+    column-major layout) and the scalar accumulators."""
+
+    def __init__(self, G, quartet, sums):
+        super().__init__()
+        self.G, self.quartet, self.sums = G, quartet, sums
+
+    def alfgpu_sweep(self, h, u, cb, ctx):
+        def colmajor(mats):  # [k][nf][row][col] -> column-major per matrix, interleaved re/im
+            a = np.ascontiguousarray(np.transpose(np.asarray(mats, np.complex128), (0, 1, 3, 2)))
+            return a.view(np.float64)
+        ph = np.array([0.8, -0.6])
+        g = colmajor(self.G[None])
+        cb(None, 1, 7, 0, g.ctypes.data_as(C.POINTER(C.c_double)), ph.ctypes.data_as(C.POINTER(C.c_double)))
+        q = colmajor(self.quartet)
+        cb(None, 0, 3, 1, q.ctypes.data_as(C.POINTER(C.c_double)), ph.ctypes.data_as(C.POINTER(C.c_double)))
+        return 0
+
+    def alfgpu_set_scalar_obs(self, h, Hp, Up):
+        n = self.N
+        self.H = np.zeros((self.F, n, n))
+        C.memmove(self.H.ctypes.data, Hp.value, self.H.nbytes)
+        self.U = np.zeros(n)
+        C.memmove(self.U.ctypes.data, Up.value, self.U.nbytes)
+        return 0
+
+    def alfgpu_get_scalar_obs(self, h, c, p):
+        C.memmove(p.value, np.ascontiguousarray(self.sums[c], np.float64).ctypes.data, 80)
+        return 0
+
+    def alfgpu_reset_scalar_obs(self, h):
+        self.log.append("reset_obs")
+        return 0
+
+
+def test_callback_matrices_arrive_row_major_and_scalar_layouts(monkeypatch):
+    m = mdl.hubbard("square", 2, 2, beta=2.0, dtau=0.1, nwrap=10)
+    N, F = m.ndim, m.n_fl
+    r = np.random.default_rng(3)
+    G = r.standard_normal((F, N, N)) + 1j * r.standard_normal((F, N, N))
+    quartet = r.standard_normal((4, F, N, N)) + 1j * r.standard_normal((4, F, N, N))
+    sums = [np.array([4, 0, 2, 0, 8, 0, 6, 0, 2, 2], float), np.array([0, 0, 6, 0, 4, 0, 6, 0, -1, 1], float)]
+    f = FakeObsLib(G, quartet, sums)
+    f.N, f.F = N, F
+    monkeypatch.setattr(_lib, "lib", lambda *a, **k: f)
+    ch = sweep.Chains(m, n_chains=2)
+    eq, tau = ch.sweep(None, measure=True)
+    (c, nt, Gr, ph), = eq
+    assert (c, nt, ph) == (1, 7, complex(0.8, -0.6))
+    np.testing.assert_array_equal(Gr, G)  # [nf][row][col], the matrix itself
+    (c, nt, q, _), = tau
+    assert (c, nt) == (0, 3) and len(q) == 4
+    for a, b in zip(q, quartet):
+        np.testing.assert_array_equal(a, b)
+    H = r.standard_normal((F, N, N))
+    ch.set_scalar_obs(H, np.arange(N, dtype=float))
+    np.testing.assert_array_equal(f.H, np.transpose(H, (0, 2, 1)))  # column-major per flavour
+    np.testing.assert_array_equal(f.U, np.arange(N))
+    ov, sign = ch.scalar_bin()
+    # per chain sums / count, then the mean over the two chains
+    # chain 0: (4, 2, 8, 6) / 2 = (2, 1, 4, 3), sign 1; chain 1: (0, 6, 4, 6) / 1, sign -1
+    np.testing.assert_allclose(ov, [1.0, 3.5, 4.0, 4.5])
+    assert sign == (1.0 + (-1.0)) / 2 and f.log[-1] == "reset_obs"
+    ch.close()
