@@ -53,3 +53,14 @@ def test_grouped_roofline_sums_the_groups():
     two = bench.sweep_roofline(b, 2000.0, 0, 2, 1000.0, "mixed", 1.0, 2000.0)
     assert abs(g["t_roof_ms"] - one["t_roof_ms"] - two["t_roof_ms"]) < 1e-9 * g["t_roof_ms"]
     assert abs(g["flops_per_step"] - one["flops_per_step"] - two["flops_per_step"]) < 1e-6 * g["flops_per_step"]
+
+
+def test_clock_summary_reports_the_median_clock_and_active_reasons():
+    c = bench.ClockSampler(0)
+    assert c.summary()["reasons"] == ["unsampled"]
+    row = lambda sm, hw, pc: [sm, "2070", "900.1", "0x0", hw, "Not Active", "Not Active", pc]
+    c.samples = [row("2070", "Not Active", "Not Active"), row("1980", "Not Active", "Active"),
+                 row("2040", "Active", "Not Active"), row("[N/A]", "Not Active", "Not Active")]
+    s = c.summary()
+    assert s["sm_mhz"] == 2040.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 4
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
