@@ -206,6 +206,14 @@ def sweep_flops(m, n_acc: float, ltau: int) -> dict:
 _TENSOR_PHASES = ("wraps", "propagate", "rank1", "tau_wraps")
 
 
+def _reported(fn, *args):
+    """An optional object of the JSON line: its failure is reported in the line, never fatal."""
+    try:
+        return fn(*args)
+    except Exception as e:  # the line must still print
+        return {"failed": f"{type(e).__name__}: {e}"}
+
+
 def sweep_roofline(m, n_acc: float, ltau: int, chains: int, ms_per_step: float, precision: str,
                    p_fp64: float, p_bf16: float) -> dict:
     """Whole-sweep roofline: t_roof = sum over phases of FLOPs / peak for one step (one sweep of
@@ -218,6 +226,8 @@ def sweep_roofline(m, n_acc: float, ltau: int, chains: int, ms_per_step: float, 
 def sweep_roofline_groups(groups, ms_per_step: float, precision: str, p_fp64: float, p_bf16: float) -> dict:
     """The same over several handles run one after the other in a step: groups of
     (model, accepted flips per chain and sweep, ltau, chains)."""
+    if isinstance(groups, Exception):
+        raise groups
     fl = {}
     for m, n_acc, ltau, chains in groups:
         for k, v in sweep_flops(m, n_acc, ltau).items():
@@ -311,9 +321,12 @@ def run_batch(args, ws, rank, local):
     n_launch = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs) - n0
     # per group for the whole-sweep roofline: the adapted Nwrap, accepted flips per chain and sweep
     import dataclasses
-    rgroups = [(dataclasses.replace(m, nwrap=ch.nwrap()),
-                sum(ch.stats(k).n_acc for k in range(len(mem))) / float(args.steps * len(mem)), 0, len(mem))
-               for ch, m, mem in hs]
+    try:
+        rgroups = [(dataclasses.replace(m, nwrap=ch.nwrap()),
+                    sum(ch.stats(k).n_acc for k in range(len(mem))) / float(args.steps * len(mem)), 0, len(mem))
+                   for ch, m, mem in hs]
+    except Exception as e:  # only the roofline object depends on it
+        rgroups = e
     h2d = d2h = 0
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -540,8 +553,8 @@ def main():
                         "h2d_bytes_per_step": rb["h2d"], "d2h_bytes_per_step": rb["d2h"]},
                 "roofline": None, "cpu_baseline": cpu, "clocks": rb["clocks"], "gpu_launches": int(rb["launches"]),
                 "precision_green": {"xmaxG": rb["xmaxG"]},
-                "sweep_roofline": sweep_roofline_groups(rb["rgroups"], 1e3 * t_dev / args.steps, args.precision,
-                                                        FP64_DMMA_TFLOPS, measured_bf16_peak()[0])}
+                "sweep_roofline": _reported(sweep_roofline_groups, rb["rgroups"], 1e3 * t_dev / args.steps,
+                                            args.precision, FP64_DMMA_TFLOPS, measured_bf16_peak()[0])}
         print(json.dumps(line))
         return
 
@@ -586,9 +599,9 @@ def main():
                  "precision_green": {"xmaxG": st2.xmaxG, "xmeanG": st2.xmeanG_sum / max(st2.ncg, 1),
                                      "xmaxP": st2.xmaxP},
                  "roofline": roofline(a2, m, r2["prof"]),
-                 "sweep_roofline": sweep_roofline(m, st2.n_acc / max(args.steps, 1), r2.get("ltau", 0), args.chains,
-                                                  1e3 * r2["t_dev"] / args.steps, "mixed", FP64_DMMA_TFLOPS,
-                                                  measured_bf16_peak()[0]),
+                 "sweep_roofline": _reported(sweep_roofline, m, st2.n_acc / max(args.steps, 1), r2.get("ltau", 0),
+                                             args.chains, 1e3 * r2["t_dev"] / args.steps, "mixed",
+                                             FP64_DMMA_TFLOPS, measured_bf16_peak()[0]),
                  "dtype": "c128 state; G wraps and UDV propagation (and the flushes of batched grids) as "
                           "FP64-accurate digit-sliced BF16 tensor-core products; per-visit arithmetic and "
                           "single-chain flushes in double-float; QR / CGR in FP64"}
@@ -610,9 +623,9 @@ def main():
         "phases": phases,
         "precision_green": {"xmaxG": st.xmaxG, "xmeanG": st.xmeanG_sum / max(st.ncg, 1), "xmaxP": st.xmaxP},
         "acceptance": st.n_acc / max(st.n_prop, 1),
-        "sweep_roofline": sweep_roofline(m, st.n_acc / max(args.steps, 1), r.get("ltau", 0), args.chains,
-                                         1e3 * r["t_dev"] / args.steps, args.precision, FP64_DMMA_TFLOPS,
-                                         measured_bf16_peak()[0]),
+        "sweep_roofline": _reported(sweep_roofline, m, st.n_acc / max(args.steps, 1), r.get("ltau", 0), args.chains,
+                                    1e3 * r["t_dev"] / args.steps, args.precision, FP64_DMMA_TFLOPS,
+                                    measured_bf16_peak()[0]),
     }
     if mixed is not None:
         line["mixed"] = mixed
