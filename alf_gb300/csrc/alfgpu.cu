@@ -25,6 +25,7 @@
 #include "tau.cuh"
 #include "ozaki.cuh"
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -2202,8 +2203,13 @@ struct NoallocScratch {
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
 namespace {
+// Per-device set-up of alfgpu_decompose_noalloc.  The first call on a device resolves the
+// scratch address under the device's mutex and publishes it with a release store after cl16
+// is written, so concurrent first calls from several host threads see either no address (and
+// take the mutex) or the address together with cl16.  A failed set-up is retried next call.
 struct NoallocDevice {
-  NoallocScratch* scratch = nullptr;
+  std::mutex mu;
+  std::atomic<NoallocScratch*> scratch{nullptr};
   int cl16 = 0;  // non-portable 16-CTA clusters enabled for the QR kernels
 };
 NoallocDevice g_noalloc_dev[64];
@@ -2217,16 +2223,24 @@ extern "C" int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, doub
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ALFGPU_ERROR_CUDA;
   NoallocDevice& nd = g_noalloc_dev[dev];
-  if (!nd.scratch) {  // first call on this device: resolve the device address of the scratch array
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return ALFGPU_ERROR_CUDA;
-    if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-        cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
-      nd.cl16 = 1;
-    cudaGetLastError();
-    nd.scratch = static_cast<NoallocScratch*>(p);
+  NoallocScratch* s = nd.scratch.load(std::memory_order_acquire);
+  if (!s) {  // first call on this device: resolve the device address of the scratch array
+    std::lock_guard<std::mutex> lock(nd.mu);
+    s = nd.scratch.load(std::memory_order_relaxed);
+    if (!s) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return ALFGPU_ERROR_CUDA;
+      }
+      if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+          cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+        nd.cl16 = 1;
+      cudaGetLastError();
+      s = static_cast<NoallocScratch*>(p);
+      nd.scratch.store(s, std::memory_order_release);
+    }
   }
-  NoallocScratch* s = nd.scratch;
   alfgpu_s ctx;  // host-side bookkeeping only; all device memory below is the caller's or the scratch
   ctx.N = ndim; ctx.F = 1; ctx.C = 1; ctx.B = 1; ctx.M = 1; ctx.L = 1; ctx.NSUN = 1; ctx.dev = dev;
   ctx.CL = cluster_size(ndim);

@@ -3,7 +3,7 @@
 // A value is the unevaluated sum hi + lo of two floats with |lo| <= ulp(hi)/2,
 // carrying ~2^-46 relative rounding per operation.  On GB300 a dependent FP64
 // instruction costs 63-76 cycles and an FP64 division ~560 (one lane or 32),
-// while a dependent FP32 FMA costs ~5 (profiles/fp64_throughput_gb300.md), so the
+// while a dependent FP32 FMA costs ~5 (measured with register-only FMA loops), so the
 // per-visit Metropolis chain runs in this arithmetic.  Algorithms: Knuth's
 // two-sum, Dekker's fast two-sum (|a| >= |b|), the FMA two-product, and one
 // Newton step for the reciprocal and square root.  Products use __fmul_rn so

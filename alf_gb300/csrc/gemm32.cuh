@@ -4,7 +4,7 @@
 // floats (hi = fl32(x), lo = fl32(x - hi)); products use the exact FMA
 // two-product and are accumulated with a two-sum, so a dot product carries a
 // ~2^-44 relative rounding instead of FP32's 2^-24.  On GB300 the FP32 pipes
-// run 64x the FP64 rate (profiles/fp64_throughput_gb300.md); a double-float
+// run 64x the FP64 rate (66 vs 1.0 TFLOP/s measured); a double-float
 // multiply-accumulate costs ~14 FP32 operations.  Same operation and options
 // as k_zgemm (gemm.cuh); operands and output may be stored as complex128 or
 // real64.  The FP32 exponent range (|x| < 3.4e38) suffices for the G wraps and

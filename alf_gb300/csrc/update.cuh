@@ -20,13 +20,16 @@
 // applied by one rank-m GEMM flush; W = Delta_S Gamma^-1 is formed at block
 // end by the same kernel.
 //
-// G is complex128 in both precision forms.  The sequential chain (ratios,
-// Metropolis test, phase), the Ghat rank-1 updates and Gamma^-1 run in FP64
-// (plain form) or double-float (mixed form, dfloat.cuh, ~2^-46 relative
-// rounding).  GB300's FP64 dependent latency (63-76 cycles, ~560 for a
-// division) sets the cost of every visit, so the chain avoids divisions and
-// square roots: the Metropolis test is division-free, the reciprocal is a
-// Newton iteration, and the phase stays unnormalised until the block ends.
+// G is complex128 in both precision forms.  The per-flavour determinants
+// Mat(1,1) (or the 2x2 determinant of a two-site vertex), the Ghat rank-1 updates
+// and Gamma^-1 run in FP64 (plain form) or double-float (mixed form, dfloat.cuh,
+// ~2^-46 relative rounding).  The accumulation of the Metropolis ratio (the
+// product over flavours, exp(Z1 alpha), the N_SUN power and the gamma ratio), the
+// weight test and the phase are FP64 in both forms.  GB300's FP64 dependent
+// latency (63-76 cycles, ~560 for a division) sets the cost of every visit, so
+// the chain avoids divisions and square roots: the Metropolis test is
+// division-free, the reciprocal is a Newton iteration, and the phase stays
+// unnormalised until the block ends.
 #pragma once
 #include "common.cuh"
 #include "arith.cuh"
@@ -115,9 +118,9 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   __shared__ Z s_mye[2][KM], s_dlt[2][KM], s_tcol[2][2][KM], s_rowt[2][KM], s_piv[2][2];
   __shared__ zd s_dlt64[2][KM];
   __shared__ int s_psite[KM], s_pvis[KM], s_pkind[KM], s_accq[KM], s_acc[2];
-  // per visit
-  __shared__ Z s_K[KM];
-  __shared__ R s_u2[KM], s_gr[KM];
+  // per visit (FP64 in both forms: the ratio accumulation)
+  __shared__ zd s_K[KM];
+  __shared__ double s_u2[KM], s_gr[KM];
   __shared__ int s_vtx[KM], s_snew[KM], s_prop[KM];
   __shared__ short s_ij[KM * KM];
   __shared__ int s_m, s_np;
@@ -165,8 +168,8 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       const int sn = (tp == 1) ? -so : (int)p.ft.flip[so + 2][ch];
       s_snew[q] = sn;
       s_prop[q] = 1.5 > u1;  // T0_proposal (Wrapgr_mod.F90:123,133); always true
-      s_u2[q] = A::mkr(uu2);
-      s_gr[q] = A::mkr(p.ft.grat[tp - 1][so + 2][sn + 2]);
+      s_u2[q] = uu2;
+      s_gr[q] = p.ft.grat[tp - 1][so + 2][sn + 2];
       zd K = zmk(1.0, 0.0);
       for (int f = 0; f < F; ++f) {
         const UpdTab e = tab[((long long)(f * M + n) * 5 + so + 2) * 3 + ch];
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       }
       // [prod_f exp(Z1 alpha)]^N_SUN gamma'/gamma: with N_SUN = 1 the gamma ratio joins K
       if (p.NSUN == 1) K = zscale(K, p.ft.grat[tp - 1][so + 2][sn + 2]);
-      s_K[q] = A::mk(K);
+      s_K[q] = K;
       for (int I = 0; I < w; ++I) {
         s_psite[p0 + I] = I ? site2[n] : site[n];
         s_pvis[p0 + I] = q;
@@ -199,7 +202,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   __syncthreads();
 
   // warp-0 state (identical in all lanes)
-  Z ph = A::mk(p.phase[c]);  // kept unnormalised (only its direction enters the weight)
+  zd ph = p.phase[c];  // FP64, kept unnormalised within a block (only its direction enters the weight)
   int m = 0, nacc = 0, pend = 0;
   long long n_prop = 0;
   auto accept_pos = [&](int v) {
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       return;
     }
     const int q = s_pvis[v];
-    Z Rt = A::zero();
+    zd Rt = zmk(0.0, 0.0);
     if (s_prop[q]) {
       // lane parity carries flavour fo: Mat(1,1) = myexp - Delta G(P,P), and for the first
       // position of a pair the 2x2 determinant D_a (myexp_b - Delta_b G'_bb)
@@ -245,21 +248,23 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
         const Z gp = A::mac(gww, A::mul(xm, gwv), gvw);
         Rm = A::mul(D, A::sub(s_mye[fo][w], A::mul(s_dlt[fo][w], gp)));
       }
-      Rt = (F == 2) ? A::mul(A::shfl(Rm, 0), A::shfl(Rm, 1)) : Rm;
+      // the ratio is accumulated in FP64: flavour product, exp(Z1 alpha), N_SUN power
+      const zd Rm64 = A::wide(Rm);
+      Rt = (F == 2) ? zmul(ArD::shfl(Rm64, 0), ArD::shfl(Rm64, 1)) : Rm64;
       if (p.NSUN == 1) {
-        Rt = A::mul(Rt, s_K[q]);  // K carries the gamma ratio (prologue)
+        Rt = zmul(Rt, s_K[q]);  // K carries the gamma ratio (prologue)
       } else {
-        Rt = A::mul(Rt, s_K[q]);
-        Z Rp = Rt;
-        for (int e = 1; e < p.NSUN; ++e) Rp = A::mul(Rp, Rt);
-        Rt = A::scale(Rp, s_gr[q]);
+        Rt = zmul(Rt, s_K[q]);
+        zd Rp = Rt;
+        for (int e = 1; e < p.NSUN; ++e) Rp = zmul(Rp, Rt);
+        Rt = zscale(Rp, s_gr[q]);
       }
-      // weight = |Re(phase R) / Re(phase)| > u  (Wrapgr_mod.F90:141-143), division-free
-      const R num = A::absr(A::re_mul(ph, Rt));
-      const R den = A::mulr(A::absr(A::re(ph)), s_u2[q]);
-      acc = A::gt(num, den);
+      // weight = |Re(phase R) / Re(phase)| > u  (Wrapgr_mod.F90:141-143), division-free, FP64
+      const double num = fabs(ph.x * Rt.x - ph.y * Rt.y);
+      const double den = fabs(ph.x) * s_u2[q];
+      acc = num > den;
       if (acc) {
-        ph = A::renorm(A::mul(ph, Rt));
+        ph = zmul(ph, Rt);
         if (kind != 1) xm = A::mul(s_dlt[fo][v], A::rcp(D));  // Delta / Mat(1,1)
         const Z x[2] = {A::shfl(xm, 0), A::shfl(xm, 1)};
 #pragma unroll
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       if (p.rec_acc) {
         const long long r = (long long)c * p.sRec + p.visit_base + p.q0 + q;
         p.rec_acc[r] = (int8_t)acc;
-        p.rec_ratio[r] = A::wide(Rt);
+        p.rec_ratio[r] = Rt;
       }
       if (acc) fl[s_vtx[q]] = (int8_t)s_snew[q];
       s_acc[v & 1] = acc;
@@ -383,7 +388,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   if (tid == 0) {
     p.m_out[c] = m;
     for (int f = 0; f < F; ++f) p.m_out[p.nChains + c * F + f] = m;
-    if (m > 0) p.phase[c] = A::unit(ph);
+    if (m > 0) p.phase[c] = ArD::unit(ph);
     long long* cn = p.cnt + 4ll * c;
     cn[0] += n_prop; cn[1] += nacc; cn[2] += nq; cn[3] += nacc;
   }

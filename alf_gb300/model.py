@@ -417,3 +417,18 @@ def config(name: str, **over) -> Model:
     if name == "kondo12x12":
         return kondo(12, 12, JK=1.5, Uf=2.0, beta=10.0, dtau=0.1, nwrap=10, **over)
     raise KeyError(name)
+
+
+def batch_groups(seed: int, n: int = 128) -> dict:
+    """The batched Hubbard workload: chain c in [0, n) draws from its own generator
+    (numpy's default_rng([seed, c])) a square L in {6, 8, 10, 12, 14, 16}, beta in
+    {4, 6, 8, 10} (dtau 0.1, so Ltrot 40..100) and U uniform in [2, 8].  Returns
+    {(L, beta): [(chain, U), ...]}: the chains grouped by (N_dim, Ltrot), one handle each."""
+    groups = {}
+    for c in range(n):
+        r = np.random.default_rng([seed, c])
+        L = int(r.choice([6, 8, 10, 12, 14, 16]))
+        beta = float(r.choice([4.0, 6.0, 8.0, 10.0]))
+        U = float(r.uniform(2.0, 8.0))
+        groups.setdefault((L, beta), []).append((c, U))
+    return groups

@@ -120,10 +120,12 @@ class Chains:
         _lib.check(self.L.alfgpu_init_state(self.h, _p(ph)), "alfgpu_init_state")
         return ph
 
-    def sweep(self, uniforms: Optional[np.ndarray] = None, measure: bool = False):
+    def sweep(self, uniforms: Optional[np.ndarray] = None, measure: bool = False, keep=None):
         """One sweep on every chain.  With ``measure``, the library's ham%Obser / ham%ObserT
         callbacks are collected: returns (eq, tau), lists of (chain, ntau, G, phase) and
-        (chain, ntau, [GT0, G0T, G00, GTT], phase), matrices as [nf][row][col]."""
+        (chain, ntau, [GT0, G0T, G00, GTT], phase), matrices as [nf][row][col].  ``keep``
+        (kind, chain, ntau) -> bool, kind 0 = equal-time and 1 = time-displaced, selects the
+        callbacks that are copied (all by default)."""
         eq, tau = [], []
         NN = self.N * self.N
 
@@ -132,6 +134,8 @@ class Chains:
             return np.transpose(a.reshape(k, self.F, self.N, self.N), (0, 1, 3, 2)).copy()
 
         def on_obs(ctx, chain, ntau, kind, G, ph):
+            if keep is not None and not keep(kind, chain, ntau):
+                return
             phase = complex(ph[0], ph[1])
             if kind == 0:
                 eq.append((chain, ntau, mats(G, 1)[0], phase))

@@ -38,10 +38,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "AFQMC sweeps/s (per chain & aggregate), mixed vs FP64 GPU at max|dG|<=1e-5"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# Measured on a GB300 by profiles/fp64_throughput_gb300.md (mma.sync m8n8k4 f64 loop).
+# FP64 peak of a GB300: a register-only loop of independent mma.sync m8n8k4 f64 accumulators
+# (608 CTAs x 256 threads) measured 1.048 TFLOP/s; DFMA gives 1.006.
 FP64_DMMA_TFLOPS = 1.048
 # DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
-# the ncu capture summarised in profiles/k_zgemm_hubbard16x16_fp64.md
+# an ncu capture of the 16x16 workload (dram__bytes_read.sum + dram__bytes_write.sum)
 HOP_TRAFFIC_BYTES = 3.30e6
 
 
@@ -163,8 +164,8 @@ def roofline(args, m, prof):
                 "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
                 "traffic": HOP_TRAFFIC_BYTES if m.ndim == 256 else None,
                 "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
-                "peak_source": "FP64 mma.sync m8n8k4 throughput measured on a GB300 "
-                               "(profiles/fp64_throughput_gb300.md); MEASURED_PEAKS.json has no FP64 figure"}
+                "peak_source": "FP64 mma.sync m8n8k4 throughput measured on a GB300 with a register-only "
+                               "loop; MEASURED_PEAKS.json has no FP64 figure"}
     else:
         peak, src = measured_bf16_peak()
         N, F = m.ndim, m.n_fl
@@ -259,16 +260,9 @@ def workload_model(name: str):
 
 
 def batch128_groups(seed: int, n: int = 128):
-    """Per chain, from its own seed: L in {6,8,10,12,14,16}, beta in {4,6,8,10} (dtau 0.1), U in
-    [2, 8]; grouped by (L, beta), i.e. by (N_dim, Ltrot)."""
-    groups = {}
-    for c in range(n):
-        r = np.random.default_rng([seed, c])
-        L = int(r.choice([6, 8, 10, 12, 14, 16]))
-        beta = float(r.choice([4.0, 6.0, 8.0, 10.0]))
-        U = float(r.uniform(2.0, 8.0))
-        groups.setdefault((L, beta), []).append((c, U))
-    return groups
+    """The 128-chain batch grouped by (N_dim, Ltrot) (alf_gb300.model.batch_groups)."""
+    from alf_gb300 import model as mdl
+    return mdl.batch_groups(seed, n)
 
 
 def run_batch(args, ws, rank, local):

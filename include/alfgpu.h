@@ -52,14 +52,22 @@ enum {
   ALFGPU_ERROR_SIZE = 105           /* size above a fixed maximum (see alfgpu_decompose_noalloc) */
 };
 
-/* Precision forms.  FP64: complex128 throughout (FP64 tensor cores for the products).
- * MIXED: the G wraps through exp(-dtau T) and the delayed-update flush GEMMs run in
- * double-float arithmetic (FP32 hi/lo pairs, ~2^-44 relative rounding) on the FP32
- * pipes; G and all state stay complex128; the UDV propagation, pivoted QR, CGR and its
- * determinant phase, and the Metropolis ratio / phase arithmetic stay FP64.
- * ALFGPU_FLAG_DF_PROPAGATION in dims.reserved[0] also moves the UDV propagation
- * products to double-float; the product of Nwrap slices is ill-conditioned
- * (1e5-1e10 at beta = 10), so this is only usable for small beta / Nwrap. */
+/* Precision forms.  FP64: complex128 throughout; every product on the FP64 pipes
+ * (mma.sync m8n8k4 f64), the per-visit Metropolis chain, QRs, solves and phases in FP64.
+ * MIXED: G and all state stay complex128.  By default the G wraps through exp(-dtau T),
+ * the UDV propagation products and the stabilisation's complex products (CGR's
+ * U_R^H U_L and D_R V_R V_L D_L, the products with Q, decompose's R P V) run on the BF16
+ * tensor cores (tcgen05) as digit-sliced products exact to ~2^-54 of the row / column
+ * scales; on grids of several chains the delayed-update flushes and the explicit Q do
+ * too (one chain keeps the double-float flush and the FP64 explicit Q).  The per-visit
+ * Metropolis ratio, its accept test, the phase update and the block-submatrix updates
+ * run in double-float (FP32 hi/lo pairs, ~2^-46 relative rounding per operation) on the
+ * FP32 pipes.  The pivoted QRs, triangular solves, determinant phases of CGR / CGR2_2
+ * and Precision Green stay FP64 arithmetic.  ALFGPU_FLAG_NO_TENSOR_GEMM replaces the
+ * tensor-core products of the wraps and flushes by double-float GEMMs;
+ * ALFGPU_FLAG_DF_PROPAGATION runs the UDV propagation products in double-float (the
+ * product of Nwrap slices is ill-conditioned, 1e5-1e10 at beta = 10, so this is only
+ * usable for small beta / Nwrap). */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
 enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
 /* Column pivoting of the stabilisation QRs.  Default: ZGEQP3's dynamic pivoting with
@@ -271,7 +279,12 @@ int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V);
  * exits); larger ndim returns ALFGPU_ERROR_SIZE without touching the buffers.
  * The first call on each device resolves the array's device address
  * (cudaGetSymbolAddress) with that device current, so make the first call on
- * a device before any stream capture.  Every call reuses the same array, and
+ * a device before any stream capture.  That set-up is guarded: host threads may
+ * make their first calls on a device at the same time.  The resolved address is
+ * kept for the life of the process and is valid only as long as the device's
+ * primary context: after cudaDeviceReset, or a reset of the primary context by
+ * another library, this entry point must not be called again in that process.
+ * Every call reuses the same array, and
  * each call writes every scratch word it later reads, so no state carries over;
  * calls that overlap on the GPU (different streams or host threads) race on
  * the shared array and must be serialised by the caller.  The call is
@@ -279,12 +292,6 @@ int alfgpu_decompose(int32_t ndim, char side, double* U, double* D, double* V);
 #define ALFGPU_NOALLOC_MAX_NDIM 256
 int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, double* V, double* detU, void* stream);
 
-/* C = A B for real column-major host matrices (m x k, k x n, m x n with leading
- * dimensions lda, ldb, ldc) on the tensor-core GEMM of the mixed form (k_oz_gemm,
- * digit-sliced BF16 with exact FP32 accumulation, ~2^-54 relative to the row and column
- * scales of A and B; k <= 512, else ALFGPU_ERROR_SIZE).  The kernel the G wraps use, exposed for testing and
- * for callers that want FP64-accurate products on the tensor cores.  Synchronous;
- * allocates and frees its own device buffers. */
 /* Device-side equal-time scalar observables of the Hubbard-type models (the Obs_scal part of
  * ham%Obser, Hamiltonian_Hubbard_smod.F90:695-801; kinetic term as
  * Predefined_Hoppings_Compute_Kin, Prog/Predefined_Hop_mod.F90:1905-1959).  At every
@@ -306,6 +313,13 @@ int alfgpu_reset_scalar_obs(alfgpu_t* h);
  * string"); the pointer stays valid until the next call on the handle. */
 const char* alfgpu_last_error(alfgpu_t* h);
 
+/* C = A B for real column-major host matrices (m x k, k x n, m x n with leading
+ * dimensions lda, ldb, ldc) on the tensor-core GEMM of the mixed form (k_oz_gemm,
+ * digit-sliced BF16 with exact FP32 accumulation, ~2^-54 relative to the row and column
+ * scales of A and B; k <= 512, else ALFGPU_ERROR_SIZE).  The kernel the G wraps use,
+ * exposed for testing and for callers that want FP64-accurate products on the tensor
+ * cores.  Synchronous; allocates and frees its own device buffers.  No counterpart in the
+ * reference. */
 int alfgpu_oz_dgemm(int32_t m, int32_t n, int32_t k, const double* A, int32_t lda, const double* B, int32_t ldb,
                     double* C, int32_t ldc, int32_t device);
 

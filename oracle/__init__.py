@@ -192,16 +192,20 @@ class Oracle:
         a = np.ctypeslib.as_array(ptr, shape=(2 * self.F * self.N * self.N,)).view(np.complex128)
         return np.transpose(a.reshape(self.F, self.N, self.N), (0, 2, 1)).copy()  # -> [nf][row][col]
 
-    def collect_measurements(self):
+    def collect_measurements(self, keep=None):
         """Collect the equal-time (ham%Obser) and time-displaced (ham%ObserT) callbacks of
-        the following sweeps: lists of (ntau, G, phase) and (ntau, [GT0, G0T, G00, GTT], phase)."""
+        the following sweeps: lists of (ntau, G, phase) and (ntau, [GT0, G0T, G00, GTT], phase).
+        ``keep`` (kind, ntau) -> bool, kind 0 = equal-time and 1 = time-displaced, selects the
+        callbacks that are copied (all by default)."""
         eq, tau = [], []
 
         def on_eq(ctx, ntau, G, ph):
-            eq.append((ntau, self._mats(G), complex(ph.re, ph.im)))
+            if keep is None or keep(0, ntau):
+                eq.append((ntau, self._mats(G), complex(ph.re, ph.im)))
 
         def on_tau(ctx, ntau, a, b, c, d, ph):
-            tau.append((ntau, [self._mats(x) for x in (a, b, c, d)], complex(ph.re, ph.im)))
+            if keep is None or keep(1, ntau):
+                tau.append((ntau, [self._mats(x) for x in (a, b, c, d)], complex(ph.re, ph.im)))
 
         self._cbs = (EQ_CB(on_eq), TAU_CB(on_tau))
         lib().oracle_set_eq_callback(self.h, self._cbs[0], None)

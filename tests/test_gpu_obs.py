@@ -32,36 +32,50 @@ def _host_sums(eq, H, U, n_sun):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_device_scalar_observables_match_host_sums(precision):
+    # the sums of one sweep are compared on a draw stream whose accept sequence agrees with
+    # the oracle's (in the mixed form a sequence may part only at a draw within rounding of
+    # its weight; then the next seed is taken): one seed must be compared
     m = mdl.hubbard("square", 4, 4, U=4.0, chem=0.3, beta=2.0, dtau=0.1, nwrap=10)
-    seed = 19
-    f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
-    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
-    o = oracle.Oracle(m)
-    o.set_fields(f0)
-    o.init_state()
-    eq_o, _ = o.collect_measurements()
-    o.sweep(u)
     H = mdl.hopping_matrix("square", 4, 4, t=1.0, chem=0.3).real
     U = np.full(m.ndim, 4.0)
-    g = Chains(m, precision=precision)
-    g.set_fields(0, f0)
-    g.init_state()
-    g.set_scalar_obs(np.stack([H, H]), U)
-    g.sweep(u[None, :])
-    if not np.array_equal(g.fields(0), o.fields()):
-        pytest.skip("accept sequences parted at a draw within rounding of its weight")
-    d = g.scalar_obs(0)
-    ref = _host_sums(eq_o, np.stack([H, H]), U, m.n_sun)
-    assert d["count"] == ref["count"] == 2 * m.ltrot - 1
-    assert d["sign"] == ref["sign"]
-    tol = 1e-10 if precision == "fp64" else 1e-5
-    for k in ("kin", "pot", "part", "ener"):
-        assert abs(d[k] - ref[k]) <= tol * max(1.0, abs(ref[k])), (k, d[k], ref[k])
-    # graph replay accumulates the same way, reset clears
-    g.reset_scalar_obs()
-    assert g.scalar_obs(0)["count"] == 0
-    g.sweep(None)
-    assert g.scalar_obs(0)["count"] == 2 * m.ltrot - 1
+    compared = 0
+    for seed in (19, 20, 21, 22):
+        f0 = rng.initial_fields(seed, 0, m.n_op, m.ltrot)
+        u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
+        o = oracle.Oracle(m)
+        o.set_fields(f0)
+        o.init_state()
+        eq_o, _ = o.collect_measurements()
+        o.record(1, green=False)
+        o.sweep(u)
+        g = Chains(m, precision=precision)
+        g.set_fields(0, f0)
+        g.init_state()
+        g.set_scalar_obs(np.stack([H, H]), U)
+        g.set_recording(True)
+        g.sweep(u[None, :])
+        rg, ro = g.record(0), o.recorded()
+        if not np.array_equal(rg["acc"], ro["acc"]):
+            assert precision == "mixed", "FP64 accept sequence differs from the oracle"
+            v = int(np.argmax(rg["acc"] != ro["acc"]))
+            w = abs(ro["ratio"][v])
+            assert abs(w - u[3 * v + 2]) < 1e-4 * max(w, 1.0), (seed, v)
+            continue
+        d = g.scalar_obs(0)
+        ref = _host_sums(eq_o, np.stack([H, H]), U, m.n_sun)
+        assert d["count"] == ref["count"] == 2 * m.ltrot - 1
+        assert d["sign"] == ref["sign"]
+        tol = 1e-10 if precision == "fp64" else 1e-5
+        for k in ("kin", "pot", "part", "ener"):
+            assert abs(d[k] - ref[k]) <= tol * max(1.0, abs(ref[k])), (k, d[k], ref[k])
+        # graph replay accumulates the same way, reset clears
+        g.reset_scalar_obs()
+        assert g.scalar_obs(0)["count"] == 0
+        g.sweep(None)
+        assert g.scalar_obs(0)["count"] == 2 * m.ltrot - 1
+        compared += 1
+        break
+    assert compared == 1
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
