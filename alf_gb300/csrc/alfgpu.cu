@@ -57,6 +57,9 @@ struct alfgpu_s {
   zd *ozGm = nullptr, *ozTm = nullptr, *ozWm = nullptr, *ozXm = nullptr;  // compact-WY explicit Q work
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
+  // digit slices used by the G wraps (and TAU_M's propagation) and by the UDV propagation: a
+  // prefix of the oz_S slices (dims.reserved[1] / [2] give the target bits; default oz_S)
+  int ozw_S = 0, ozp_S = 0;
   unsigned short* ozE[4] = {nullptr, nullptr, nullptr, nullptr};  // expT, expTinv as A; expT, expTinv as B
   int* ozEe[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned short *ozGA = nullptr, *ozGB = nullptr, *ozXA = nullptr, *ozYB = nullptr;
@@ -369,10 +372,13 @@ static int oz_slice(alfgpu_s* h, const void* src, int mode, long long sr, long l
 static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int Nn, int Kpad, int S,
                    int bits, int bn, int nst, int RpadA, int RpadB, int modA, int modB, const int* expA,
                    const int* expB, int omode, int osub, void* out, long long ldr, long long ldc, long long sout,
-                   int batch, const zd* rsc = nullptr, long long srsc = 0) {
+                   int batch, const zd* rsc = nullptr, long long srsc = 0, int SbA = 0, int SbB = 0,
+                   const zd* csc = nullptr, long long scsc = 0) {
   OzGemmParams p;
   memset(&p, 0, sizeof(p));
   p.M = M; p.N = Nn; p.nkc = Kpad / OZ_KC; p.S = S; p.bits = bits; p.nst = nst; p.nd = S + 1;
+  p.SbA = SbA > 0 ? SbA : S; p.SbB = SbB > 0 ? SbB : S;
+  p.csc = csc; p.scsc = scsc;
   p.L = oz_shift(Kpad, bits, S, p.nd);
   p.RpadA = RpadA; p.RpadB = RpadB; p.modA = modA; p.modB = modB; p.expA = expA; p.expB = expB;
   p.omode = omode; p.osub = osub; p.out = out; p.ldr = ldr; p.ldc = ldc; p.sout = sout; p.err = h->err;
@@ -742,11 +748,11 @@ static int wrapur_u(alfgpu_s* h, UDVSet& u, int ntau, int ntau1) {
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
     RET(slice_scale(h, nt));
     if (oz_propagate(h)) {  // U <- diag(S) expT U on the tensor cores, in place (U is sliced first)
-      RET(oz_slice(h, u.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->oz_S, h->oz_bits,
+      RET(oz_slice(h, u.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->ozp_S, h->oz_bits,
                    h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
-      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->oz_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->ozp_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
                   h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, u.U, 1, N, (long long)N * N, B, h->S,
-                  N));
+                  N, h->oz_S, h->ozp_S));
       continue;
     }
     GemmParams p = gsq(h, B);
@@ -769,10 +775,11 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
   for (int nt = ntau1; nt >= ntau + 1; --nt) {
     RET(slice_scale(h, nt));
     if (oz_propagate(h)) {  // U <- expT diag(conj S) U on the tensor cores (S real), in place
-      RET(oz_slice(h, h->udvl.U, OZ_CROWS, N, 1, (long long)N * N, 0, h->S, N, N, N, nullptr, h->oz_S, h->oz_bits,
+      RET(oz_slice(h, h->udvl.U, OZ_CROWS, N, 1, (long long)N * N, 0, h->S, N, N, N, nullptr, h->ozp_S, h->oz_bits,
                    h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
-      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->oz_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
-                  h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, h->udvl.U, 1, N, (long long)N * N, B));
+      RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->ozp_S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+                  h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, h->udvl.U, 1, N, (long long)N * N, B,
+                  nullptr, 0, h->oz_S, h->ozp_S));
       continue;
     }
     GemmParams q = gsq(h, B);
@@ -1051,6 +1058,29 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
   return 0;
 }
 
+// TAU_M's propagation products on the tensor-core GEMM (mixed form, real slice scales), in
+// place (the operand is sliced before the product overwrites it), with the G wraps' digit count:
+// PROPR   X <- diag(S) expT X          (tau_m_mod.F90:213-236)
+// PROPRM1 X <- X expTinv diag(Sinv)    (tau_m_mod.F90:238-263)
+static bool oz_tau(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_complex; }
+static int oz_propr(alfgpu_s* h, zd* X) {
+  const int N = h->N, B = h->B, S = h->ozw_S;
+  const long long NN = (long long)N * N;
+  RET(oz_slice(h, X, OZ_CROWS, N, 1, NN, 0, nullptr, 0, N, N, nullptr, S, h->oz_bits, h->oz_Rp2N, h->oz_Kpad,
+               h->ozGB, h->ozGBe, B));
+  return oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+                 h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, X, 1, N, NN, B, h->S, N, h->oz_S, S);
+}
+static int oz_proprm1(alfgpu_s* h, zd* X) {
+  const int N = h->N, B = h->B, S = h->ozw_S;
+  const long long NN = (long long)N * N;
+  RET(oz_slice(h, X, OZ_CROWS, 1, N, NN, 0, nullptr, 0, N, N, nullptr, S, h->oz_bits, h->oz_Rp2N, h->oz_Kpad,
+               h->ozGA, h->ozGAe, B));
+  return oz_gemm(h, h->tmGA, h->tmE[3], 2 * N, N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_Rp2N,
+                 h->oz_RpN, 0, h->F, h->ozGAe, h->ozEe[3], OZ_OUT_ROWS, 0, X, 1, N, NN, B, nullptr, 0, S, h->oz_S,
+                 h->Sinv, N);
+}
+
 // TAU_M (tau_m_mod.F90:56-211), finite temperature, after the sweep: GT0, G0T, G00, GTT for
 // every slice, ObserT each slice, CGR2_2 and Control_Precision_tau every Nwrap block.
 static int tau_m(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx) {
@@ -1066,6 +1096,12 @@ static int tau_m(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx) {
     const int NT1 = NT + 1;
     RET(slice_scale(h, NT1));
     prof_begin(h, ALFGPU_PROF_HOP);
+    if (oz_tau(h)) {
+      RET(oz_propr(h, h->GT0));     // PROPR(GT0)
+      RET(oz_proprm1(h, h->G0T));   // PROPRM1(G0T)
+      RET(oz_proprm1(h, h->GTT));   // PROPRM1 then PROPR (GTT)
+      RET(oz_propr(h, h->GTT));
+    } else {
     {  // PROPR(GT0): GT0 = S (expT GT0)
       GemmParams p = gsq(h, B);
       p.A = h->expT; p.realA = 1; p.modA = F; p.B = h->GT0; p.C = h->T1; p.rs = h->S; p.sRS = N;
@@ -1085,6 +1121,7 @@ static int tau_m(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx) {
       GemmParams q = gsq(h, B);
       q.A = h->expT; q.realA = 1; q.modA = F; q.B = h->T1; q.C = h->GTT; q.rs = h->S; q.sRS = N;
       RET(gemm(h, q));
+    }
     }
     prof_end(h);
     RET(obs_tau(h, cb, ctx, NT1));
@@ -1124,25 +1161,26 @@ static int hop_impl(alfgpu_s* h, int up, int with_scale) {
   if (h->mixed && h->oz && !(with_scale && h->eexp_complex)) {
     // up:   T1 = expT diag(S) G (row-major), G = T1 diag(Sinv) expTinv
     // down: T1 = G diag(S) expT (column-major), G = expTinv diag(Sinv) T1
+    // the wraps use the first ozw_S digit slices (the expT slices hold oz_S per flavour)
     const long long NN = (long long)N * N;
-    const int S = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
+    const int S = h->ozw_S, SE = h->oz_S, bits = h->oz_bits, Kp = h->oz_Kpad, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
     const int bn = h->oz_bn, nst = h->oz_nst;
     const zd* s1 = with_scale ? h->S : nullptr;
     const zd* s2 = with_scale ? h->Sinv : nullptr;
     if (up) {
       RET(oz_slice(h, h->G, OZ_CROWS, N, 1, NN, 0, s1, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGB, h->ozGBe, B));
       RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, Kp, S, bits, bn, nst, RpN, Rp2, F, 0, h->ozEe[0], h->ozGBe,
-                  OZ_OUT_COLS, 0, h->T1, N, 1, NN, B));
+                  OZ_OUT_COLS, 0, h->T1, N, 1, NN, B, nullptr, 0, SE, S));
       RET(oz_slice(h, h->T1, OZ_CROWS, N, 1, NN, 0, s2, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGA, h->ozGAe, B));
       RET(oz_gemm(h, h->tmGA, h->tmE[3], 2 * N, N, Kp, S, bits, bn, nst, Rp2, RpN, 0, F, h->ozGAe, h->ozEe[3],
-                  OZ_OUT_ROWS, 0, h->G, 1, N, NN, B));
+                  OZ_OUT_ROWS, 0, h->G, 1, N, NN, B, nullptr, 0, S, SE));
     } else {
       RET(oz_slice(h, h->G, OZ_CROWS, 1, N, NN, 0, s1, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGA, h->ozGAe, B));
       RET(oz_gemm(h, h->tmGA, h->tmE[2], 2 * N, N, Kp, S, bits, bn, nst, Rp2, RpN, 0, F, h->ozGAe, h->ozEe[2],
-                  OZ_OUT_ROWS, 0, h->T1, 1, N, NN, B));
+                  OZ_OUT_ROWS, 0, h->T1, 1, N, NN, B, nullptr, 0, S, SE));
       RET(oz_slice(h, h->T1, OZ_CROWS, N, 1, NN, 0, s2, N, N, N, nullptr, S, bits, Rp2, Kp, h->ozGB, h->ozGBe, B));
       RET(oz_gemm(h, h->tmE[1], h->tmGB, N, 2 * N, Kp, S, bits, bn, nst, RpN, Rp2, F, 0, h->ozEe[1], h->ozGBe,
-                  OZ_OUT_COLS, 0, h->G, 1, N, NN, B));
+                  OZ_OUT_COLS, 0, h->G, 1, N, NN, B, nullptr, 0, SE, S));
     }
     return 0;
   }
@@ -1293,6 +1331,15 @@ static int oz_setup(alfgpu_s* h) {
   h->oz_RpN = oz_round(N, OZ_BM);
   h->oz_Rp2N = oz_round(2 * N, OZ_BM);
   if (oz_pick(h->oz_Kpad, &h->oz_bits, &h->oz_S) || oz_pick(2 * UPD_KMAX, &h->ozf_bits, &h->ozf_S)) return 0;
+  // digit slices of the G wraps / TAU_M propagation (reserved[1]) and the UDV propagation
+  // (reserved[2]): the target bits rounded up to whole slices, at most oz_S
+  auto slices_for = [&](int target) {
+    if (target <= 0) return h->oz_S;
+    const int s = (target + h->oz_bits - 1) / h->oz_bits;
+    return std::max(2, std::min(h->oz_S, s));
+  };
+  h->ozw_S = slices_for(h->d.reserved[1]);
+  h->ozp_S = slices_for(h->d.reserved[2]);
   // CTAs of one wrap product at BN = 32; fewer than two per SM: the narrow tile
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);

@@ -16,7 +16,11 @@
 // FP64-level on the O(1) entries of Green functions and hopping exponentials; FP32
 // products (2^-24) are not enough there (they are amplified by the stabilisation
 // interval).  Complex products are real GEMMs on interleaved real/imaginary rows
-// (k_oz_slice modes) with the complex element assembled in the epilogue.
+// (k_oz_slice modes) with the complex element assembled in the epilogue.  The first S'
+// digits of an S-digit slicing are the S'-digit slicing of the same element (same row
+// exponent and digit width), so a product may use a prefix of a buffer's slices (SbA /
+// SbB give the buffers' own slice counts): fewer slices trade accuracy, 2^-(b S'), for
+// (S' + 1)(S' + 2)/2 - 2 instead of (S + 1)(S + 2)/2 - 2 digit products.
 //
 //   k_oz_slice  FP64 -> BF16 digit slices [batch][S][Rpad][Kpad] (K contiguous) and the
 //               row exponents, integer arithmetic only (the FP64 pipe is 1/64 of FP32)
@@ -400,6 +404,8 @@ struct OzGemmParams {
   void* out; long long ldr, ldc, sout;  // element strides (complex128 for _COLS/_ROWS, float64 for _REAL)
   int* err;                  // bit 2: a bounded wait gave up
   const zd* rsc; long long srsc;  // optional real scale of output row m (real part used), per batch
+  const zd* csc; long long scsc;  // optional real scale of output column n (OZ_OUT_ROWS; real part), per batch
+  int SbA, SbB;              // slices per batch entry in the A / B slice buffers (>= S: the first S are used)
 };
 
 static inline size_t oz_smem_bytes(int bn, int S, int nkc, int nst) {
@@ -460,7 +466,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   const uint32_t chunkA = OZ_BM * 128, chunkB = BN * 128;
 
   if (tid == 0) {  // producer
-    const int rowA0 = bA * S * p.RpadA + m0, rowB0 = bB * S * p.RpadB + n0;
+    const int rowA0 = bA * p.SbA * p.RpadA + m0, rowB0 = bB * p.SbB * p.RpadB + n0;
     oz_mbar_expect_tx(bfull, (uint32_t)(S * nkc) * chunkB);
     for (int t = 0; t < S; ++t)
       for (int kc = 0; kc < nkc; ++kc)
@@ -545,6 +551,13 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
       const double s = p.rsc[(size_t)b * p.srsc + m].x;
 #pragma unroll
       for (int j = 0; j < HB; ++j) v[j] *= s;
+    }
+    if (p.csc) {  // OZ_OUT_ROWS: real column n is complex column n
+#pragma unroll
+      for (int j = 0; j < HB; ++j) {
+        const int n = n0 + c0 + j;
+        if (n < p.N) v[j] *= p.csc[(size_t)b * p.scsc + n].x;
+      }
     }
     if (p.omode == OZ_OUT_REAL) {
       double* o = (double*)p.out + (size_t)b * p.sout;

@@ -50,12 +50,14 @@ def _p(a: np.ndarray):
 class Chains:
     def __init__(self, model: Model, n_chains: int = 1, precision: str = "fp64", delay_k: int = 0,
                  device: int = 0, ltau: int = 0, models: Optional[Sequence[Model]] = None,
-                 pivoting: str = "default", flags: int = 0):
+                 pivoting: str = "default", flags: int = 0, wrap_bits: int = 0, propagate_bits: int = 0):
         """``pivoting``: "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)
         for every stabilisation QR; "norms" orders the columns once by their norms (ALF's
         STABLOG pivoting) and factors them with the blocked QR; "norms-cgr" /
         "norms-decompose" do so at one call site; "default" is "exact" in the FP64 form and
-        "norms-cgr" in the mixed form."""
+        "norms-cgr" in the mixed form.  ``wrap_bits`` / ``propagate_bits`` (mixed form): target
+        bits of the digit-sliced tensor-core products of the G wraps (and TAU_M) / of the UDV
+        propagation (dims.reserved[1] / [2]; 0 = the full ~54)."""
         self.L = _lib.lib()
         self.model = model
         self.C = n_chains
@@ -63,6 +65,8 @@ class Chains:
         d = _lib.Dims(model.ndim, model.n_fl, model.n_sun, model.n_op, model.ltrot, model.nwrap, n_chains,
                       PRECISIONS[precision], delay_k, ltau, device)
         d.reserved[0] = PIVOTING[pivoting] | flags
+        d.reserved[1] = wrap_bits
+        d.reserved[2] = propagate_bits
         h = C.c_void_p()
         _lib.check(self.L.alfgpu_create(C.byref(h), C.byref(d)), "alfgpu_create")
         self.h = h

@@ -1,25 +1,31 @@
 #!/usr/bin/env python
 """Benchmark: AFQMC sweeps/s of ALF's finite-temperature sweep on a GB300.
 
-Workload (default): Hubbard model on a 16x16 square lattice, N_dim = 256,
-t = 1, U = 4, mu = 0, beta = 10, dtau = 0.1 (Ltrot = 100), Nwrap = 10, Mz
-decoupling with four-valued fields, one Markov chain.  A step is one full
-sequential sweep (up pass, down pass, 2*Nstm stabilisations).
+Default workload: Hubbard model on a 16x16 square lattice, N_dim = 256, t = 1, U = 4,
+mu = 0, beta = 10, dtau = 0.1 (Ltrot = 100), Nwrap = 10, Mz decoupling with four-valued
+fields; independent Markov chains, aggregate sweeps/s.  A step is one full sequential
+sweep (up pass, down pass, 2*Nstm stabilisations) of every chain.
 
-value: sweeps/s with all state resident on the device, timed with CUDA events
-       on the library's stream (device draw stream, no host traffic).
-mixed: (FP64 runs, one GPU) the same measurements for the mixed form on the same
-       workload, and max |G_mixed - G_fp64| after one sweep on identical fields and draws.
-e2e:   the same metric through the C ABI with host buffers: each step copies
-       the host draws in (6*M*Ltrot doubles) and reads G back (N^2*N_FL complex),
-       both inside the timed region.
---impl reference: ALF's algorithm on the host cores (the CPU restatement that
-       calls the same LAPACK; the Fortran reference cannot be built here), one
-       chain, all host threads given to its BLAS, each step a bounded sample of
-       a sweep (a fixed number of time slices with their stabilisations) scaled
-       to sweeps/s.
-Multi-GPU (torchrun): every rank runs an independent chain (replicas); value is
-the total sweeps of all ranks / the max over ranks of the timed region.
+value:     aggregate sweeps/s of the batched mixed form: C chains (16 by default) in one
+           handle, all state resident on the device, timed with CUDA events on the
+           library's stream (device draw stream, L2 flushed between steps).
+fp64:      the same for the plain FP64 form on the same workload and chain count, and
+           mixed_over_fp64 = value / fp64.value (the spec ratio).
+per_chain: one chain per handle in both forms (the single-chain rate).
+vs_fp64:   max |G_mixed - G_fp64| after one sweep on identical fields and draws.
+e2e:       the headline through the C ABI with host buffers: each step copies every
+           chain's host draws in (6*M*Ltrot doubles per chain) and reads G of chain 0 back,
+           both inside the timed region.
+--impl reference: ALF's own use of a host (Documentation/performance.tex:29-37): one
+           single-threaded walker per host core, each an independent chain on its own
+           seed, running the CPU restatement of ALF's sweep (the same LAPACK calls; the
+           Fortran reference has no compiler here).  A step is one whole sweep of every
+           walker; value = walkers x steps / time.  The rate of one chain with all host
+           threads given to its BLAS is measured beside it.
+--config batch128: 128 chains with per-chain L, beta, U in one handle per (N_dim, Ltrot)
+           group; the groups sweep concurrently from one host thread each.
+Multi-GPU (torchrun): every rank runs its own chains (replicas); value is the total
+sweeps of all ranks / the max over ranks of the timed region.
 """
 from __future__ import annotations
 
@@ -41,9 +47,12 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # FP64 peak of a GB300: a register-only loop of independent mma.sync m8n8k4 f64 accumulators
 # (608 CTAs x 256 threads) measured 1.048 TFLOP/s; DFMA gives 1.006.
 FP64_DMMA_TFLOPS = 1.048
-# DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours), from
-# an ncu capture of the 16x16 workload (dram__bytes_read.sum + dram__bytes_write.sum)
+# DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours, one chain),
+# from an ncu capture of the 16x16 workload (dram__bytes_read.sum + dram__bytes_write.sum)
 HOP_TRAFFIC_BYTES = 3.30e6
+# default chains per GPU of each workload (the batched forms of the benchmark configurations)
+DEFAULT_CHAINS = {"hubbard4x4": 1, "hubbard16x16": 16, "honeycomb12x12": 1, "kondo12x12": 32, "batch128": 128}
+L2_NOTE = "GPU arm: L2 flushed between timed steps (256 MB write); host arm: not applicable"
 
 
 def measured_bf16_peak():
@@ -54,7 +63,7 @@ def measured_bf16_peak():
         return 1900.0, "fallback 1.9 PFLOP/s bf16 burst"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -62,22 +71,31 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="hubbard16x16",
                     choices=["hubbard4x4", "hubbard16x16", "honeycomb12x12", "kondo12x12", "batch128"],
-                    help="hubbard16x16: one 16x16 chain; honeycomb12x12: 12x12 honeycomb, beta 20, TAU_M every "
+                    help="hubbard16x16: 16x16 Hubbard chains; honeycomb12x12: 12x12 honeycomb, beta 20, TAU_M every "
                          "sweep; kondo12x12: Kondo bilayer (ham_Uf = 0), TAU_M every sweep; batch128: 128 Hubbard "
                          "chains with per-chain L, beta, U, one handle per (N_dim, Ltrot) group")
     ap.add_argument("--ltau", type=int, default=-1, help="TAU_M every sweep (default: the config's)")
     ap.add_argument("--drift-bound", type=float, default=1e-5,
                     help="batch128: Nwrap of a group is halved until its Precision Green is below this")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"], help="the headline form")
     ap.add_argument("--flags", type=int, default=0, help="dims.reserved[0] flag bits (include/alfgpu.h)")
     ap.add_argument("--pivoting", default="default", choices=["default", "exact", "norms", "norms-cgr", "norms-decompose"])
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--chains", type=int, default=1, help="independent chains per GPU (batched)")
+    ap.add_argument("--chains", type=int, default=-1, help="independent chains per GPU (default: the config's)")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="keep the default delay depth")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serial-groups", action="store_true", help="batch128: sweep the groups one after another")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
-                    help="FP64 runs: skip the mixed-form measurement reported beside the headline")
-    return ap.parse_args()
+                    help="skip the other form and the one-chain runs reported beside the headline")
+    ap.add_argument("--walkers", type=int, default=-1, help="--impl reference: host walkers (default: all cores)")
+    ap.add_argument("--wrap-bits", type=int, default=0,
+                    help="mixed form: target bits of the G-wrap / TAU_M tensor-core products (0: full)")
+    ap.add_argument("--propagate-bits", type=int, default=0,
+                    help="mixed form: target bits of the UDV-propagation tensor-core products (0: full)")
+    a = ap.parse_args(argv)
+    if a.chains < 1:
+        a.chains = DEFAULT_CHAINS[a.config]
+    return a
 
 
 def dist_env():
@@ -134,8 +152,8 @@ class ClockSampler:
 
 
 def algorithmic_flops(m, phase: str, launches: int, n_acc: int) -> float:
-    """Algorithmic FLOPs of one phase over `launches` launch groups (real-flop convention:
-    complex MAC = 8, real x complex MAC = 4; LAPACK counts for QR)."""
+    """Algorithmic FLOPs of one phase over `launches` launch groups of one chain (real-flop
+    convention: complex MAC = 8, real x complex MAC = 4; LAPACK counts for QR)."""
     N, F = m.ndim, m.n_fl
     if phase == "hop":        # 2 real x complex N^3 products per flavour per group
         return launches * 2 * F * 4.0 * N ** 3
@@ -150,7 +168,16 @@ def algorithmic_flops(m, phase: str, launches: int, n_acc: int) -> float:
     return None
 
 
-def roofline(args, m, prof):
+def digit_pairs(n: int):
+    """(bits, slices, digit-pair products per algorithmic product) of the digit-sliced
+    tensor-core GEMM at inner dimension n, as the library picks them (ozaki.cuh oz_pick)."""
+    kpad = (n + 63) // 64 * 64
+    bits, S = next((b, (54 + b - 1) // b) for b in range(7, 3, -1)
+                   if ((54 + b - 1) // b) * kpad * ((1 << b) - 1) ** 2 < 2 ** 24)
+    return bits, S, S * (S + 1) // 2 + (S - 1)
+
+
+def roofline(precision: str, chains: int, m, prof):
     """Roofline object of the G-wrap GEMM, the largest consumer of the complex products with a
     clean algorithmic count (2 real x complex N^3 products per flavour per slice, 2 L slices
     per sweep).  FP64 form: k_zgemm against the measured FP64 MMA rate.  Mixed form:
@@ -158,30 +185,26 @@ def roofline(args, m, prof):
     algorithmic count is the same as FP64's, the BF16 products actually executed are
     reported beside it (tensor_op_tflops)."""
     hop_ms, hop_n = prof.get("hop", (0.0, 0))
-    flops = algorithmic_flops(m, "hop", hop_n, 0) * args.chains
-    if args.precision == "fp64":
+    flops = algorithmic_flops(m, "hop", hop_n, 0) * chains
+    if precision == "fp64":
         roof = {"bound": "tensor", "kernel": "k_zgemm (G wraps, FP64 mma.sync)", "achieved": None,
                 "peak": FP64_DMMA_TFLOPS, "unit": "TFLOP/s", "frac": None,
-                "traffic": HOP_TRAFFIC_BYTES if m.ndim == 256 else None,
-                "algorithmic_flops_per_launch": args.chains * m.n_fl * 4.0 * m.ndim ** 3,
+                "traffic": HOP_TRAFFIC_BYTES * chains if m.ndim == 256 else None,
+                "algorithmic_flops_per_launch": chains * m.n_fl * 4.0 * m.ndim ** 3,
                 "peak_source": "FP64 mma.sync m8n8k4 throughput measured on a GB300 with a register-only "
                                "loop; MEASURED_PEAKS.json has no FP64 figure"}
     else:
         peak, src = measured_bf16_peak()
-        N, F = m.ndim, m.n_fl
-        kpad = (N + 63) // 64 * 64
-        bits, S = next((b, (54 + b - 1) // b) for b in range(7, 3, -1)
-                       if ((54 + b - 1) // b) * kpad * ((1 << b) - 1) ** 2 < 2 ** 24)
-        pairs = S * (S + 1) // 2 + (S - 1)  # digit pairs of the S + 1 accumulated diagonals
+        _, _, pairs = digit_pairs(m.ndim)
         roof = {"bound": "tensor", "kernel": "k_oz_slice + k_oz_gemm (G wraps, digit-sliced BF16 on tcgen05)",
                 "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": None,
-                "algorithmic_flops_per_launch": args.chains * F * 4.0 * N ** 3,
+                "algorithmic_flops_per_launch": chains * m.n_fl * 4.0 * m.ndim ** 3,
                 "bf16_products_per_algorithmic_product": pairs,
                 "peak_source": src + "; of measured"}
     if flops and hop_ms > 0:
         roof["achieved"] = flops / (hop_ms / 1e3) / 1e12
         roof["frac"] = roof["achieved"] / roof["peak"]
-        if args.precision != "fp64":
+        if precision != "fp64":
             roof["tensor_op_tflops"] = roof["achieved"] * roof["bf16_products_per_algorithmic_product"]
     return roof
 
@@ -225,8 +248,8 @@ def sweep_roofline(m, n_acc: float, ltau: int, chains: int, ms_per_step: float, 
 
 
 def sweep_roofline_groups(groups, ms_per_step: float, precision: str, p_fp64: float, p_bf16: float) -> dict:
-    """The same over several handles run one after the other in a step: groups of
-    (model, accepted flips per chain and sweep, ltau, chains)."""
+    """The same over several handles swept in one step: groups of (model, accepted flips per
+    chain and sweep, ltau, chains)."""
     if isinstance(groups, Exception):
         raise groups
     fl = {}
@@ -265,105 +288,154 @@ def batch128_groups(seed: int, n: int = 128):
     return mdl.batch_groups(seed, n)
 
 
-def run_batch(args, ws, rank, local):
-    """Config batch128: one handle per (N_dim, Ltrot) group with per-chain U; a step is one
-    sweep of every chain (groups one after the other on the GPU)."""
-    import torch
-    from alf_gb300 import model as mdl, rng, replicas
-    from alf_gb300.sweep import Chains
-    torch.cuda.set_device(local)
-    groups = batch128_groups(replicas.replica_seed(args.seed, rank))
-    hs = []
-    for (L, beta), members in sorted(groups.items()):
-        models = [mdl.hubbard("square", L, L, U=U, beta=beta, dtau=0.1, nwrap=10) for _, U in members]
-        ch = Chains(models[0], n_chains=len(members), precision=args.precision, device=local,
-                    pivoting=args.pivoting, flags=args.flags, models=models)
-        for k, (c, _) in enumerate(members):
-            s = replicas.replica_seed(args.seed, rank, c)
-            ch.set_fields(k, rng.initial_fields(s, k, models[0].n_op, models[0].ltrot))
-        ch.init_state()
-        for k, (c, _) in enumerate(members):
-            ch.set_rng(k, replicas.replica_seed(args.seed, rank, c), rng.sweep_counter_base(models[0].n_op, models[0].ltrot, 0))
-        hs.append((ch, models[0], members))
-    nchains = sum(len(x[2]) for x in hs)
-    streams = [torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local) for ch, _, _ in hs]
-    for _ in range(args.warmup):
-        for ch, m, mem in hs:
-            try:
-                ch.sweep(None)
-            except Exception as e:
-                raise RuntimeError(f"group L={m.params.get('L1')} Ltrot={m.ltrot} chains={len(mem)}: {e}") from e
-    # drift control: per group, halve Nwrap until Precision Green <= the bound (untimed sweeps)
-    nwraps = []
-    for ch, m, mem in hs:
-        nw, worst = ch.adapt_nwrap(bound=args.drift_bound)
-        nwraps.append((nw, worst))
-    for ch, _, _ in hs:
-        ch.reset_stats()
-    torch.cuda.synchronize()
-    n0 = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs)
-    ms = 0.0
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
-            for (ch, _, _), st in zip(hs, streams):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(st)
-                ch.sweep(None)
-                e1.record(st)
-                e1.synchronize()
-                ms += e0.elapsed_time(e1)
-    n_launch = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs) - n0
-    # per group for the whole-sweep roofline: the adapted Nwrap, accepted flips per chain and sweep
-    import dataclasses
+def bench_config(args, m, ltau) -> dict:
+    """The `config` object of both arms' lines (identical by construction: the workload and
+    how the aggregate is formed; how each arm runs it is in its `arm` object)."""
+    if args.config == "batch128":
+        desc = ("batch128: 128 Hubbard chains on square L x L lattices, per chain from its own seed L in "
+                "{6,...,16}, beta in {4,6,8,10}, dtau 0.1, U in [2,8], Nwrap 10 (halved per group until Precision "
+                f"Green <= {args.drift_bound:g}), Mz four-valued fields")
+    elif args.config == "kondo12x12":
+        desc = (f"kondo12x12: Kondo bilayer square 12x12, N_dim={m.ndim}, J_K=1.5, ham_Uf=0, beta={m.beta}, "
+                f"dtau={m.dtau}, Ltrot={m.ltrot}, Nwrap={m.nwrap}, N_SUN=2, N_FL=1, four-valued fields, "
+                f"TAU_M every sweep: {bool(ltau)}")
+    else:
+        desc = (f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
+                f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
+                f"Nwrap={m.nwrap}, Mz four-valued fields, TAU_M every sweep: {bool(ltau)}")
+    return {"workload": desc, "aggregate": "independent Markov chains on their own seeds; sweeps/s summed over chains",
+            "step": "one full sweep of every chain", "l2": L2_NOTE}
+
+
+# ---------------------------------------------------------------------------------------------
+# the host arm: ALF's one walker per core
+# ---------------------------------------------------------------------------------------------
+def _host_walker(conn, config: str, seed: int, chain: int):
+    """One host walker: a single-threaded chain of the CPU restatement of ALF's sweep."""
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
     try:
-        rgroups = [(dataclasses.replace(m, nwrap=ch.nwrap()),
-                    sum(ch.stats(k).n_acc for k in range(len(mem))) / float(args.steps * len(mem)), 0, len(mem))
-                   for ch, m, mem in hs]
-    except Exception as e:  # only the roofline object depends on it
-        rgroups = e
-    h2d = d2h = 0
+        import oracle
+        from alf_gb300 import replicas, rng
+        m, ltau = workload_model(config)
+        s = replicas.replica_seed(seed, 0, chain)
+        o = oracle.Oracle(m, ltau=ltau, threads=1)
+        o.set_fields(rng.initial_fields(s, chain, m.n_op, m.ltrot))
+        o.init_state()
+        conn.send("ready")
+        k = 0
+        while conn.recv() == "sweep":
+            o.sweep(rng.sweep_uniforms(s, chain, m.n_op, m.ltrot, k))
+            k += 1
+            conn.send(k)
+    except Exception as e:  # reported by the parent
+        conn.send(f"error: {type(e).__name__}: {e}")
+    finally:
+        conn.close()
+
+
+def host_walkers_rate(config: str, seed: int, walkers: int, steps: int, warmup: int) -> dict:
+    """Aggregate sweeps/s of `walkers` independent single-threaded host walkers (spawned
+    processes, each on its own chain): every step sends one whole sweep to every walker and
+    waits for all; value = walkers x steps / time of the timed steps."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    pipes, procs = [], []
+    try:
+        for c in range(walkers):
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_host_walker, args=(b, config, seed, c), daemon=True)
+            p.start()
+            pipes.append(a)
+            procs.append(p)
+        for a in pipes:
+            r = a.recv()
+            if r != "ready":
+                raise RuntimeError(r)
+        times = []
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            for a in pipes:
+                a.send("sweep")
+            for a in pipes:
+                r = a.recv()
+                if isinstance(r, str):
+                    raise RuntimeError(r)
+            if i >= warmup:
+                times.append(time.perf_counter() - t0)
+        t = float(sum(times))
+        return {"value": walkers * steps / t, "walkers": walkers, "steps": steps, "seconds": t,
+                "s_per_step": times}
+    finally:
+        for a in pipes:
+            try:
+                a.send("stop")
+            except Exception:
+                pass
+        for p in procs:
+            p.join(timeout=30)
+            if p.is_alive():
+                p.kill()
+
+
+def one_chain_all_threads_rate(m, ltau: int, seed: int, threads: int, sweeps: int = 1) -> dict:
+    """Sweeps/s of one chain of the CPU restatement with `threads` BLAS threads, whole sweeps
+    after one untimed sweep."""
+    import oracle
+    from alf_gb300 import replicas, rng
+    s = replicas.replica_seed(seed, 0, 0)
+    o = oracle.Oracle(m, ltau=ltau, threads=threads)
+    o.set_fields(rng.initial_fields(s, 0, m.n_op, m.ltrot))
+    o.init_state()
+    o.sweep(rng.sweep_uniforms(s, 0, m.n_op, m.ltrot, 0))
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        for ch, m, members in hs:
-            u = np.stack([rng.sweep_uniforms(replicas.replica_seed(args.seed, rank, c), k, m.n_op, m.ltrot, 1000 + i)
-                          for k, (c, _) in enumerate(members)])
-            ch.sweep(u)
-            g = ch.green(0)
-            if i == 0:
-                h2d += u.nbytes
-                d2h += g.nbytes
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    xmax = max(ch.stats(k).xmaxG for ch, _, mem in hs for k in range(len(mem)))
-    out = dict(t_dev=ms / 1e3, t_e2e=e2e_s, clocks=clk.summary(), launches=n_launch, h2d=h2d, d2h=d2h,
-               nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem),
-                                        "nwrap": nw, "xmaxG_at_adapt": worst}
-                                       for (_, m, mem), (nw, worst) in zip(hs, nwraps)], xmaxG=xmax,
-               rgroups=rgroups)
-    for ch, _, _ in hs:
-        ch.close()
-    return out
+    for k in range(sweeps):
+        o.sweep(rng.sweep_uniforms(s, 0, m.n_op, m.ltrot, 1 + k))
+    dt = time.perf_counter() - t0
+    return {"value": sweeps / dt, "threads": threads, "sweeps": sweeps, "seconds": dt}
 
 
-def run_ours(args, ws, rank, local):
+def host_baseline(args, m, ltau, steps: int, warmup: int) -> dict:
+    """cpu_baseline object: the host walkers' aggregate (ALF's model) with the one-chain
+    all-threads figure beside it."""
+    cores = os.cpu_count() or 1
+    walkers = args.walkers if args.walkers > 0 else cores
+    agg = host_walkers_rate(args.config, args.seed, walkers, steps, warmup)
+    one = one_chain_all_threads_rate(m, ltau, args.seed, cores)
+    return {"value": agg["value"], "unit": "sweeps/s", "cores": walkers, "kind": "port",
+            "sample": f"{walkers} single-threaded walkers (one per host core, own seeds), {steps} whole sweeps "
+                      f"each after {warmup} untimed ({agg['seconds']:.1f} s timed); CPU restatement of ALF's "
+                      "default-STAB sweep calling OpenBLAS LAPACK; the Fortran reference has no compiler here",
+            "walkers": walkers, "s_per_step": agg["s_per_step"],
+            "one_chain_all_threads": {"value": one["value"], "unit": "sweeps/s", "threads": one["threads"],
+                                      "sample": f"{one['sweeps']} whole sweep(s) of one chain after one untimed"}}
+
+
+# ---------------------------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------------------------
+def run_ours(args, ws, rank, local, precision: str, chains: int, steps: int, warmup: int, e2e: bool = True):
+    """One handle of `chains` chains in `precision`: delay autotune (untimed), warm-up, the
+    device-timed steps, optionally the e2e steps through host buffers, and a two-sweep phase
+    profile.  Returns the measurements."""
     import torch
-    from alf_gb300 import model as mdl, rng
-    from alf_gb300 import replicas
+    from alf_gb300 import replicas, rng
     from alf_gb300.sweep import Chains
 
     torch.cuda.set_device(local)
     m, ltau = workload_model(args.config)
     if args.ltau >= 0:
         ltau = args.ltau
-    C = args.chains
-    seed = replicas.replica_seed(args.seed, rank)
-    ch = Chains(m, n_chains=C, precision=args.precision, device=local, pivoting=args.pivoting, flags=args.flags,
-                ltau=ltau)
+    C = chains
+    seeds = [replicas.replica_seed(args.seed, rank, c) for c in range(C)]
+    ch = Chains(m, n_chains=C, precision=precision, device=local, pivoting=args.pivoting, flags=args.flags,
+                ltau=ltau, wrap_bits=args.wrap_bits, propagate_bits=args.propagate_bits)
     for c in range(C):
-        ch.set_fields(c, rng.initial_fields(replicas.replica_seed(args.seed, rank, c), c, m.n_op, m.ltrot))
+        ch.set_fields(c, rng.initial_fields(seeds[c], c, m.n_op, m.ltrot))
     ch.init_state()
     for c in range(C):
-        ch.set_rng(c, replicas.replica_seed(args.seed, rank, c), rng.sweep_counter_base(m.n_op, m.ltrot, 0))
+        ch.set_rng(c, seeds[c], rng.sweep_counter_base(m.n_op, m.ltrot, 0))
     delay = ch.tune_delay(1) if args.tune else ch.delay()  # untimed (thermalisation) sweeps
     stream = torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local)
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > 129 MB L2
@@ -373,14 +445,14 @@ def run_ours(args, ws, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ch.sweep(None)
     ch.reset_stats()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     barrier()
     n0 = ch.L.alfgpu_launch_count(ch.h)
     with ClockSampler(local) as clk:
-        for i in range(args.steps):
+        for i in range(steps):
             l2.add_(1.0)  # flush L2 between timed steps (outside the timed region)
             torch.cuda.synchronize()
             ev[i][0].record(stream)
@@ -389,34 +461,63 @@ def run_ours(args, ws, rank, local):
         barrier()
     n_launch = ch.L.alfgpu_launch_count(ch.h) - n0
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    st = ch.stats(0)
-    n_acc = st.n_acc
-    # e2e through the C ABI with host buffers
-    u_host = [np.stack([rng.sweep_uniforms(replicas.replica_seed(args.seed, rank, c), c, m.n_op, m.ltrot, 1000 + i)
-                        for c in range(C)]) for i in range(args.steps)]
-    G_host = np.zeros((m.n_fl, m.ndim, m.ndim), np.complex128)
-    h2d = u_host[0].nbytes
-    d2h = G_host.nbytes
-    barrier()
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        ch.sweep(u_host[i])
-        G_host = ch.green(0)
-    barrier()
-    e2e_s = time.perf_counter() - t0
+    st = [ch.stats(c) for c in range(C)]
+    n_acc = sum(s.n_acc for s in st) / float(C * steps)
+    h2d = d2h = 0
+    e2e_s = None
+    if e2e:  # through the C ABI with host buffers
+        u_host = [np.stack([rng.sweep_uniforms(seeds[c], c, m.n_op, m.ltrot, 1000 + i) for c in range(C)])
+                  for i in range(steps)]
+        G_host = np.zeros((m.n_fl, m.ndim, m.ndim), np.complex128)
+        h2d = u_host[0].nbytes
+        d2h = G_host.nbytes
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            ch.sweep(u_host[i])
+            G_host = ch.green(0)
+        barrier()
+        e2e_s = time.perf_counter() - t0
     # phase profile of two sweeps (separate pass; events on the library stream)
     ch.set_profiling(True)
     for _ in range(2):
         ch.sweep(None)
     prof = ch.profile()
     ch.set_profiling(False)
-    # launch count per sweep from the profile pass
-    t_dev, t_e2e = replicas.max_over_ranks([ms / 1e3, e2e_s], device=f"cuda:{local}")
-    return dict(m=m, t_dev=t_dev, t_e2e=t_e2e, clocks=clk.summary(), prof=prof, n_acc=n_acc, h2d=h2d, d2h=d2h,
-                stats=st, chains=ch, launches=n_launch, delay=delay, ltau=ltau)
+    t = replicas.max_over_ranks([ms / 1e3] + ([e2e_s] if e2e else []), device=f"cuda:{local}")
+    out = dict(m=m, t_dev=t[0], t_e2e=t[1] if e2e else None, clocks=clk.summary(), prof=prof, n_acc=n_acc,
+               h2d=h2d, d2h=d2h, launches=n_launch, delay=delay, ltau=ltau, steps=steps, chains=C,
+               precision=precision, acceptance=sum(s.n_acc for s in st) / max(sum(s.n_prop for s in st), 1),
+               precision_green={"xmaxG": max(s.xmaxG for s in st),
+                                "xmeanG": sum(s.xmeanG_sum for s in st) / max(sum(s.ncg for s in st), 1),
+                                "xmaxP": max(s.xmaxP for s in st)})
+    if ltau:
+        out["precision_green"]["xmax_tau"] = max(s.xmax_tau for s in st)
+    ch.close()
+    return out
 
 
-def mixed_vs_fp64(m, seed: int, local: int, flags: int):
+def form_summary(ws, r) -> dict:
+    """The measurements of one run_ours result as a JSON object."""
+    from alf_gb300 import replicas
+    m = r["m"]
+    ms_step = 1e3 * r["t_dev"] / r["steps"]
+    d = {"value": replicas.whole_job_rate(ws, r["chains"], r["steps"], r["t_dev"]), "unit": "sweeps/s",
+         "chains_per_gpu": r["chains"], "steps": r["steps"], "ms_per_step": ms_step,
+         "per_chain_sweeps_per_s": 1e3 / ms_step, "gpu_launches": int(r["launches"]), "delay_depth": r["delay"],
+         "clocks": r["clocks"],
+         "phases": {k: {"ms_per_sweep": v[0] / 2.0, "launch_groups_per_sweep": v[1] / 2.0}
+                    for k, v in r["prof"].items()},
+         "precision_green": r["precision_green"], "acceptance": r["acceptance"],
+         "roofline": _reported(roofline, r["precision"], r["chains"], m, r["prof"]),
+         "sweep_roofline": _reported(sweep_roofline, m, r["n_acc"], r["ltau"], r["chains"], ms_step, r["precision"],
+                                     FP64_DMMA_TFLOPS, measured_bf16_peak()[0])}
+    if r["t_e2e"]:
+        d["e2e"] = replicas.whole_job_rate(ws, r["chains"], r["steps"], r["t_e2e"])
+    return d
+
+
+def mixed_vs_fp64(m, seed: int, local: int, flags: int, ltau: int, wrap_bits: int = 0, propagate_bits: int = 0):
     """max |G_mixed - G_fp64| over both flavours after one sweep from the same fields and
     the same host draws (the accept sequences agree unless a draw falls within rounding of
     its Metropolis weight), and the mixed form's own Precision Green of that sweep."""
@@ -426,7 +527,8 @@ def mixed_vs_fp64(m, seed: int, local: int, flags: int):
     u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)[None, :]
     gs = []
     for prec in ("fp64", "mixed"):
-        ch = Chains(m, n_chains=1, precision=prec, device=local, flags=flags)
+        ch = Chains(m, n_chains=1, precision=prec, device=local, flags=flags, ltau=ltau, wrap_bits=wrap_bits,
+                    propagate_bits=propagate_bits)
         ch.set_fields(0, f0)
         ch.init_state()
         ch.sweep(u)
@@ -437,18 +539,122 @@ def mixed_vs_fp64(m, seed: int, local: int, flags: int):
             "xmaxG_mixed": gs[1][2], "xmaxG_fp64": gs[0][2], "sweeps": 1}
 
 
-def cpu_oracle_rate(m, seed: int, threads: int, slices: int, ltau: int = 0):
-    """Sweeps/s of the CPU restatement on a bounded sample (slices time slices incl. stabilisations)."""
-    import oracle
-    from alf_gb300 import rng
-    o = oracle.Oracle(m, ltau=ltau, threads=threads)
-    o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
-    o.init_state()
-    u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
-    t0 = time.perf_counter()
-    o.sweep_chunk(u, slices)
-    dt = time.perf_counter() - t0
-    return (slices / (2.0 * m.ltrot)) / dt, dt
+def run_batch(args, ws, rank, local, precision: str, steps: int, warmup: int, e2e: bool = True):
+    """Config batch128: one handle per (N_dim, Ltrot) group with per-chain U; a step is one
+    sweep of every chain.  By default the groups sweep concurrently, one host thread per
+    group (each handle launches on its own stream; the C ABI releases the GIL), and the step
+    is timed on the device from an event that every group stream waits for to an event that
+    waits for every group's end."""
+    import concurrent.futures as cf
+    import dataclasses
+    import torch
+    from alf_gb300 import model as mdl, rng, replicas
+    from alf_gb300.sweep import Chains
+    torch.cuda.set_device(local)
+    groups = batch128_groups(replicas.replica_seed(args.seed, rank))
+    hs = []
+    for (L, beta), members in sorted(groups.items()):
+        models = [mdl.hubbard("square", L, L, U=U, beta=beta, dtau=0.1, nwrap=10) for _, U in members]
+        ch = Chains(models[0], n_chains=len(members), precision=precision, device=local,
+                    pivoting=args.pivoting, flags=args.flags, models=models, wrap_bits=args.wrap_bits,
+                    propagate_bits=args.propagate_bits)
+        for k, (c, _) in enumerate(members):
+            s = replicas.replica_seed(args.seed, rank, c)
+            ch.set_fields(k, rng.initial_fields(s, k, models[0].n_op, models[0].ltrot))
+        ch.init_state()
+        for k, (c, _) in enumerate(members):
+            ch.set_rng(k, replicas.replica_seed(args.seed, rank, c),
+                       rng.sweep_counter_base(models[0].n_op, models[0].ltrot, 0))
+        hs.append((ch, models[0], members))
+    nchains = sum(len(x[2]) for x in hs)
+    streams = [torch.cuda.ExternalStream(ch.L.alfgpu_stream(ch.h), device=local) for ch, _, _ in hs]
+    pool = cf.ThreadPoolExecutor(max_workers=len(hs))
+
+    def each(fn):
+        if args.serial_groups:
+            return [fn(i) for i in range(len(hs))]
+        return list(pool.map(fn, range(len(hs))))
+
+    def sweep_group(i):
+        ch, m, mem = hs[i]
+        try:
+            ch.sweep(None)
+        except Exception as e:
+            raise RuntimeError(f"group L={m.params.get('L1')} Ltrot={m.ltrot} chains={len(mem)}: {e}") from e
+
+    for _ in range(warmup):
+        each(sweep_group)
+    # drift control: per group, halve Nwrap until Precision Green <= the bound (untimed sweeps)
+    nwraps = each(lambda i: hs[i][0].adapt_nwrap(bound=args.drift_bound))
+    for ch, _, _ in hs:
+        ch.reset_stats()
+    torch.cuda.synchronize()
+    n0 = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs)
+    ms = 0.0
+    cur = torch.cuda.current_stream(local)
+    with ClockSampler(local) as clk:
+        for i in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ends = [torch.cuda.Event() for _ in hs]
+            e0.record(cur)
+
+            def timed(k):
+                streams[k].wait_event(e0)
+                sweep_group(k)
+                ends[k].record(streams[k])
+
+            each(timed)
+            for e in ends:
+                cur.wait_event(e)
+            e1.record(cur)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+    n_launch = sum(ch.L.alfgpu_launch_count(ch.h) for ch, _, _ in hs) - n0
+    # per group for the whole-sweep roofline: the adapted Nwrap, accepted flips per chain and sweep
+    try:
+        rgroups = [(dataclasses.replace(m, nwrap=ch.nwrap()),
+                    sum(ch.stats(k).n_acc for k in range(len(mem))) / float(steps * len(mem)), 0, len(mem))
+                   for ch, m, mem in hs]
+    except Exception as e:  # only the roofline object depends on it
+        rgroups = e
+    xmax = max(ch.stats(k).xmaxG for ch, _, mem in hs for k in range(len(mem)))
+    h2d = d2h = 0
+    e2e_s = None
+    if e2e:
+        us = [[np.stack([rng.sweep_uniforms(replicas.replica_seed(args.seed, rank, c), k, m.n_op, m.ltrot, 1000 + i)
+                         for k, (c, _) in enumerate(members)]) for ch, m, members in hs] for i in range(steps)]
+        h2d = sum(u.nbytes for u in us[0])
+        d2h = sum(m.n_fl * m.ndim * m.ndim * 16 for _, m, _ in hs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            def host_step(k, i=i):
+                hs[k][0].sweep(us[i][k])
+                return hs[k][0].green(0)
+            each(host_step)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+    pool.shutdown()
+    out = dict(t_dev=ms / 1e3, t_e2e=e2e_s, clocks=clk.summary(), launches=n_launch, h2d=h2d, d2h=d2h,
+               nchains=nchains, groups=[{"L": m.params.get("L1"), "Ltrot": m.ltrot, "chains": len(mem),
+                                        "nwrap": nw, "xmaxG_at_adapt": worst}
+                                       for (_, m, mem), (nw, worst) in zip(hs, nwraps)], xmaxG=xmax,
+               rgroups=rgroups, steps=steps)
+    for ch, _, _ in hs:
+        ch.close()
+    return out
+
+
+def batch_summary(ws, rb, precision) -> dict:
+    ms_step = 1e3 * rb["t_dev"] / rb["steps"]
+    d = {"value": ws * rb["nchains"] * rb["steps"] / rb["t_dev"], "unit": "sweeps/s", "chains_per_gpu": rb["nchains"],
+         "steps": rb["steps"], "ms_per_step": ms_step, "gpu_launches": int(rb["launches"]), "clocks": rb["clocks"],
+         "groups": rb["groups"], "precision_green": {"xmaxG": rb["xmaxG"]},
+         "sweep_roofline": _reported(sweep_roofline_groups, rb["rgroups"], ms_step, precision, FP64_DMMA_TFLOPS,
+                                     measured_bf16_peak()[0])}
+    if rb["t_e2e"]:
+        d["e2e"] = ws * rb["nchains"] * rb["steps"] / rb["t_e2e"]
+    return d
 
 
 def batch_cpu_baseline(seed: int, slices: int = 10):
@@ -456,13 +662,21 @@ def batch_cpu_baseline(seed: int, slices: int = 10):
     slices of one chain, by default Nwrap of them with the one stabilisation they end in, so
     the sample holds the sweep's own mix; scaled to a sweep); a step costs the sum
     over all chains, so the aggregate rate is chains / sum of per-chain sweep times."""
-    from alf_gb300 import model as mdl
+    import oracle
+    from alf_gb300 import model as mdl, rng
     groups = batch128_groups(seed)
     t_step, t_sample, n = 0.0, 0.0, 0
     for (L, beta), members in sorted(groups.items()):
         m = mdl.hubbard("square", L, L, U=members[0][1], beta=beta, dtau=0.1, nwrap=10)
-        rate, dt = cpu_oracle_rate(m, seed, 1, min(slices, 2 * m.ltrot), 0)
-        t_step += len(members) / rate
+        o = oracle.Oracle(m, threads=1)
+        o.set_fields(rng.initial_fields(seed, 0, m.n_op, m.ltrot))
+        o.init_state()
+        u = rng.sweep_uniforms(seed, 0, m.n_op, m.ltrot, 0)
+        ns = min(slices, 2 * m.ltrot)
+        t0 = time.perf_counter()
+        o.sweep_chunk(u, ns)
+        dt = time.perf_counter() - t0
+        t_step += len(members) * dt * (2.0 * m.ltrot / ns)
         t_sample += dt
         n += len(members)
     return {"value": n / t_step, "unit": "sweeps/s", "cores": 1, "kind": "port",
@@ -477,154 +691,105 @@ def main():
     if ws > 1:
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    from alf_gb300 import replicas
     m, ltau0 = workload_model(args.config)
     ltau = ltau0 if args.ltau < 0 else args.ltau
-    if args.config == "batch128":
-        desc = ("batch128: 128 Hubbard chains on square L x L lattices, per chain from its own seed L in "
-                "{6,...,16}, beta in {4,6,8,10}, dtau 0.1, U in [2,8], Nwrap 10 (halved per group until Precision "
-                f"Green <= {args.drift_bound:g}), Mz fields; one handle per (N_dim, Ltrot) group")
-    elif args.config == "kondo12x12":
-        desc = (f"kondo12x12: Kondo bilayer square 12x12, N_dim={m.ndim}, J_K=1.5, ham_Uf=0, beta={m.beta}, "
-                f"dtau={m.dtau}, Ltrot={m.ltrot}, Nwrap={m.nwrap}, N_SUN=2, N_FL=1, four-valued fields, "
-                f"TAU_M every sweep: {bool(ltau)}, "
-                + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"))
-    else:
-        desc = (f"{args.config}: {m.params.get('lattice')} {m.params.get('L1')}x{m.params.get('L2')}, "
-                f"N_dim={m.ndim}, U={m.params.get('U')}, beta={m.beta}, dtau={m.dtau}, Ltrot={m.ltrot}, "
-                f"Nwrap={m.nwrap}, Mz four-valued fields, TAU_M every sweep: {bool(ltau)}, "
-                + ("one chain per GPU" if args.chains == 1 else f"{args.chains} independent chains per GPU"))
-    workload = {"workload": desc,
-                "chains_per_gpu": args.chains, "precision": args.precision, "pivoting": args.pivoting, "flags": args.flags, "l2": "flushed between timed steps (256 MB write)",
-                "draws": "device counter stream (value); host arrays through the C ABI (e2e)"}
+    common = {"metric": METRIC, "unit": "sweeps/s", "steps": args.steps, "warmup": args.warmup,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+              "data": "synthetic (seeded fields and draws)", "config": bench_config(args, m, ltau)}
+
     if args.impl == "reference":
         if rank != 0:
             return
-        cores = os.cpu_count() or 1
-        slices = 20 if m.ndim >= 200 else 2 * m.ltrot
-        rates = []
-        for i in range(args.warmup + args.steps):
-            r, dt = cpu_oracle_rate(m, args.seed, cores, slices, ltau)
-            if i >= args.warmup:
-                rates.append(r)
-        v = float(np.mean(rates))
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded fields and draws)",
-                "config": dict(workload, chains_per_gpu=1, parallelism="host cores",
-                               l2="not applicable (host run; the sample's working set is the chain's own state)",
-                               draws="host arrays of the same counter stream"),
-                "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{slices} time slices of one sweep (with their stabilisations"
-                          + ("; TAU_M, which runs after the down pass, is outside the sample" if ltau else "")
-                          + ") per step, "
-                                           f"CPU restatement of ALF's default-STAB sweep calling OpenBLAS LAPACK "
-                                           f"with {cores} threads; the Fortran reference has no compiler here"},
-                "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if args.config == "batch128":
+            cpu = batch_cpu_baseline(args.seed)
+            arm = {"parallelism": "one host core", "sample": cpu["sample"]}
+        else:
+            cpu = host_baseline(args, m, ltau, args.steps, args.warmup)
+            arm = {"parallelism": f"{cpu['walkers']} host walkers (single-threaded processes, one chain each)",
+                   "draws": "host arrays of the counter stream", "one_chain_all_threads": cpu["one_chain_all_threads"]}
+        v = cpu["value"]
+        line = dict(common, impl="reference", value=v, n_gpus=args.gpus,
+                    ms_per_step=1e3 * cpu.get("walkers", 1) / v, dtype="c128", arm=arm, cpu_baseline=cpu,
+                    e2e={"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
         print(json.dumps(line))
         return
 
+    other = "fp64" if args.precision == "mixed" else "mixed"
+    cmp_steps, cmp_warm = min(args.steps, 5), min(args.warmup, 3)
     if args.config == "batch128":
-        rb = run_batch(args, ws, rank, local)
+        rb = run_batch(args, ws, rank, local, args.precision, args.steps, args.warmup)
         if rank != 0:
             return
-        from alf_gb300 import replicas
-        t_dev, t_e2e = rb["t_dev"], rb["t_e2e"]
+        head = batch_summary(ws, rb, args.precision)
+        line = dict(common, value=head["value"], n_gpus=ws, ms_per_step=head["ms_per_step"])
+        other_sum = None
+        if args.compare and ws == 1:
+            ro = run_batch(args, ws, rank, local, other, cmp_steps, cmp_warm, e2e=False)
+            other_sum = batch_summary(ws, ro, other)
         cpu = None
         if not args.no_cpu_baseline:
-            try:
-                cpu = batch_cpu_baseline(replicas.replica_seed(args.seed, rank))
-            except Exception as e:  # the baseline is reported, never required
-                cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
-        value = ws * rb["nchains"] * args.steps / t_dev
-        line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None,
-                "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products, df64 visits",
-                "data": "synthetic (seeded fields and draws)",
-                "config": dict(workload, chains_per_gpu=rb["nchains"], groups=rb["groups"],
-                               parallelism=f"replicas x{ws}", delay_depth="default"),
-                "e2e": {"value": ws * rb["nchains"] * args.steps / t_e2e, "unit": "sweeps/s",
-                        "h2d_bytes_per_step": rb["h2d"], "d2h_bytes_per_step": rb["d2h"]},
-                "roofline": None, "cpu_baseline": cpu, "clocks": rb["clocks"], "gpu_launches": int(rb["launches"]),
-                "precision_green": {"xmaxG": rb["xmaxG"]},
-                "sweep_roofline": _reported(sweep_roofline_groups, rb["rgroups"], 1e3 * t_dev / args.steps,
-                                            args.precision, FP64_DMMA_TFLOPS, measured_bf16_peak()[0])}
+            cpu = _reported(batch_cpu_baseline, replicas.replica_seed(args.seed, rank))
+        line.update({
+            "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products",
+            "arm": {"precision": args.precision, "chains_per_gpu": head["chains_per_gpu"], "groups": head["groups"],
+                    "parallelism": f"replicas x{ws}; groups " + ("one after another" if args.serial_groups else
+                                                                  "concurrent, one host thread each"),
+                    "draws": "device counter stream (value); host arrays through the C ABI (e2e)"},
+            "e2e": {"value": head.get("e2e"), "unit": "sweeps/s", "h2d_bytes_per_step": rb["h2d"],
+                    "d2h_bytes_per_step": rb["d2h"]},
+            "roofline": None, "cpu_baseline": cpu, "clocks": head["clocks"], "gpu_launches": head["gpu_launches"],
+            "precision_green": head["precision_green"], "sweep_roofline": head["sweep_roofline"]})
+        if other_sum is not None:
+            line[other] = other_sum
+            line["mixed_over_fp64"] = (head["value"] / other_sum["value"] if args.precision == "mixed"
+                                       else other_sum["value"] / head["value"])
         print(json.dumps(line))
         return
 
-    r = run_ours(args, ws, rank, local)
+    r = run_ours(args, ws, rank, local, args.precision, args.chains, args.steps, args.warmup, e2e=True)
     if rank != 0:
         return
-    m = r["m"]
-    from alf_gb300 import replicas
-    value = replicas.whole_job_rate(ws, args.chains, args.steps, r["t_dev"])
-    e2e = replicas.whole_job_rate(ws, args.chains, args.steps, r["t_e2e"])
-    prof = r["prof"]
-    # Roofline of the dominant kernel: the complex GEMM (k_zgemm on FP64 DMMA; k_dfgemm in
-    # the mixed form) carries the largest share of the launch list, and its largest
-    # consumer with a clean algorithmic count is the G wrap (2 real x complex N^3
-    # products per flavour per slice, 2 L slices per sweep).
-    roof = roofline(args, m, prof)
-    phases = {k: {"ms_per_sweep": v[0] / 2.0, "launch_groups_per_sweep": v[1] / 2.0} for k, v in prof.items()}
-    launches = int(r["launches"])
+    head = form_summary(ws, r)
+    line = dict(common, value=head["value"], n_gpus=ws, ms_per_step=head["ms_per_step"])
+    extra = {}
+    if args.compare and ws == 1:
+        ro = run_ours(args, ws, rank, local, other, args.chains, cmp_steps, cmp_warm, e2e=False)
+        extra[other] = form_summary(ws, ro)
+        extra["mixed_over_fp64"] = (head["value"] / extra[other]["value"] if args.precision == "mixed"
+                                    else extra[other]["value"] / head["value"])
+        if args.chains > 1:
+            pc = {}
+            for prec in ("fp64", "mixed"):
+                s1 = form_summary(ws, run_ours(args, ws, rank, local, prec, 1, cmp_steps, cmp_warm, e2e=False))
+                pc[prec] = {k: s1[k] for k in ("value", "unit", "ms_per_step", "delay_depth", "clocks", "phases",
+                                               "roofline", "sweep_roofline", "precision_green")}
+            pc["mixed_over_fp64"] = pc["mixed"]["value"] / pc["fp64"]["value"]
+            extra["per_chain"] = pc
+        extra["vs_fp64"] = _reported(mixed_vs_fp64, m, args.seed, local, args.flags, ltau, args.wrap_bits,
+                                     args.propagate_bits)
     cpu = None
     if not args.no_cpu_baseline:
-        try:
-            ns = 2 * m.ltrot if m.ndim <= 256 else 40  # one full sweep (~6 s for 16x16 on one core)
-            rate, dt = cpu_oracle_rate(m, args.seed, 1, ns, r.get("ltau", 0))
-            cpu = {"value": rate, "unit": "sweeps/s", "cores": 1, "kind": "port",
-                   "sample": f"{ns} time slices with their stabilisations ({dt:.1f} s), CPU restatement of ALF's "
-                             f"sweep with single-threaded OpenBLAS"}
-        except Exception as e:  # the baseline is reported, never required
-            cpu = {"value": None, "unit": "sweeps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
-    st = r["stats"]
-    mixed = None
-    if args.precision == "fp64" and args.compare and ws == 1:
-        import copy
-        a2 = copy.copy(args)
-        a2.precision = "mixed"
-        r2 = run_ours(a2, ws, rank, local)
-        st2 = r2["stats"]
-        mixed = {"value": replicas.whole_job_rate(ws, args.chains, args.steps, r2["t_dev"]), "unit": "sweeps/s",
-                 "e2e": replicas.whole_job_rate(ws, args.chains, args.steps, r2["t_e2e"]),
-                 "ms_per_step": 1e3 * r2["t_dev"] / args.steps, "gpu_launches": int(r2["launches"]),
-                 "delay_depth": r2["delay"], "clocks": r2["clocks"],
-                 "phases": {k: {"ms_per_sweep": v[0] / 2.0} for k, v in r2["prof"].items()},
-                 "precision_green": {"xmaxG": st2.xmaxG, "xmeanG": st2.xmeanG_sum / max(st2.ncg, 1),
-                                     "xmaxP": st2.xmaxP},
-                 "roofline": roofline(a2, m, r2["prof"]),
-                 "sweep_roofline": _reported(sweep_roofline, m, st2.n_acc / max(args.steps, 1), r2.get("ltau", 0),
-                                             args.chains, 1e3 * r2["t_dev"] / args.steps, "mixed",
-                                             FP64_DMMA_TFLOPS, measured_bf16_peak()[0]),
-                 "dtype": "c128 state; G wraps and UDV propagation (and the flushes of batched grids) as "
-                          "FP64-accurate digit-sliced BF16 tensor-core products; per-visit arithmetic and "
-                          "single-chain flushes in double-float; QR / CGR in FP64"}
-        r2["chains"].close()
-        try:
-            mixed["vs_fp64"] = mixed_vs_fp64(m, args.seed, local, args.flags)
-        except Exception as e:
-            mixed["vs_fp64"] = {"failed": str(e)}
-    line = {
-        "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products, df64 visits",
-        "data": "synthetic (seeded fields and draws)",
-        "config": dict(workload, parallelism=f"replicas x{ws}", delay_depth=r["delay"],
-                       delay_depth_source="autotuned (alfgpu_tune_delay)" if args.tune else "default"),
-        "e2e": {"value": e2e, "unit": "sweeps/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
-        "roofline": roof, "cpu_baseline": cpu, "clocks": r["clocks"], "gpu_launches": launches,
-        "phases": phases,
-        "precision_green": {"xmaxG": st.xmaxG, "xmeanG": st.xmeanG_sum / max(st.ncg, 1), "xmaxP": st.xmaxP},
-        "acceptance": st.n_acc / max(st.n_prop, 1),
-        "sweep_roofline": _reported(sweep_roofline, m, st.n_acc / max(args.steps, 1), r.get("ltau", 0), args.chains,
-                                    1e3 * r["t_dev"] / args.steps, args.precision, FP64_DMMA_TFLOPS,
-                                    measured_bf16_peak()[0]),
-    }
-    if mixed is not None:
-        line["mixed"] = mixed
+        cpu = _reported(host_baseline, args, m, ltau, 1, 1)
+    line.update({
+        "dtype": "c128" if args.precision == "fp64" else
+        "c128 state; G wraps, UDV propagation, stabilisation products (and batched flushes / explicit Q) as "
+        "FP64-accurate digit-sliced BF16 tensor-core products; per-visit determinants in double-float with FP64 "
+        "ratio and phase accumulation; pivoted QR, solves and phases FP64",
+        "arm": {"precision": args.precision, "chains_per_gpu": args.chains, "pivoting": args.pivoting,
+                "flags": args.flags, "wrap_bits": args.wrap_bits, "propagate_bits": args.propagate_bits,
+                "delay_depth": r["delay"],
+                "delay_depth_source": "autotuned (alfgpu_tune_delay)" if args.tune else "default",
+                "parallelism": f"replicas x{ws}, {args.chains} chains per GPU in one handle",
+                "draws": "device counter stream (value); host arrays through the C ABI (e2e)"},
+        "e2e": {"value": head["e2e"], "unit": "sweeps/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "roofline": head["roofline"], "cpu_baseline": cpu, "clocks": head["clocks"],
+        "gpu_launches": head["gpu_launches"], "phases": head["phases"], "precision_green": head["precision_green"],
+        "acceptance": head["acceptance"], "per_chain_sweeps_per_s": head["per_chain_sweeps_per_s"],
+        "sweep_roofline": head["sweep_roofline"]})
+    line.update(extra)
     print(json.dumps(line))
-    r["chains"].close()
 
 
 if __name__ == "__main__":

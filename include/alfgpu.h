@@ -114,6 +114,14 @@ enum { ALFGPU_FLAG_TENSOR_WIDE = 512 };
  * CTAs on every SM; these flags force the half-size or the full-size cluster. */
 enum { ALFGPU_FLAG_QR_HALF_CLUSTER = 1024, ALFGPU_FLAG_QR_FULL_CLUSTER = 2048 };
 
+/* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
+ * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the
+ * UDV propagation (reserved[2]); 0 keeps the full count (~54 bits, FP64-class).  The digits
+ * are b bits wide (b = 7 for N_dim <= 128, 6 up to 448, 5 beyond), so a target rounds up to whole
+ * digits; S digits cost (S + 1)(S + 2)/2 - 2 BF16 products per product (53 for S = 9, 43
+ * for S = 8) and bound the error by 2^-(b S) of the row / column scales. */
+enum { ALFGPU_DIMS_WRAP_BITS = 1, ALFGPU_DIMS_PROPAGATE_BITS = 2 };  /* indices into dims.reserved */
+
 typedef struct alfgpu_s alfgpu_t;
 
 typedef struct {

@@ -64,3 +64,14 @@ def test_clock_summary_reports_the_median_clock_and_active_reasons():
     s = c.summary()
     assert s["sm_mhz"] == 2040.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 4
     assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
+
+
+def test_both_arms_share_one_config_object():
+    # the reference arm and the GPU arm describe the same workload with the same object; how
+    # each arm runs it lives in its own `arm` object
+    a = bench.parse(["--impl", "reference"])
+    b = bench.parse([])
+    m, lt = bench.workload_model(a.config)
+    assert bench.bench_config(a, m, lt) == bench.bench_config(b, m, lt)
+    assert b.chains == 16 and b.precision == "mixed" and a.config == b.config == "hubbard16x16"
+    assert bench.parse(["--config", "kondo12x12"]).chains == 32

@@ -88,7 +88,9 @@ def test_small_config_observables_ten_bins_of_twenty_sweeps():
     rg, _ = bins.ana_vec(bg, sg)
     ro, _ = bins.ana_vec(bo, so)
     for (mg, eg), (mo, eo) in zip(rg, ro):
-        assert abs(mg - mo) <= 1e-9 * max(1.0, abs(mo)) and abs(eg - eo) <= 1e-7 * max(eo, 1e-12)
+        # Part is exactly N at half filling: its jackknife error is itself rounding
+        floor = 1e-9 * max(1.0, abs(mo))
+        assert abs(mg - mo) <= floor and abs(eg - eo) <= 1e-7 * eo + floor, (mg, mo, eg, eo)
     # an independent chain (the GPU's own device draw stream, another seed) against the
     # oracle's bins: the jackknife means agree within the combined error bars
     g2 = Chains(m)
@@ -229,7 +231,8 @@ def test_honeycomb12x12_beta20_fp64_parity_with_tau_m(honeycomb_run):
     assert relmax(g.green(0), ro.green) < RTOL
     assert abs(g.phase()[0] - ro.phase) < 1e-10
     sg, so = g.stats(0), ro.stats
-    assert sg.n_acc == so.n_acc and sg.ncg_tau == so.ncg_tau == m.nstm
+    # Control_Precision_tau compares four blocks per flavour at each of the Nstm CGR2_2 points
+    assert sg.n_acc == so.n_acc and sg.ncg_tau == so.ncg_tau == 4 * m.n_fl * m.nstm
     band = max(1e-10, 10.0 * so.xmax_tau)
     assert sg.xmax_tau <= band
     wq = _check_tau(tau_g, ro.tau, band)
