@@ -74,6 +74,7 @@ def lib(build_if_missing: bool = True):
         "alfgpu_error_string": ([C.c_int], C.c_char_p),
         "alfgpu_upload_hopping": ([vp, vp, vp], C.c_int),
         "alfgpu_upload_vertices": ([vp, C.c_int32, C.POINTER(Vertices)], C.c_int),
+        "alfgpu_upload_checkerboard": ([vp, C.c_int32, C.c_int32, vp, vp, vp, vp], C.c_int),
         "alfgpu_set_fields": ([vp, C.c_int32, vp], C.c_int),
         "alfgpu_set_fields_c128": ([vp, C.c_int32, vp], C.c_int),
         "alfgpu_get_fields": ([vp, C.c_int32, vp], C.c_int),
@@ -106,6 +107,9 @@ def lib(build_if_missing: bool = True):
         "alfgpu_get_nwrap": ([vp, C.POINTER(C.c_int32)], C.c_int),
         "alfgpu_oz_dgemm": ([C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, C.c_int32,
                              C.c_int32], C.c_int),
+        "alfgpu_set_lattice_obs": ([vp, C.c_int32, C.c_int32, vp, vp], C.c_int),
+        "alfgpu_get_lattice_obs": ([vp, C.c_int32, C.c_int32, vp, vp, vp], C.c_int),
+        "alfgpu_reset_lattice_obs": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

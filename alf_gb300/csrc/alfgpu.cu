@@ -24,6 +24,7 @@
 #include "update.cuh"
 #include "tau.cuh"
 #include "ozaki.cuh"
+#include "obs_latt.cuh"
 
 #include <atomic>
 #include <map>
@@ -51,6 +52,11 @@ struct alfgpu_s {
   // device-side equal-time scalar observables (alfgpu_set_scalar_obs)
   int obs_scal = 0, obs_nsun = 1;
   double *obs_HT = nullptr, *obs_trH = nullptr, *obs_U = nullptr, *obs_acc = nullptr;
+  // device-side lattice-resolved observables (alfgpu_set_lattice_obs): [0] equal time, [1] TAU_M
+  int obs_latt = 0, lo_ncell = 0, lo_norb = 0, lo_nnames = 0;
+  int *lo_site = nullptr, *lo_jof = nullptr;
+  zd *lo_acc[2] = {nullptr, nullptr}, *lo_acc0[2] = {nullptr, nullptr};
+  double* lo_cnt[2] = {nullptr, nullptr};
   int oz = 0, eexp_complex = 0;
   int oz_narrow = 0;  // small grids: BN = 16 tiles; the flush keeps the double-float GEMM (measured faster there)
   int oz_stab = 0;    // the stabilisation's complex products on the tensor-core GEMM too
@@ -67,8 +73,11 @@ struct alfgpu_s {
   CUtensorMap tmE[4], tmGA, tmGB, tmXA, tmYB;
   int exact_qrp = 0;       // current call: ZGEQP3 column pivoting (cluster kernel), else blocked pre-pivoted QR
   int exact_dec = 0, exact_cgr = 0;  // per call site: decompose_UDV_state / CGR
-  int qrr_ok = 0;                    // k_qrp_rows fits (shared memory) and can be launched
+  int qrr_ok = 0;                    // k_qrp_rows can be launched: rows in shared memory (1) or in qrr_ws (2)
   int CLr = 1;                       // k_qrp_rows cluster size (CL, or CL / 2 on batched grids)
+  zd* qrr_ws = nullptr;              // row workspace of k_qrp_rows<ArD, true> (qrr_ok == 2)
+  int qr2_mode = 0, CL2 = 1;         // CGR2_2's 2N x 2N QR: 0 k_qrp, 1 / 2 as qrr_ok; its cluster size
+  zd* qr2_ws = nullptr;
   // time-displaced Green functions (ltau = 1)
   int ltau = 0;
   // CUDA graphs of the sweep: [0] device draws, [1] host draws (copied before the launch)
@@ -106,6 +115,27 @@ struct alfgpu_s {
   std::vector<int> blk_start[2], blk_cnt[2];  // delayed-update blocks of the up / down pass (visit positions)
   std::vector<int> hv_site, hv_site2;          // flavour-0 vertex sites (host), for re-blocking
   std::vector<int8_t> hv_nsite;
+  // Vector vertices (single-site vertices on a site of a rotated pair, e.g. Kondo's U_f next to
+  // its J_K vertex): the slice's vertices split into phases, ranges [ph_n0, ph_n1) of vertices
+  // with disjoint supports; updates run in the frame of the phase's start and each phase's
+  // wraps are applied explicitly (pairblock = 1).  Without them one implicit phase whose wraps
+  // are deferred into the next hopping product.
+  int pairblock = 0;
+  std::vector<int> ph_n0, ph_n1, ph_of;        // phases and the phase of each vertex
+  std::vector<int> hv_blk2;                    // flavour-0: second site of each vertex's support or -1
+  std::vector<int> blk_phase_end[2];           // per block of each pass: phase that ends with it, or -1
+  int8_t* v_kind = nullptr;                    // [chain][F*M] 0 one site, 1 two diagonal positions, 2 vector
+  int* v_blk2 = nullptr;                       // [chain][F*M] second site of the support or -1
+  double* v_vc = nullptr;                      // [chain][F*M][2] vector coefficients (c_a, c_b)
+  int* sites2_out = nullptr;                   // accepted vector positions of a block: site b, coefficients
+  double* coef_out = nullptr;
+  int8_t* fields_old = nullptr;                // [chain][M] the slice's fields before its updates
+  // checkerboard hopping (alfgpu_upload_checkerboard): bond operators per flavour in Op_T order,
+  // families of disjoint bonds; replaces the dense hopping products
+  int cb = 0, cb_ncheck = 0;
+  std::vector<int> cb_fam;
+  int* cb_P = nullptr;
+  double *cb_mat = nullptr, *cb_inv = nullptr;
   std::vector<double> h_expT, h_expTinv;      // hopping exponentials as uploaded (original basis)
   bool rot = false;                           // two-site vertices: the sweep runs in the rotated basis
   std::vector<std::pair<int, int>> rot_pairs;
@@ -257,17 +287,27 @@ static int cluster_size(int N) {
   return 1;
 }
 
-// Resident clusters of CL CTAs for k_qrp_rows on an N x N matrix (0: it does not fit).  The
-// shared-memory limits it raises are process-global and only ever raised.
-static int qrr_clusters(int N, int CL) {
-  const size_t sm = qrr_smem_bytes(N, CL);
+// Resident clusters of CL CTAs for k_qrp_rows on an N x N matrix (0: it does not fit), rows in
+// shared memory or (grows) in the global workspace.  The shared-memory limits it raises are
+// process-global and only ever raised.
+static int qrr_clusters(int N, int CL, bool grows = false) {
+  const size_t sm = qrr_smem_bytes(N, CL, grows);
   if (sm > 227 * 1024) return 0;
-  if (raise_smem_limit(k_qrp_rows<ArD>, sm) != cudaSuccess || raise_smem_limit(k_qrp_rows<ArF>, sm) != cudaSuccess) {
+  if (grows) {
+    if (raise_smem_limit(k_qrp_rows<ArD, true>, sm) != cudaSuccess ||
+        (CL > 8 && cudaFuncSetAttribute(k_qrp_rows<ArD, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                       cudaSuccess)) {
+      cudaGetLastError();
+      return 0;
+    }
+  } else if (raise_smem_limit(k_qrp_rows<ArD>, sm) != cudaSuccess ||
+             raise_smem_limit(k_qrp_rows<ArF>, sm) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
-  if (CL > 8 && (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-                 cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+  if (!grows && CL > 8 &&
+      (cudaFuncSetAttribute(k_qrp_rows<ArD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+       cudaFuncSetAttribute(k_qrp_rows<ArF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
     cudaGetLastError();
     return 0;
   }
@@ -281,9 +321,63 @@ static int qrr_clusters(int N, int CL) {
   at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
   cfg.attrs = at; cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_qrp_rows<ArD>, &cfg) != cudaSuccess) n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, grows ? k_qrp_rows<ArD, true> : k_qrp_rows<ArD>, &cfg) != cudaSuccess) n = 0;
   cudaGetLastError();
   return n;
+}
+
+// Cluster size and row storage of the exact pivoted QR of B matrices N x N: the largest
+// cluster (up to CL) whose rows fit shared memory (mode 1) or, failing that, with the rows in a
+// global workspace (mode 2); a launch whose full-size clusters would put more than two CTAs on
+// every SM takes half-size clusters (unless forced by the flags).  Mode 0: neither fits.
+static int qrr_plan(int N, int CL, int B, int flags, int dev, int* CLout) {
+  int nsm = 152;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaGetLastError();
+  for (int mode = 1; mode <= 2; ++mode) {
+    const bool grows = mode == 2;
+    if (qrr_clusters(N, CL, grows) <= 0) continue;
+    *CLout = CL;
+    if (CL >= 4) {
+      const bool want = (flags & ALFGPU_FLAG_QR_HALF_CLUSTER) ||
+                        (!(flags & ALFGPU_FLAG_QR_FULL_CLUSTER) && (long long)B * CL > 2ll * nsm);
+      if (want && qrr_clusters(N, CL / 2, grows) > 0) *CLout = CL / 2;
+    }
+    return mode;
+  }
+  return 0;
+}
+
+// One launch of the exact pivoted QR on clusters of CL CTAs (rows in shared memory, or in ws when
+// grows), then k_bqr_finish: R (normalised rows) above, reflectors below, tau, jpvt, D, info.
+static int launch_qrr(alfgpu_s* h, const zd* Ain, zd* A, int N, int CL, bool grows, zd* ws, zd* tau, int* jpvt,
+                      double* D, QRInfo* info, const double* colscale, int df) {
+  const int B = h->B;
+  const long long NN = (long long)N * N;
+  QRRowsParams q;
+  memset(&q, 0, sizeof(q));
+  q.Ain = Ain; q.A = A; q.lda = N; q.sA = NN; q.N = N;
+  q.Araw = df ? h->QRdf : nullptr;
+  q.colscale = colscale; q.sCS = N;
+  q.tau = tau; q.sT = N; q.jpvt = jpvt; q.sP = N; q.D = D; q.sD = N; q.info = info;
+  q.Arows = grows ? ws : nullptr;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(CL, B, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = qrr_smem_bytes(N, CL, grows);
+  cfg.stream = h->st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  h->launches++;
+  if (grows) CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArD, true>, q));
+  else if (df) CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArF>, q));
+  else CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArD>, q));
+  k_bqr_finish<<<dim3((N + 7) / 8, B), 256, (size_t)N * sizeof(double), h->st>>>(A, N, NN, N, tau, N, D, N, info);
+  CKL();
+  return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -338,6 +432,19 @@ static int launch_orgqr(alfgpu_s* h, zd* A, int nb) {
   return 0;
 }
 
+
+// Triangular solves (ZTRSM) of p.nvec right-hand sides per matrix: TRSV_V vectors per CTA
+// when their shared memory fits, else one per CTA.
+static int trsv(alfgpu_s* h, const TrsvParams& t) {
+  const size_t sm = trsv_v_smem(t.N);
+  if (sm <= 200 * 1024 && raise_smem_limit(k_trsv_v<TRSV_V>, sm) == cudaSuccess) {
+    k_trsv_v<TRSV_V><<<dim3((t.nvec + TRSV_V - 1) / TRSV_V, h->B), 256, sm, h->st>>>(t);
+  } else {
+    cudaGetLastError();
+    k_trsv<<<dim3(t.nvec, h->B), 256, 3 * (size_t)t.N * sizeof(zd), h->st>>>(t);
+  }
+  return 0;  // the caller checks the launch (CKL)
+}
 
 static int gemm(alfgpu_s* h, const GemmParams& p) {
   int nl = 1;
@@ -449,7 +556,9 @@ static int oz_zgemm(alfgpu_s* h, const GemmParams& g) {
 
 // The mixed form's UDV propagation runs on the tensor-core GEMM (FP64-accurate) when the
 // slice scales are real.
-static bool oz_propagate(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_complex && !h->mixed_propagate; }
+static bool oz_propagate(alfgpu_s* h) {
+  return h->mixed && h->oz && (!h->eexp_complex || h->pairblock) && !h->mixed_propagate;
+}
 
 // Stabilisation products (UDV propagation, decompose, CGR): double-float in the mixed
 // form, FP64 otherwise.
@@ -534,27 +643,10 @@ static int qr_any(alfgpu_s* h, const zd* Ain, const double* colscale, zd* Aout, 
   }
   prof_begin(h, ALFGPU_PROF_QR);
   if (exact) {
-    QRRowsParams q;
-    q.Ain = Ain; q.A = Aout; q.lda = N; q.sA = NN; q.N = N;
-    q.Araw = df ? h->QRdf : nullptr;
-    q.colscale = colscale; q.sCS = N;
-    q.tau = h->tau; q.sT = N; q.jpvt = h->jpvt; q.sP = N; q.D = h->DUP; q.sD = N; q.info = h->info;
-    cudaLaunchConfig_t cfg;
-    memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3(h->CLr, B, 1);
-    cfg.blockDim = dim3(256, 1, 1);
-    cfg.dynamicSmemBytes = qrr_smem_bytes(N, h->CLr);
-    cfg.stream = h->st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = h->CLr; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-    cfg.attrs = at; cfg.numAttrs = 1;
-    h->launches++;
-    if (df) CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArF>, q));
-    else CK(cudaLaunchKernelEx(&cfg, k_qrp_rows<ArD>, q));
-    h->qr_df = df;
-    k_bqr_finish<<<g8, 256, (size_t)N * sizeof(double), h->st>>>(Aout, N, NN, N, h->tau, N, h->DUP, N, h->info);
-    CKL();
+    const bool grows = h->qrr_ok == 2;
+    RET(launch_qrr(h, Ain, Aout, N, h->CLr, grows, h->qrr_ws, h->tau, h->jpvt, h->DUP, h->info, colscale,
+                   grows ? 0 : df));
+    h->qr_df = grows ? 0 : df;
     prof_end(h);
     return 0;
   }
@@ -741,11 +833,102 @@ static int decompose(alfgpu_s* h, UDVSet& s, int left) {
   return 0;
 }
 
+// Explicit wraps of vertex phase ph on the B matrices X: left (rows) or right (columns)
+// multiplication by E_ph(s) (inv = 0) or E_ph(-s) (inv = 1), entries conjugated with cj; the
+// fields of slice nt1, or the snapshot of the slice's fields before its updates (snap).
+static int vtx_phase(alfgpu_s* h, zd* X, int ph, int nt1, bool snap, int inv, int cj, bool rows) {
+  VtxPhase p;
+  p.fl = snap ? h->fields_old : h->fields + (long long)(nt1 - 1) * h->M;
+  p.fstride = snap ? h->M : (long long)h->L * h->M;
+  p.kind = h->v_kind; p.site = h->v_site; p.site2 = h->v_blk2; p.coef = h->v_vc; p.Eexp = h->v_Eexp;
+  p.sK = (long long)h->F * h->M; p.F = h->F; p.M = h->M; p.N = h->N;
+  p.n0 = h->ph_n0[ph]; p.n1 = h->ph_n1[ph]; p.inv = inv; p.cj = cj;
+  const long long nthr = (long long)h->N * (p.n1 - p.n0);
+  const dim3 grid((unsigned)((nthr + 255) / 256), h->B);
+  const long long NN = (long long)h->N * h->N;
+  if (rows) k_vtx_rows<<<grid, 256, 0, h->st>>>(X, NN, p);
+  else k_vtx_cols<<<grid, 256, 0, h->st>>>(X, NN, p);
+  CKL();
+  return 0;
+}
+// The slice's vertex product P = E_K ... E_1 (phases in visit order, fields of slice nt1):
+// X <- P X, X <- P^dagger X, X <- X P^-1.
+static int vtx_left(alfgpu_s* h, zd* X, int nt1) {
+  for (size_t ph = 0; ph < h->ph_n0.size(); ++ph) RET(vtx_phase(h, X, (int)ph, nt1, false, 0, 0, true));
+  return 0;
+}
+static int vtx_left_adj(alfgpu_s* h, zd* X, int nt1) {
+  for (int ph = (int)h->ph_n0.size() - 1; ph >= 0; --ph) RET(vtx_phase(h, X, ph, nt1, false, 0, 1, true));
+  return 0;
+}
+static int vtx_right_inv(alfgpu_s* h, zd* X, int nt1) {
+  for (size_t ph = 0; ph < h->ph_n0.size(); ++ph) RET(vtx_phase(h, X, (int)ph, nt1, false, 1, 0, false));
+  return 0;
+}
+
+// Checkerboard hopping on the B matrices X (Hop_mod.F90:143-250 with the bond operators in Op_T
+// order): each family's disjoint bonds in one launch, families in the order of the routine.
+enum { CB_MMTHR, CB_MMTHR_M1, CB_MMTHL, CB_MMTHL_M1, CB_MMTHLC };
+static int cb_apply(alfgpu_s* h, zd* X, int which) {
+  const int nfam = (int)h->cb_fam.size() - 1;
+  const bool rows = which == CB_MMTHR || which == CB_MMTHR_M1 || which == CB_MMTHLC;
+  const bool inv = which == CB_MMTHR_M1 || which == CB_MMTHL_M1;
+  const bool reverse = which == CB_MMTHR || which == CB_MMTHL_M1;  // the last family first
+  const long long NN = (long long)h->N * h->N;
+  for (int q = 0; q < nfam; ++q) {
+    const int fm = reverse ? nfam - 1 - q : q;
+    const int b0 = h->cb_fam[fm], b1 = h->cb_fam[fm + 1];
+    if (b1 <= b0) continue;
+    const dim3 grid((unsigned)(((long long)h->N * (b1 - b0) + 255) / 256), h->B);
+    if (rows)
+      k_bond_rows<<<grid, 256, 0, h->st>>>(X, NN, h->N, h->F, h->cb_P, inv ? h->cb_inv : h->cb_mat, h->cb_ncheck, b0,
+                                           b1);
+    else
+      k_bond_cols<<<grid, 256, 0, h->st>>>(X, NN, h->N, h->F, h->cb_P, inv ? h->cb_inv : h->cb_mat, h->cb_ncheck, b0,
+                                           b1);
+    CKL();
+  }
+  return 0;
+}
+static int scale_rc(alfgpu_s* h, zd* X, const zd* rs, int rconj, const zd* cs) {
+  const dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
+  k_scale_rc<<<grid, 256, 0, h->st>>>(X, h->N, rs, rconj, cs);
+  CKL();
+  return 0;
+}
+
 // WRAPUR (wrapur_mod.F90:101-124): U <- prod_nt [D_nt expT] U, then decompose (side R)
 static int wrapur_u(alfgpu_s* h, UDVSet& u, int ntau, int ntau1) {
   const int N = h->N, B = h->B;
   prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau + 1; nt <= ntau1; ++nt) {
+    if (h->cb) {  // U <- P (B_T U) with the bond operators (Hop_mod_mmthr), then the vertices
+      RET(cb_apply(h, u.U, CB_MMTHR));
+      if (h->pairblock) {
+        RET(vtx_left(h, u.U, nt));
+      } else {
+        RET(slice_scale(h, nt));
+        RET(scale_rc(h, u.U, h->S, 0, nullptr));
+      }
+      continue;
+    }
+    if (h->pairblock) {  // U <- P (expT U): the product, then the slice's explicit vertex phases
+      if (oz_propagate(h)) {
+        RET(oz_slice(h, u.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->ozp_S, h->oz_bits,
+                     h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
+        RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->ozp_S, h->oz_bits, h->oz_bn, h->oz_nst,
+                    h->oz_RpN, h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, u.U, 1, N,
+                    (long long)N * N, B, nullptr, 0, h->oz_S, h->ozp_S));
+      } else {
+        GemmParams p = gsq(h, B);
+        p.A = h->expT; p.realA = 1; p.modA = h->F;
+        p.B = u.U; p.C = h->T1;
+        RET(gemm_s(h, p));
+        RET(copy_mats(h, u.U, h->T1, (size_t)B * N * N));
+      }
+      RET(vtx_left(h, u.U, nt));
+      continue;
+    }
     RET(slice_scale(h, nt));
     if (oz_propagate(h)) {  // U <- diag(S) expT U on the tensor cores, in place (U is sliced first)
       RET(oz_slice(h, u.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->ozp_S, h->oz_bits,
@@ -773,6 +956,33 @@ static int wrapul(alfgpu_s* h, int ntau1, int ntau) {
   const int N = h->N, B = h->B;
   prof_begin(h, ALFGPU_PROF_PROPAGATE);
   for (int nt = ntau1; nt >= ntau + 1; --nt) {
+    if (h->cb) {  // U <- B_T^T (P^dagger U): the vertices, then the bonds (Hop_mod_mmthlc)
+      if (h->pairblock) {
+        RET(vtx_left_adj(h, h->udvl.U, nt));
+      } else {
+        RET(slice_scale(h, nt));
+        RET(scale_rc(h, h->udvl.U, h->S, 1, nullptr));
+      }
+      RET(cb_apply(h, h->udvl.U, CB_MMTHLC));
+      continue;
+    }
+    if (h->pairblock) {  // U <- expT (P^dagger U): the slice's explicit vertex phases, then the product
+      RET(vtx_left_adj(h, h->udvl.U, nt));
+      if (oz_propagate(h)) {
+        RET(oz_slice(h, h->udvl.U, OZ_CROWS, N, 1, (long long)N * N, 0, nullptr, 0, N, N, nullptr, h->ozp_S,
+                     h->oz_bits, h->oz_Rp2N, h->oz_Kpad, h->ozGB, h->ozGBe, B));
+        RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, h->ozp_S, h->oz_bits, h->oz_bn, h->oz_nst,
+                    h->oz_RpN, h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, h->udvl.U, 1, N,
+                    (long long)N * N, B, nullptr, 0, h->oz_S, h->ozp_S));
+      } else {
+        GemmParams q = gsq(h, B);
+        q.A = h->expT; q.realA = 1; q.modA = h->F;
+        q.B = h->udvl.U; q.C = h->T1;
+        RET(gemm_s(h, q));
+        RET(copy_mats(h, h->udvl.U, h->T1, (size_t)B * N * N));
+      }
+      continue;
+    }
     RET(slice_scale(h, nt));
     if (oz_propagate(h)) {  // U <- expT diag(conj S) U on the tensor cores (S real), in place
       RET(oz_slice(h, h->udvl.U, OZ_CROWS, N, 1, (long long)N * N, 0, h->S, N, N, N, nullptr, h->ozp_S, h->oz_bits,
@@ -841,7 +1051,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
+    RET(trsv(h, t));
     prof_end(h);
     CKL();
     // G = U_L * P RHS (ZLAPMR backward folded into the B load)
@@ -859,7 +1069,7 @@ static int cgr(alfgpu_s* h, int nvar, const UDVSet& ur, const UDVSet& ul, zd* Go
     t.T = QR; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = 1; t.estride = N; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 1;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
+    RET(trsv(h, t));
     prof_end(h);
     CKL();
     // G = (RHS P) U_R^H (ZLAPMT backward folded into the A load)
@@ -919,8 +1129,17 @@ static int ensure_obs_host(alfgpu_s* h) {
 
 // ham%Obser(GR, PHASE, ntau1) for every chain (main.F90:757-772, 788-803).  With a pending
 // vertex scaling (up pass), G in ALF's frame is S G Sinv, formed into the work matrix Gw.
+static LattObsParams latt_params(alfgpu_s* h, int kind) {
+  LattObsParams p;
+  p.N = h->N; p.F = h->F; p.nsun = h->NSUN; p.ncell = h->lo_ncell; p.norb = h->lo_norb; p.nnames = h->lo_nnames;
+  p.L1 = kind ? h->L + 1 : 1;
+  p.site_of = h->lo_site; p.jof = h->lo_jof; p.phase = h->phase;
+  p.acc = h->lo_acc[kind]; p.acc0 = h->lo_acc0[kind]; p.cnt = h->lo_cnt[kind];
+  return p;
+}
+
 static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pending) {
-  if (!cb && !h->obs_scal) return 0;
+  if (!cb && !h->obs_scal && !h->obs_latt) return 0;
   const long long NN = (long long)h->N * h->N;
   const zd* src = h->G;
   if (pending || h->rot) {
@@ -938,6 +1157,11 @@ static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pendi
                                         h->obs_acc);
     CKL();
   }
+  if (h->obs_latt) {
+    const int nout = h->lo_ncell * h->lo_norb * h->lo_norb;
+    k_obs_latt_eq<<<dim3((nout + 127) / 128, h->C), 128, 0, h->st>>>(src, latt_params(h, 0));
+    CKL();
+  }
   if (!cb) return 0;
   RET(ensure_obs_host(h));
   CK(cudaMemcpyAsync(h->obs_host, src, (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
@@ -950,13 +1174,19 @@ static int obs_eq(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int ntau1, int pendi
 
 // ham%ObserT(NT, GT0, G0T, G00, GTT, PHASE) for every chain (tau_m_mod.F90:116, 168)
 static int obs_tau(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int nt) {
-  if (!cb) return 0;
-  RET(ensure_obs_host(h));
+  if (!cb && !h->obs_latt) return 0;
   const long long NN = (long long)h->N * h->N;
   dim3 grid((unsigned)((NN + 255) / 256), h->B);
   k_gather_quartet<<<grid, 256, 0, h->st>>>(h->GT0, h->G0T, h->G00, h->GTT, h->Gq, h->N, h->F);
   CKL();
   RET(rotate_out(h, h->Gq, 4 * h->B));
+  if (h->obs_latt) {
+    const int nout = h->lo_ncell * h->lo_norb * h->lo_norb;
+    k_obs_latt_tau<<<dim3((nout + 127) / 128, h->C), 128, 0, h->st>>>(h->Gq, nt, latt_params(h, 1));
+    CKL();
+  }
+  if (!cb) return 0;
+  RET(ensure_obs_host(h));
   CK(cudaMemcpyAsync(h->tau_host, h->Gq, 4 * (size_t)h->B * NN * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->phase_host, h->phase, (size_t)h->C * sizeof(zd), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -968,6 +1198,8 @@ static int obs_tau(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx, int nt) {
 // ---- CGR2_2 ---------------------------------------------------------------------------------
 // Column-pivoted QR (ZGEQP3 semantics, cluster kernel) of the N2 x N2 matrices A in place.
 static int qrp_n(alfgpu_s* h, zd* A, int N2, zd* tau, int* jpvt, double* D, double* vn, QRInfo* info) {
+  if (h->qr2_mode)  // the row-distributed cluster QR, in place (rows read before any output is written)
+    return launch_qrr(h, A, A, N2, h->CL2, h->qr2_mode == 2, h->qr2_ws, tau, jpvt, D, info, nullptr, 0);
   QRParams q;
   memset(&q, 0, sizeof(q));
   q.A = A; q.lda = N2; q.sA = (long long)N2 * N2; q.N = N2;
@@ -1019,7 +1251,7 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
     t.T = h->QRw; t.ldt = N; t.sT = NN; t.B = h->RHS; t.vstride = N; t.estride = 1; t.sB = NN;
     t.N = N; t.nvec = N; t.lower = 0; t.conj_io = 0;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N, B), 256, 3 * N * sizeof(zd), h->st>>>(t);
+    RET(trsv(h, t));
     prof_end(h);
     CKL();
   }
@@ -1040,7 +1272,7 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
     t.N = N2; t.nvec = N2; t.lower = 1; t.conj_io = 0; t.trans = 1;
     t.oscale = nullptr;
     prof_begin(h, ALFGPU_PROF_SOLVE);
-    k_trsv<<<dim3(N2, B), 256, 3 * N2 * sizeof(zd), h->st>>>(t);
+    RET(trsv(h, t));
     prof_end(h);
     CKL();
   }
@@ -1062,23 +1294,28 @@ static int cgr2_2(alfgpu_s* h, const UDVSet& udv2, const UDVSet& udv1) {
 // place (the operand is sliced before the product overwrites it), with the G wraps' digit count:
 // PROPR   X <- diag(S) expT X          (tau_m_mod.F90:213-236)
 // PROPRM1 X <- X expTinv diag(Sinv)    (tau_m_mod.F90:238-263)
-static bool oz_tau(alfgpu_s* h) { return h->mixed && h->oz && !h->eexp_complex; }
-static int oz_propr(alfgpu_s* h, zd* X) {
+// With vector vertices (pairblock) the slice's vertex product is applied explicitly after the
+// product instead of as a row / column scale.
+static bool oz_tau(alfgpu_s* h) { return h->mixed && h->oz && (!h->eexp_complex || h->pairblock); }
+static int oz_propr(alfgpu_s* h, zd* X, int nt1) {
   const int N = h->N, B = h->B, S = h->ozw_S;
   const long long NN = (long long)N * N;
   RET(oz_slice(h, X, OZ_CROWS, N, 1, NN, 0, nullptr, 0, N, N, nullptr, S, h->oz_bits, h->oz_Rp2N, h->oz_Kpad,
                h->ozGB, h->ozGBe, B));
-  return oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
-                 h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, X, 1, N, NN, B, h->S, N, h->oz_S, S);
+  RET(oz_gemm(h, h->tmE[0], h->tmGB, N, 2 * N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_RpN,
+              h->oz_Rp2N, h->F, 0, h->ozEe[0], h->ozGBe, OZ_OUT_COLS, 0, X, 1, N, NN, B,
+              h->pairblock ? nullptr : h->S, N, h->oz_S, S));
+  return h->pairblock ? vtx_left(h, X, nt1) : 0;
 }
-static int oz_proprm1(alfgpu_s* h, zd* X) {
+static int oz_proprm1(alfgpu_s* h, zd* X, int nt1) {
   const int N = h->N, B = h->B, S = h->ozw_S;
   const long long NN = (long long)N * N;
   RET(oz_slice(h, X, OZ_CROWS, 1, N, NN, 0, nullptr, 0, N, N, nullptr, S, h->oz_bits, h->oz_Rp2N, h->oz_Kpad,
                h->ozGA, h->ozGAe, B));
-  return oz_gemm(h, h->tmGA, h->tmE[3], 2 * N, N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_Rp2N,
-                 h->oz_RpN, 0, h->F, h->ozGAe, h->ozEe[3], OZ_OUT_ROWS, 0, X, 1, N, NN, B, nullptr, 0, S, h->oz_S,
-                 h->Sinv, N);
+  RET(oz_gemm(h, h->tmGA, h->tmE[3], 2 * N, N, h->oz_Kpad, S, h->oz_bits, h->oz_bn, h->oz_nst, h->oz_Rp2N,
+              h->oz_RpN, 0, h->F, h->ozGAe, h->ozEe[3], OZ_OUT_ROWS, 0, X, 1, N, NN, B, nullptr, 0, S, h->oz_S,
+              h->pairblock ? nullptr : h->Sinv, N));
+  return h->pairblock ? vtx_right_inv(h, X, nt1) : 0;
 }
 
 // TAU_M (tau_m_mod.F90:56-211), finite temperature, after the sweep: GT0, G0T, G00, GTT for
@@ -1094,33 +1331,56 @@ static int tau_m(alfgpu_s* h, alfgpu_obs_cb cb, void* ctx) {
   int NST = 1;
   for (int NT = 0; NT < L; ++NT) {
     const int NT1 = NT + 1;
-    RET(slice_scale(h, NT1));
+    const bool pb = h->pairblock;
+    if (!pb) RET(slice_scale(h, NT1));
     prof_begin(h, ALFGPU_PROF_HOP);
-    if (oz_tau(h)) {
-      RET(oz_propr(h, h->GT0));     // PROPR(GT0)
-      RET(oz_proprm1(h, h->G0T));   // PROPRM1(G0T)
-      RET(oz_proprm1(h, h->GTT));   // PROPRM1 then PROPR (GTT)
-      RET(oz_propr(h, h->GTT));
+    if (h->cb) {  // PROPR X <- P B_T X, PROPRM1 X <- X B_T^-1 P^-1 with the bond operators
+      zd* Xs[3] = {h->GT0, h->G0T, h->GTT};
+      for (int k = 0; k < 3; ++k) {
+        if (k >= 1) {  // PROPRM1 (G0T, then the first half of GTT)
+          RET(cb_apply(h, Xs[k], CB_MMTHL_M1));
+          if (pb) RET(vtx_right_inv(h, Xs[k], NT1));
+          else RET(scale_rc(h, Xs[k], nullptr, 0, h->Sinv));
+        }
+        if (k != 1) {  // PROPR (GT0, then the second half of GTT)
+          RET(cb_apply(h, Xs[k], CB_MMTHR));
+          if (pb) RET(vtx_left(h, Xs[k], NT1));
+          else RET(scale_rc(h, Xs[k], h->S, 0, nullptr));
+        }
+      }
+    } else if (oz_tau(h)) {
+      RET(oz_propr(h, h->GT0, NT1));     // PROPR(GT0)
+      RET(oz_proprm1(h, h->G0T, NT1));   // PROPRM1(G0T)
+      RET(oz_proprm1(h, h->GTT, NT1));   // PROPRM1 then PROPR (GTT)
+      RET(oz_propr(h, h->GTT, NT1));
     } else {
     {  // PROPR(GT0): GT0 = S (expT GT0)
       GemmParams p = gsq(h, B);
-      p.A = h->expT; p.realA = 1; p.modA = F; p.B = h->GT0; p.C = h->T1; p.rs = h->S; p.sRS = N;
+      p.A = h->expT; p.realA = 1; p.modA = F; p.B = h->GT0; p.C = h->T1;
+      if (!pb) { p.rs = h->S; p.sRS = N; }
       RET(gemm(h, p));
       std::swap(h->GT0, h->T1);
+      if (pb) RET(vtx_left(h, h->GT0, NT1));
     }
     {  // PROPRM1(G0T): G0T = (G0T expTinv) Sinv
       GemmParams p = gsq(h, B);
-      p.A = h->G0T; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1; p.cs = h->Sinv; p.sCS = N;
+      p.A = h->G0T; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1;
+      if (!pb) { p.cs = h->Sinv; p.sCS = N; }
       RET(gemm(h, p));
       std::swap(h->G0T, h->T1);
+      if (pb) RET(vtx_right_inv(h, h->G0T, NT1));
     }
     {  // PROPRM1 then PROPR (GTT): GTT = S expT (GTT expTinv Sinv)
       GemmParams p = gsq(h, B);
-      p.A = h->GTT; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1; p.cs = h->Sinv; p.sCS = N;
+      p.A = h->GTT; p.B = h->expTinv; p.realB = 1; p.modB = F; p.C = h->T1;
+      if (!pb) { p.cs = h->Sinv; p.sCS = N; }
       RET(gemm(h, p));
+      if (pb) RET(vtx_right_inv(h, h->T1, NT1));
       GemmParams q = gsq(h, B);
-      q.A = h->expT; q.realA = 1; q.modA = F; q.B = h->T1; q.C = h->GTT; q.rs = h->S; q.sRS = N;
+      q.A = h->expT; q.realA = 1; q.modA = F; q.B = h->T1; q.C = h->GTT;
+      if (!pb) { q.rs = h->S; q.sRS = N; }
       RET(gemm(h, q));
+      if (pb) RET(vtx_left(h, h->GTT, NT1));
     }
     }
     prof_end(h);
@@ -1158,6 +1418,11 @@ static int hop(alfgpu_s* h, int up, int with_scale) {
 }
 static int hop_impl(alfgpu_s* h, int up, int with_scale) {
   const int N = h->N, F = h->F, B = h->B;
+  if (h->cb) {  // WRAPGRUP: mmthr, mmthl_m1; WRAPGRDO: mmthl, mmthr_m1 (bond passes, both forms)
+    if (with_scale) RET(scale_rc(h, h->G, up ? h->S : h->Sinv, 0, up ? h->Sinv : h->S));
+    RET(cb_apply(h, h->G, up ? CB_MMTHR : CB_MMTHL));
+    return cb_apply(h, h->G, up ? CB_MMTHL_M1 : CB_MMTHR_M1);
+  }
   if (h->mixed && h->oz && !(with_scale && h->eexp_complex)) {
     // up:   T1 = expT diag(S) G (row-major), G = T1 diag(Sinv) expTinv
     // down: T1 = G diag(S) expT (column-major), G = expTinv diag(Sinv) T1
@@ -1256,18 +1521,23 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.phase = h->phase; u.m_out = h->m; u.W = h->W; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
+    if (h->pairblock) {
+      u.vsite2 = h->v_blk2; u.vcoef = h->v_vc; u.sites2_out = h->sites2_out; u.coef_out = h->coef_out;
+    }
     prof_begin(h, ALFGPU_PROF_UPDATE);
     if (h->mixed) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
     else k_update<ArD><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
     prof_end(h);
     CKL();
     prof_begin(h, ALFGPU_PROF_FLUSH);
+    const int* s2o = h->pairblock ? h->sites2_out : nullptr;
+    const double* co = h->pairblock ? h->coef_out : nullptr;
     if (h->mixed)
       k_flush_xy<ArF><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
-                                                                         h->X, h->Y);
+                                                                         h->X, h->Y, s2o, co);
     else
       k_flush_xy<ArD><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
-                                                                         h->X, h->Y);
+                                                                         h->X, h->Y, s2o, co);
     CKL();
     void* Gst = h->G;
     void* Xst = h->X;
@@ -1295,6 +1565,20 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     } else if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
     else RET(gemm(h, p));
     prof_end(h);
+    // a phase ends with this block: its vertex wraps, explicit (up pass: E(s_old) G E(s_old)^-1 with
+    // the fields before the slice's updates; down pass: E(s_new)^-1 G E(s_new))
+    const int ph = h->pairblock ? h->blk_phase_end[dir][blk] : -1;
+    if (ph >= 0) {
+      prof_begin(h, ALFGPU_PROF_HOP);
+      if (dir == 0) {
+        RET(vtx_phase(h, h->G, ph, nt1, true, 0, 0, true));
+        RET(vtx_phase(h, h->G, ph, nt1, true, 1, 0, false));
+      } else {
+        RET(vtx_phase(h, h->G, ph, nt1, false, 1, 0, true));
+        RET(vtx_phase(h, h->G, ph, nt1, false, 0, 0, false));
+      }
+      prof_end(h);
+    }
   }
   return 0;
 }
@@ -1455,19 +1739,11 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   // takes clusters of CL / 2 CTAs: the same FP64 work in half as many CTAs, each pivot step's
   // cluster exchange and barriers shared by half as many (16 chains of the 16x16 Hubbard model:
   // 512 -> 256 CTAs on 152 SMs, QR time per sweep 501 -> 478 ms).  A grid that fits keeps CL.
-  {
-    h->qrr_ok = qrr_clusters(h->N, h->CL) > 0;
-    h->CLr = h->CL;
-    if (h->qrr_ok && h->CL >= 4) {
-      const int fl = d.reserved[0];
-      int nsm = 152;
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev);
-      cudaGetLastError();
-      const bool want = (fl & ALFGPU_FLAG_QR_HALF_CLUSTER) ||
-                        (!(fl & ALFGPU_FLAG_QR_FULL_CLUSTER) && (long long)h->B * h->CL > 2ll * nsm);
-      if (want && qrr_clusters(h->N, h->CL / 2) > 0) h->CLr = h->CL / 2;
-    }
-  }
+  // Rows that do not fit shared memory (N_dim above ~420, CGR2_2's 2N system) stay in a global
+  // workspace per CTA (mode 2) instead of falling back to the column-distributed k_qrp.
+  h->CLr = h->CL;
+  h->qrr_ok = qrr_plan(h->N, h->CL, h->B, d.reserved[0], h->dev, &h->CLr);
+  if (d.ltau) h->qr2_mode = qrr_plan(2 * d.ndim, cluster_size(2 * d.ndim), h->B, d.reserved[0], h->dev, &h->CL2);
   // the blocked QR keeps at most BQR_ROWS panel rows per CTA and BQR_LROWS rows per lane
   if (h->N > 32 * BQR_LROWS || (h->N + h->CL - 1) / h->CL > BQR_ROWS) h->exact_dec = h->exact_cgr = 1;
   const size_t N = h->N, NN = N * N, B = h->B, C = h->C, F = h->F, M = h->M, L = h->L;
@@ -1476,6 +1752,9 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->v_site, C * F * M); r |= dalloc(h, &h->v_g, C * F * M); r |= dalloc(h, &h->v_alpha, C * F * M);
   r |= dalloc(h, &h->v_E, C * F * M); r |= dalloc(h, &h->v_type, C * F * M); r |= dalloc(h, &h->v_Eexp, C * F * M * 10);
   r |= dalloc(h, &h->v_site2, C * F * M); r |= dalloc(h, &h->v_nsite, C * F * M);
+  r |= dalloc(h, &h->v_kind, C * F * M); r |= dalloc(h, &h->v_blk2, C * F * M); r |= dalloc(h, &h->v_vc, 2 * C * F * M);
+  r |= dalloc(h, &h->sites2_out, C * UPD_KMAX); r |= dalloc(h, &h->coef_out, 2 * C * UPD_KMAX);
+  r |= dalloc(h, &h->fields_old, C * M);
   r |= dalloc(h, &h->v_tab, C * F * M * 15);
   r |= dalloc(h, &h->v_sptr, C * F * (N + 1)); r |= dalloc(h, &h->v_slist, C * F * 2 * M);
   r |= dalloc(h, &h->fields, C * L * M);
@@ -1509,6 +1788,8 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     r |= dalloc(h, &h->Gq, 4 * B * NN);
   }
   if (h->df_qr) r |= dalloc(h, &h->QRdf, B * NN);
+  if (h->qrr_ok == 2) r |= dalloc(h, &h->qrr_ws, B * qrr_rows_elems(h->N, h->CLr));
+  if (h->qr2_mode == 2) r |= dalloc(h, &h->qr2_ws, B * qrr_rows_elems(2 * h->N, h->CL2));
   r |= dalloc(h, &h->Vtmp, B * NN);
   r |= dalloc(h, &h->tau, B * N); r |= dalloc(h, &h->jpvt, B * N); r |= dalloc(h, &h->perm, B * N);
   r |= dalloc(h, &h->iperm, B * N); r |= dalloc(h, &h->DUP, B * N); r |= dalloc(h, &h->vn, B * 2 * N);
@@ -1624,24 +1905,29 @@ static int make_blocks(alfgpu_s* h) {
   for (int dir = 0; dir < 2; ++dir) {
     std::vector<int>& st = h->blk_start[dir];
     std::vector<int>& nc = h->blk_cnt[dir];
-    st.clear(); nc.clear();
+    std::vector<int>& pe = h->blk_phase_end[dir];
+    st.clear(); nc.clear(); pe.clear();
     std::vector<int> seen(N, 0);
-    int npos = 0;
+    int npos = 0, prev_ph = -1;
     for (int pos = 0; pos < M; ++pos) {
       const int n = dir == 0 ? pos : M - 1 - pos;
-      const int s1 = h->hv_site[n], s2 = h->hv_site2[n], w = h->hv_nsite[n];
+      const int s1 = h->hv_site[n], s2 = h->hv_blk2[n], w = h->hv_nsite[n];
       if (s2 == s1) return ALFGPU_ERROR_UNSUPPORTED;
       const bool clash = seen[s1] || (s2 >= 0 && seen[s2]);
-      if (st.empty() || npos + w > h->kblk || clash) {
-        st.push_back(pos); nc.push_back(0);
+      const int ph = h->pairblock ? h->ph_of[n] : 0;
+      if (st.empty() || npos + w > h->kblk || clash || ph != prev_ph) {
+        if (!st.empty() && ph != prev_ph) pe.back() = prev_ph;  // the previous block closes its phase
+        st.push_back(pos); nc.push_back(0); pe.push_back(-1);
         std::fill(seen.begin(), seen.end(), 0);
         npos = 0;
       }
+      prev_ph = ph;
       seen[s1] = 1;
       if (s2 >= 0) seen[s2] = 1;
       npos += w;
       nc.back()++;
     }
+    if (!pe.empty()) pe.back() = prev_ph;
   }
   return 0;
 }
@@ -1697,23 +1983,68 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
       const size_t k = (size_t)f * M + n;
       if (site[k] != site[n] || site2[k] != site2[n] || v->op_diag[k] != v->op_diag[n]) return ALFGPU_ERROR_UNSUPPORTED;
     }
-  // rotated pairs must be disjoint and untouched by any other vertex
+  // Kinds: 0 one position, 1 two diagonal positions (a non-diagonal vertex in the rotated basis
+  // or a diagonal two-site one), 2 vector (a single-site vertex on a site of a rotated pair: in
+  // the rotated basis e_a becomes u = W^T e_a on the pair).  Rotated pairs are disjoint, each of
+  // their sites belongs to exactly one non-diagonal vertex, and other vertices touch them only
+  // as single-site (vector) vertices.
+  std::vector<int8_t> kind(K, 0);
+  std::vector<int> blk2(K, -1);
+  std::vector<double> vc(2 * K, 0.0);
+  for (size_t k = 0; k < K; ++k)
+    if (nsite[k] == 2) { kind[k] = 1; blk2[k] = site2[k]; }
+  int pairblock = 0;
+  std::vector<int> ph_of, ph_n0, ph_n1;
   if (have_rot) {
-    std::vector<int> cnt(N, 0), inpair(N, 0);
-    for (int n = 0; n < M; ++n) {
-      cnt[site[n]]++;
-      if (site2[n] >= 0) cnt[site2[n]]++;
-      if (!v->op_diag[n]) { inpair[site[n]] = 1; inpair[site2[n]] = 1; }
+    std::vector<int> partner(N, -1), slot(N, -1), cnt_nd(N, 0);
+    for (const auto& pr : pairs) {
+      partner[pr.first] = pr.second; partner[pr.second] = pr.first;
+      slot[pr.first] = 0; slot[pr.second] = 1;
     }
+    for (int n = 0; n < M; ++n)
+      if (!v->op_diag[n]) { cnt_nd[site[n]]++; cnt_nd[v->op_P[2 * n + 1]]++; }
     for (int i = 0; i < N; ++i)
-      if (inpair[i] && cnt[i] != 1) return ALFGPU_ERROR_UNSUPPORTED;
+      if (partner[i] >= 0 && cnt_nd[i] != 1) return ALFGPU_ERROR_UNSUPPORTED;
+    for (size_t k = 0; k < K; ++k) {
+      if (!v->op_diag[k]) continue;
+      const int a = v->op_P[2 * k];
+      if (v->op_n[k] == 2) {
+        if (partner[a] >= 0 || partner[v->op_P[2 * k + 1]] >= 0) return ALFGPU_ERROR_UNSUPPORTED;
+        continue;
+      }
+      if (partner[a] < 0) continue;
+      kind[k] = 2;
+      blk2[k] = partner[a];
+      vc[2 * k] = slot[a] == 0 ? U[0] : U[3];      // coefficient on a
+      vc[2 * k + 1] = slot[a] == 0 ? U[2] : U[1];  // coefficient on its partner
+      pairblock = 1;
+    }
     if (chain >= 0 && (!h->rot || h->rot_pairs != pairs)) {
       if (h->vert_ok) return ALFGPU_ERROR_UNSUPPORTED;  // per-chain tables share one basis
     }
   }
+  if (pairblock) {  // phases: a vertex whose support meets the current phase's opens the next one
+    std::vector<int> mark(N, -1);
+    int cur = 0;
+    ph_of.assign(M, 0);
+    ph_n0.push_back(0);
+    for (int n = 0; n < M; ++n) {
+      const int a = site[n], b = blk2[n];
+      if (mark[a] == cur || (b >= 0 && mark[b] == cur)) { ph_n1.push_back(n); ph_n0.push_back(n); ++cur; }
+      mark[a] = cur;
+      if (b >= 0) mark[b] = cur;
+      ph_of[n] = cur;
+    }
+    ph_n1.push_back(M);
+  }
+  if (chain >= 0 && h->vert_ok && (pairblock != h->pairblock || ph_n0 != h->ph_n0))
+    return ALFGPU_ERROR_UNSUPPORTED;  // the chains of a handle share one phase structure
+  h->pairblock = pairblock;
+  h->ph_of = ph_of; h->ph_n0 = ph_n0; h->ph_n1 = ph_n1;
   h->hv_site.assign(site.begin(), site.begin() + M);
   h->hv_site2.assign(site2.begin(), site2.begin() + M);
   h->hv_nsite.assign(nsite.begin(), nsite.begin() + M);
+  h->hv_blk2.assign(blk2.begin(), blk2.begin() + M);
   RET(make_blocks(h));
   // transition factors for every (vertex, old field, flip choice); type-1 fields flip sign
   std::vector<UpdTab> tab(K * 15);
@@ -1768,6 +2099,9 @@ int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v)
     CK(cudaMemcpy(h->v_alpha + c * K, al.data(), K * sizeof(zd), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_type + c * K, ty.data(), K, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->v_Eexp + c * K * 10, ee.data(), K * 10 * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_kind + c * K, kind.data(), K, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_blk2 + c * K, blk2.data(), K * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->v_vc + 2 * c * K, vc.data(), 2 * K * sizeof(double), cudaMemcpyHostToDevice));
   }
   const bool rot_changed = have_rot != h->rot || (have_rot && (pairs != h->rot_pairs || memcmp(U, h->rot_U, sizeof(U))));
   h->rot = have_rot;
@@ -1883,14 +2217,20 @@ static int sweep_body(alfgpu_s* h, const double* dr, alfgpu_obs_cb cb, void* ctx
   RET(udv_reset(h, h->udvr));
   int NST = 1;
   int pending = 0;
+  const int pb = h->pairblock;  // vector vertices: every phase's wraps are explicit, none deferred
   for (int ntau = 0; ntau < L; ++ntau) {
     const int ntau1 = ntau + 1;
     RET(hop(h, 1, pending));
-    RET(slice_scale(h, ntau1));  // vertex wraps of this slice use the fields before their update
+    if (pb) {  // the slice's fields before their update, for the explicit phase wraps
+      k_copy_fields<<<dim3((M + 255) / 256, h->C), 256, 0, h->st>>>(h->fields, L, M, ntau1, h->fields_old);
+      CKL();
+    } else {
+      RET(slice_scale(h, ntau1));  // vertex wraps of this slice use the fields before their update
+    }
     RET(update_slice(h, ntau1, 0, ntau * M, dr));
-    pending = 1;
+    pending = pb ? 0 : 1;
     if (ntau1 == h->stab_nt[NST]) {
-      {
+      if (pending) {
         dim3 grid((unsigned)(((long long)h->N * h->N + 255) / 256), h->B);
         k_apply_scale<<<grid, 256, 0, h->st>>>(h->G, h->S, h->Sinv, h->N);
         CKL();
@@ -1911,8 +2251,8 @@ static int sweep_body(alfgpu_s* h, const double* dr, alfgpu_obs_cb cb, void* ctx
   for (int ntau = L; ntau >= 1; --ntau) {
     const int ntau1 = ntau - 1;
     RET(update_slice(h, ntau, 1, L * M + (L - ntau) * M, dr));
-    RET(slice_scale(h, ntau));  // Op_Wrapdo N_type=1 uses the updated fields
-    RET(hop(h, 0, 1));
+    if (!pb) RET(slice_scale(h, ntau));  // Op_Wrapdo N_type=1 uses the updated fields
+    RET(hop(h, 0, pb ? 0 : 1));
     if (ntau1 >= 1) RET(obs_eq(h, cb, ctx, ntau1, 0));
     if (NST >= 1 && h->stab_nt[NST] == ntau1 && ntau1 != 0) {
       RET(wrapul(h, h->stab_nt[NST + 1], ntau1));
@@ -2407,5 +2747,124 @@ int alfgpu_reset_scalar_obs(alfgpu_t* h) {
   CK(cudaSetDevice(h->dev));
   CK(cudaMemsetAsync(h->obs_acc, 0, 10 * (size_t)h->C * sizeof(double), h->st));
   CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+// ---- device-side lattice-resolved observables ----------------------------------------------
+int alfgpu_set_lattice_obs(alfgpu_t* h, int32_t ncell, int32_t norb, const int32_t* site_of, const int32_t* jof) {
+  if (!h) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  if (!site_of || !jof) {  // off
+    h->obs_latt = 0;
+    drop_graphs(h);
+    return 0;
+  }
+  if (ncell < 1 || norb < 1 || (long long)ncell * norb != h->N) return ALFGPU_ERROR_ARGUMENT;
+  std::vector<int> seen(h->N, 0);
+  for (long long e = 0; e < (long long)ncell * norb; ++e) {
+    if (site_of[e] < 0 || site_of[e] >= h->N || seen[site_of[e]]) return ALFGPU_ERROR_ARGUMENT;
+    seen[site_of[e]] = 1;
+  }
+  for (int I = 0; I < ncell; ++I) {
+    std::vector<int> cs(ncell, 0);
+    for (int R = 0; R < ncell; ++R) {
+      const int J = jof[(long long)I * ncell + R];
+      if (J < 0 || J >= ncell || cs[J]) return ALFGPU_ERROR_ARGUMENT;
+      cs[J] = 1;
+    }
+  }
+  const int nnames = h->F == 2 ? 5 : 3;
+  if (h->obs_latt || h->lo_site) {
+    if (ncell != h->lo_ncell || norb != h->lo_norb) return ALFGPU_ERROR_ARGUMENT;  // one lattice per handle
+  } else {
+    const size_t C = h->C, no2 = (size_t)norb * norb;
+    int r = 0;
+    r |= dalloc(h, &h->lo_site, (size_t)ncell * norb); r |= dalloc(h, &h->lo_jof, (size_t)ncell * ncell);
+    r |= dalloc(h, &h->lo_acc[0], C * nnames * ncell * no2); r |= dalloc(h, &h->lo_acc0[0], C * nnames * norb);
+    r |= dalloc(h, &h->lo_cnt[0], 2 * C);
+    if (h->ltau) {
+      r |= dalloc(h, &h->lo_acc[1], C * nnames * ncell * (size_t)(h->L + 1) * no2);
+      r |= dalloc(h, &h->lo_acc0[1], C * nnames * norb); r |= dalloc(h, &h->lo_cnt[1], 2 * C);
+      if (!h->Gq) r |= dalloc(h, &h->Gq, 4 * (size_t)h->B * h->N * h->N);
+    }
+    if (r) return ALFGPU_ERROR_CUDA;
+  }
+  h->lo_ncell = ncell; h->lo_norb = norb; h->lo_nnames = nnames;
+  CK(cudaMemcpy(h->lo_site, site_of, (size_t)ncell * norb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->lo_jof, jof, (size_t)ncell * ncell * sizeof(int), cudaMemcpyHostToDevice));
+  h->obs_latt = 1;
+  drop_graphs(h);
+  return alfgpu_reset_lattice_obs(h);
+}
+
+int alfgpu_reset_lattice_obs(alfgpu_t* h) {
+  if (!h || !h->lo_site) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  const size_t C = h->C, no2 = (size_t)h->lo_norb * h->lo_norb, nn = h->lo_nnames;
+  for (int k = 0; k < 2; ++k) {
+    if (!h->lo_acc[k]) continue;
+    const size_t L1 = k ? (size_t)h->L + 1 : 1;
+    CK(cudaMemsetAsync(h->lo_acc[k], 0, C * nn * h->lo_ncell * L1 * no2 * sizeof(zd), h->st));
+    CK(cudaMemsetAsync(h->lo_acc0[k], 0, C * nn * h->lo_norb * sizeof(zd), h->st));
+    CK(cudaMemsetAsync(h->lo_cnt[k], 0, 2 * C * sizeof(double), h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int alfgpu_get_lattice_obs(alfgpu_t* h, int32_t chain, int32_t kind, double* latt, double* latt0, double* cnt) {
+  if (!h || !h->lo_site || chain < 0 || chain >= h->C || kind < 0 || kind > 1 || !h->lo_acc[kind])
+    return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  const size_t no2 = (size_t)h->lo_norb * h->lo_norb, nn = h->lo_nnames;
+  const size_t L1 = kind ? (size_t)h->L + 1 : 1;
+  const size_t n = nn * h->lo_ncell * L1 * no2, n0 = nn * h->lo_norb;
+  if (latt) CK(cudaMemcpy(latt, h->lo_acc[kind] + chain * n, n * sizeof(zd), cudaMemcpyDeviceToHost));
+  if (latt0) CK(cudaMemcpy(latt0, h->lo_acc0[kind] + chain * n0, n0 * sizeof(zd), cudaMemcpyDeviceToHost));
+  if (cnt) CK(cudaMemcpy(cnt, h->lo_cnt[kind] + 2 * chain, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// ---- checkerboard hopping ------------------------------------------------------------------
+int alfgpu_upload_checkerboard(alfgpu_t* h, int32_t ncheck, int32_t nfam, const int32_t* fam, const int32_t* P,
+                               const double* mat, const double* inv) {
+  if (!h || ncheck < 0 || (ncheck > 0 && (!fam || !P || !mat || !inv || nfam < 1))) return ALFGPU_ERROR_ARGUMENT;
+  CK(cudaSetDevice(h->dev));
+  if (ncheck == 0) {  // back to the dense exponentials of alfgpu_upload_hopping
+    h->cb = 0;
+    drop_graphs(h);
+    return 0;
+  }
+  if (h->rot) return ALFGPU_ERROR_UNSUPPORTED;  // bonds in the rotated basis of two-site vertices: not built
+  const int N = h->N, F = h->F;
+  if (fam[0] != 0 || fam[nfam] != ncheck) return ALFGPU_ERROR_ARGUMENT;
+  for (int q = 0; q < nfam; ++q) {
+    if (fam[q + 1] < fam[q]) return ALFGPU_ERROR_ARGUMENT;
+    for (int f = 0; f < F; ++f) {  // the bonds of a family are disjoint
+      std::vector<int> seen(N, 0);
+      for (int nc = fam[q]; nc < fam[q + 1]; ++nc)
+        for (int e = 0; e < 2; ++e) {
+          const int s = P[2 * ((size_t)f * ncheck + nc) + e];
+          if (s < 0 || s >= N || seen[s]) return ALFGPU_ERROR_HAMILTONIAN;
+          seen[s] = 1;
+        }
+    }
+  }
+  for (size_t k = 0; k < 4ull * F * ncheck; ++k)
+    if (!std::isfinite(mat[k]) || !std::isfinite(inv[k])) return ALFGPU_ERROR_HAMILTONIAN;
+  if (ncheck > h->cb_ncheck) {
+    int r = 0;
+    r |= dalloc(h, &h->cb_P, 2ull * F * ncheck);
+    r |= dalloc(h, &h->cb_mat, 4ull * F * ncheck); r |= dalloc(h, &h->cb_inv, 4ull * F * ncheck);
+    if (r) return ALFGPU_ERROR_CUDA;
+  }
+  CK(cudaMemcpy(h->cb_P, P, 2ull * F * ncheck * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->cb_mat, mat, 4ull * F * ncheck * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->cb_inv, inv, 4ull * F * ncheck * sizeof(double), cudaMemcpyHostToDevice));
+  h->cb_ncheck = ncheck;
+  h->cb_fam.assign(fam, fam + nfam + 1);
+  h->cb = 1;
+  drop_graphs(h);
   return 0;
 }

@@ -329,3 +329,136 @@ __global__ void __launch_bounds__(256) k_obs_scal(const zd* G, const zd* phase, 
     a[9] += 1.0;
   }
 }
+
+// ---- explicit vertex wraps of one phase (models with vector vertices) --------------------------
+// A phase is a range [n0, n1) of vertices with pairwise disjoint supports in the rotated basis.
+// Vertex n acts on its support with the block
+//   kind 0 (one site a):            e_0
+//   kind 1 (pair (a, b), diagonal): diag(e_0, e_1)
+//   kind 2 (pair (a, b), vector u): I + (e_0 - 1) u u^T,  u = (c_a, c_b) real, |u| = 1
+// where e_m = E_exp(m, s) of the vertex's field s (Op%E_exp of Operator_mod.F90:472-529), with
+// s -> -s for the inverse (inv) and every entry conjugated for the adjoint (cj; the blocks
+// are symmetric).  fl points at the slice's fields of chain 0 ([chain] stride fstride).
+struct VtxPhase {
+  const int8_t* fl; long long fstride;
+  const int8_t* kind; const int* site; const int* site2; const double* coef;  // [chain][F*M]
+  const zd* Eexp;                                                              // [chain][F*M][2][5]
+  long long sK;                                                                // F * M
+  int F, M, N, n0, n1, inv, cj;
+};
+
+ALF_DEV void vtx_block(const VtxPhase& p, int b, int n, int* a, int* c, zd m[4], int* two) {
+  const int ch = b / p.F, f = b % p.F;
+  const long long k = (long long)ch * p.sK + (long long)f * p.M + n;
+  int s = p.fl[(long long)ch * p.fstride + n];
+  if (p.inv) s = -s;
+  const zd* ee = p.Eexp + k * 10;
+  const zd e0 = ee[s + 2];
+  const int kd = p.kind[k];
+  *a = p.site[k];
+  *two = kd != 0;
+  if (kd == 0) {
+    m[0] = e0;
+  } else if (kd == 1) {
+    *c = p.site2[k];
+    m[0] = e0; m[1] = zmk(0.0, 0.0); m[2] = zmk(0.0, 0.0); m[3] = ee[5 + s + 2];
+  } else {
+    *c = p.site2[k];
+    const double ua = p.coef[2 * k], ub = p.coef[2 * k + 1];
+    const zd d = zmk(e0.x - 1.0, e0.y);
+    m[0] = zadd(zmk(1.0, 0.0), zscale(d, ua * ua));
+    m[1] = zscale(d, ua * ub);  // (b, a) entry
+    m[2] = m[1];                 // (a, b) entry
+    m[3] = zadd(zmk(1.0, 0.0), zscale(d, ub * ub));
+  }
+  if (p.cj)
+    for (int e = 0; e < 4; ++e) m[e] = zconj(m[e]);
+}
+
+// X <- E X (rows of every vertex's support), grid (ceil(N * (n1 - n0) / 256), B)
+__global__ void k_vtx_rows(zd* X, long long sX, VtxPhase p) {
+  const int b = blockIdx.y;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  const int nv = p.n1 - p.n0;
+  if (e >= (long long)p.N * nv) return;
+  const int j = (int)(e % p.N), n = p.n0 + (int)(e / p.N);
+  int a = 0, c = 0, two = 0;
+  zd m[4];
+  vtx_block(p, b, n, &a, &c, m, &two);
+  zd* col = X + b * sX + (long long)j * p.N;
+  if (!two) { col[a] = zmul(m[0], col[a]); return; }
+  const zd xa = col[a], xc = col[c];
+  col[a] = zadd(zmul(m[0], xa), zmul(m[2], xc));
+  col[c] = zadd(zmul(m[1], xa), zmul(m[3], xc));
+}
+
+// X <- X E (columns of every vertex's support), grid (ceil(N * (n1 - n0) / 256), B)
+__global__ void k_vtx_cols(zd* X, long long sX, VtxPhase p) {
+  const int b = blockIdx.y;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  const int nv = p.n1 - p.n0;
+  if (e >= (long long)p.N * nv) return;
+  const int i = (int)(e % p.N), n = p.n0 + (int)(e / p.N);
+  int a = 0, c = 0, two = 0;
+  zd m[4];
+  vtx_block(p, b, n, &a, &c, m, &two);
+  zd* Xb = X + b * sX;
+  if (!two) { Xb[i + (long long)a * p.N] = zmul(Xb[i + (long long)a * p.N], m[0]); return; }
+  const zd xa = Xb[i + (long long)a * p.N], xc = Xb[i + (long long)c * p.N];
+  Xb[i + (long long)a * p.N] = zadd(zmul(xa, m[0]), zmul(xc, m[1]));
+  Xb[i + (long long)c * p.N] = zadd(zmul(xa, m[2]), zmul(xc, m[3]));
+}
+
+// copy of one slice's fields of every chain (the fields before the slice's updates)
+__global__ void k_copy_fields(const int8_t* fields, int L, int M, int nt1, int8_t* out) {
+  const int c = blockIdx.y;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < M; n += gridDim.x * blockDim.x)
+    out[(long long)c * M + n] = fields[(long long)c * L * M + (long long)(nt1 - 1) * M + n];
+}
+
+// ---- checkerboard hopping: bond operators of one family ------------------------------------
+// Bonds [b0, b1) of a family are disjoint two-site operators (P [F][ncheck][2], E [F][ncheck][4]
+// real, column-major 2 x 2); batch entry b uses flavour b % F.  The RealExpOpT lmult / rmult of
+// each bond (Prog/OpTTypes_mod.F90:135-304): rows (X <- E X) or columns (X <- X E).
+// grid (ceil(N (b1 - b0) / 256), B)
+__global__ void k_bond_rows(zd* X, long long sX, int N, int F, const int* P, const double* E, int ncheck, int b0,
+                            int b1) {
+  const int b = blockIdx.y, f = b % F;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= (long long)N * (b1 - b0)) return;
+  const int j = (int)(e % N), nc = b0 + (int)(e / N);
+  const long long k = (long long)f * ncheck + nc;
+  const int a = P[2 * k], c = P[2 * k + 1];
+  const double* m = E + 4 * k;
+  zd* col = X + b * sX + (long long)j * N;
+  const zd xa = col[a], xc = col[c];
+  col[a] = zadd(zscale(xa, m[0]), zscale(xc, m[2]));
+  col[c] = zadd(zscale(xa, m[1]), zscale(xc, m[3]));
+}
+__global__ void k_bond_cols(zd* X, long long sX, int N, int F, const int* P, const double* E, int ncheck, int b0,
+                            int b1) {
+  const int b = blockIdx.y, f = b % F;
+  const long long e = blockIdx.x * 256ll + threadIdx.x;
+  if (e >= (long long)N * (b1 - b0)) return;
+  const int i = (int)(e % N), nc = b0 + (int)(e / N);
+  const long long k = (long long)f * ncheck + nc;
+  const int a = P[2 * k], c = P[2 * k + 1];
+  const double* m = E + 4 * k;
+  zd* Xb = X + b * sX;
+  const zd xa = Xb[i + (long long)a * N], xc = Xb[i + (long long)c * N];
+  Xb[i + (long long)a * N] = zadd(zscale(xa, m[0]), zscale(xc, m[1]));
+  Xb[i + (long long)c * N] = zadd(zscale(xa, m[2]), zscale(xc, m[3]));
+}
+
+// X(i, j) *= rs(i) (conjugated with rconj) * cs(j); rs or cs may be null.  grid (ceil(N N / 256), B)
+__global__ void k_scale_rc(zd* X, int N, const zd* rs, int rconj, const zd* cs) {
+  const int b = blockIdx.y;
+  const long long NN = (long long)N * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < NN; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % N), j = (int)(e / N);
+    zd v = X[b * NN + e];
+    if (rs) v = zmul(rconj ? zconj(rs[(long long)b * N + i]) : rs[(long long)b * N + i], v);
+    if (cs) v = zmul(v, cs[(long long)b * N + j]);
+    X[b * NN + e] = v;
+  }
+}

@@ -330,6 +330,62 @@ __global__ void __launch_bounds__(256) k_trsv(TrsvParams p) {
   }
 }
 
+// The same solve for V right-hand sides per CTA (vectors V blockIdx.x .. + V - 1): thread t
+// works on vector t % V and rows t / V, t / V + 256 / V, ...; the V threads of a row read the
+// same triangle entry (one broadcast load feeds V products) and one barrier per row serves V
+// vectors.  Dynamic shared memory: (2 V + 1) N complex values.  Same arithmetic per vector as
+// k_trsv.
+template <int V>
+__global__ void __launch_bounds__(256) k_trsv_v(TrsvParams p) {
+  const int b = blockIdx.y, v0 = blockIdx.x * V, N = p.N, tid = threadIdx.x;
+  const zd* T = p.T + b * p.sT;
+  zd* Bb = p.B + b * p.sB;
+  extern __shared__ zd tsm[];
+  zd* xs = tsm;            // [V][N]
+  zd* xo = xs + V * N;     // [V][N]
+  zd* dinv = xo + V * N;   // [N]
+  auto Tij = [&](int i, int j) -> zd {
+    return p.trans ? zconj(T[j + (long long)i * p.ldt]) : T[i + (long long)j * p.ldt];
+  };
+  for (int e = tid; e < V * N; e += 256) {
+    const int v = e / N, i = e % N;
+    zd t = zmk(0.0, 0.0);
+    if (v0 + v < p.nvec) {
+      t = Bb[(long long)(v0 + v) * p.vstride + (long long)i * p.estride];
+      if (p.conj_io) t = zconj(t);
+    }
+    xs[v * N + i] = t;
+  }
+  for (int i = tid; i < N; i += 256) dinv[i] = zinv(Tij(i, i));
+  __syncthreads();
+  const int v = tid % V, r0 = tid / V, rs = 256 / V;
+  zd* x = xs + v * N;
+  if (!p.lower) {
+    for (int i = N - 1; i >= 0; --i) {
+      const zd xi = zmul(x[i], dinv[i]);
+      if (r0 == 0) xo[v * N + i] = xi;
+      for (int r = r0; r < i; r += rs) x[r] = zsub(x[r], zmul(Tij(r, i), xi));
+      __syncthreads();
+    }
+  } else {
+    for (int i = 0; i < N; ++i) {
+      const zd xi = zmul(x[i], dinv[i]);
+      if (r0 == 0) xo[v * N + i] = xi;
+      for (int r = i + 1 + r0; r < N; r += rs) x[r] = zsub(x[r], zmul(Tij(r, i), xi));
+      __syncthreads();
+    }
+  }
+  for (int e = tid; e < V * N; e += 256) {
+    const int vv = e / N, i = e % N;
+    if (v0 + vv >= p.nvec) continue;
+    zd t = xo[vv * N + i];
+    if (p.oscale) t = zscale(t, p.oscale[(long long)b * N + i]);
+    Bb[(long long)(v0 + vv) * p.vstride + (long long)i * p.estride] = p.conj_io ? zconj(t) : t;
+  }
+}
+#define TRSV_V 8
+static inline size_t trsv_v_smem(int N) { return (size_t)(2 * TRSV_V + 1) * N * 16; }
+
 // out(j, i) = conj(in(i, j)) (or plain transpose), batched, N x N.
 __global__ void k_transpose(const zd* in, long long ldi, long long sI, zd* out, long long ldo, long long sO, int N,
                             int conj) {

@@ -395,6 +395,11 @@ __global__ void __launch_bounds__(256) k_bqr_finish(zd* A, long long lda, long l
 // squared (the pivot order is the same, the downdate becomes a subtraction).
 // Outputs as k_qrp before normalisation: R above, reflectors below, tau, jpvt,
 // D = |R_jj|, info.psign; k_bqr_finish then normalises and forms the products.
+// GROWS = true keeps each CTA's rows in a global workspace (Arows, one nrl x N block per
+// CTA, L2-resident) instead of shared memory, for matrices whose rows do not fit a
+// cluster's shared memory (CGR2_2's 2N system at N_dim = 288: 36 rows x 576 columns per
+// CTA); the exchange arrays stay in shared memory, and the arithmetic and its order are
+// the same as with the rows in shared memory.
 struct QRRowsParams {
   const zd* Ain;             // input (may equal A)
   zd* A; long long lda, sA;  // output: R above the diagonal, reflectors below (FP64)
@@ -405,13 +410,17 @@ struct QRRowsParams {
   int* jpvt; long long sP;
   double* D; long long sD;
   QRInfo* info;
+  void* Arows;               // GROWS: workspace of B x CL x nrl x N values of the kernel's arithmetic
 };
 
-static inline size_t qrr_smem_bytes(int N, int CL) {
+static inline size_t qrr_smem_bytes(int N, int CL, bool grows = false) {
   const size_t nrl = (size_t)((N + CL - 1) / CL);
   const size_t npad = (size_t)((N + 1) & ~1);  // keeps the 16-byte arrays after it aligned
-  return nrl * N * 16 + 6ull * N * 16 + 2ull * N * 8 + npad * 8 + (size_t)N * sizeof(int) + nrl * 16 + 64;
+  return (grows ? 0 : nrl * N * 16) + 6ull * N * 16 + 2ull * N * 8 + npad * 8 + (size_t)N * sizeof(int) + nrl * 16 +
+         64;
 }
+// Elements of the GROWS workspace per matrix.
+static inline size_t qrr_rows_elems(int N, int CL) { return (size_t)CL * ((N + CL - 1) / CL) * N; }
 
 template <class Z>
 ALF_DEV Z dsm_ld16(uint32_t addr) {  // 16-byte value from a peer CTA's shared memory
@@ -477,7 +486,7 @@ ALF_DEV void qrr_argmax(typename A::R& v, int& i) {  // warp argmax, first index
 // ArF factors the unscaled columns instead: with the same pivots QR(U D) = Q (R_U D)
 // (a Householder reflector does not change when its column is scaled), so only the
 // pivot keys ||U_c|| d_c (FP64), D and the R output carry the scales.
-template <class A>
+template <class A, bool GROWS = false>
 __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
   typedef typename A::Z Z;
   typedef typename A::R R;
@@ -486,8 +495,10 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
   const int nrl = (N + (int)CL - 1) / (int)CL;
   const int nmine = (N - (int)rank + (int)CL - 1) / (int)CL;  // rows rank, rank+CL, ...
   extern __shared__ __align__(16) unsigned char qrr_raw[];
-  Z* Ar = reinterpret_cast<Z*>(qrr_raw);  // [nrl][N] row-major: Ar[il*N + c] = A(rank + il*CL, c)
-  Z* xs = Ar + (size_t)nrl * N;           // [2][N] partial sums (read remotely)
+  // [nrl][N] row-major: Ar[il*N + c] = A(rank + il*CL, c), in shared memory or the workspace
+  Z* Ar = GROWS ? reinterpret_cast<Z*>(p.Arows) + ((size_t)b * CL + rank) * (size_t)nrl * N
+                : reinterpret_cast<Z*>(qrr_raw);
+  Z* xs = GROWS ? reinterpret_cast<Z*>(qrr_raw) : Ar + (size_t)nrl * N;  // [2][N] partial sums (read remotely)
   Z* xr = xs + 2 * N;                     // [2][N] pivot row (owner)
   Z* tot = xr + 2 * N;                    // [N]
   Z* prow = tot + N;                      // [N]

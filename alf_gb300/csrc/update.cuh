@@ -69,6 +69,12 @@ struct UpdParams {
   long long* cnt;       // [chain][4] n_prop, n_acc, n_prop_eff, n_acc_eff
   int8_t* rec_acc; zd* rec_ratio; long long sRec;
   FieldTables ft;
+  // vector vertices (a single-site vertex on a site of a rotated pair: in the rotated basis its
+  // one position is the real unit vector u = c_a e_a + c_b e_b); null when the model has none
+  const int* vsite2;    // [chain][F*M] site b of a vector vertex, -1 otherwise
+  const double* vcoef;  // [chain][F*M][2] (c_a, c_b)
+  int* sites2_out;      // [chain][UPD_KMAX] accepted positions: site b or -1
+  double* coef_out;     // [chain][UPD_KMAX][2]
 };
 
 ALF_DEV int nranf3(double r) {
@@ -118,6 +124,8 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   __shared__ Z s_mye[2][KM], s_dlt[2][KM], s_tcol[2][2][KM], s_rowt[2][KM], s_piv[2][2];
   __shared__ zd s_dlt64[2][KM];
   __shared__ int s_psite[KM], s_pvis[KM], s_pkind[KM], s_accq[KM], s_acc[2];
+  __shared__ int s_psite2[KM];      // vector positions: site b, else -1
+  __shared__ double s_pc[KM][2];    // vector positions: (c_a, c_b)
   // per visit (FP64 in both forms: the ratio accumulation)
   __shared__ zd s_K[KM];
   __shared__ double s_u2[KM], s_gr[KM];
@@ -183,10 +191,16 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
       // [prod_f exp(Z1 alpha)]^N_SUN gamma'/gamma: with N_SUN = 1 the gamma ratio joins K
       if (p.NSUN == 1) K = zscale(K, p.ft.grat[tp - 1][so + 2][sn + 2]);
       s_K[q] = K;
+      const int vb = p.vsite2 ? p.vsite2[(long long)c * p.V.sK + n] : -1;
       for (int I = 0; I < w; ++I) {
         s_psite[p0 + I] = I ? site2[n] : site[n];
         s_pvis[p0 + I] = q;
         s_pkind[p0 + I] = (w == 2) ? (I ? 2 : 1) : 0;  // 0 single, 1 first of a pair, 2 second
+        s_psite2[p0 + I] = (w == 1) ? vb : -1;
+        if (vb >= 0) {
+          s_pc[p0 + I][0] = p.vcoef[2 * ((long long)c * p.V.sK + n)];
+          s_pc[p0 + I][1] = p.vcoef[2 * ((long long)c * p.V.sK + n) + 1];
+        }
       }
     }
   }
@@ -195,7 +209,19 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   for (int a = warp; a < np; a += NW)
     if (lane < np)
       for (int f = 0; f < F; ++f) {
-        const Z v = A::mk(G[f * NN + s_psite[a] + (long long)s_psite[lane] * N]);
+        zd g = G[f * NN + s_psite[a] + (long long)s_psite[lane] * N];
+        if (p.vsite2 && (s_psite2[a] >= 0 || s_psite2[lane] >= 0)) {
+          // Ghat(a, l) = v_a^T G v_l over the (up to two) sites of each position
+          const int ia[2] = {s_psite[a], s_psite2[a]}, il[2] = {s_psite[lane], s_psite2[lane]};
+          const double ca[2] = {s_psite2[a] >= 0 ? s_pc[a][0] : 1.0, s_psite2[a] >= 0 ? s_pc[a][1] : 0.0};
+          const double cl[2] = {s_psite2[lane] >= 0 ? s_pc[lane][0] : 1.0, s_psite2[lane] >= 0 ? s_pc[lane][1] : 0.0};
+          g = zmk(0.0, 0.0);
+          for (int x = 0; x < 2; ++x)
+            for (int y = 0; y < 2; ++y)
+              if (ia[x] >= 0 && il[y] >= 0 && ca[x] != 0.0 && cl[y] != 0.0)
+                g = zadd(g, zscale(G[f * NN + ia[x] + (long long)il[y] * N], ca[x] * cl[y]));
+        }
+        const Z v = A::mk(g);
         Gh[(f * KM + a) * LD + lane] = v;
         G0[(f * KM + a) * LD + lane] = v;
       }
@@ -209,6 +235,13 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
     if (lane == 0) {
       s_accq[m] = v;
       p.sites_out[(long long)c * KM + m] = s_psite[v];
+      if (p.sites2_out) {
+        p.sites2_out[(long long)c * KM + m] = s_psite2[v];
+        if (s_psite2[v] >= 0) {
+          p.coef_out[2 * ((long long)c * KM + m)] = s_pc[v][0];
+          p.coef_out[2 * ((long long)c * KM + m) + 1] = s_pc[v][1];
+        }
+      }
       for (int f = 0; f < F; ++f) p.delta_out[((long long)c * 2 + f) * KM + m] = s_dlt64[f][v];
     }
     m += 1;
@@ -398,13 +431,14 @@ constexpr size_t upd_smem_bytes() { return 2ull * 2 * UPD_KMAX * (UPD_KMAX + 1) 
 
 // Flush operands for G = G0 - X Y (one launch, spread over the GPU; the m x m x N product of
 // Y in the precision form's arithmetic, double-float in the mixed form):
-//   X(:, l) = G0(:, s_l)
-//   Y(l, :) = sum_l' W(l,l') (e_{s_l'} - G0(s_l', :))
+//   X(:, l) = G0 v_l
+//   Y(l, :) = sum_l' W(l,l') (v_l'^T - v_l'^T G0)
+// with v_l = e_{s_l}, or c_a e_a + c_b e_b for a vector position (sites2 / coefs, may be null).
 // block 32 x 8 threads = (l, column / row); grid (ceil(N/8), chains*flavours).
 // X: [chain][2][N][KMAX] col-major (ld N); Y: [chain][2][KMAX][N] col-major (ld KMAX).
 template <class A>
 __global__ void k_flush_xy(const zd* Gv, long long sG, int N, int F, const int* m_in, const int* sites, const zd* W,
-                           zd* X, zd* Y) {
+                           zd* X, zd* Y, const int* sites2 = nullptr, const double* coefs = nullptr) {
   typedef typename A::Z Z;
   const int b = blockIdx.y, c = b / F, f = b % F;
   const int m = m_in[c];
@@ -422,8 +456,18 @@ __global__ void k_flush_xy(const zd* Gv, long long sG, int N, int F, const int* 
   const long long xy = ((long long)c * 2 + f) * N * UPD_KMAX;
   if (col < N && tx < m) {
     const int s = st[tx];
-    X[xy + col + (long long)tx * N] = Gf[col + (long long)s * N];  // row `col` of X
-    gb[ty][tx] = A::mk(zsub(zmk(s == col ? 1.0 : 0.0, 0.0), Gf[s + (long long)col * N]));
+    const int s2 = sites2 ? sites2[(long long)c * UPD_KMAX + tx] : -1;
+    if (s2 < 0) {
+      X[xy + col + (long long)tx * N] = Gf[col + (long long)s * N];  // row `col` of X
+      gb[ty][tx] = A::mk(zsub(zmk(s == col ? 1.0 : 0.0, 0.0), Gf[s + (long long)col * N]));
+    } else {
+      const double ca = coefs[2 * ((long long)c * UPD_KMAX + tx)], cb = coefs[2 * ((long long)c * UPD_KMAX + tx) + 1];
+      X[xy + col + (long long)tx * N] =
+          zadd(zscale(Gf[col + (long long)s * N], ca), zscale(Gf[col + (long long)s2 * N], cb));
+      const double e = (s == col ? ca : 0.0) + (s2 == col ? cb : 0.0);
+      gb[ty][tx] = A::mk(zsub(zmk(e, 0.0), zadd(zscale(Gf[s + (long long)col * N], ca),
+                                                zscale(Gf[s2 + (long long)col * N], cb))));
+    }
   }
   __syncthreads();
   if (col < N && tx < m) {

@@ -261,6 +261,68 @@ def exp_hopping(O: np.ndarray, dtau: float):
     return mats[0], mats[1]
 
 
+def checkerboard_ops(lattice: str, L1: int, L2: int, dtau: float, t: float = 1.0, chem: float = 0.0,
+                     site_order: str = "natural") -> dict:
+    """Checkerboard ``Op_T`` of the square and honeycomb lattices: one two-site operator per
+    bond, in ALF's family order (Predefined_Hop_mod.F90:331-361 square: four families, the a2
+    and a1 bonds of the cells with even i1 + i2, then those of the odd cells (even L1, L2);
+    :893-904 honeycomb: three families, one per bond of the unit cell).  Each operator is
+    ``O = [[T_loc(no_I)/m(no_I), T], [conj T, T_loc(no_J)/m(no_J)]]`` on (I1, J1) with the
+    orbital multiplicities m of the bond table and ``g = -dtau`` (Predefined_Hop_mod.F90:
+    1780-1835).  Returns P [Ncheck][2] (0-based sites), mat = exp(g O), inv = exp(-g O)
+    [Ncheck][2][2], and fam: the first operator of each family and Ncheck."""
+    lat = lattice.upper()
+    if lat == "SQUARE":
+        if L1 % 2 or L2 % 2:
+            raise ValueError("the square-lattice checkerboard decomposition needs even L1 and L2")
+        norb, bonds = 1, [(0, 0, 0, 1), (0, 0, 1, 0)]
+        fam_of = lambda n1, n2: [(0 if (n1 + n2) % 2 == 0 else 2) + b for b in range(2)]
+        nfam = 4
+    elif lat == "HONEYCOMB":
+        norb, bonds = 2, [(0, 1, 0, 0), (1, 0, 0, 1), (0, 1, 1, -1)]
+        fam_of = lambda n1, n2: [0, 1, 2]
+        nfam = 3
+    else:
+        raise ValueError(f"no checkerboard decomposition for {lattice!r}")
+    mult = [0] * norb
+    for (oi, oj, _, _) in bonds:
+        mult[oi] += 1
+        mult[oj] += 1
+    perm = _site_permutation(lattice, L1, L2, norb, site_order)
+    new_of = np.arange(L1 * L2 * norb) if perm is None else np.argsort(perm)
+    fams = [[] for _ in range(nfam)]
+    for I in alf_cell_order(lattice, L1, L2):  # the cells in Latt%List order
+        n1, n2 = I % L1, I // L1
+        for b, f in enumerate(fam_of(n1, n2)):
+            oi, oj, d1, d2 = bonds[b]
+            J = _cell(n1 + d1, n2 + d2, L1, L2)
+            fams[f].append((int(new_of[I * norb + oi]), int(new_of[J * norb + oj]),
+                            np.array([[-chem / mult[oi], -t], [-t, -chem / mult[oj]]])))
+    P, mats, invs, fam = [], [], [], []
+    for ops in fams:
+        fam.append(len(P))
+        for i, j, O in ops:
+            m, mi = exp_hopping(O, dtau)
+            P.append((i, j))
+            mats.append(m)
+            invs.append(mi)
+    fam.append(len(P))
+    return {"P": np.array(P, np.int32), "mat": np.array(mats), "inv": np.array(invs), "fam": fam}
+
+
+def checkerboard_product(cb: dict, N: int, inverse: bool = False) -> np.ndarray:
+    """Dense B_T = E_1 E_2 ... E_Ncheck (or its inverse E_Ncheck^-1 ... E_1^-1) of the bond
+    operators, the matrix Hop_mod_mmthr applies."""
+    B = np.eye(N)
+    seq = range(len(cb["P"])) if not inverse else range(len(cb["P"]) - 1, -1, -1)
+    for nc in seq:
+        i, j = cb["P"][nc]
+        E = np.eye(N)
+        E[np.ix_([i, j], [i, j])] = cb["inv" if inverse else "mat"][nc]
+        B = B @ E
+    return B
+
+
 # ----------------------------------------------------------------------------
 # Model container
 # ----------------------------------------------------------------------------
@@ -284,6 +346,7 @@ class Model:
     expTinv: np.ndarray
     vertices: List[List[Vertex]]
     params: dict = field(default_factory=dict)
+    checkerboard: Optional[dict] = None  # checkerboard_ops of each flavour's Op_T, or None (dense)
 
     @property
     def n_op(self) -> int:
@@ -333,6 +396,13 @@ class Model:
                     out["op_Mexp"][k, s, :nn, :nn] = v.M_exp[s].T
         out["expT"] = np.ascontiguousarray(np.stack([m.T for m in self.expT]))   # col-major per flavour
         out["expTinv"] = np.ascontiguousarray(np.stack([m.T for m in self.expTinv]))
+        if self.checkerboard is not None:  # [F][Ncheck][2] sites, [F][Ncheck][4] column-major 2 x 2
+            out["cb_P"] = np.ascontiguousarray(np.stack([c["P"] for c in self.checkerboard]), dtype=np.int32)
+            out["cb_mat"] = np.ascontiguousarray(np.stack([np.transpose(c["mat"], (0, 2, 1)).reshape(-1, 4)
+                                                           for c in self.checkerboard]))
+            out["cb_inv"] = np.ascontiguousarray(np.stack([np.transpose(c["inv"], (0, 2, 1)).reshape(-1, 4)
+                                                           for c in self.checkerboard]))
+            out["cb_fam"] = np.ascontiguousarray(self.checkerboard[0]["fam"], dtype=np.int32)
         return out
 
 
@@ -346,7 +416,8 @@ def _mz_pair(site: int, dtau: float, U: float):
 
 def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U: float = 4.0,
             chem: float = 0.0, beta: float = 4.0, dtau: float = 0.1, nwrap: int = 10,
-            n_sun_input: int = 2, tperp: float = 0.0, site_order: str = "natural") -> Model:
+            n_sun_input: int = 2, tperp: float = 0.0, site_order: str = "natural",
+            checkerboard: bool = False) -> Model:
     """Mz Hubbard model with dense hopping, as ``Ham_Set`` builds it.
 
     ``N_FL = 2`` and ``N_SUN`` is halved (Hamiltonian_Hubbard_smod.F90:264-266);
@@ -357,7 +428,12 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
     n_sun = n_sun_input // 2
     O = hopping_matrix(lattice, L1, L2, t=t, chem=chem, tperp=tperp, site_order=site_order)
     N = O.shape[0]
-    mat, inv = exp_hopping(O, dtau)
+    cb = None
+    if checkerboard:  # Checkerboard = .T.: the product of the bond exponentials replaces exp(-dtau T)
+        cb = checkerboard_ops(lattice, L1, L2, dtau, t=t, chem=chem, site_order=site_order)
+        mat, inv = checkerboard_product(cb, N), checkerboard_product(cb, N, inverse=True)
+    else:
+        mat, inv = exp_hopping(O, dtau)
     up, do = [], []
     u_eff = U / n_sun
     for i in range(N):
@@ -368,7 +444,8 @@ def hubbard(lattice: str = "square", L1: int = 4, L2: int = 4, t: float = 1.0, U
                  ltrot=ltrot, nwrap=nwrap, dtau=dtau, beta=beta, expT=[mat, mat.copy()],
                  expTinv=[inv, inv.copy()], vertices=[up, do],
                  params=dict(lattice=lattice, L1=L1, L2=L2, t=t, U=U, chem=chem, tperp=tperp,
-                             site_order=site_order))
+                             site_order=site_order, checkerboard=checkerboard),
+                 checkerboard=None if cb is None else [cb, cb])
 
 
 def kondo(L1: int = 12, L2: int = 12, t: float = 1.0, JK: float = 1.5, Uf: float = 2.0,

@@ -73,6 +73,11 @@ class Chains:
         self._keep = []
         pk = model.pack()
         _lib.check(self.L.alfgpu_upload_hopping(self.h, _p(pk["expT"]), _p(pk["expTinv"])), "alfgpu_upload_hopping")
+        if "cb_P" in pk:  # checkerboard Op_T: the bond operators replace the dense products
+            self._keep.append(pk)
+            _lib.check(self.L.alfgpu_upload_checkerboard(self.h, pk["cb_P"].shape[1], len(pk["cb_fam"]) - 1,
+                                                         _p(pk["cb_fam"]), _p(pk["cb_P"]), _p(pk["cb_mat"]),
+                                                         _p(pk["cb_inv"])), "alfgpu_upload_checkerboard")
         if models is None:
             self._upload_vertices(-1, pk)
         else:
@@ -206,6 +211,59 @@ class Chains:
         if reset:
             self.reset_scalar_obs()
         return b
+
+    # --- device-side lattice-resolved observables ------------------------------------------------
+    def set_lattice_obs(self, latt=None):
+        """Accumulate the predefined lattice observables (lattice_obs.EQ_NAMES / EQ_NAMES_SUN, as
+        lattice_obs.EqualTimeObs and TimeDisplacedObs form them on the host) on the device at
+        every ham%Obser point and, with TAU_M, every ham%ObserT slice.  latt: a
+        lattice_obs.Lattice of the model's lattice and site order; None switches it off."""
+        if latt is None:
+            _lib.check(self.L.alfgpu_set_lattice_obs(self.h, 0, 0, None, None), "alfgpu_set_lattice_obs")
+            return
+        site_of = np.zeros((latt.N, latt.norb), np.int32)
+        site_of[latt.site_cell, latt.site_orb] = np.arange(latt.N * latt.norb)
+        jof = np.zeros((latt.N, latt.N), np.int32)
+        I = np.repeat(np.arange(latt.N), latt.N)
+        J = np.tile(np.arange(latt.N), latt.N)
+        jof[I, latt.imj[I, J]] = J
+        self._latt = latt
+        self._keep.append((site_of, jof))
+        _lib.check(self.L.alfgpu_set_lattice_obs(self.h, latt.N, latt.norb, _p(site_of), _p(jof)),
+                   "alfgpu_set_lattice_obs")
+
+    def reset_lattice_obs(self):
+        _lib.check(self.L.alfgpu_reset_lattice_obs(self.h), "alfgpu_reset_lattice_obs")
+
+    def lattice_obs(self, chain: int = 0, kind: int = 0) -> dict:
+        """Accumulators of one chain (kind 0: equal time, 1: time displaced): per observable
+        Obs_Latt [R][nt][no][no] and Obs_Latt0 [no] (complex), with the count and sign sum."""
+        from .lattice_obs import names_for
+        latt = self._latt
+        names = names_for(self.F)
+        nt = 1 if kind == 0 else self.Lt + 1
+        a = np.zeros((len(names), latt.N, nt, latt.norb, latt.norb), np.complex128)
+        a0 = np.zeros((len(names), latt.norb), np.complex128)
+        cs = np.zeros(2, np.float64)
+        _lib.check(self.L.alfgpu_get_lattice_obs(self.h, chain, kind, _p(a), _p(a0), _p(cs)),
+                   "alfgpu_get_lattice_obs")
+        return {"obs": {k: a[i] for i, k in enumerate(names)}, "obs0": {k: a0[i] for i, k in enumerate(names)},
+                "count": int(cs[0]), "sign": float(cs[1])}
+
+    def lattice_bin(self, chain: int = 0, kind: int = 0, reset: bool = False) -> dict:
+        """Print_bin_Latt's normalisation of one chain's accumulators, as EqualTimeObs.bin()
+        (kind 0) or TimeDisplacedObs.bin() (kind 1) returns it: Obs_Latt / N,
+        Obs_Latt0 / (N Ns Ntau), Ave_sign / N."""
+        d = self.lattice_obs(chain, kind)
+        n, ns = d["count"], self._latt.N
+        if n == 0:
+            raise ValueError("an empty bin")
+        ntau = 1 if kind == 0 else self.Lt + 1
+        out = {k: {"latt": d["obs"][k] / n, "latt0": d["obs0"][k] / (n * ns * ntau), "sign": d["sign"] / n}
+               for k in d["obs"]}
+        if reset:
+            self.reset_lattice_obs()
+        return out
 
     # --- checkpoint / resume (the reference's confout files) ------------------------------------
     def checkpoint(self, path: str):

@@ -186,6 +186,17 @@ const char* alfgpu_error_string(int code);
  * (Prog/OpTTypes_mod.F90:92-133), n_fl x Ndim x Ndim column-major, shared by all
  * chains.  Vertex tables are per chain (chain = -1 uploads the same tables to all). */
 int alfgpu_upload_hopping(alfgpu_t* h, const double* expT, const double* expTinv);
+/* Checkerboard hopping (Checkerboard = .T.; Op_T built by Predefined_Hop_mod.F90:1773-1839 as
+ * one two-site operator per bond): ncheck bond operators per flavour in Op_T order, P
+ * [n_fl][ncheck][2] 0-based sites, mat = exp(g O) and inv = exp(-g O) [n_fl][ncheck][4]
+ * real column-major 2 x 2, grouped into nfam families of disjoint bonds (operators
+ * fam[q] .. fam[q+1]-1, fam[0] = 0, fam[nfam] = ncheck).  Every hopping product of the sweep,
+ * the UDV propagation and TAU_M then applies the bonds in the order of the Hop_mod routine it
+ * replaces (Hop_mod.F90:143-250: B_T = E_1 ... E_ncheck), one launch per family, in place of
+ * the dense exp(-dtau T) products of alfgpu_upload_hopping; ncheck = 0 returns to those.  Not
+ * for models with two-site vertices (ALFGPU_ERROR_UNSUPPORTED). */
+int alfgpu_upload_checkerboard(alfgpu_t* h, int32_t ncheck, int32_t nfam, const int32_t* fam, const int32_t* P,
+                               const double* mat, const double* inv);
 int alfgpu_upload_vertices(alfgpu_t* h, int32_t chain, const alfgpu_vertices* v);
 
 /* Fields nsigma%f(n, nt): int8 values in {+-1, +-2}, Ltrot x n_op (n fastest). */
@@ -316,6 +327,24 @@ int alfgpu_decompose_noalloc(int32_t ndim, char side, double* U, double* D, doub
 int alfgpu_set_scalar_obs(alfgpu_t* h, const double* H, const double* U);
 int alfgpu_get_scalar_obs(alfgpu_t* h, int32_t chain, double* sums);
 int alfgpu_reset_scalar_obs(alfgpu_t* h);
+
+/* Device-side lattice-resolved observables: the predefined measurements of ham%Obser and
+ * ham%ObserT (Prog/Predefined_Obs_mod.F90:137-600: N_FL = 2 Green, SpinZ, SpinXY, SpinT, Den;
+ * N_FL = 1 Green, SpinZ (SpinSUN), Den), accumulated per chain on the device at every
+ * measurement point of the sweep (equal time) and every slice of TAU_M (time displaced), so a
+ * measuring sweep copies no Green function to the host.  The lattice: site_of[cell * norb + o]
+ * = the site of orbital o of cell `cell` (ncell * norb = Ndim), jof[I * ncell + R] = the cell J
+ * with imj(I, J) = R (Make_lattice's imj, Libraries/Modules/lattices_v3_mod.F90:88-336).
+ * site_of = jof = NULL switches it off.  alfgpu_get_lattice_obs(kind 0: equal time, 1: time
+ * displaced) returns per observable (in the order above) Obs_Latt(R, nt, no_I, no_J) as
+ * [name][R][nt][no_I][no_J] complex (nt: 1 slice, or Ltrot + 1 for kind 1), Obs_Latt0 as
+ * [name][no] complex, and (measurements, sum of ZS); each G contributes Phase / Re(Phase)
+ * sign(Re(Phase)) times its measurement; a bin is the accumulators between two resets
+ * (Print_bin_Latt divides by the count, Prog/observables_mod.F90:355-500).  No counterpart in
+ * the reference's interface (the Fortran side measures on the host). */
+int alfgpu_set_lattice_obs(alfgpu_t* h, int32_t ncell, int32_t norb, const int32_t* site_of, const int32_t* jof);
+int alfgpu_get_lattice_obs(alfgpu_t* h, int32_t chain, int32_t kind, double* latt, double* latt0, double* count_sign);
+int alfgpu_reset_lattice_obs(alfgpu_t* h);
 
 /* The CUDA call behind the last ALFGPU_ERROR_CUDA of this handle ("file:line: CUDA error
  * string"); the pointer stays valid until the next call on the handle. */

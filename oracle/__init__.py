@@ -125,6 +125,11 @@ class Oracle:
                                 _ptr(pk["op_Mexp"]))
         if rc:
             raise RuntimeError(f"oracle_set_model rc={rc}")
+        if "cb_P" in pk:  # checkerboard Op_T: the bond operators replace the dense exponentials
+            ncheck = pk["cb_P"].shape[1]
+            rc = L.oracle_set_checkerboard(self.h, ncheck, _ptr(pk["cb_P"]), _ptr(pk["cb_mat"]), _ptr(pk["cb_inv"]))
+            if rc:
+                raise RuntimeError(f"oracle_set_checkerboard rc={rc}")
         self._rec = None
 
     def __del__(self):

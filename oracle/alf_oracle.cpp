@@ -155,6 +155,11 @@ struct Oracle {
   SweepCursor cur;
   vector<int> stab_nt;
   vector<double> expT, expTinv;  // F x N x N
+  // checkerboard Op_T (Predefined_Hop_mod.F90:1773-1839): Ncheck two-site bond operators per
+  // flavour in Op_T order, P [F][Ncheck][2], mat = exp(g O) and inv = exp(-g O) [F][Ncheck][4]
+  int ncheck = 0;
+  vector<int> cb_P;
+  vector<double> cb_mat, cb_inv;
   // vertices, k = nf*M + n
   vector<int> op_n, op_nz, op_diag, op_type, op_P;
   vector<zc> op_g, op_alpha, op_U, op_Eexp, op_Mexp;
@@ -264,12 +269,47 @@ static void rmult_real(Oracle& o, const double* A, zc* X) {  // X = X * A
 }
 static const double* mat(Oracle& o, int nf) { return o.expT.data() + (size_t)nf * o.N * o.N; }
 static const double* inv(Oracle& o, int nf) { return o.expTinv.data() + (size_t)nf * o.N * o.N; }
-// Hop_mod.F90:143-250
-static void hop_mmthr(Oracle& o, zc* X, int nf) { lmult_real(o, mat(o, nf), X); }
-static void hop_mmthr_m1(Oracle& o, zc* X, int nf) { lmult_real(o, inv(o, nf), X); }
-static void hop_mmthl(Oracle& o, zc* X, int nf) { rmult_real(o, mat(o, nf), X); }
-static void hop_mmthl_m1(Oracle& o, zc* X, int nf) { rmult_real(o, inv(o, nf), X); }
-static void hop_mmthlc(Oracle& o, zc* X, int nf) { lmult_real(o, mat(o, nf), X); }
+// One checkerboard bond operator (2 x 2, column-major E) on rows (X <- E X) or columns (X <- X E)
+// P1, P2 of X: the two-site RealExpOpT lmult / rmult (OpTTypes_mod.F90:135-304).
+static void bond_l(Oracle& o, zc* X, int nf, int nc, const vector<double>& E) {
+  const int N = o.N, a = o.cb_P[2 * ((size_t)nf * o.ncheck + nc)], b = o.cb_P[2 * ((size_t)nf * o.ncheck + nc) + 1];
+  const double* e = E.data() + 4 * ((size_t)nf * o.ncheck + nc);
+  for (int j = 0; j < N; ++j) {
+    const zc xa = X[a + (size_t)j * N], xb = X[b + (size_t)j * N];
+    X[a + (size_t)j * N] = e[0] * xa + e[2] * xb;
+    X[b + (size_t)j * N] = e[1] * xa + e[3] * xb;
+  }
+}
+static void bond_r(Oracle& o, zc* X, int nf, int nc, const vector<double>& E) {
+  const int N = o.N, a = o.cb_P[2 * ((size_t)nf * o.ncheck + nc)], b = o.cb_P[2 * ((size_t)nf * o.ncheck + nc) + 1];
+  const double* e = E.data() + 4 * ((size_t)nf * o.ncheck + nc);
+  for (int i = 0; i < N; ++i) {
+    const zc xa = X[i + (size_t)a * N], xb = X[i + (size_t)b * N];
+    X[i + (size_t)a * N] = xa * e[0] + xb * e[1];
+    X[i + (size_t)b * N] = xa * e[2] + xb * e[3];
+  }
+}
+// Hop_mod.F90:143-250 (dense: one Op_T; checkerboard: the bond operators in the order of each routine)
+static void hop_mmthr(Oracle& o, zc* X, int nf) {  // B_T X: nc = Ncheck .. 1, lmult
+  if (!o.ncheck) return lmult_real(o, mat(o, nf), X);
+  for (int nc = o.ncheck - 1; nc >= 0; --nc) bond_l(o, X, nf, nc, o.cb_mat);
+}
+static void hop_mmthr_m1(Oracle& o, zc* X, int nf) {  // B_T^-1 X: nc = 1 .. Ncheck, lmultinv
+  if (!o.ncheck) return lmult_real(o, inv(o, nf), X);
+  for (int nc = 0; nc < o.ncheck; ++nc) bond_l(o, X, nf, nc, o.cb_inv);
+}
+static void hop_mmthl(Oracle& o, zc* X, int nf) {  // X B_T: nc = 1 .. Ncheck, rmult
+  if (!o.ncheck) return rmult_real(o, mat(o, nf), X);
+  for (int nc = 0; nc < o.ncheck; ++nc) bond_r(o, X, nf, nc, o.cb_mat);
+}
+static void hop_mmthl_m1(Oracle& o, zc* X, int nf) {  // X B_T^-1: nc = Ncheck .. 1, rmultinv
+  if (!o.ncheck) return rmult_real(o, inv(o, nf), X);
+  for (int nc = o.ncheck - 1; nc >= 0; --nc) bond_r(o, X, nf, nc, o.cb_inv);
+}
+static void hop_mmthlc(Oracle& o, zc* X, int nf) {  // nc = 1 .. Ncheck, lmult (B_T^T X for symmetric bonds)
+  if (!o.ncheck) return lmult_real(o, mat(o, nf), X);
+  for (int nc = 0; nc < o.ncheck; ++nc) bond_l(o, X, nf, nc, o.cb_mat);
+}
 
 // ---------------------------------------------------------------------------
 // Operator_mod small x large products (ZSLGEMM semantics, N_op <= 2)
@@ -906,6 +946,19 @@ int oracle_set_model(void* h, const double* expT, const double* expTinv, const i
   for (size_t k = 0; k < K; ++k)
     for (int a = 0; a < o.op_n[k]; ++a)
       if (o.op_P[2 * k + a] < 0 || o.op_P[2 * k + a] >= o.N) return 6;  // ERROR_HAMILTONIAN
+  return 0;
+}
+
+// Checkerboard hopping: ncheck bond operators per flavour (P 0-based, [F][ncheck][2]; mat, inv
+// [F][ncheck][4] column-major 2 x 2), replacing the dense exponentials; ncheck = 0 restores them.
+int oracle_set_checkerboard(void* h, int ncheck, const int* P, const double* mat, const double* inv) {
+  Oracle& o = *(Oracle*)h;
+  o.ncheck = ncheck;
+  o.cb_P.assign(P, P + 2 * (size_t)o.F * ncheck);
+  o.cb_mat.assign(mat, mat + 4 * (size_t)o.F * ncheck);
+  o.cb_inv.assign(inv, inv + 4 * (size_t)o.F * ncheck);
+  for (int v : o.cb_P)
+    if (v < 0 || v >= o.N) return 6;  // ERROR_HAMILTONIAN
   return 0;
 }
 

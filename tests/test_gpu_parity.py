@@ -82,6 +82,37 @@ def test_cgr_matches_naive_15cgr_and_oracle():
         assert abs(ph - pho) < 1e-10
 
 
+def test_decompose_and_cgr_with_rows_beyond_shared_memory():
+    # N_dim = 480: the exact pivoted QR keeps each CTA's 30 rows x 480 columns in a global
+    # workspace (they do not fit a 16-CTA cluster's shared memory); same results as the oracle
+    rs = np.random.default_rng(480)
+    N = 480
+    for side in ("r", "l"):
+        U, D, V = np.eye(N, dtype=complex), np.ones(N, complex), np.eye(N, dtype=complex)
+        Uo, Do, Vo = U.copy(), D.copy(), V.copy()
+        P = np.eye(N, dtype=complex)
+        for _ in range(2):
+            X = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+            U, Uo, P = X @ U, X @ Uo, X @ P
+            U, D, V = gpu_decompose(side, U, D, V)
+            Uo, Do, Vo = oracle.decompose(side, Uo, Do, Vo)
+            R = U @ np.diag(D) @ (V if side == "r" else V.conj().T)
+            assert _relmax(R, P) < 1e-10
+            assert np.max(np.abs(U.conj().T @ U - np.eye(N))) < 1e-12
+            assert _relmax(D, Do) < 1e-10
+    q = lambda: np.linalg.qr(rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N)))[0]
+    UR, UL = q(), q()
+    VR = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+    VL = rs.standard_normal((N, N)) + 1j * rs.standard_normal((N, N))
+    DR = np.exp(np.linspace(8, -8, N)).astype(complex)
+    DL = np.exp(np.linspace(6, -6, N)).astype(complex)
+    for nvar in (1, 2):
+        G, ph = gpu_cgr(nvar, UR, DR, VR, UL, DL, VL)
+        Go, pho = oracle.cgr(nvar, UR, DR, VR, UL, DL, VL)
+        assert _relmax(G, Go) < 1e-10
+        assert abs(ph - pho) < 1e-10
+
+
 def _variant_ratios(m, f0, seed, sweeps, chain):
     oracle.set_variant(1)
     try:
@@ -360,3 +391,11 @@ def test_checkpoint_resume_continues_on_the_same_draws(tmp_path):
     for c in range(2):
         np.testing.assert_array_equal(h.fields(c), g.fields(c))
         assert _relmax(h.green(c), g.green(c)) < 1e-8
+
+
+@pytest.mark.parametrize("lattice,L1,L2", [("square", 4, 4), ("honeycomb", 3, 3)])
+def test_checkerboard_hopping_parity(lattice, L1, L2):
+    # Checkerboard = .T.: the hopping products are the bond operators of each family, applied in
+    # the order of each Hop_mod routine (the oracle restates that order bond by bond)
+    m = mdl.hubbard(lattice, L1, L2, U=4.0, chem=0.2, beta=1.0, dtau=0.1, nwrap=5, checkerboard=True)
+    _run_pair(m, seed=12, sweeps=2)

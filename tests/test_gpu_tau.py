@@ -60,3 +60,26 @@ def test_equal_time_measurements_match_oracle():
     for (c, nt, Gg, phg), (nt_o, Go, pho) in zip(eq_g, eq_o):
         assert np.max(np.abs(Gg - Go)) <= band, nt
         assert abs(phg - pho) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tau_m_with_checkerboard_hopping(precision):
+    # TAU_M's PROPR / PROPRM1 with the bond operators (both forms: the bonds are O(N^2) passes)
+    m = mdl.hubbard("honeycomb", 2, 2, U=5.0, beta=0.5, dtau=0.05, nwrap=5, checkerboard=True)
+    f0 = rng.initial_fields(3, 0, m.n_op, m.ltrot)
+    u = rng.sweep_uniforms(3, 0, m.n_op, m.ltrot, 0)
+    o = oracle.Oracle(m, ltau=1)
+    o.set_fields(f0)
+    o.init_state()
+    _, tau_o = o.collect_measurements()
+    o.sweep(u)
+    g = Chains(m, ltau=1, precision=precision)
+    g.set_fields(0, f0)
+    g.init_state()
+    _, tau_g = g.sweep(u[None, :], measure=True)
+    np.testing.assert_array_equal(g.fields(0), o.fields())
+    band = max(1e-10, 10.0 * o.stats().xmax_tau) if precision == "fp64" else 1e-5
+    assert len(tau_g) == len(tau_o) == m.ltrot + 1
+    for (c, nt, qg, _), (nt_o, qo, _) in zip(tau_g, tau_o):
+        for k in range(4):
+            assert np.max(np.abs(qg[k] - qo[k])) <= band, (nt, k)

@@ -68,10 +68,17 @@ def _small_hubbard(lattice="square", L1=4, L2=2, beta=1.0, nwrap=5, U=4.0):
     return mdl.hubbard(lattice, L1, L2, U=U, beta=beta, dtau=0.1, nwrap=nwrap)
 
 
-@pytest.mark.parametrize("kind", ["hubbard", "kondo"])
+@pytest.mark.parametrize("kind", ["hubbard", "kondo", "checkerboard", "checkerboard-honeycomb"])
 def test_sweep_identities(kind):
+    # checkerboard: the oracle applies the bond operators one by one in the order of each
+    # Hop_mod routine; the dense formulas use their product B_T = E_1 ... E_Ncheck (and B_T^T
+    # where the left UDV state propagates), so a wrong order or a missing transpose shows
     if kind == "hubbard":
         m = _small_hubbard()
+    elif kind == "checkerboard":
+        m = mdl.hubbard("square", 4, 4, U=4.0, chem=0.2, beta=1.0, dtau=0.1, nwrap=5, checkerboard=True)
+    elif kind == "checkerboard-honeycomb":
+        m = mdl.hubbard("honeycomb", 2, 2, U=4.0, beta=1.0, dtau=0.1, nwrap=5, checkerboard=True)
     else:
         m = mdl.kondo(2, 2, JK=1.5, Uf=2.0, beta=1.0, dtau=0.1, nwrap=5)
     seed, chain = 11, 0
@@ -139,3 +146,25 @@ def test_oracle_tau_m_propagation_matches_cgr2_2():
     np.testing.assert_array_equal(gt0, g00)
     np.testing.assert_array_equal(gtt, g00)
     np.testing.assert_allclose(g0t, g00 - np.eye(m.ndim)[None], atol=1e-15)
+
+
+def test_checkerboard_families_follow_the_reference():
+    # test_checkerboard_decomposition (Predefined_Hop_mod.F90:171-246): the bonds of a family are
+    # disjoint, and together the families hold every nearest-neighbour bond of the dense Op_T once
+    for lat, L1, L2, nfam in (("square", 4, 4, 4), ("square", 6, 4, 4), ("honeycomb", 3, 3, 3)):
+        cb = mdl.checkerboard_ops(lat, L1, L2, 0.1)
+        assert len(cb["fam"]) == nfam + 1
+        for f in range(nfam):
+            sites = cb["P"][cb["fam"][f]:cb["fam"][f + 1]].ravel()
+            assert len(set(sites.tolist())) == len(sites)
+        O = mdl.hopping_matrix(lat, L1, L2)
+        dense = {tuple(sorted((i, j))) for i, j in zip(*np.nonzero(np.triu(O, 1)))}
+        bonds = [tuple(sorted(p)) for p in cb["P"].tolist()]
+        assert sorted(bonds) == sorted(dense)
+        # the product of the bond exponentials is exp(-dtau T) up to the Trotter error O(dtau^2)
+        for dt in (0.1, 0.05):
+            c = mdl.checkerboard_ops(lat, L1, L2, dt, chem=0.3)
+            B = mdl.checkerboard_product(c, O.shape[0])
+            w, Z = np.linalg.eigh(mdl.hopping_matrix(lat, L1, L2, chem=0.3))
+            ex = (Z * np.exp(-dt * w)[None, :]) @ Z.conj().T
+            assert np.max(np.abs(B - ex)) < 1.2 * dt ** 2
