@@ -307,8 +307,8 @@ class Chains:
     def adapt_nwrap(self, bound: float = 1e-5, sweeps: int = 1):
         """Shorten Nwrap while the drift is too large: run `sweeps` device-draw sweeps, and if
         any chain's Precision Green (max |G_wrapped - G_fresh|) exceeds `bound` (or the sweep
-        stops with ALF's ERROR_UNSTABLE_MATRIX), halve Nwrap, rebuild G and the UDV stack from
-        the current fields and try again.  The sweeps advance the chains (use them as
+        stops with ALF's ERROR_UNSTABLE_MATRIX or a NaN in G), halve Nwrap, rebuild G and the
+        UDV stack from the current fields and try again.  The sweeps advance the chains (use them as
         thermalisation).  Returns (nwrap, worst Precision Green)."""
         while True:
             self.reset_stats()
@@ -317,7 +317,9 @@ class Chains:
                     self.sweep(None)
                 worst = max(self.stats(c).xmaxG for c in range(self.C))
             except _lib.AlfGpuError as e:
-                if e.code != 3:  # ERROR_UNSTABLE_MATRIX: ALF's abort at Precision Green > 10
+                # ERROR_UNSTABLE_MATRIX (ALF's abort at Precision Green > 10) or a NaN in G (the
+                # same instability past the point where the comparison is defined)
+                if e.code not in (3, 103):
                     raise
                 worst = float("inf")
             nw = self.nwrap()

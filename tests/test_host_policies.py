@@ -16,8 +16,8 @@ class FakeLib:
     gives each sweep's Precision Green; unstable(nwrap) makes the sweep stop with ALF's
     ERROR_UNSTABLE_MATRIX (3)."""
 
-    def __init__(self, drift=lambda nw: 1e-7, unstable=lambda nw: False, sweep_rc=0):
-        self.drift, self.unstable, self.sweep_rc = drift, unstable, sweep_rc
+    def __init__(self, drift=lambda nw: 1e-7, unstable=lambda nw: False, sweep_rc=0, unstable_rc=3):
+        self.drift, self.unstable, self.sweep_rc, self.unstable_rc = drift, unstable, sweep_rc, unstable_rc
         self.log = []
 
     def alfgpu_create(self, hp, dp):
@@ -83,7 +83,7 @@ class FakeLib:
         self.log.append(("sweep", self.nw))
         if self.sweep_rc:
             return self.sweep_rc
-        return 3 if self.unstable(self.nw) else 0
+        return self.unstable_rc if self.unstable(self.nw) else 0
 
     def alfgpu_last_error(self, h):
         return b"cudaLaunchKernelEx at alfgpu.cu:1"
@@ -120,6 +120,15 @@ def test_adapt_nwrap_halves_until_the_drift_bound_holds(fake):
     f.log.clear()
     nw, worst = ch.adapt_nwrap(bound=1e-7)  # 5 -> 2 -> 1 (Nwrap 1 ends the search)
     assert nw == 1 and [e for e in f.log if e[0] == "set_nwrap"] == [("set_nwrap", 2), ("set_nwrap", 1)]
+    ch.close()
+
+
+def test_adapt_nwrap_treats_a_nan_in_g_as_instability(fake):
+    # ERROR_NAN (103) is the same instability past the point where Precision Green is defined
+    f = fake(drift=lambda nw: 1e-7 * nw ** 3, unstable=lambda nw: nw >= 10, unstable_rc=103)
+    ch = _chains()
+    nw, worst = ch.adapt_nwrap(bound=2e-5)
+    assert nw == 5 and abs(worst - 1.25e-5) < 1e-12
     ch.close()
 
 
