@@ -1553,7 +1553,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
     p.kdyn = h->m + h->C;  // per-(chain, flavour) rank, written by k_update
-    if (h->mixed && h->oz && !h->oz_narrow) {
+    if (h->mixed && h->oz && !h->oz_narrow && !(h->d.reserved[0] & ALFGPU_FLAG_DF_FLUSH)) {
       // G -= X Y as one real product: [Re X | Im X] times the K-doubled complex rows of Y
       const int Kf = 2 * UPD_KMAX;
       RET(oz_slice(h, h->X, OZ_CKA, 1, N, p.sA, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,

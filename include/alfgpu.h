@@ -113,6 +113,10 @@ enum { ALFGPU_FLAG_TENSOR_WIDE = 512 };
  * the default size when the full-size clusters of a batched launch would put more than two
  * CTAs on every SM; these flags force the half-size or the full-size cluster. */
 enum { ALFGPU_FLAG_QR_HALF_CLUSTER = 1024, ALFGPU_FLAG_QR_FULL_CLUSTER = 2048 };
+/* Mixed form, grids of several chains: the delayed-update flush G -= X Y on the double-float
+ * GEMM, whose loop stops at the block's accepted count, instead of the tensor-core GEMM
+ * (K padded to 64, digit-sliced). */
+enum { ALFGPU_FLAG_DF_FLUSH = 4096 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the

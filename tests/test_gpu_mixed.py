@@ -1,7 +1,9 @@
-"""Mixed-precision form (G wraps and delayed-update flushes as digit-sliced BF16
-tensor-core products, per-visit Metropolis arithmetic in double-float on the FP32
-pipes; complex128 storage; FP64 UDV propagation, pivoted QR and CGR) against the FP64
-CPU oracle on the same fields and draws.
+"""Mixed-precision form against the FP64 CPU oracle on the same fields and draws.  The form:
+complex128 storage; G wraps, UDV propagation and the stabilisation's complex products as
+digit-sliced BF16 tensor-core products (FP64-accurate); on grids of several chains the
+delayed-update flush and the explicit Q on the tensor cores too; the per-visit Metropolis
+arithmetic in double-float with the ratio and phase accumulated in FP64; pivoted QRs,
+triangular solves and phases in FP64.
 
 Acceptance bound: max |G_mixed - G_fp64| <= 1e-5 at every stabilisation point
 (the freshly computed CGR result) while the accept/reject sequences agree, and
@@ -12,7 +14,7 @@ import pytest
 
 import oracle
 from alf_gb300 import model as mdl, rng
-from alf_gb300.sweep import Chains
+from alf_gb300.sweep import FLAG_DF_FLUSH, FLAG_TENSOR_WIDE, Chains
 from parity_util import compare_record
 
 pytestmark = pytest.mark.gpu
@@ -139,12 +141,15 @@ def test_mixed_tau_m_quartets_vs_fp64_oracle():
     assert compared == 1
 
 
-def test_mixed_batched_chains_with_own_couplings_vs_oracle():
+@pytest.mark.parametrize("flags", [0, FLAG_TENSOR_WIDE, FLAG_TENSOR_WIDE | FLAG_DF_FLUSH],
+                         ids=["default", "wide", "wide-df-flush"])
+def test_mixed_batched_chains_with_own_couplings_vs_oracle(flags):
     # one handle, two chains with different U (per-chain vertex tables): each within 1e-5 of
-    # its own FP64 oracle run
+    # its own FP64 oracle run; "wide": the grid takes the batched-grid choices (flush on the
+    # tensor cores, compact-WY explicit Q); "wide-df-flush": the same with the double-float flush
     ms = [mdl.hubbard("square", 6, 6, U=U, beta=2.0, dtau=0.1, nwrap=10) for U in (3.0, 7.0)]
     seeds = (12, 13)
-    g = Chains(ms[0], n_chains=2, precision="mixed", models=ms)
+    g = Chains(ms[0], n_chains=2, precision="mixed", models=ms, flags=flags)
     for c in range(2):
         g.set_fields(c, rng.initial_fields(seeds[c], c, ms[c].n_op, ms[c].ltrot))
     g.init_state()
