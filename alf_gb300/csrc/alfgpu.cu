@@ -328,13 +328,14 @@ static int qrr_clusters(int N, int CL, bool grows = false) {
 
 // Cluster size and row storage of the exact pivoted QR of B matrices N x N: the largest
 // cluster (up to CL) whose rows fit shared memory (mode 1) or, failing that, with the rows in a
-// global workspace (mode 2); a launch whose full-size clusters would put more than two CTAs on
-// every SM takes half-size clusters (unless forced by the flags).  Mode 0: neither fits.
+// global workspace (mode 2; ALFGPU_FLAG_QR_GLOBAL_ROWS: mode 2 only); a launch whose full-size
+// clusters would put more than two CTAs on every SM takes half-size clusters (unless forced by
+// the flags).  Mode 0: neither fits.
 static int qrr_plan(int N, int CL, int B, int flags, int dev, int* CLout) {
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaGetLastError();
-  for (int mode = 1; mode <= 2; ++mode) {
+  for (int mode = (flags & ALFGPU_FLAG_QR_GLOBAL_ROWS) ? 2 : 1; mode <= 2; ++mode) {
     const bool grows = mode == 2;
     if (qrr_clusters(N, CL, grows) <= 0) continue;
     *CLout = CL;

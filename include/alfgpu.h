@@ -117,6 +117,10 @@ enum { ALFGPU_FLAG_QR_HALF_CLUSTER = 1024, ALFGPU_FLAG_QR_FULL_CLUSTER = 2048 };
  * GEMM, whose loop stops at the block's accepted count, instead of the tensor-core GEMM
  * (K padded to 64, digit-sliced). */
 enum { ALFGPU_FLAG_DF_FLUSH = 4096 };
+/* The exact pivoted QR keeps each CTA's rows in a global (L2-resident) workspace even where
+ * they fit in shared memory: a CTA then needs little shared memory, so several clusters share
+ * an SM and a batched launch runs in fewer waves. */
+enum { ALFGPU_FLAG_QR_GLOBAL_ROWS = 8192 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the
