@@ -49,7 +49,10 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_DMMA_TFLOPS = 1.048
 # DRAM bytes (read + write) of one G-wrap GEMM launch (N_dim = 256, two flavours, one chain),
 # from an ncu capture of the 16x16 workload (dram__bytes_read.sum + dram__bytes_write.sum)
-HOP_TRAFFIC_BYTES = 3.30e6
+HOP_TRAFFIC_BYTES = 3.28e6
+# the same for the mixed form's G-wrap k_oz_gemm launch of the 16-chain handle (78.1 MB read,
+# 8.3 MB written: the digit slices of G and the output), per chain
+OZ_HOP_TRAFFIC_BYTES_PER_CHAIN = 86.5e6 / 16
 # default chains per GPU of each workload (the batched forms of the benchmark configurations)
 DEFAULT_CHAINS = {"hubbard4x4": 1, "hubbard16x16": 16, "honeycomb12x12": 1, "kondo12x12": 32, "batch128": 128}
 L2_NOTE = "GPU arm: L2 flushed between timed steps (256 MB write); host arm: not applicable"
@@ -197,7 +200,8 @@ def roofline(precision: str, chains: int, m, prof):
         peak, src = measured_bf16_peak()
         _, _, pairs = digit_pairs(m.ndim)
         roof = {"bound": "tensor", "kernel": "k_oz_slice + k_oz_gemm (G wraps, digit-sliced BF16 on tcgen05)",
-                "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": None,
+                "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None,
+                "traffic": OZ_HOP_TRAFFIC_BYTES_PER_CHAIN * chains if m.ndim == 256 else None,
                 "algorithmic_flops_per_launch": chains * m.n_fl * 4.0 * m.ndim ** 3,
                 "bf16_products_per_algorithmic_product": pairs,
                 "peak_source": src + "; of measured"}
@@ -205,7 +209,11 @@ def roofline(precision: str, chains: int, m, prof):
         roof["achieved"] = flops / (hop_ms / 1e3) / 1e12
         roof["frac"] = roof["achieved"] / roof["peak"]
         if precision != "fp64":
+            # the BF16 digit products the tensor cores execute, against the same BF16 peak, and the
+            # FP64-accurate algorithmic rate against the FP64 rate it replaces
             roof["tensor_op_tflops"] = roof["achieved"] * roof["bf16_products_per_algorithmic_product"]
+            roof["tensor_op_frac"] = roof["tensor_op_tflops"] / roof["peak"]
+            roof["achieved_over_fp64_peak"] = roof["achieved"] / FP64_DMMA_TFLOPS
     return roof
 
 
