@@ -101,6 +101,13 @@ struct alfgpu_s {
   zd* QRdf = nullptr;                // [B][N][N] reflectors in double-float (16-byte elements)
   std::vector<int> stab_nt;
   cudaStream_t st = nullptr;
+  // second stream of the sweep: a block's Metropolis visits run on it while the previous
+  // block's flush runs on st (update_slice); ev_fork: st -> st2, ev_join: st2 -> st
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int overlap = 1;
+  zd *Gsnap = nullptr, *Gsub = nullptr;  // [chain][F][KMAX][KMAX] next block's submatrix
+  int *posn = nullptr, *npos = nullptr;  // [chain][KMAX], [chain] next block's positions
   cudaError_t last_cuda = cudaSuccess;
   int last_line = 0;        // source line of the CUDA call that failed
   char last_msg[160] = {0};
@@ -326,27 +333,33 @@ static int qrr_clusters(int N, int CL, bool grows = false) {
   return n;
 }
 
-// Cluster size and row storage of the exact pivoted QR of B matrices N x N: the largest
-// cluster (up to CL) whose rows fit shared memory (mode 1) or, failing that, with the rows in a
-// global workspace (mode 2; ALFGPU_FLAG_QR_GLOBAL_ROWS: mode 2 only); a launch whose full-size
-// clusters would put more than two CTAs on every SM takes half-size clusters (unless forced by
-// the flags).  Mode 0: neither fits.
+// Cluster size and row storage of the exact pivoted QR of B matrices N x N.  For each row
+// storage, rows in shared memory (mode 1) and rows in a global workspace (mode 2), the cluster
+// size is CL, or CL / 2 when full-size clusters would put more than two CTAs on every SM (the
+// flags force either); the plan takes shared-memory rows unless the global-row layout needs
+// fewer waves of clusters (its CTAs need little shared memory, so several share an SM), or
+// ALFGPU_FLAG_QR_GLOBAL_ROWS asks for it.  Mode 0: neither fits.
 static int qrr_plan(int N, int CL, int B, int flags, int dev, int* CLout) {
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaGetLastError();
+  int best = 0, best_cl = CL;
+  long long best_waves = 0;
   for (int mode = (flags & ALFGPU_FLAG_QR_GLOBAL_ROWS) ? 2 : 1; mode <= 2; ++mode) {
     const bool grows = mode == 2;
-    if (qrr_clusters(N, CL, grows) <= 0) continue;
-    *CLout = CL;
+    int cl = CL, active = qrr_clusters(N, CL, grows);
+    if (active <= 0) continue;
     if (CL >= 4) {
       const bool want = (flags & ALFGPU_FLAG_QR_HALF_CLUSTER) ||
                         (!(flags & ALFGPU_FLAG_QR_FULL_CLUSTER) && (long long)B * CL > 2ll * nsm);
-      if (want && qrr_clusters(N, CL / 2, grows) > 0) *CLout = CL / 2;
+      const int a2 = want ? qrr_clusters(N, CL / 2, grows) : 0;
+      if (a2 > 0) { cl = CL / 2; active = a2; }
     }
-    return mode;
+    const long long waves = (B + active - 1) / active;
+    if (!best || waves < best_waves) { best = mode; best_cl = cl; best_waves = waves; }
   }
-  return 0;
+  *CLout = best_cl;
+  return best;
 }
 
 // One launch of the exact pivoted QR on clusters of CL CTAs (rows in shared memory, or in ws when
@@ -1502,10 +1515,35 @@ static int hop_impl(alfgpu_s* h, int up, int with_scale) {
 }
 
 // Metropolis updates of one slice in blocks of kblk visits, each followed by its flush.
+// The slice's delayed-update blocks.  Per block: the Metropolis visits (k_update), the flush
+// operands (k_flush_xy) and the flush G -= X Y.  With h->overlap (no vector vertices, no phase
+// profile) the visits of block k + 1 run on the second stream while the flush of block k runs on
+// st: before the flush, k_sub_gather snapshots G over block k + 1's positions, and k_sub_stage
+// applies block k's updates to that snapshot (the same Woodbury form), so block k + 1 starts from
+// its submatrix without waiting for the full-matrix flush.  The rank array m is kept per block
+// parity because the flush of block k reads it while block k + 1 writes its own.
 static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const double* draws_dev) {
   const int N = h->N, F = h->F, M = h->M;
   const long long NN = (long long)N * N;
-  for (size_t blk = 0; blk < h->blk_start[dir].size(); ++blk) {
+  const size_t nblk = h->blk_start[dir].size();
+  const bool ov = h->overlap && !h->pairblock && !h->profiling && nblk > 1;
+  const long long msz = (long long)h->C + h->B;
+  VertexDev V;
+  V.site = h->v_site; V.site2 = h->v_site2; V.nsite = h->v_nsite; V.type = h->v_type; V.sK = (long long)F * M;
+  if (ov) {  // the slice's G is ready on st: the first block's visits may start on st2
+    CK(cudaEventRecord(h->ev_fork, h->st));
+    CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+  }
+  for (size_t blk = 0; blk < nblk; ++blk) {
+    int* mb = h->m + (ov ? (long long)(blk & 1) * msz : 0);
+    cudaStream_t su = ov ? h->st2 : h->st;
+    if (ov && blk > 0) {  // block blk's submatrix after block blk - 1's updates
+      const int* mprev = h->m + (long long)((blk - 1) & 1) * msz;
+      const dim3 gs((UPD_KMAX + 7) / 8, h->B), bs(32, 8);
+      if (h->mixed) k_sub_stage<ArF><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
+      else k_sub_stage<ArD><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
+      CKL();
+    }
     UpdParams u;
     memset(&u, 0, sizeof(u));
     u.N = N; u.F = F; u.M = M; u.L = h->L; u.NSUN = h->NSUN;
@@ -1519,27 +1557,39 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     u.fields = h->fields;
     u.draws = draws_dev; u.sDraws = 6ll * M * h->L;
     u.rngkey = h->rngkey; u.rngctr = h->rngctr;
-    u.phase = h->phase; u.m_out = h->m; u.W = h->W; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
+    u.phase = h->phase; u.m_out = mb; u.W = h->W; u.sites_out = h->sites; u.delta_out = h->dlt; u.cnt = h->cnt;
+    u.Gsub = (ov && blk > 0) ? h->Gsub : nullptr;
     if (h->recording) { u.rec_acc = h->rec_acc; u.rec_ratio = h->rec_ratio; u.sRec = 2ll * M * h->L; }
     u.ft = h->ft;
     if (h->pairblock) {
       u.vsite2 = h->v_blk2; u.vcoef = h->v_vc; u.sites2_out = h->sites2_out; u.coef_out = h->coef_out;
     }
     prof_begin(h, ALFGPU_PROF_UPDATE);
-    if (h->mixed) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
-    else k_update<ArD><<<h->C, UPD_THREADS, upd_smem_bytes(), h->st>>>(u);
+    if (h->mixed) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), su>>>(u);
+    else k_update<ArD><<<h->C, UPD_THREADS, upd_smem_bytes(), su>>>(u);
     prof_end(h);
     CKL();
+    if (ov) {  // the flush operands need this block's decisions (and the previous flush, on st)
+      CK(cudaEventRecord(h->ev_join, h->st2));
+      CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
+    }
     prof_begin(h, ALFGPU_PROF_FLUSH);
     const int* s2o = h->pairblock ? h->sites2_out : nullptr;
     const double* co = h->pairblock ? h->coef_out : nullptr;
     if (h->mixed)
-      k_flush_xy<ArF><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
+      k_flush_xy<ArF><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, mb, h->sites, h->W,
                                                                          h->X, h->Y, s2o, co);
     else
-      k_flush_xy<ArD><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, h->m, h->sites, h->W,
+      k_flush_xy<ArD><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, mb, h->sites, h->W,
                                                                          h->X, h->Y, s2o, co);
     CKL();
+    if (ov && blk + 1 < nblk) {  // snapshot for the next block, then let its visits start
+      k_sub_gather<<<h->B, 256, 0, h->st>>>(h->G, F * NN, N, F, M, V, dir, h->blk_start[dir][blk + 1],
+                                            h->blk_cnt[dir][blk + 1], h->Gsnap, h->posn, h->npos);
+      CKL();
+      CK(cudaEventRecord(h->ev_fork, h->st));
+      CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+    }
     void* Gst = h->G;
     void* Xst = h->X;
     void* Yst = h->Y;
@@ -1553,7 +1603,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     p.batch = h->B;
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
-    p.kdyn = h->m + h->C;  // per-(chain, flavour) rank, written by k_update
+    p.kdyn = mb + h->C;  // per-(chain, flavour) rank, written by k_update
     if (h->mixed && h->oz && !h->oz_narrow && !(h->d.reserved[0] & ALFGPU_FLAG_DF_FLUSH)) {
       // G -= X Y as one real product: [Re X | Im X] times the K-doubled complex rows of Y
       const int Kf = 2 * UPD_KMAX;
@@ -1703,7 +1753,12 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   fill_tables(h->ft);
   auto fail = [&](int code) { alfgpu_destroy(h); return code; };
   if (cudaSetDevice(d.device) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return fail(ALFGPU_ERROR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+    return fail(ALFGPU_ERROR_CUDA);
+  h->overlap = !(d.reserved[0] & ALFGPU_FLAG_NO_OVERLAP);
   if (h->CL > 8) {
     if (cudaFuncSetAttribute(k_qrp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
         cudaFuncSetAttribute(k_orgqr, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
@@ -1796,7 +1851,9 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
   r |= dalloc(h, &h->iperm, B * N); r |= dalloc(h, &h->DUP, B * N); r |= dalloc(h, &h->vn, B * 2 * N);
   r |= dalloc(h, &h->info, B); r |= dalloc(h, &h->dphase, B); r |= dalloc(h, &h->cmp, 2 * B);
   r |= dalloc(h, &h->opang, B);
-  r |= dalloc(h, &h->m, C + B); r |= dalloc(h, &h->sites, C * UPD_KMAX);
+  r |= dalloc(h, &h->m, 2 * (C + B)); r |= dalloc(h, &h->sites, C * UPD_KMAX);  // m: one set per block parity
+  r |= dalloc(h, &h->Gsnap, B * UPD_KMAX * UPD_KMAX); r |= dalloc(h, &h->Gsub, B * UPD_KMAX * UPD_KMAX);
+  r |= dalloc(h, &h->posn, C * UPD_KMAX); r |= dalloc(h, &h->npos, C);
   r |= dalloc(h, &h->W, C * 2 * UPD_KMAX * UPD_KMAX); r |= dalloc(h, &h->dlt, C * 2 * UPD_KMAX);
   r |= dalloc(h, &h->X, C * 2 * N * UPD_KMAX); r |= dalloc(h, &h->Y, C * 2 * N * UPD_KMAX);
   r |= dalloc(h, &h->phase, C); r |= dalloc(h, &h->cnt, 4 * C); r |= dalloc(h, &h->stat, 8 * C);
@@ -1825,6 +1882,9 @@ void alfgpu_destroy(alfgpu_t* h) {
   if (h->tau_host) cudaFreeHost(h->tau_host);
   if (h->phase_host) cudaFreeHost(h->phase_host);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->st2) cudaStreamDestroy(h->st2);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }

@@ -20,7 +20,7 @@ struct ArD {
   static ALF_DEV Z sub(Z a, Z b) { return zsub(a, b); }
   static ALF_DEV Z add(Z a, Z b) { return zadd(a, b); }
   static ALF_DEV Z neg(Z a) { return zmk(-a.x, -a.y); }
-  static ALF_DEV Z mac(Z c, Z a, Z b) { return zadd(c, zmul(a, b)); }
+  static ALF_DEV Z mac(Z c, Z a, Z b) { return zfma(a, b, c); }
   static ALF_DEV Z scale(Z a, R s) { return zscale(a, s); }
   static ALF_DEV R re_mul(Z a, Z b) { return a.x * b.x - a.y * b.y; }
   static ALF_DEV R re(Z a) { return a.x; }

@@ -15,6 +15,12 @@ ALF_HD zd zadd(zd a, zd b) { return zmk(a.x + b.x, a.y + b.y); }
 ALF_HD zd zsub(zd a, zd b) { return zmk(a.x - b.x, a.y - b.y); }
 ALF_HD zd zmul(zd a, zd b) { return zmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 ALF_HD zd zconj(zd a) { return zmk(a.x, -a.y); }
+// c + a b and c - a b as two FMA chains (four FP64 instructions; zadd(c, zmul(a, b)) takes a
+// multiply, an FMA and an add per component)
+ALF_HD zd zfma(zd a, zd b, zd c) { return zmk(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y))); }
+ALF_HD zd zfms(zd a, zd b, zd c) {
+  return zmk(fma(-a.x, b.x, fma(a.y, b.y, c.x)), fma(-a.x, b.y, fma(-a.y, b.x, c.y)));
+}
 ALF_HD zd zscale(zd a, double s) { return zmk(a.x * s, a.y * s); }
 ALF_HD double zabs(zd a) { return hypot(a.x, a.y); }
 ALF_HD zd zneg(zd a) { return zmk(-a.x, -a.y); }

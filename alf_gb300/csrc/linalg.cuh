@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(QRParams p) {
       zd* col = A + (long long)c * lda;
       zd s = zmk(0.0, 0.0);
       if (ct.x != 0.0 || ct.y != 0.0) {
-        for (int r = j + lane; r < N; r += 32) s = zadd(s, zmul(zconj(vsh[r]), col[r]));
+        for (int r = j + lane; r < N; r += 32) s = zfma(zconj(vsh[r]), col[r], s);
         s = warp_zsum(s);
         zd f = zmul(ct, s);
         for (int r = j + lane; r < N; r += 32) col[r] = zsub(col[r], zmul(vsh[r], f));
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_orgqr(OrgqrParams p) {
         if (c <= i) continue;
         zd* col = A + (long long)c * lda;
         zd s = zmk(0.0, 0.0);
-        for (int r = i + lane; r < N; r += 32) s = zadd(s, zmul(zconj(vsh[r]), col[r]));
+        for (int r = i + lane; r < N; r += 32) s = zfma(zconj(vsh[r]), col[r], s);
         s = warp_zsum(s);
         zd f = zmul(ti, s);
         for (int r = i + lane; r < N; r += 32) col[r] = zsub(col[r], zmul(vsh[r], f));
@@ -364,14 +364,14 @@ __global__ void __launch_bounds__(256) k_trsv_v(TrsvParams p) {
     for (int i = N - 1; i >= 0; --i) {
       const zd xi = zmul(x[i], dinv[i]);
       if (r0 == 0) xo[v * N + i] = xi;
-      for (int r = r0; r < i; r += rs) x[r] = zsub(x[r], zmul(Tij(r, i), xi));
+      for (int r = r0; r < i; r += rs) x[r] = zfms(Tij(r, i), xi, x[r]);
       __syncthreads();
     }
   } else {
     for (int i = 0; i < N; ++i) {
       const zd xi = zmul(x[i], dinv[i]);
       if (r0 == 0) xo[v * N + i] = xi;
-      for (int r = i + 1 + r0; r < N; r += rs) x[r] = zsub(x[r], zmul(Tij(r, i), xi));
+      for (int r = i + 1 + r0; r < N; r += rs) x[r] = zfms(Tij(r, i), xi, x[r]);
       __syncthreads();
     }
   }

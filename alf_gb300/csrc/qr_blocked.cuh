@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
     zd acc = zmk(0.0, 0.0);
     if (j >= k && j < nb)
       for (int il = g; il < nr; il += 8)
-        if (r0 + il > kc) acc = zadd(acc, zmul(zconj(P[il][k]), P[il][j]));
+        if (r0 + il > kc) acc = zfma(zconj(P[il][k]), P[il][j], acc);
     red[g][j] = acc;
     if (rank == owner && j < nb && g == 0) xr[par][j] = P[kc - r0][j];
     __syncthreads();
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) k_bqr_panel(BQRPanel p) {
         const int i = r0 + il;
         if (i > kc) {
           if (j == k) P[il][k] = vi[q];
-          else P[il][j] = zsub(P[il][j], zmul(vi[q], f));
+          else P[il][j] = zfms(vi[q], f, P[il][j]);
         } else if (i == kc) {
           if (j == k) P[il][k] = zmk(beta, 0.0);
           else P[il][j] = zsub(P[il][j], f);
@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(256) k_bqr_larft(const zd* Gm, const zd* tau, 
     if (warp > 0) {
       zd acc = zmk(0.0, 0.0);
       for (int l2 = warp - 1; l2 < i; l2 += 7)
-        if (lane <= l2) acc = zadd(acc, zmul(ts[lane][l2], zs[l2]));
+        if (lane <= l2) acc = zfma(ts[lane][l2], zs[l2], acc);
       part[warp][lane] = acc;
     }
     __syncthreads();
@@ -860,7 +860,7 @@ __global__ void k_bqr_vt(const zd* F, long long ldf, long long sF, const zd* T, 
     const int c = j0 + l;
     if (r < c) continue;
     const zd v = (r == c) ? zmk(1.0, 0.0) : f[r + c * ldf];
-    acc = zadd(acc, zmul(v, adj ? zconj(ts[i][l]) : ts[l][i]));
+    acc = zfma(v, adj ? zconj(ts[i][l]) : ts[l][i], acc);
   }
   X[b * sX + r + (long long)i * N] = acc;
 }

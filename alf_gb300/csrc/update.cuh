@@ -75,7 +75,81 @@ struct UpdParams {
   const double* vcoef;  // [chain][F*M][2] (c_a, c_b)
   int* sites2_out;      // [chain][UPD_KMAX] accepted positions: site b or -1
   double* coef_out;     // [chain][UPD_KMAX][2]
+  // optional: the block submatrix Ghat = G(P, P) over this block's positions P, staged by
+  // k_sub_stage while the previous block's flush still runs ([chain][F][KMAX][KMAX], row a =
+  // position a); null: read from G
+  const zd* Gsub;
 };
+
+// Positions of the block of visits q0 .. q0 + nq - 1 (slice order dir) of chain c: the site of
+// every non-zero eigenvalue, in the order k_update numbers them (exclusive prefix sum of the
+// vertex sizes over the visits).  Warp-level: every lane of the calling warp takes part;
+// returns the position count, writes pos[0 .. np).
+ALF_DEV int block_positions(const VertexDev& V, int c, int M, int dir, int q0, int nq, int* pos) {
+  const int lane = threadIdx.x & 31;
+  const int* site = V.site + (long long)c * V.sK;
+  const int* site2 = V.site2 + (long long)c * V.sK;
+  const int8_t* nsite = V.nsite + (long long)c * V.sK;
+  int w = 0, n = 0;
+  if (lane < nq) {
+    n = dir == 0 ? q0 + lane : M - 1 - (q0 + lane);
+    w = nsite[n];
+  }
+  int incl = w;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int p0 = incl - w;
+  for (int I = 0; I < w; ++I) pos[p0 + I] = I ? site2[n] : site[n];
+  return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+// Snapshot of G over the positions of the next block, taken before the current block's flush
+// writes G: Gsnap[chain][f][a][l] = G(P_a, P_l).  Also stores the positions (pos[chain][KMAX],
+// npos[chain]).  grid (chains * F), 256 threads.
+__global__ void k_sub_gather(const zd* G, long long sG, int N, int F, int M, VertexDev V, int dir, int q0, int nq,
+                             zd* Gsnap, int* pos, int* npos) {
+  const int b = blockIdx.x, c = b / F, f = b % F, tid = threadIdx.x;
+  __shared__ int sp[UPD_KMAX];
+  __shared__ int snp;
+  if (tid < 32) {
+    const int np = block_positions(V, c, M, dir, q0, nq, sp);
+    if (tid == 0) snp = np;
+  }
+  __syncthreads();
+  const int np = snp;
+  if (f == 0) {
+    for (int a = tid; a < np; a += 256) pos[(long long)c * UPD_KMAX + a] = sp[a];
+    if (tid == 0) npos[c] = np;
+  }
+  const zd* Gf = G + (long long)c * sG + (long long)f * N * N;
+  zd* out = Gsnap + (long long)b * UPD_KMAX * UPD_KMAX;
+  for (int e = tid; e < np * np; e += 256) {
+    const int a = e / np, l = e % np;
+    out[a * UPD_KMAX + l] = Gf[sp[a] + (long long)sp[l] * N];
+  }
+}
+
+// The next block's submatrix after the current block's accepted updates, from the snapshot
+// and the flush operands: Gsub(a, l) = Gsnap(a, l) - sum_k X(P_a, k) Y(k, P_l), k < m (the same
+// Woodbury form the flush applies to all of G).  Arithmetic A (the precision form's).
+// grid (ceil(KMAX / 8), chains * F), block (32, 8): (l, a).
+template <class A>
+__global__ void k_sub_stage(const zd* Gsnap, const int* pos, const int* npos, const int* m_in, int N, int F,
+                            const zd* X, const zd* Y, zd* Gsub) {
+  typedef typename A::Z Z;
+  const int b = blockIdx.y, c = b / F, f = b % F;
+  const int l = threadIdx.x, a = blockIdx.x * 8 + threadIdx.y;
+  const int np = npos[c], m = m_in[c];
+  if (a >= np || l >= np) return;
+  const long long o = (long long)b * UPD_KMAX * UPD_KMAX + a * UPD_KMAX + l;
+  const int pa = pos[(long long)c * UPD_KMAX + a], pl = pos[(long long)c * UPD_KMAX + l];
+  const long long xy = ((long long)c * 2 + f) * N * UPD_KMAX;
+  Z acc = A::zero();
+  for (int k = 0; k < m; ++k) acc = A::mac(acc, A::mk(X[xy + pa + (long long)k * N]), A::mk(Y[xy + k + (long long)pl * UPD_KMAX]));
+  Gsub[o] = A::wide(A::sub(A::mk(Gsnap[o]), acc));
+}
 
 ALF_DEV int nranf3(double r) {
   // nint(r*3 + 0.5) clamped to [1,3] (random_wrap_mod.F90:159-168); no contraction.
@@ -209,7 +283,8 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(UpdParams p) {
   for (int a = warp; a < np; a += NW)
     if (lane < np)
       for (int f = 0; f < F; ++f) {
-        zd g = G[f * NN + s_psite[a] + (long long)s_psite[lane] * N];
+        zd g = p.Gsub ? p.Gsub[(((long long)c * F + f) * KM + a) * KM + lane]
+                      : G[f * NN + s_psite[a] + (long long)s_psite[lane] * N];
         if (p.vsite2 && (s_psite2[a] >= 0 || s_psite2[lane] >= 0)) {
           // Ghat(a, l) = v_a^T G v_l over the (up to two) sites of each position
           const int ia[2] = {s_psite[a], s_psite2[a]}, il[2] = {s_psite[lane], s_psite2[lane]};

@@ -118,9 +118,15 @@ enum { ALFGPU_FLAG_QR_HALF_CLUSTER = 1024, ALFGPU_FLAG_QR_FULL_CLUSTER = 2048 };
  * (K padded to 64, digit-sliced). */
 enum { ALFGPU_FLAG_DF_FLUSH = 4096 };
 /* The exact pivoted QR keeps each CTA's rows in a global (L2-resident) workspace even where
- * they fit in shared memory: a CTA then needs little shared memory, so several clusters share
- * an SM and a batched launch runs in fewer waves. */
+ * they fit in shared memory.  A CTA then needs little shared memory, so several clusters share
+ * an SM; by default this layout is taken when it needs fewer waves of clusters than rows in
+ * shared memory (batched grids), and this flag takes it always. */
 enum { ALFGPU_FLAG_QR_GLOBAL_ROWS = 8192 };
+/* alfgpu_sweep runs a delayed-update block's Metropolis visits on a second stream while the
+ * previous block's flush runs (the block's submatrix is staged from a snapshot of G and the
+ * flush operands; models with vector vertices and profiled sweeps keep the serial order).
+ * This flag keeps the serial order always. */
+enum { ALFGPU_FLAG_NO_OVERLAP = 16384 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the

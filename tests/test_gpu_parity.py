@@ -296,6 +296,29 @@ def test_graph_replay_matches_stream_path():
     assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overlapped_blocks_match_the_serial_order(precision):
+    # a block's visits start from its submatrix staged while the previous block's flush runs
+    # (second stream); the serial order reads it from the flushed G.  Same Woodbury updates in
+    # another summation order: identical decisions, G equal to rounding.
+    from alf_gb300.sweep import FLAG_NO_OVERLAP
+    m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    C, seed = 2, 41
+    out = []
+    for flags in (0, FLAG_NO_OVERLAP):
+        g = Chains(m, n_chains=C, precision=precision, flags=flags)
+        for c in range(C):
+            g.set_fields(c, rng.initial_fields(seed + c, c, m.n_op, m.ltrot))
+        g.init_state()
+        for s in range(2):
+            g.sweep(np.stack([rng.sweep_uniforms(seed + c, c, m.n_op, m.ltrot, s) for c in range(C)]))
+        out.append([(g.fields(c), g.green(c), g.stats(c).n_acc) for c in range(C)])
+    for c in range(C):
+        np.testing.assert_array_equal(out[0][c][0], out[1][c][0])
+        assert out[0][c][2] == out[1][c][2]
+        assert _relmax(out[0][c][1], out[1][c][1]) < (RTOL if precision == "fp64" else 1e-8)
+
+
 def test_delay_depth_changes_only_rounding_and_autotuner_picks_a_candidate():
     # the delay depth regroups the same Sherman-Morrison sequence; results agree to rounding
     m = mdl.hubbard("square", 6, 6, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
