@@ -1684,6 +1684,14 @@ static int oz_setup(alfgpu_s* h) {
   if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
     return 0;
+  if (!narrow && (h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_PAIRS)) {
+    // K = 64 products (flush, compact-WY update) on 16-wide tiles with a ring small enough for
+    // two CTAs per SM: (S + 1) x 16 TMEM columns round to 256 of the SM's 512
+    int st = 8;
+    while (st > 2 && 2 * oz_smem_bytes(16, h->ozf_S, 1, st) > 227 * 1024) --st;
+    h->ozf_bn = 16;
+    h->ozf_nst = st;
+  }
   if (!oz_encoder()) return 0;
   const size_t S = h->oz_S, Sf = h->ozf_S, Kp = h->oz_Kpad, Kf = 2 * UPD_KMAX, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
   int r = 0;

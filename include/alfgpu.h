@@ -127,6 +127,9 @@ enum { ALFGPU_FLAG_QR_GLOBAL_ROWS = 8192 };
  * flush operands; models with vector vertices and profiled sweeps keep the serial order).
  * This flag keeps the serial order always. */
 enum { ALFGPU_FLAG_NO_OVERLAP = 16384 };
+/* Mixed form, grids of several chains: the K = 64 tensor-core products (delayed-update flush,
+ * compact-WY update of the explicit Q) on 16-wide tiles sized so that two CTAs share an SM. */
+enum { ALFGPU_FLAG_OZ_FLUSH_PAIRS = 32768 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the
