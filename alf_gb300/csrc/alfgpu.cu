@@ -1526,7 +1526,11 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
   const int N = h->N, F = h->F, M = h->M;
   const long long NN = (long long)N * N;
   const size_t nblk = h->blk_start[dir].size();
-  const bool ov = h->overlap && !h->pairblock && !h->profiling && nblk > 1;
+  // the overlap needs room on the SMs next to the flush: the tensor-core flush fills them
+  // (one CTA per SM by shared memory and TMEM), so it is used with the FP64 / double-float flush
+  const bool ozf = h->mixed && h->oz && !h->oz_narrow && !(h->d.reserved[0] & ALFGPU_FLAG_DF_FLUSH);
+  const bool ov = h->overlap && !ozf && !h->pairblock && !h->profiling && nblk > 1;
+  const bool dfv = h->mixed && !(h->d.reserved[0] & ALFGPU_FLAG_FP64_VISITS);  // visits in double-float
   const long long msz = (long long)h->C + h->B;
   VertexDev V;
   V.site = h->v_site; V.site2 = h->v_site2; V.nsite = h->v_nsite; V.type = h->v_type; V.sK = (long long)F * M;
@@ -1540,7 +1544,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     if (ov && blk > 0) {  // block blk's submatrix after block blk - 1's updates
       const int* mprev = h->m + (long long)((blk - 1) & 1) * msz;
       const dim3 gs((UPD_KMAX + 7) / 8, h->B), bs(32, 8);
-      if (h->mixed) k_sub_stage<ArF><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
+      if (dfv) k_sub_stage<ArF><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
       else k_sub_stage<ArD><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
       CKL();
     }
@@ -1565,7 +1569,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
       u.vsite2 = h->v_blk2; u.vcoef = h->v_vc; u.sites2_out = h->sites2_out; u.coef_out = h->coef_out;
     }
     prof_begin(h, ALFGPU_PROF_UPDATE);
-    if (h->mixed) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), su>>>(u);
+    if (dfv) k_update<ArF><<<h->C, UPD_THREADS, upd_smem_bytes(), su>>>(u);
     else k_update<ArD><<<h->C, UPD_THREADS, upd_smem_bytes(), su>>>(u);
     prof_end(h);
     CKL();
@@ -1576,7 +1580,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     prof_begin(h, ALFGPU_PROF_FLUSH);
     const int* s2o = h->pairblock ? h->sites2_out : nullptr;
     const double* co = h->pairblock ? h->coef_out : nullptr;
-    if (h->mixed)
+    if (dfv)
       k_flush_xy<ArF><<<dim3((N + 7) / 8, h->B), dim3(32, 8), 0, h->st>>>(h->G, F * NN, N, F, mb, h->sites, h->W,
                                                                          h->X, h->Y, s2o, co);
     else
@@ -1604,7 +1608,7 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     // X / Y keep two flavour slots per chain; per-batch rank K = m[chain]
     if (F == 1) { p.sA = 2ll * N * UPD_KMAX; p.sB = 2ll * N * UPD_KMAX; }
     p.kdyn = mb + h->C;  // per-(chain, flavour) rank, written by k_update
-    if (h->mixed && h->oz && !h->oz_narrow && !(h->d.reserved[0] & ALFGPU_FLAG_DF_FLUSH)) {
+    if (ozf) {
       // G -= X Y as one real product: [Re X | Im X] times the K-doubled complex rows of Y
       const int Kf = 2 * UPD_KMAX;
       RET(oz_slice(h, h->X, OZ_CKA, 1, N, p.sA, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,

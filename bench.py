@@ -54,7 +54,7 @@ HOP_TRAFFIC_BYTES = 3.28e6
 # 8.3 MB written: the digit slices of G and the output), per chain
 OZ_HOP_TRAFFIC_BYTES_PER_CHAIN = 86.5e6 / 16
 # default chains per GPU of each workload (the batched forms of the benchmark configurations)
-DEFAULT_CHAINS = {"hubbard4x4": 1, "hubbard16x16": 16, "honeycomb12x12": 1, "kondo12x12": 32, "batch128": 128}
+DEFAULT_CHAINS = {"hubbard4x4": 1, "hubbard16x16": 16, "honeycomb12x12": 8, "kondo12x12": 32, "batch128": 128}
 L2_NOTE = "GPU arm: L2 flushed between timed steps (256 MB write); host arm: not applicable"
 
 

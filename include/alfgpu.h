@@ -130,6 +130,9 @@ enum { ALFGPU_FLAG_NO_OVERLAP = 16384 };
 /* Mixed form, grids of several chains: the K = 64 tensor-core products (delayed-update flush,
  * compact-WY update of the explicit Q) on 16-wide tiles sized so that two CTAs share an SM. */
 enum { ALFGPU_FLAG_OZ_FLUSH_PAIRS = 32768 };
+/* Mixed form: the per-visit Metropolis arithmetic, the block-submatrix updates, Gamma^-1 and
+ * the flush operand Y in FP64 (k_update<ArD>) instead of double-float. */
+enum { ALFGPU_FLAG_FP64_VISITS = 65536 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the
@@ -274,7 +277,10 @@ int alfgpu_set_recording(alfgpu_t* h, int32_t enable);
 int alfgpu_get_record(alfgpu_t* h, int32_t chain, int8_t* acc, double* ratio, double* G_fresh,
                       double* G_wrapped, double* phase);
 
-/* Stream the library launches on (a cudaStream_t), for callers that overlap work. */
+/* Stream the library launches on (a cudaStream_t), for callers that overlap work.  Work the
+ * sweep puts on its second stream (see ALFGPU_FLAG_NO_OVERLAP) is joined back into this stream
+ * before the sweep's next launch on it, so an event recorded or a synchronisation on this stream
+ * after alfgpu_sweep covers the whole sweep. */
 void* alfgpu_stream(alfgpu_t* h);
 
 /* Phase profiling (diagnostics): while enabled, CUDA events on the library
