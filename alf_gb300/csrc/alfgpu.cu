@@ -63,6 +63,7 @@ struct alfgpu_s {
   zd *ozGm = nullptr, *ozTm = nullptr, *ozWm = nullptr, *ozXm = nullptr;  // compact-WY explicit Q work
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
+  int ozf_pairs = 0;  // flush tiles leave room for two flush CTAs and one k_update CTA per SM
   // digit slices used by the G wraps (and TAU_M's propagation) and by the UDV propagation: a
   // prefix of the oz_S slices (dims.reserved[1] / [2] give the target bits; default oz_S)
   int ozw_S = 0, ozp_S = 0;
@@ -1526,10 +1527,10 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
   const int N = h->N, F = h->F, M = h->M;
   const long long NN = (long long)N * N;
   const size_t nblk = h->blk_start[dir].size();
-  // the overlap needs room on the SMs next to the flush: the tensor-core flush fills them
-  // (one CTA per SM by shared memory and TMEM), so it is used with the FP64 / double-float flush
+  // the overlap needs room on the SMs next to the flush: the default tensor-core flush tiles fill
+  // them (one CTA per SM by shared memory and TMEM), the paired tiles leave room for k_update
   const bool ozf = h->mixed && h->oz && !h->oz_narrow && !(h->d.reserved[0] & ALFGPU_FLAG_DF_FLUSH);
-  const bool ov = h->overlap && !ozf && !h->pairblock && !h->profiling && nblk > 1;
+  const bool ov = h->overlap && (!ozf || h->ozf_pairs) && !h->pairblock && !h->profiling && nblk > 1;
   const bool dfv = h->mixed && !(h->d.reserved[0] & ALFGPU_FLAG_FP64_VISITS);  // visits in double-float
   const long long msz = (long long)h->C + h->B;
   VertexDev V;
@@ -1690,11 +1691,13 @@ static int oz_setup(alfgpu_s* h) {
     return 0;
   if (!narrow && (h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_PAIRS)) {
     // K = 64 products (flush, compact-WY update) on 16-wide tiles with a ring small enough for
-    // two CTAs per SM: (S + 1) x 16 TMEM columns round to 256 of the SM's 512
+    // two CTAs per SM ((S + 1) x 16 TMEM columns round to 256 of the SM's 512) and room beside
+    // them for one k_update CTA, so the next block's visits can overlap the flush
     int st = 8;
-    while (st > 2 && 2 * oz_smem_bytes(16, h->ozf_S, 1, st) > 227 * 1024) --st;
+    while (st > 2 && 2 * oz_smem_bytes(16, h->ozf_S, 1, st) + upd_smem_bytes() + 16 * 1024 > 227 * 1024) --st;
     h->ozf_bn = 16;
     h->ozf_nst = st;
+    h->ozf_pairs = 1;
   }
   if (!oz_encoder()) return 0;
   const size_t S = h->oz_S, Sf = h->ozf_S, Kp = h->oz_Kpad, Kf = 2 * UPD_KMAX, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;
