@@ -1689,7 +1689,7 @@ static int oz_setup(alfgpu_s* h) {
   if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
     return 0;
-  if (!narrow && (h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_PAIRS)) {
+  if (!narrow && !(h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_SINGLE)) {
     // K = 64 products (flush, compact-WY update) on 16-wide tiles with a ring small enough for
     // two CTAs per SM ((S + 1) x 16 TMEM columns round to 256 of the SM's 512) and room beside
     // them for one k_update CTA, so the next block's visits can overlap the flush
@@ -1760,7 +1760,7 @@ int alfgpu_create(alfgpu_t** out, const alfgpu_dims* dims) {
     const int fl = d.reserved[0];
     const bool force = fl & ALFGPU_FLAG_EXACT_QRP;
     h->exact_dec = force || !(fl & ALFGPU_FLAG_NORM_PIVOT_DECOMPOSE);
-    h->exact_cgr = force || (!(fl & ALFGPU_FLAG_NORM_PIVOT_CGR) && d.precision != ALFGPU_PRECISION_MIXED);
+    h->exact_cgr = force || !(fl & ALFGPU_FLAG_NORM_PIVOT_CGR);
   }
   h->df_stab = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_GEMM);
   h->df_qr = h->mixed && (d.reserved[0] & ALFGPU_FLAG_DF_STAB_QR);

@@ -41,7 +41,7 @@ FLAG_QR_FULL_CLUSTER = 2048
 FLAG_DF_FLUSH = 4096
 FLAG_QR_GLOBAL_ROWS = 8192
 FLAG_NO_OVERLAP = 16384
-FLAG_OZ_FLUSH_PAIRS = 32768
+FLAG_OZ_FLUSH_SINGLE = 32768
 FLAG_FP64_VISITS = 65536
 # "default": ZGEQP3 everywhere in the FP64 form; norm-pivoted CGR in the mixed form
 PIVOTING = {"default": 0, "exact": FLAG_EXACT_QRP, "norms": FLAG_NORM_PIVOT,
@@ -59,8 +59,7 @@ class Chains:
         """``pivoting``: "exact" uses ZGEQP3's dynamic column pivoting (ALF's default branch)
         for every stabilisation QR; "norms" orders the columns once by their norms (ALF's
         STABLOG pivoting) and factors them with the blocked QR; "norms-cgr" /
-        "norms-decompose" do so at one call site; "default" is "exact" in the FP64 form and
-        "norms-cgr" in the mixed form.  ``wrap_bits`` / ``propagate_bits`` (mixed form): target
+        "norms-decompose" do so at one call site; "default" is "exact".  ``wrap_bits`` / ``propagate_bits`` (mixed form): target
         bits of the digit-sliced tensor-core products of the G wraps (and TAU_M) / of the UDV
         propagation (dims.reserved[1] / [2]; 0 = the full ~54)."""
         self.L = _lib.lib()

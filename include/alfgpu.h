@@ -70,18 +70,18 @@ enum {
  * usable for small beta / Nwrap). */
 enum { ALFGPU_PRECISION_FP64 = 0, ALFGPU_PRECISION_MIXED = 1 };
 enum { ALFGPU_FLAG_DF_PROPAGATION = 1 };
-/* Column pivoting of the stabilisation QRs.  Default: ZGEQP3's dynamic pivoting with
- * norm downdates (Prog/QDRP_decompose_mod.F90:60-101, the reference's default branch) on
- * one thread-block cluster per matrix, for every QR; in the mixed form the QR of CGR
- * (cgr1_mod.F90:223) instead orders the columns once by their norms and factors them
- * with the blocked unpivoted QR (the pivoting of ALF's STABLOG branch,
- * Prog/udv_state_mod.F90:503-542), whose trailing work runs on all SMs.
- * ALFGPU_FLAG_NORM_PIVOT_CGR / _DECOMPOSE select norm pivoting for that call site;
- * ALFGPU_FLAG_EXACT_QRP forces ZGEQP3 pivoting everywhere (also in the mixed form).
- * Measured on the 16x16 beta = 10 Hubbard chain: norm pivoting in decompose raises
- * Precision Green from ~7e-7 to 3e-4; in CGR only to ~1e-6, and G at every
- * stabilisation point still agrees with the ZGEQP3 oracle to 1e-10.  ZGEQP3 pivoting is
- * always used for Ndim > 512. */
+/* Column pivoting of the stabilisation QRs.  Default, in both precision forms: ZGEQP3's
+ * dynamic pivoting with norm downdates (Prog/QDRP_decompose_mod.F90:60-101, the
+ * reference's default branch) on one thread-block cluster per matrix, for every QR.
+ * ALFGPU_FLAG_NORM_PIVOT_CGR / _DECOMPOSE instead order the columns of that call site's
+ * QR once by their norms and factor them with the blocked unpivoted QR (the pivoting of
+ * ALF's STABLOG branch, Prog/udv_state_mod.F90:503-542), whose trailing work runs on all
+ * SMs; ALFGPU_FLAG_EXACT_QRP forces ZGEQP3 pivoting everywhere.  Measured on the 16x16
+ * beta = 10 Hubbard model: norm pivoting in decompose raises Precision Green from ~7e-7
+ * to 3e-4 (one chain); in CGR, over 16 chains x 7 sweeps of the mixed form, the largest
+ * Precision Green rises from 8.7e-6 to 1.3e-5 and the sweep is slower (15.2 vs 14.8
+ * sweeps/s), while G at every stabilisation point still agrees with the ZGEQP3 oracle to
+ * 1e-10.  ZGEQP3 pivoting is always used for Ndim > 512. */
 enum { ALFGPU_FLAG_EXACT_QRP = 2, ALFGPU_FLAG_NORM_PIVOT_CGR = 4, ALFGPU_FLAG_NORM_PIVOT_DECOMPOSE = 8,
        ALFGPU_FLAG_NORM_PIVOT = 12 };
 /* Mixed form only, opt-in: run parts of the stabilisation in double-float instead of
@@ -128,8 +128,10 @@ enum { ALFGPU_FLAG_QR_GLOBAL_ROWS = 8192 };
  * This flag keeps the serial order always. */
 enum { ALFGPU_FLAG_NO_OVERLAP = 16384 };
 /* Mixed form, grids of several chains: the K = 64 tensor-core products (delayed-update flush,
- * compact-WY update of the explicit Q) on 16-wide tiles sized so that two CTAs share an SM. */
-enum { ALFGPU_FLAG_OZ_FLUSH_PAIRS = 32768 };
+ * compact-WY update of the explicit Q) run on 16-wide tiles sized so that two of their CTAs and
+ * one k_update CTA share an SM (the next block's visits overlap the flush).  This flag keeps the
+ * 32-wide tiles of one CTA per SM (and the serial order of visits and flush). */
+enum { ALFGPU_FLAG_OZ_FLUSH_SINGLE = 32768 };
 /* Mixed form: the per-visit Metropolis arithmetic, the block-submatrix updates, Gamma^-1 and
  * the flush operand Y in FP64 (k_update<ArD>) instead of double-float. */
 enum { ALFGPU_FLAG_FP64_VISITS = 65536 };
