@@ -1686,7 +1686,8 @@ static int oz_setup(alfgpu_s* h) {
   const long long tiles = (long long)((N + OZ_BM - 1) / OZ_BM) * ((2 * N + 31) / 32) * (long long)B;
   const int narrow = tiles < 2ll * nsm && !(h->d.reserved[0] & ALFGPU_FLAG_TENSOR_WIDE);
   h->oz_narrow = narrow;
-  if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst, narrow) ||
+  if (oz_pick_tile(h->oz_S, h->oz_Kpad / OZ_KC, &h->oz_bn, &h->oz_nst,
+                   narrow || (h->d.reserved[0] & ALFGPU_FLAG_OZ_DEEP_RING)) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
     return 0;
   if (!narrow && !(h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_SINGLE)) {

@@ -135,6 +135,9 @@ enum { ALFGPU_FLAG_OZ_FLUSH_SINGLE = 32768 };
 /* Mixed form: the per-visit Metropolis arithmetic, the block-submatrix updates, Gamma^-1 and
  * the flush operand Y in FP64 (k_update<ArD>) instead of double-float. */
 enum { ALFGPU_FLAG_FP64_VISITS = 65536 };
+/* Mixed form: the K = N_dim tensor-core products (G wraps, UDV propagation, stabilisation
+ * products) on 16-wide tiles with the deeper A ring of one-chain grids, also on batched grids. */
+enum { ALFGPU_FLAG_OZ_DEEP_RING = 131072 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the

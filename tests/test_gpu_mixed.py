@@ -14,7 +14,8 @@ import pytest
 
 import oracle
 from alf_gb300 import model as mdl, rng
-from alf_gb300.sweep import FLAG_DF_FLUSH, FLAG_FP64_VISITS, FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE, Chains
+from alf_gb300.sweep import (FLAG_DF_FLUSH, FLAG_FP64_VISITS, FLAG_OZ_DEEP_RING, FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE,
+                             Chains)
 from parity_util import compare_record
 
 pytestmark = pytest.mark.gpu
@@ -142,14 +143,17 @@ def test_mixed_tau_m_quartets_vs_fp64_oracle():
 
 
 @pytest.mark.parametrize("flags", [0, FLAG_TENSOR_WIDE, FLAG_TENSOR_WIDE | FLAG_DF_FLUSH,
-                                   FLAG_TENSOR_WIDE | FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE | FLAG_FP64_VISITS],
-                         ids=["default", "wide", "wide-df-flush", "wide-flush-single", "wide-fp64-visits"])
+                                   FLAG_TENSOR_WIDE | FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE | FLAG_FP64_VISITS,
+                                   FLAG_TENSOR_WIDE | FLAG_OZ_DEEP_RING],
+                         ids=["default", "wide", "wide-df-flush", "wide-flush-single", "wide-fp64-visits",
+                              "wide-deep-ring"])
 def test_mixed_batched_chains_with_own_couplings_vs_oracle(flags):
     # one handle, two chains with different U (per-chain vertex tables): each within 1e-5 of
     # its own FP64 oracle run; "wide": the grid takes the batched-grid choices (flush on the
     # tensor cores, compact-WY explicit Q); "wide-df-flush": the same with the double-float flush;
     # "wide-flush-single": the K = 64 products on 16-wide tiles, two CTAs per SM; "wide-fp64-visits":
-    # the visits, block updates and flush operands in FP64
+    # the visits, block updates and flush operands in FP64; "wide-deep-ring": the K = N products on
+    # 16-wide tiles with the deeper A ring
     ms = [mdl.hubbard("square", 6, 6, U=U, beta=2.0, dtau=0.1, nwrap=10) for U in (3.0, 7.0)]
     seeds = (12, 13)
     g = Chains(ms[0], n_chains=2, precision="mixed", models=ms, flags=flags)
