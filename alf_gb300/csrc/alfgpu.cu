@@ -64,6 +64,7 @@ struct alfgpu_s {
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
   int ozf_pairs = 0;  // flush tiles leave room for two flush CTAs and one k_update CTA per SM
+  int ozf_grid = 0;   // with ozf_pairs: CTAs of the persistent K = 64 launches (two per SM)
   // digit slices used by the G wraps (and TAU_M's propagation) and by the UDV propagation: a
   // prefix of the oz_S slices (dims.reserved[1] / [2] give the target bits; default oz_S)
   int ozw_S = 0, ozp_S = 0;
@@ -495,7 +496,7 @@ static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, in
                    int bits, int bn, int nst, int RpadA, int RpadB, int modA, int modB, const int* expA,
                    const int* expB, int omode, int osub, void* out, long long ldr, long long ldc, long long sout,
                    int batch, const zd* rsc = nullptr, long long srsc = 0, int SbA = 0, int SbB = 0,
-                   const zd* csc = nullptr, long long scsc = 0) {
+                   const zd* csc = nullptr, long long scsc = 0, int persist_ctas = 0) {
   OzGemmParams p;
   memset(&p, 0, sizeof(p));
   p.M = M; p.N = Nn; p.nkc = Kpad / OZ_KC; p.S = S; p.bits = bits; p.nst = nst; p.nd = S + 1;
@@ -505,7 +506,12 @@ static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, in
   p.RpadA = RpadA; p.RpadB = RpadB; p.modA = modA; p.modB = modB; p.expA = expA; p.expB = expB;
   p.omode = omode; p.osub = osub; p.out = out; p.ldr = ldr; p.ldc = ldc; p.sout = sout; p.err = h->err;
   p.rsc = rsc; p.srsc = srsc;
-  const dim3 grid((Nn + bn - 1) / bn, (M + OZ_BM - 1) / OZ_BM, batch);
+  dim3 grid((Nn + bn - 1) / bn, (M + OZ_BM - 1) / OZ_BM, batch);
+  const long long ntile = (long long)grid.x * grid.y * grid.z;
+  if (persist_ctas > 0 && ntile > persist_ctas) {  // a bounded grid, each CTA looping over tiles
+    p.persist = 1; p.tiles_n = (int)grid.x; p.tiles_m = (int)grid.y; p.tiles_b = (int)grid.z;
+    grid = dim3((unsigned)persist_ctas, 1, 1);
+  }
   const size_t sm = oz_smem_bytes(bn, S, p.nkc, nst);
   if (bn == 32) k_oz_gemm<32><<<grid, 256, sm, h->st>>>(ta, tb, p);
   else k_oz_gemm<16><<<grid, 256, sm, h->st>>>(ta, tb, p);
@@ -749,7 +755,7 @@ static int wy_apply(alfgpu_s* h, const zd* F, int j0, int w, zd* C, int ncol, in
   CK(oz_launch_slice(xa, B, h->st));
   CK(oz_launch_slice(yb, B, h->st));
   return oz_gemm(h, h->tmXA, h->tmYB, N, 2 * ncol, 64, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN, Rp2,
-                 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, C, 1, N, NN, B);
+                 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, C, 1, N, NN, B, nullptr, 0, 0, 0, nullptr, 0, h->ozf_grid);
 }
 
 // Explicit Q (ZUNGQR) in compact-WY form on the tensor-core GEMM (mixed form, batched
@@ -1543,10 +1549,11 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
     int* mb = h->m + (ov ? (long long)(blk & 1) * msz : 0);
     cudaStream_t su = ov ? h->st2 : h->st;
     if (ov && blk > 0) {  // block blk's submatrix after block blk - 1's updates
+      // FP64 in both forms: this submatrix is the block's G0, whose Gamma^-1 sets the next flush
+      // (double-float here raised the mixed form's largest Precision Green from 9e-6 to 6e-5)
       const int* mprev = h->m + (long long)((blk - 1) & 1) * msz;
       const dim3 gs((UPD_KMAX + 7) / 8, h->B), bs(32, 8);
-      if (dfv) k_sub_stage<ArF><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
-      else k_sub_stage<ArD><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
+      k_sub_stage<ArD><<<gs, bs, 0, su>>>(h->Gsnap, h->posn, h->npos, mprev, N, F, h->X, h->Y, h->Gsub);
       CKL();
     }
     UpdParams u;
@@ -1617,7 +1624,8 @@ static int update_slice(alfgpu_s* h, int nt1, int dir, int visit_base, const dou
       RET(oz_slice(h, h->Y, OZ_CKB, UPD_KMAX, 1, p.sB, 0, nullptr, 0, N, UPD_KMAX, p.kdyn, h->ozf_S, h->ozf_bits,
                    h->oz_Rp2N, Kf, h->ozYB, h->ozYBe, h->B));
       RET(oz_gemm(h, h->tmXA, h->tmYB, N, 2 * N, Kf, h->ozf_S, h->ozf_bits, h->ozf_bn, h->ozf_nst, h->oz_RpN,
-                  h->oz_Rp2N, 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, h->G, 1, N, NN, h->B));
+                  h->oz_Rp2N, 0, 0, h->ozXAe, h->ozYBe, OZ_OUT_COLS, 1, h->G, 1, N, NN, h->B, nullptr, 0, 0, 0,
+                  nullptr, 0, h->ozf_grid));
     } else if (h->mixed) RET(gemm32(h, p, ST_C128, ST_C128, ST_C128));
     else RET(gemm(h, p));
     prof_end(h);
@@ -1699,6 +1707,7 @@ static int oz_setup(alfgpu_s* h) {
     h->ozf_bn = 16;
     h->ozf_nst = st;
     h->ozf_pairs = 1;
+    h->ozf_grid = 2 * nsm;  // more CTAs would take the room beside them (TMEM is not a launch resource)
   }
   if (!oz_encoder()) return 0;
   const size_t S = h->oz_S, Sf = h->ozf_S, Kp = h->oz_Kpad, Kf = 2 * UPD_KMAX, RpN = h->oz_RpN, Rp2 = h->oz_Rp2N;

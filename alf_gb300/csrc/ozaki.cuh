@@ -406,6 +406,10 @@ struct OzGemmParams {
   const zd* rsc; long long srsc;  // optional real scale of output row m (real part used), per batch
   const zd* csc; long long scsc;  // optional real scale of output column n (OZ_OUT_ROWS; real part), per batch
   int SbA, SbB;              // slices per batch entry in the A / B slice buffers (>= S: the first S are used)
+  // persist > 0: the grid is smaller than the tile count and each CTA takes tiles blockIdx.x,
+  // blockIdx.x + gridDim.x, ... of the tiles_n x tiles_m x batch tiles (N-tile fastest); 0: one
+  // tile per CTA at (blockIdx.x, blockIdx.y, blockIdx.z)
+  int persist, tiles_n, tiles_m, tiles_b;
 };
 
 static inline size_t oz_smem_bytes(int bn, int S, int nkc, int nst) {
@@ -422,8 +426,6 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   constexpr int HB = BN / 2;  // columns per epilogue thread
   extern __shared__ unsigned char oz_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int b = blockIdx.z, m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * BN;
-  const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
   const int S = p.S, nkc = p.nkc, NST = p.nst, ND = p.nd;
   const uint32_t raw = oz_smem(oz_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -464,6 +466,22 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   const uint32_t tbase = *tslot;
   const int total = S * nkc;
   const uint32_t chunkA = OZ_BM * 128, chunkB = BN * 128;
+  const int ntile = p.persist ? p.tiles_n * p.tiles_m * p.tiles_b : 1;
+  // ring stage and phase of a chunk follow its count over all tiles of this CTA (g); bfull and
+  // done complete once per tile (parity = tile iteration & 1)
+  int it = 0;
+  for (int tix = p.persist ? (int)blockIdx.x : 0; tix < ntile; tix += p.persist ? (int)gridDim.x : ntile, ++it) {
+  int b, m0, n0;
+  if (p.persist) {
+    n0 = (tix % p.tiles_n) * BN;
+    m0 = ((tix / p.tiles_n) % p.tiles_m) * OZ_BM;
+    b = tix / (p.tiles_n * p.tiles_m);
+  } else {
+    b = blockIdx.z; m0 = blockIdx.y * OZ_BM; n0 = blockIdx.x * BN;
+  }
+  const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
+  const long long g0 = (long long)it * total;  // count of this tile's first A chunk
+  const uint32_t tpar = (uint32_t)(it & 1);
 
   if (tid == 0) {  // producer
     const int rowA0 = bA * p.SbA * p.RpadA + m0, rowB0 = bB * p.SbB * p.RpadB + n0;
@@ -474,8 +492,9 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     int loaded = 0;
     bool ok = true;
     for (; loaded < total; ++loaded) {
-      const int st = loaded % NST;
-      if (loaded >= NST && !oz_mbar_wait(empty0 + 8u * st, (uint32_t)(((loaded / NST) - 1) & 1))) { ok = false; break; }
+      const long long g = g0 + loaded;
+      const int st = (int)(g % NST);
+      if (g >= NST && !oz_mbar_wait(empty0 + 8u * st, (uint32_t)(((g / NST) - 1) & 1))) { ok = false; break; }
       if (*abort_flag) break;
       oz_mbar_expect_tx(full0 + 8u * st, chunkA);
       oz_tma_2d(sA + (uint32_t)st * chunkA, &tmA, (loaded % nkc) * OZ_KC, rowA0 + (loaded / nkc) * p.RpadA,
@@ -483,18 +502,21 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     }
     if (!ok) { atomicOr(p.err, 4); *abort_flag = 1; }
     if (*abort_flag) {  // let every copy issued by this thread land before the CTA exits
-      oz_mbar_wait(bfull, 0);
-      for (int q = *consumed_sh; q < loaded; ++q) oz_mbar_wait(full0 + 8u * (q % NST), (uint32_t)((q / NST) & 1));
+      oz_mbar_wait(bfull, tpar);
+      for (long long q = g0 + *consumed_sh; q < g0 + loaded; ++q)
+        oz_mbar_wait(full0 + 8u * (uint32_t)(q % NST), (uint32_t)((q / NST) & 1));
     }
   } else if (tid == 32) {  // MMA issuer
-    bool ok = oz_mbar_wait(bfull, 0);
+    oz_fence_after();  // the previous tile's TMEM reads are done (barrier below)
+    bool ok = oz_mbar_wait(bfull, tpar);
     // descriptors differ only in the start-address field: advance them by (bytes >> 4)
     const uint64_t dA0 = oz_desc(sA), dB0 = oz_desc(sB);
     constexpr int TMAX = 256 / BN;  // B blocks per MMA (N <= 256)
     int q = 0;
     for (; ok && q < total; ++q) {
-      const int st = q % NST, s = q / nkc, kc = q % nkc;
-      if (!oz_mbar_wait(full0 + 8u * st, (uint32_t)((q / NST) & 1))) { ok = false; break; }
+      const long long g = g0 + q;
+      const int st = (int)(g % NST), s = q / nkc, kc = q % nkc;
+      if (!oz_mbar_wait(full0 + 8u * st, (uint32_t)((g / NST) & 1))) { ok = false; break; }
       oz_fence_after();
       const uint64_t dA = dA0 + (uint64_t)((st * chunkA) >> 4);
       // A_s times the contiguous blocks B_0 .. B_{nt-1} of this K chunk in one MMA (N = nt BN),
@@ -517,10 +539,10 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     oz_commit(done);  // arrives when every MMA issued above has completed
   }
   __syncwarp();
-  const bool done_ok = oz_mbar_wait(done, 0);
+  const bool done_ok = oz_mbar_wait(done, tpar);
   oz_fence_after();
   __syncthreads();
-  if (!done_ok && lane == 0) atomicOr(p.err, 4);
+  if (!done_ok && lane == 0) { atomicOr(p.err, 4); *abort_flag = 1; }
   if (done_ok && !*abort_flag) {
     const int quarter = warp & 3, half = warp >> 2;
     const int c0 = half * HB;  // first tile column of this thread
@@ -639,7 +661,10 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     }
   }
   oz_fence_before();
-  __syncthreads();
+  if (tid == 0) *consumed_sh = 0;  // the next tile's chunk count (read by the producer on abort)
+  __syncthreads();  // TMEM reads and the shared B blocks are free for the next tile
+  if (*abort_flag || !done_ok) break;
+  }  // tiles
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(ncols) : "memory");
 }
 

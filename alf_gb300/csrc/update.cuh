@@ -133,7 +133,7 @@ __global__ void k_sub_gather(const zd* G, long long sG, int N, int F, int M, Ver
 
 // The next block's submatrix after the current block's accepted updates, from the snapshot
 // and the flush operands: Gsub(a, l) = Gsnap(a, l) - sum_k X(P_a, k) Y(k, P_l), k < m (the same
-// Woodbury form the flush applies to all of G).  Arithmetic A (the precision form's).
+// Woodbury form the flush applies to all of G).
 // grid (ceil(KMAX / 8), chains * F), block (32, 8): (l, a).
 template <class A>
 __global__ void k_sub_stage(const zd* Gsnap, const int* pos, const int* npos, const int* m_in, int N, int F,
