@@ -278,8 +278,9 @@ def sweep_roofline_groups(groups, ms_per_step: float, precision: str, p_fp64: fl
 
 
 def workload_model(name: str):
-    """(model, ltau) of a named workload.  Kondo: the library runs the J_K vertices in their
-    shared eigenbasis and rejects U_f vertices, so ham_Uf = 0."""
+    """(model, ltau) of a named workload.  Kondo: the configuration leaves ham_Uf open; the bench
+    runs the J_K vertices alone (ham_Uf = 0).  The library also runs the reference default
+    ham_Uf = 2 (U_f as vector vertices in the J_K eigenbasis, parity-tested)."""
     from alf_gb300 import model as mdl
     if name == "kondo12x12":
         return mdl.kondo(12, 12, JK=1.5, Uf=0.0, beta=10.0, dtau=0.1, nwrap=10), 1
@@ -423,7 +424,8 @@ def host_baseline(args, m, ltau, steps: int, warmup: int) -> dict:
 # ---------------------------------------------------------------------------------------------
 # the GPU arm
 # ---------------------------------------------------------------------------------------------
-def run_ours(args, ws, rank, local, precision: str, chains: int, steps: int, warmup: int, e2e: bool = True):
+def run_ours(args, ws, rank, local, precision: str, chains: int, steps: int, warmup: int, e2e: bool = True,
+             measure: bool = False):
     """One handle of `chains` chains in `precision`: delay autotune (untimed), warm-up, the
     device-timed steps, optionally the e2e steps through host buffers, and a two-sweep phase
     profile.  Returns the measurements."""
@@ -486,6 +488,29 @@ def run_ours(args, ws, rank, local, precision: str, chains: int, steps: int, war
             G_host = ch.green(0)
         barrier()
         e2e_s = time.perf_counter() - t0
+    # a measuring sweep: ham%Obser's scalar (Kin, Pot, Part, Ener) and lattice (Green, SpinZ, SpinXY,
+    # SpinT, Den) observables accumulated on the device at every slice, no G copies (graph replay)
+    meas = None
+    if measure and args.config in ("hubbard16x16", "hubbard4x4"):
+        from alf_gb300 import lattice_obs as lo, model as mdl
+        L1 = int(m.params.get("L1", 16))
+        ch.set_scalar_obs(np.stack([mdl.hopping_matrix("square", L1, L1, t=1.0).real] * m.n_fl),
+                          np.full(m.ndim, float(m.params.get("U", 4.0))))
+        ch.set_lattice_obs(lo.Lattice("square", L1, L1))
+        ch.sweep(None)  # capture
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ch.sweep(None)
+        e1.record(stream)
+        barrier()
+        tm = e0.elapsed_time(e1) / 1e3
+        cnt = ch.scalar_obs(0)["count"]
+        meas = {"value": C * steps / tm, "unit": "sweeps/s", "measurements_per_chain": cnt,
+                "observables": "Kin, Pot, Part, Ener; Green, SpinZ, SpinXY, SpinT, Den (equal time, every slice)"}
+        ch.set_scalar_obs()
+        ch.set_lattice_obs(None)
     # phase profile of two sweeps (separate pass; events on the library stream)
     ch.set_profiling(True)
     for _ in range(2):
@@ -493,7 +518,7 @@ def run_ours(args, ws, rank, local, precision: str, chains: int, steps: int, war
     prof = ch.profile()
     ch.set_profiling(False)
     t = replicas.max_over_ranks([ms / 1e3] + ([e2e_s] if e2e else []), device=f"cuda:{local}")
-    out = dict(m=m, t_dev=t[0], t_e2e=t[1] if e2e else None, clocks=clk.summary(), prof=prof, n_acc=n_acc,
+    out = dict(m=m, t_dev=t[0], t_e2e=t[1] if e2e else None, clocks=clk.summary(), prof=prof, n_acc=n_acc, meas=meas,
                h2d=h2d, d2h=d2h, launches=n_launch, delay=delay, ltau=ltau, steps=steps, chains=C,
                precision=precision, acceptance=sum(s.n_acc for s in st) / max(sum(s.n_prop for s in st), 1),
                precision_green={"xmaxG": max(s.xmaxG for s in st),
@@ -755,7 +780,8 @@ def main():
         print(json.dumps(line))
         return
 
-    r = run_ours(args, ws, rank, local, args.precision, args.chains, args.steps, args.warmup, e2e=True)
+    r = run_ours(args, ws, rank, local, args.precision, args.chains, args.steps, args.warmup, e2e=True,
+                 measure=args.compare)
     if rank != 0:
         return
     head = form_summary(ws, r)
@@ -796,6 +822,8 @@ def main():
         "gpu_launches": head["gpu_launches"], "phases": head["phases"], "precision_green": head["precision_green"],
         "acceptance": head["acceptance"], "per_chain_sweeps_per_s": head["per_chain_sweeps_per_s"],
         "sweep_roofline": head["sweep_roofline"]})
+    if r.get("meas"):
+        line["measuring_sweeps"] = r["meas"]
     line.update(extra)
     print(json.dumps(line))
 
