@@ -513,8 +513,14 @@ static int oz_gemm(alfgpu_s* h, const CUtensorMap& ta, const CUtensorMap& tb, in
     grid = dim3((unsigned)persist_ctas, 1, 1);
   }
   const size_t sm = oz_smem_bytes(bn, S, p.nkc, nst);
-  if (bn == 32) k_oz_gemm<32><<<grid, 256, sm, h->st>>>(ta, tb, p);
-  else k_oz_gemm<16><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  if (p.persist) {
+    if (bn == 32) k_oz_gemm<32, true><<<grid, 256, sm, h->st>>>(ta, tb, p);
+    else k_oz_gemm<16, true><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  } else if (bn == 32) {
+    k_oz_gemm<32><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  } else {
+    k_oz_gemm<16><<<grid, 256, sm, h->st>>>(ta, tb, p);
+  }
   h->launches++;
   CKL();
   return 0;
@@ -1732,10 +1738,23 @@ static int oz_setup(alfgpu_s* h) {
   const size_t sm2 = oz_smem_bytes(h->ozf_bn, h->ozf_S, 1, h->ozf_nst);
   const int sm32 = (int)std::max(h->oz_bn == 32 ? sm1 : 0, h->ozf_bn == 32 ? sm2 : 0);
   const int sm16 = (int)std::max(h->oz_bn == 16 ? sm1 : 0, h->ozf_bn == 16 ? sm2 : 0);
-  if (sm32 && raise_smem_limit(k_oz_gemm<32>, (size_t)sm32) != cudaSuccess)
+  if (sm32 && (raise_smem_limit(k_oz_gemm<32>, (size_t)sm32) != cudaSuccess ||
+               raise_smem_limit(k_oz_gemm<32, true>, (size_t)sm32) != cudaSuccess))
     return ALFGPU_ERROR_CUDA;
-  if (sm16 && raise_smem_limit(k_oz_gemm<16>, (size_t)sm16) != cudaSuccess)
+  if (sm16 && (raise_smem_limit(k_oz_gemm<16>, (size_t)sm16) != cudaSuccess ||
+               raise_smem_limit(k_oz_gemm<16, true>, (size_t)sm16) != cudaSuccess))
     return ALFGPU_ERROR_CUDA;
+  if (h->ozf_pairs) {
+    // the paired flush CTAs and the overlapped k_update CTA share an SM only if the SM is set up
+    // with its largest shared-memory carveout while the flush runs
+    if (cudaFuncSetAttribute(k_oz_gemm<16, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaFuncSetAttribute(k_update<ArF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaFuncSetAttribute(k_update<ArD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+      return ALFGPU_ERROR_CUDA;
+  }
   h->oz = 1;
   return 0;
 }

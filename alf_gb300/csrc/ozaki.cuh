@@ -406,9 +406,9 @@ struct OzGemmParams {
   const zd* rsc; long long srsc;  // optional real scale of output row m (real part used), per batch
   const zd* csc; long long scsc;  // optional real scale of output column n (OZ_OUT_ROWS; real part), per batch
   int SbA, SbB;              // slices per batch entry in the A / B slice buffers (>= S: the first S are used)
-  // persist > 0: the grid is smaller than the tile count and each CTA takes tiles blockIdx.x,
-  // blockIdx.x + gridDim.x, ... of the tiles_n x tiles_m x batch tiles (N-tile fastest); 0: one
-  // tile per CTA at (blockIdx.x, blockIdx.y, blockIdx.z)
+  // k_oz_gemm<BN, true>: the grid is smaller than the tile count and each CTA takes tiles
+  // blockIdx.x, blockIdx.x + gridDim.x, ... of the tiles_n x tiles_m x tiles_b tiles (N-tile
+  // fastest); <BN, false>: one tile per CTA at (blockIdx.x, blockIdx.y, blockIdx.z)
   int persist, tiles_n, tiles_m, tiles_b;
 };
 
@@ -420,7 +420,7 @@ static inline size_t oz_smem_bytes(int bn, int S, int nkc, int nst) {
 // as stages free up), warp 1 lane 0 issues the MMAs and commits each ring stage back to the
 // producer; then all eight warps read TMEM: warp w takes TMEM lanes 32 (w % 4) .. + 31
 // (its sub-partition's) and columns (w / 4) BN/2 .. + BN/2 - 1.
-template <int BN>
+template <int BN, bool PERSIST = false>
 __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUtensorMap tmA,
                                                     const __grid_constant__ CUtensorMap tmB, OzGemmParams p) {
   constexpr int HB = BN / 2;  // columns per epilogue thread
@@ -466,13 +466,13 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   const uint32_t tbase = *tslot;
   const int total = S * nkc;
   const uint32_t chunkA = OZ_BM * 128, chunkB = BN * 128;
-  const int ntile = p.persist ? p.tiles_n * p.tiles_m * p.tiles_b : 1;
+  const int ntile = PERSIST ? p.tiles_n * p.tiles_m * p.tiles_b : 1;
   // ring stage and phase of a chunk follow its count over all tiles of this CTA (g); bfull and
   // done complete once per tile (parity = tile iteration & 1)
   int it = 0;
-  for (int tix = p.persist ? (int)blockIdx.x : 0; tix < ntile; tix += p.persist ? (int)gridDim.x : ntile, ++it) {
+  for (int tix = PERSIST ? (int)blockIdx.x : 0; tix < ntile; tix += PERSIST ? (int)gridDim.x : ntile, ++it) {
   int b, m0, n0;
-  if (p.persist) {
+  if (PERSIST) {
     n0 = (tix % p.tiles_n) * BN;
     m0 = ((tix / p.tiles_n) % p.tiles_m) * OZ_BM;
     b = tix / (p.tiles_n * p.tiles_m);
