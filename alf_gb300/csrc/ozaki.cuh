@@ -467,8 +467,10 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   const int total = S * nkc;
   const uint32_t chunkA = OZ_BM * 128, chunkB = BN * 128;
   const int ntile = PERSIST ? p.tiles_n * p.tiles_m * p.tiles_b : 1;
-  // ring stage and phase of a chunk follow its count over all tiles of this CTA (g); bfull and
-  // done complete once per tile (parity = tile iteration & 1)
+  // ring stage and round of a chunk follow its count over all tiles of this CTA, kept as running
+  // (stage, round) pairs by the producer and the MMA issuer; bfull and done complete once per
+  // tile (parity = tile iteration & 1)
+  int pst = 0, pround = 0, mst = 0, mround = 0;
   int it = 0;
   for (int tix = PERSIST ? (int)blockIdx.x : 0; tix < ntile; tix += PERSIST ? (int)gridDim.x : ntile, ++it) {
   int b, m0, n0;
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     b = blockIdx.z; m0 = blockIdx.y * OZ_BM; n0 = blockIdx.x * BN;
   }
   const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
-  const long long g0 = (long long)it * total;  // count of this tile's first A chunk
+  const int g0 = it * total;  // count of this tile's first A chunk
   const uint32_t tpar = (uint32_t)(it & 1);
 
   if (tid == 0) {  // producer
@@ -491,19 +493,19 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
         oz_tma_2d(sB + (uint32_t)(kc * (S + 1) + t) * chunkB, &tmB, kc * OZ_KC, rowB0 + t * p.RpadB, bfull);
     int loaded = 0;
     bool ok = true;
-    for (; loaded < total; ++loaded) {
-      const long long g = g0 + loaded;
-      const int st = (int)(g % NST);
-      if (g >= NST && !oz_mbar_wait(empty0 + 8u * st, (uint32_t)(((g / NST) - 1) & 1))) { ok = false; break; }
+    for (int s = 0, kc = 0; loaded < total; ++loaded) {
+      const int st = pst;
+      if (pround > 0 && !oz_mbar_wait(empty0 + 8u * st, (uint32_t)((pround - 1) & 1))) { ok = false; break; }
       if (*abort_flag) break;
       oz_mbar_expect_tx(full0 + 8u * st, chunkA);
-      oz_tma_2d(sA + (uint32_t)st * chunkA, &tmA, (loaded % nkc) * OZ_KC, rowA0 + (loaded / nkc) * p.RpadA,
-                full0 + 8u * st);
+      oz_tma_2d(sA + (uint32_t)st * chunkA, &tmA, kc * OZ_KC, rowA0 + s * p.RpadA, full0 + 8u * st);
+      if (++pst == NST) { pst = 0; ++pround; }
+      if (++kc == nkc) { kc = 0; ++s; }
     }
     if (!ok) { atomicOr(p.err, 4); *abort_flag = 1; }
     if (*abort_flag) {  // let every copy issued by this thread land before the CTA exits
       oz_mbar_wait(bfull, tpar);
-      for (long long q = g0 + *consumed_sh; q < g0 + loaded; ++q)
+      for (int q = g0 + *consumed_sh; q < g0 + loaded; ++q)
         oz_mbar_wait(full0 + 8u * (uint32_t)(q % NST), (uint32_t)((q / NST) & 1));
     }
   } else if (tid == 32) {  // MMA issuer
@@ -513,10 +515,9 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     const uint64_t dA0 = oz_desc(sA), dB0 = oz_desc(sB);
     constexpr int TMAX = 256 / BN;  // B blocks per MMA (N <= 256)
     int q = 0;
-    for (; ok && q < total; ++q) {
-      const long long g = g0 + q;
-      const int st = (int)(g % NST), s = q / nkc, kc = q % nkc;
-      if (!oz_mbar_wait(full0 + 8u * st, (uint32_t)((g / NST) & 1))) { ok = false; break; }
+    for (int s = 0, kc = 0; ok && q < total; ++q) {
+      const int st = mst;
+      if (!oz_mbar_wait(full0 + 8u * st, (uint32_t)(mround & 1))) { ok = false; break; }
       oz_fence_after();
       const uint64_t dA = dA0 + (uint64_t)((st * chunkA) >> 4);
       // A_s times the contiguous blocks B_0 .. B_{nt-1} of this K chunk in one MMA (N = nt BN),
@@ -534,6 +535,8 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
       }
       oz_commit(empty0 + 8u * st);
       *consumed_sh = q + 1;
+      if (++mst == NST) { mst = 0; ++mround; }
+      if (++kc == nkc) { kc = 0; ++s; }
     }
     if (!ok) { atomicOr(p.err, 4); *abort_flag = 1; }
     oz_commit(done);  // arrives when every MMA issued above has completed
