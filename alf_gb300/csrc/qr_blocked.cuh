@@ -551,98 +551,118 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
   int par = 1;
   __syncthreads();
 
-  for (int j = 0; j < N; ++j) {
-    // pivot: first maximum of the norms vn1[j..N) (times the column scales, ArF)
-    int pv;
-    if (sep && scaled) {
-      double bv = -1.0;
-      int bi = N;
-      for (int c = j + tid; c < N; c += 256) {
-        const double v = sqrt(A::rwide(vn1[c])) * cs[c];
-        if (v > bv) { bv = v; bi = c; }
-      }
-      qrr_argmax<ArD>(bv, bi);
-      if (lane == 0) { s_bvd[warp] = bv; s_bi[warp] = bi; }
-      __syncthreads();
-      if (tid == 0) {
-        double v = s_bvd[0];
-        int i = s_bi[0];
-        for (int w = 1; w < 8; ++w)
-          if (s_bvd[w] > v || (s_bvd[w] == v && s_bi[w] < i)) { v = s_bvd[w]; i = s_bi[w]; }
-        s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
-      }
-    } else if (!sep) {
-      // FP64 norms are >= 0: they order like their IEEE bit patterns, compared on the integer
-      // pipes (NaN maps below every norm, so it is never chosen)
-      long long bv = -1;
-      int bi = N;
-      for (int c = j + tid; c < N; c += 256) {
-        long long v = __double_as_longlong(A::rwide(vn1[c]));
-        if ((v & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) v = -1;  // NaN
-        if (v == (long long)0x8000000000000000ull) v = 0;                  // -0 ranks as +0
-        if (v > bv) { bv = v; bi = c; }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-      }
-      if (lane == 0) { s_bi[warp] = bi; s_bvd[warp] = __longlong_as_double(bv); }
-      __syncthreads();
-      if (tid == 0) {
-        long long v = __double_as_longlong(s_bvd[0]);
-        int i = s_bi[0];
-        for (int w = 1; w < 8; ++w) {
-          const long long u = __double_as_longlong(s_bvd[w]);
-          if (u > v || (u == v && s_bi[w] < i)) { v = u; i = s_bi[w]; }
+  // Pivot search over the norms vn1[j0..N): the first maximum (times the column scales, ArF).
+  auto find_pivot = [&](int j0) -> int {
+      if (sep && scaled) {
+        double bv = -1.0;
+        int bi = N;
+        for (int c = j0 + tid; c < N; c += 256) {
+          const double v = sqrt(A::rwide(vn1[c])) * cs[c];
+          if (v > bv) { bv = v; bi = c; }
         }
-        s_pv = (i >= j && i < N) ? i : j;
+        qrr_argmax<ArD>(bv, bi);
+        if (lane == 0) { s_bvd[warp] = bv; s_bi[warp] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+          double v = s_bvd[0];
+          int i = s_bi[0];
+          for (int w = 1; w < 8; ++w)
+            if (s_bvd[w] > v || (s_bvd[w] == v && s_bi[w] < i)) { v = s_bvd[w]; i = s_bi[w]; }
+          s_pv = (i >= j0 && i < N) ? i : j0;  // NaN norms: keep the column in place
+        }
+      } else if (!sep) {
+        // FP64 norms are >= 0: they order like their IEEE bit patterns, compared on the integer
+        // pipes (NaN maps below every norm, so it is never chosen)
+        long long bv = -1;
+        int bi = N;
+        for (int c = j0 + tid; c < N; c += 256) {
+          long long v = __double_as_longlong(A::rwide(vn1[c]));
+          if ((v & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) v = -1;  // NaN
+          if (v == (long long)0x8000000000000000ull) v = 0;                  // -0 ranks as +0
+          if (v > bv) { bv = v; bi = c; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { s_bi[warp] = bi; s_bvd[warp] = __longlong_as_double(bv); }
+        __syncthreads();
+        if (tid == 0) {
+          long long v = __double_as_longlong(s_bvd[0]);
+          int i = s_bi[0];
+          for (int w = 1; w < 8; ++w) {
+            const long long u = __double_as_longlong(s_bvd[w]);
+            if (u > v || (u == v && s_bi[w] < i)) { v = u; i = s_bi[w]; }
+          }
+          s_pv = (i >= j0 && i < N) ? i : j0;
+        }
+      } else {
+        R bv = mone;
+        int bi = N;
+        for (int c = j0 + tid; c < N; c += 256) {
+          const R v = vn1[c];
+          if (A::gt(v, bv)) { bv = v; bi = c; }
+        }
+        qrr_argmax<A>(bv, bi);
+        if (lane == 0) { s_bv[warp] = bv; s_bi[warp] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+          R v = s_bv[0];
+          int i = s_bi[0];
+          for (int w = 1; w < 8; ++w)
+            if (A::gt(s_bv[w], v) || (!A::gt(v, s_bv[w]) && s_bi[w] < i)) { v = s_bv[w]; i = s_bi[w]; }
+          s_pv = (i >= j0 && i < N) ? i : j0;  // NaN norms: keep the column in place
+        }
       }
-    } else {
-      R bv = mone;
-      int bi = N;
-      for (int c = j + tid; c < N; c += 256) {
-        const R v = vn1[c];
-        if (A::gt(v, bv)) { bv = v; bi = c; }
-      }
-      qrr_argmax<A>(bv, bi);
-      if (lane == 0) { s_bv[warp] = bv; s_bi[warp] = bi; }
       __syncthreads();
-      if (tid == 0) {
-        R v = s_bv[0];
-        int i = s_bi[0];
-        for (int w = 1; w < 8; ++w)
-          if (A::gt(s_bv[w], v) || (!A::gt(v, s_bv[w]) && s_bi[w] < i)) { v = s_bv[w]; i = s_bi[w]; }
-        s_pv = (i >= j && i < N) ? i : j;  // NaN norms: keep the column in place
-      }
+      return s_pv;
+  };
+  // Exchange columns a and pv of the own rows, the permutation, norms, scales and (with_f) the
+  // per-column update factors held in tot.
+  auto swap_cols = [&](int a, int pv, bool with_f) {
+    if (pv == a) return;
+    for (int il = tid; il < nmine; il += 256) {
+      const Z t = Ar[(size_t)il * N + pv];
+      Ar[(size_t)il * N + pv] = Ar[(size_t)il * N + a];
+      Ar[(size_t)il * N + a] = t;
+    }
+    if (tid == 0) {
+      const int tj = jp[pv]; jp[pv] = jp[a]; jp[a] = tj;
+      vn1[pv] = vn1[a]; vn2[pv] = vn2[a];
+      const double ts = cs[pv]; cs[pv] = cs[a]; cs[a] = ts;
+      if (with_f) { const Z tf = tot[pv]; tot[pv] = tot[a]; tot[a] = tf; }
     }
     __syncthreads();
-    pv = s_pv;
-    if (pv != j) {
-      for (int il = tid; il < nmine; il += 256) {
-        const Z t = Ar[(size_t)il * N + pv];
-        Ar[(size_t)il * N + pv] = Ar[(size_t)il * N + j];
-        Ar[(size_t)il * N + j] = t;
-      }
-      if (tid == 0) {
-        const int t = jp[pv]; jp[pv] = jp[j]; jp[j] = t;
-        vn1[pv] = vn1[j]; vn2[pv] = vn2[j];
-        const double ts = cs[pv]; cs[pv] = cs[j]; cs[j] = ts;
-      }
-      __syncthreads();
-    }
-    // partials over own rows i > j; the owner of row j publishes it.  With few columns
-    // left, K = 1 << lk threads share a column (rows interleaved, xor-shuffle sum), so the
-    // FP64 work spreads over all four sub-partitions.
+  };
+  // K = 1 << lk threads per column when few columns remain (rows interleaved, xor-shuffle sums), so
+  // the FP64 work spreads over all four sub-partitions.
+  auto kmap = [&](int j0, int il0j) {
+    int lk = 0;
+    while (lk < 4 && ((N - j0) << (lk + 1)) <= 256 && (1 << lk) < nmine - il0j) ++lk;
+    return lk;
+  };
+  // first own row > j0
+  auto first_row = [&](int j0) { return (j0 >= (int)rank) ? (j0 - (int)rank) / (int)CL + 1 : 0; };
+
+  // Step j needs the pivot of column j in place and the partial sums of its columns published.
+  // Step j normally ends with one pass over its rows that applies its reflector to the trailing
+  // columns and, in the same pass, forms step j + 1's partial sums with the updated values
+  // (step j + 1's pivot is chosen first: its norms need only the updated pivot row).  A step
+  // whose norm downdates need a recomputation applies its reflector alone and the next step
+  // starts from its own pivot search.
+  bool pre = false;
+  for (int j = 0; j < N; ++j) {
     const unsigned owner = (unsigned)(j % (int)CL);
     const int ilj = j / (int)CL;
-    const int il0 = (j >= (int)rank) ? (j - (int)rank) / (int)CL + 1 : 0;  // first own row > j
-    Z* xsp = xs + par * N;
-    Z* xrp = xr + par * N;
+    const int il0 = first_row(j);
     const int ncol = N - j;
-    int lk = 0;
-    while (lk < 4 && (ncol << (lk + 1)) <= 256 && (1 << lk) < nmine - il0) ++lk;
-    {
+    if (!pre) {
+      swap_cols(j, find_pivot(j), false);
+      // partials over own rows i > j; the owner of row j publishes it
+      Z* xsp = xs + par * N;
+      Z* xrp = xr + par * N;
+      const int lk = kmap(j, il0);
       const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
       const unsigned gm = qrr_gmask(lk, ci);
       for (int c = j + warp * cpw + ci; c < N; c += 8 * cpw) {
@@ -661,6 +681,9 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
         }
       }
     }
+    pre = false;
+    Z* xsp = xs + par * N;
+    Z* xrp = xr + par * N;
     cluster_sync();
     {
       int l4 = 0;
@@ -701,70 +724,129 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
     const bool trivial = s_triv;
     const R beta = A::re(s_zb);
     const Z t = s_zt, scal = s_zs;
-    // H^H on columns c > j (a_c -= conj(tau) v (v^H a_c)), reflector into column j, and the
-    // norm downdate with the updated pivot-row entry.  The norms are kept squared, so
-    // ZGEQP3's downdate vn1 *= sqrt(max(0, 1 - (|a|/vn1)^2)) and its recompute test
-    // (vn1/vn2)^2 max(0, 1 - (|a|/vn1)^2) <= tol3z need no division or square root.
+    // Per column c > j (scalars only): the update factor f = conj(tau) (a_jc + conj(scal) x_c)
+    // (kept in tot[c]), the updated pivot-row entry (written by its owner), and ZGEQP3's norm
+    // downdate.  The norms are kept squared, so the downdate vn1 *= sqrt(max(0, 1 - (|a|/vn1)^2))
+    // and the recompute test (vn1/vn2)^2 max(0, 1 - (|a|/vn1)^2) <= tol3z need no division or
+    // square root.  Then the reflector into column j.
     int need = 0;
-    {
-      const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
-      for (int c = j + warp * cpw + ci; c < N; c += 8 * cpw) {
-        if (c == j) {
-          if (!trivial) {
-            for (int il = il0 + s; il < nmine; il += K) Ar[(size_t)il * N + j] = vsh[il];
-            if (rank == owner && s == 0) Ar[(size_t)ilj * N + j] = A::mkz(beta, A::rzero());
-          }
-          continue;
-        }
-        Z anew = prow[c];
-        if (!trivial) {
-          const Z f = A::mul(A::conj(t), A::mac(prow[c], A::conj(scal), tot[c]));
-          const Z nf = A::neg(f);
-          for (int il = il0 + s; il < nmine; il += K)
-            Ar[(size_t)il * N + c] = A::mac(Ar[(size_t)il * N + c], vsh[il], nf);
-          anew = A::sub(anew, f);
-          if (rank == owner && s == 0) Ar[(size_t)ilj * N + c] = anew;
-        }
-        if (s == 0) {
-          const R v1 = vn1[c];
-          if (!A::rzero_p(v1)) {
-            const R rest = A::rmax0(A::rsub(v1, A::abs2(anew)));
-            if (!A::gt(rest, A::mulr(tol3z, vn2[c]))) {
-              if (j < N - 1) { need = 1; vn1[c] = mone; }  // recomputed below
-              else { vn1[c] = A::rzero(); vn2[c] = A::rzero(); }
-            } else {
-              vn1[c] = rest;
-            }
-          }
+    for (int c = j + 1 + tid; c < N; c += 256) {
+      Z anew = prow[c], f = A::zero();
+      if (!trivial) {
+        f = A::mul(A::conj(t), A::mac(prow[c], A::conj(scal), tot[c]));
+        anew = A::sub(anew, f);
+        if (rank == owner) Ar[(size_t)ilj * N + c] = anew;
+      }
+      tot[c] = f;
+      const R v1 = vn1[c];
+      if (!A::rzero_p(v1)) {
+        const R rest = A::rmax0(A::rsub(v1, A::abs2(anew)));
+        if (!A::gt(rest, A::mulr(tol3z, vn2[c]))) {
+          if (j < N - 1) { need = 1; vn1[c] = mone; }  // recomputed below
+          else { vn1[c] = A::rzero(); vn2[c] = A::rzero(); }
+        } else {
+          vn1[c] = rest;
         }
       }
+    }
+    if (!trivial) {
+      for (int il = il0 + tid; il < nmine; il += 256) Ar[(size_t)il * N + j] = vsh[il];
+      if (rank == owner && tid == 0) Ar[(size_t)ilj * N + j] = A::mkz(beta, A::rzero());
     }
     if (rank == owner && tid == 0) {
       p.tau[b * p.sT + j] = A::wide(t);
       p.D[b * p.sD + j] = (trivial ? sqrt(A::rwide(A::abs2(alpha))) : fabs(A::rwide(beta))) * cs[j];
     }
-    if (__syncthreads_or(need)) {
-      // exact norms of the flagged columns over rows > j (post-update)
-      Z* xq = xs + par * N;
-      for (int c = j + 1 + tid; c < N; c += 256) {
-        R s0 = A::rzero();
-        if (A::rneg_p(vn1[c]))
-          for (int il = il0; il < nmine; ++il) s0 = A::radd(s0, A::abs2(Ar[(size_t)il * N + c]));
-        xq[c] = A::mkz(s0, A::rzero());
+    const bool recompute = __syncthreads_or(need);
+    if (recompute || j + 1 >= N) {
+      // H^H on the columns c > j alone: a_c -= v f_c over own rows > j
+      if (!trivial) {
+        const int lk = kmap(j, il0);
+        const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
+        for (int c = j + 1 + warp * cpw + ci; c < N; c += 8 * cpw) {
+          const Z nf = A::neg(tot[c]);
+          for (int il = il0 + s; il < nmine; il += K)
+            Ar[(size_t)il * N + c] = A::mac(Ar[(size_t)il * N + c], vsh[il], nf);
+        }
       }
-      cluster_sync();
-      for (int c = j + 1 + tid; c < N; c += 256) {
-        if (!A::rneg_p(vn1[c])) continue;
-        Z s[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
-#pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (q < (int)CL) s[q & 3] = A::add(s[q & 3], dsm_ld16<Z>(dsmem_addr(&xq[c], q)));
-        const R nrm2 = A::re(A::add(A::add(s[0], s[1]), A::add(s[2], s[3])));
-        vn1[c] = nrm2; vn2[c] = nrm2;
-      }
-      par ^= 1;
       __syncthreads();
+      if (recompute) {
+        // exact norms of the flagged columns over rows > j (post-update)
+        Z* xq = xs + par * N;
+        for (int c = j + 1 + tid; c < N; c += 256) {
+          R s0 = A::rzero();
+          if (A::rneg_p(vn1[c]))
+            for (int il = il0; il < nmine; ++il) s0 = A::radd(s0, A::abs2(Ar[(size_t)il * N + c]));
+          xq[c] = A::mkz(s0, A::rzero());
+        }
+        cluster_sync();
+        for (int c = j + 1 + tid; c < N; c += 256) {
+          if (!A::rneg_p(vn1[c])) continue;
+          Z sq[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            if (q < (int)CL) sq[q & 3] = A::add(sq[q & 3], dsm_ld16<Z>(dsmem_addr(&xq[c], q)));
+          const R nrm2 = A::re(A::add(A::add(sq[0], sq[1]), A::add(sq[2], sq[3])));
+          vn1[c] = nrm2; vn2[c] = nrm2;
+        }
+        par ^= 1;
+        __syncthreads();
+      }
+      continue;
     }
+    // step j + 1's pivot (the norms are final), then one pass: the update of step j and the
+    // partial sums of step j + 1 over the updated values
+    const int j1 = j + 1;
+    swap_cols(j1, find_pivot(j1), true);
+    const unsigned owner1 = (unsigned)(j1 % (int)CL);
+    const int ilj1 = j1 / (int)CL;
+    const int il01 = first_row(j1);
+    if (!trivial) {  // step j + 1's pivot column first: every other column's sums read it
+      const Z nf = A::neg(tot[j1]);
+      for (int il = il0 + tid; il < nmine; il += 256)
+        Ar[(size_t)il * N + j1] = A::mac(Ar[(size_t)il * N + j1], vsh[il], nf);
+    }
+    __syncthreads();
+    {
+      Z* xsp1 = xs + par * N;
+      Z* xrp1 = xr + par * N;
+      const int lk = kmap(j1, il01);
+      const int K = 1 << lk, cpw = 32 >> lk, s = lane / cpw, ci = lane % cpw;
+      const unsigned gm = qrr_gmask(lk, ci);
+      for (int c = j1 + warp * cpw + ci; c < N; c += 8 * cpw) {
+        const bool upd = !trivial && c > j1;
+        const Z nf = A::neg(tot[c]);
+        Z s0 = A::zero(), s1 = s0;
+        int il = il0 + s;
+        for (; il + K < nmine; il += 2 * K) {
+          Z v0 = Ar[(size_t)il * N + c], v1 = Ar[(size_t)(il + K) * N + c];
+          if (upd) {
+            v0 = A::mac(v0, vsh[il], nf);
+            v1 = A::mac(v1, vsh[il + K], nf);
+            Ar[(size_t)il * N + c] = v0;
+            Ar[(size_t)(il + K) * N + c] = v1;
+          }
+          if (il >= il01) s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j1]), v0);
+          s1 = A::mac(s1, A::conj(Ar[(size_t)(il + K) * N + j1]), v1);  // il + K > il0 >= il01 - 1
+        }
+        if (il < nmine) {
+          Z v0 = Ar[(size_t)il * N + c];
+          if (upd) {
+            v0 = A::mac(v0, vsh[il], nf);
+            Ar[(size_t)il * N + c] = v0;
+          }
+          if (il >= il01) s0 = A::mac(s0, A::conj(Ar[(size_t)il * N + j1]), v0);
+        }
+        Z acc = A::add(s0, s1);
+        for (int o = cpw; o < 32; o <<= 1) acc = A::add(acc, qrr_shfl_xor(acc, o, gm));
+        __syncwarp(gm);  // the group's updates of row j + 1 are visible to its publishing lane
+        if (s == 0) {
+          xsp1[c] = acc;
+          if (rank == owner1) xrp1[c] = Ar[(size_t)ilj1 * N + c];
+        }
+      }
+    }
+    pre = true;
   }
   Z* raw = p.Araw ? reinterpret_cast<Z*>(p.Araw) + b * p.sA : nullptr;
   for (long long e = tid; e < (long long)nmine * N; e += 256) {
