@@ -45,7 +45,9 @@ enum { OZ_REAL = 0, OZ_CROWS = 1, OZ_CKA = 2, OZ_CKB = 3 };
 enum { OZ_OUT_COLS = 0, OZ_OUT_ROWS = 1, OZ_OUT_REAL = 2, OZ_OUT_CPLX = 3 };
 #define OZ_KC 64          // K chunk of one TMA box (128 bytes of BF16)
 #define OZ_BM 128         // MMA M
-#define OZ_TARGET_BITS 54
+#ifndef OZ_TARGET_BITS
+#define OZ_TARGET_BITS 54  // digits x bits per slice >= this (an FP64 mantissa and one guard bit)
+#endif
 
 // ---------------------------------------------------------------------------------------
 // Slicing
