@@ -64,7 +64,7 @@ struct alfgpu_s {
   int oz_bits = 0, oz_S = 0, oz_bn = 32, oz_nst = 2, oz_Kpad = 0, oz_RpN = 0, oz_Rp2N = 0;  // wraps (K = N)
   int ozf_bits = 0, ozf_S = 0, ozf_bn = 32, ozf_nst = 2;                                   // flush (K = 2 kmax)
   int ozf_pairs = 0;  // flush tiles leave room for two flush CTAs and one k_update CTA per SM
-  int ozf_grid = 0;   // with ozf_pairs: CTAs of the persistent K = 64 launches (two per SM)
+  int ozf_grid = 0;   // CTAs of the persistent K = 64 launches (paired tiles: two per SM; resident: one)
   // digit slices used by the G wraps (and TAU_M's propagation) and by the UDV propagation: a
   // prefix of the oz_S slices (dims.reserved[1] / [2] give the target bits; default oz_S)
   int ozw_S = 0, ozp_S = 0;
@@ -1704,7 +1704,15 @@ static int oz_setup(alfgpu_s* h) {
                    narrow || (h->d.reserved[0] & ALFGPU_FLAG_OZ_DEEP_RING)) ||
       oz_pick_tile(h->ozf_S, 2 * UPD_KMAX / OZ_KC, &h->ozf_bn, &h->ozf_nst, narrow))
     return 0;
-  if (!narrow && !(h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_SINGLE)) {
+  if (!narrow && (h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_RESIDENT)) {
+    // K = 64 products as persistent CTAs, one per SM, that keep a tile's A digit slices in a ring
+    // of S stages and reuse them for the following tiles of the same M-tile
+    if (oz_smem_bytes(32, h->ozf_S, 1, h->ozf_S) <= 227 * 1024) {
+      h->ozf_bn = 32;
+      h->ozf_nst = h->ozf_S;
+      h->ozf_grid = nsm;
+    }
+  } else if (!narrow && !(h->d.reserved[0] & ALFGPU_FLAG_OZ_FLUSH_SINGLE)) {
     // K = 64 products (flush, compact-WY update) on 16-wide tiles with a ring small enough for
     // two CTAs per SM ((S + 1) x 16 TMEM columns round to 256 of the SM's 512) and room beside
     // them for one k_update CTA, so the next block's visits can overlap the flush

@@ -474,7 +474,20 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   // tile (parity = tile iteration & 1)
   int pst = 0, pround = 0, mst = 0, mround = 0;
   int it = 0;
-  for (int tix = PERSIST ? (int)blockIdx.x : 0; tix < ntile; tix += PERSIST ? (int)gridDim.x : ntile, ++it) {
+  // A-resident mode (persistent, every A chunk of a tile fits the ring): a CTA takes a contiguous
+  // range of tiles, N-tile fastest, so consecutive tiles share their A chunks, which are loaded
+  // into stages 0 .. total - 1 only when the (batch, M-tile) changes; the ring's empty barriers
+  // are not used (the previous tile's MMAs are complete before the next tile starts)
+  const bool resident = PERSIST && total <= NST;
+  int t_begin = 0, t_end = 1, t_step = 1;
+  if (PERSIST && resident) {
+    t_begin = (int)((long long)ntile * blockIdx.x / gridDim.x);
+    t_end = (int)((long long)ntile * (blockIdx.x + 1) / gridDim.x);
+  } else if (PERSIST) {
+    t_begin = (int)blockIdx.x; t_end = ntile; t_step = (int)gridDim.x;
+  }
+  int keyA_prev = -1, aloads = 0;
+  for (int tix = t_begin; tix < t_end; tix += t_step, ++it) {
   int b, m0, n0;
   if (PERSIST) {
     n0 = (tix % p.tiles_n) * BN;
@@ -486,6 +499,10 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
   const int bA = p.modA > 0 ? b % p.modA : b, bB = p.modB > 0 ? b % p.modB : b;
   const int g0 = it * total;  // count of this tile's first A chunk
   const uint32_t tpar = (uint32_t)(it & 1);
+  const int keyA = bA * p.tiles_m + m0 / OZ_BM;
+  const bool loadA = !resident || keyA != keyA_prev;
+  if (resident && loadA) { keyA_prev = keyA; ++aloads; }
+  const uint32_t apar = (uint32_t)((aloads - 1) & 1);  // resident A: parity of its load
 
   if (tid == 0) {  // producer
     const int rowA0 = bA * p.SbA * p.RpadA + m0, rowB0 = bB * p.SbB * p.RpadB + n0;
@@ -495,7 +512,15 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
         oz_tma_2d(sB + (uint32_t)(kc * (S + 1) + t) * chunkB, &tmB, kc * OZ_KC, rowB0 + t * p.RpadB, bfull);
     int loaded = 0;
     bool ok = true;
-    for (int s = 0, kc = 0; loaded < total; ++loaded) {
+    if (resident) {
+      if (loadA)
+        for (int l = 0; l < total; ++l) {
+          oz_mbar_expect_tx(full0 + 8u * l, chunkA);
+          oz_tma_2d(sA + (uint32_t)l * chunkA, &tmA, (l % nkc) * OZ_KC, rowA0 + (l / nkc) * p.RpadA, full0 + 8u * l);
+        }
+      loaded = total;
+    }
+    for (int s = 0, kc = 0; !resident && loaded < total; ++loaded) {
       const int st = pst;
       if (pround > 0 && !oz_mbar_wait(empty0 + 8u * st, (uint32_t)((pround - 1) & 1))) { ok = false; break; }
       if (*abort_flag) break;
@@ -507,8 +532,13 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     if (!ok) { atomicOr(p.err, 4); *abort_flag = 1; }
     if (*abort_flag) {  // let every copy issued by this thread land before the CTA exits
       oz_mbar_wait(bfull, tpar);
-      for (int q = g0 + *consumed_sh; q < g0 + loaded; ++q)
-        oz_mbar_wait(full0 + 8u * (uint32_t)(q % NST), (uint32_t)((q / NST) & 1));
+      if (resident) {
+        if (loadA)
+          for (int l = 0; l < total; ++l) oz_mbar_wait(full0 + 8u * l, apar);
+      } else {
+        for (int q = g0 + *consumed_sh; q < g0 + loaded; ++q)
+          oz_mbar_wait(full0 + 8u * (uint32_t)(q % NST), (uint32_t)((q / NST) & 1));
+      }
     }
   } else if (tid == 32) {  // MMA issuer
     oz_fence_after();  // the previous tile's TMEM reads are done (barrier below)
@@ -518,8 +548,8 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
     constexpr int TMAX = 256 / BN;  // B blocks per MMA (N <= 256)
     int q = 0;
     for (int s = 0, kc = 0; ok && q < total; ++q) {
-      const int st = mst;
-      if (!oz_mbar_wait(full0 + 8u * st, (uint32_t)(mround & 1))) { ok = false; break; }
+      const int st = resident ? q : mst;
+      if (!oz_mbar_wait(full0 + 8u * st, resident ? apar : (uint32_t)(mround & 1))) { ok = false; break; }
       oz_fence_after();
       const uint64_t dA = dA0 + (uint64_t)((st * chunkA) >> 4);
       // A_s times the contiguous blocks B_0 .. B_{nt-1} of this K chunk in one MMA (N = nt BN),
@@ -535,9 +565,11 @@ __global__ void __launch_bounds__(256, 1) k_oz_gemm(const __grid_constant__ CUte
           oz_mma(tbase + (uint32_t)((s + t0) * BN), dA + 2u * kk, dB, oz_idesc(n * BN), acc);
         }
       }
-      oz_commit(empty0 + 8u * st);
+      if (!resident) {
+        oz_commit(empty0 + 8u * st);
+        if (++mst == NST) { mst = 0; ++mround; }
+      }
       *consumed_sh = q + 1;
-      if (++mst == NST) { mst = 0; ++mround; }
       if (++kc == nkc) { kc = 0; ++s; }
     }
     if (!ok) { atomicOr(p.err, 4); *abort_flag = 1; }

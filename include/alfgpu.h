@@ -138,6 +138,10 @@ enum { ALFGPU_FLAG_FP64_VISITS = 65536 };
 /* Mixed form: the K = N_dim tensor-core products (G wraps, UDV propagation, stabilisation
  * products) on 16-wide tiles with the deeper A ring of one-chain grids, also on batched grids. */
 enum { ALFGPU_FLAG_OZ_DEEP_RING = 131072 };
+/* Mixed form, grids of several chains: the K = 64 tensor-core products as persistent CTAs, one
+ * per SM, each over a contiguous range of output tiles whose A digit slices stay in shared
+ * memory from one tile to the next (no overlap of the visits with the flush). */
+enum { ALFGPU_FLAG_OZ_FLUSH_RESIDENT = 262144 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the

@@ -14,8 +14,8 @@ import pytest
 
 import oracle
 from alf_gb300 import model as mdl, rng
-from alf_gb300.sweep import (FLAG_DF_FLUSH, FLAG_FP64_VISITS, FLAG_OZ_DEEP_RING, FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE,
-                             Chains)
+from alf_gb300.sweep import (FLAG_DF_FLUSH, FLAG_FP64_VISITS, FLAG_OZ_DEEP_RING, FLAG_OZ_FLUSH_RESIDENT,
+                             FLAG_OZ_FLUSH_SINGLE, FLAG_TENSOR_WIDE, Chains)
 from parity_util import compare_record
 
 pytestmark = pytest.mark.gpu
@@ -185,3 +185,34 @@ def test_mixed_wide_grid_paths_vs_fp64_oracle():
     assert w < BOUND
     w = _compare(mdl.config("hubbard16x16"), seed=1, sweeps=1, flags=FLAG_TENSOR_WIDE)
     assert w < BOUND
+
+
+@pytest.mark.parametrize("flags", [0, FLAG_OZ_FLUSH_RESIDENT], ids=["paired-tiles", "resident-a"])
+def test_mixed_persistent_k64_products_vs_oracle(flags):
+    # four 16x16 chains: the flush and the compact-WY updates (K = 64) have more output tiles than
+    # the persistent grid, so each CTA loops over tiles (paired 16-wide tiles by default; with
+    # the resident option one CTA per SM keeps a tile's A slices for the next tiles)
+    m = mdl.hubbard("square", 16, 16, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
+    C, seed = 4, 21
+    g = Chains(m, n_chains=C, precision="mixed", flags=flags)
+    fs = [rng.initial_fields(seed + c, c, m.n_op, m.ltrot) for c in range(C)]
+    for c in range(C):
+        g.set_fields(c, fs[c])
+    g.init_state()
+    us = np.stack([rng.sweep_uniforms(seed + c, c, m.n_op, m.ltrot, 0) for c in range(C)])
+    g.set_recording(True)
+    g.sweep(us)
+    compared = 0
+    for c in range(C):
+        o = oracle.Oracle(m)
+        o.set_fields(fs[c])
+        o.init_state()
+        o.record(1)
+        o.sweep(us[c])
+        res = compare_record(g.record(c), o.recorded(), us[c], m.n_op, m.ltrot, m.nwrap, g_tol=BOUND,
+                             relative=False, exact_sequence=False, ratio_median=1e-5)
+        compared += res["points_compared"]
+        if res["parting_visit"] is None:
+            np.testing.assert_array_equal(g.fields(c), o.fields())
+            assert np.max(np.abs(g.green(c) - o.green())) < BOUND, c
+    assert compared >= C
