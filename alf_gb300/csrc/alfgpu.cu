@@ -377,6 +377,7 @@ static int launch_qrr(alfgpu_s* h, const zd* Ain, zd* A, int N, int CL, bool gro
   q.colscale = colscale; q.sCS = N;
   q.tau = tau; q.sT = N; q.jpvt = jpvt; q.sP = N; q.D = D; q.sD = N; q.info = info;
   q.Arows = grows ? ws : nullptr;
+  q.two_pass = (h->d.reserved[0] & ALFGPU_FLAG_QR_TWO_PASS) ? 1 : 0;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(CL, B, 1);

@@ -411,6 +411,7 @@ struct QRRowsParams {
   double* D; long long sD;
   QRInfo* info;
   void* Arows;               // GROWS: workspace of B x CL x nrl x N values of the kernel's arithmetic
+  int two_pass;              // 1: every step applies its reflector and forms the next sums in separate passes
 };
 
 static inline size_t qrr_smem_bytes(int N, int CL, bool grows = false) {
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(256) k_qrp_rows(QRRowsParams p) {
       p.D[b * p.sD + j] = (trivial ? sqrt(A::rwide(A::abs2(alpha))) : fabs(A::rwide(beta))) * cs[j];
     }
     const bool recompute = __syncthreads_or(need);
-    if (recompute || j + 1 >= N) {
+    if (recompute || j + 1 >= N || p.two_pass) {
       // H^H on the columns c > j alone: a_c -= v f_c over own rows > j
       if (!trivial) {
         const int lk = kmap(j, il0);

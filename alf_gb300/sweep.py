@@ -45,6 +45,7 @@ FLAG_OZ_FLUSH_SINGLE = 32768
 FLAG_FP64_VISITS = 65536
 FLAG_OZ_DEEP_RING = 131072
 FLAG_OZ_FLUSH_RESIDENT = 262144
+FLAG_QR_TWO_PASS = 524288
 # "default": ZGEQP3 everywhere in the FP64 form; norm-pivoted CGR in the mixed form
 PIVOTING = {"default": 0, "exact": FLAG_EXACT_QRP, "norms": FLAG_NORM_PIVOT,
             "norms-cgr": FLAG_NORM_PIVOT_CGR, "norms-decompose": FLAG_NORM_PIVOT_DECOMPOSE}

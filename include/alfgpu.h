@@ -142,6 +142,9 @@ enum { ALFGPU_FLAG_OZ_DEEP_RING = 131072 };
  * per SM, each over a contiguous range of output tiles whose A digit slices stay in shared
  * memory from one tile to the next (no overlap of the visits with the flush). */
 enum { ALFGPU_FLAG_OZ_FLUSH_RESIDENT = 262144 };
+/* The exact pivoted QR applies each step's reflector and forms the next step's partial sums in
+ * two passes over the rows (by default one pass does both, the next pivot chosen first). */
+enum { ALFGPU_FLAG_QR_TWO_PASS = 524288 };
 
 /* dims.reserved[1] / dims.reserved[2] (mixed form, tensor-core products only): target bits of
  * the digit-sliced products of the G wraps and TAU_M's propagation (reserved[1]) and of the

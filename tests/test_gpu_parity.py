@@ -20,7 +20,7 @@ import pytest
 
 import oracle
 from alf_gb300 import model as mdl, rng
-from alf_gb300.sweep import FLAG_QR_GLOBAL_ROWS, FLAG_QR_HALF_CLUSTER, Chains, cgr as gpu_cgr, decompose as gpu_decompose
+from alf_gb300.sweep import FLAG_QR_GLOBAL_ROWS, FLAG_QR_HALF_CLUSTER, FLAG_QR_TWO_PASS, Chains, cgr as gpu_cgr, decompose as gpu_decompose
 
 pytestmark = pytest.mark.gpu
 
@@ -192,11 +192,13 @@ def test_sweep_hubbard_8x8_half_cluster_qr_parity():
     _run_pair(m, seed=4, sweeps=1, flags=FLAG_QR_HALF_CLUSTER)
 
 
-@pytest.mark.parametrize("flags", [FLAG_QR_GLOBAL_ROWS, FLAG_QR_GLOBAL_ROWS | FLAG_QR_HALF_CLUSTER],
-                         ids=["global-rows", "global-rows-half"])
+@pytest.mark.parametrize("flags", [FLAG_QR_GLOBAL_ROWS, FLAG_QR_GLOBAL_ROWS | FLAG_QR_HALF_CLUSTER,
+                                   FLAG_QR_TWO_PASS, FLAG_QR_GLOBAL_ROWS | FLAG_QR_TWO_PASS],
+                         ids=["global-rows", "global-rows-half", "two-pass", "global-rows-two-pass"])
 def test_sweep_hubbard_8x8_global_rows_qr_parity(flags):
     # the exact pivoted QR with every CTA's rows in the global workspace although they fit in
-    # shared memory (the same arithmetic and order as the shared-memory rows)
+    # shared memory (the same arithmetic and order as the shared-memory rows), and with the update
+    # and the next step's partial sums in separate passes
     m = mdl.hubbard("square", 8, 8, U=4.0, beta=2.0, dtau=0.1, nwrap=10)
     _run_pair(m, seed=4, sweeps=1, flags=flags)
 
