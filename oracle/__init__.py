@@ -283,3 +283,22 @@ def decompose(side: str, U, D, V):
     Dc = np.ascontiguousarray(D, np.complex128).copy()
     lib().oracle_decompose(N, _c.c_char(side.encode()), _ptr(Uc), _ptr(Dc), _ptr(Vc))
     return Uc.T.copy(), Dc, Vc.T.copy()
+
+
+def solve_extended_case(inp, UCT, VINV):
+    """The reference's solve_extended_System test case (testsuite/Prog.tests/
+    17-solve-extended-system.F90) on the oracle: QDRP of the 2N x 2N ``inp``, U3 = Q, V3 = the
+    normalised R with its columns moved back by the pivots, D3, and
+    HLP = solve_extended_System(UCT, VINV) (row-major numpy in and out)."""
+    N = UCT.shape[0]
+    N2 = 2 * N
+    cm = lambda A: np.ascontiguousarray(np.asarray(A, np.complex128).T)
+    A = cm(inp)
+    U, V = np.zeros((N2, N2), np.complex128), np.zeros((N2, N2), np.complex128)
+    H = np.zeros((N2, N2), np.complex128)
+    D = np.zeros(N2, np.complex128)
+    uct, vinv = cm(UCT), cm(VINV)
+    rc = lib().oracle_solve_extended_case(N, _ptr(A), _ptr(uct), _ptr(vinv), _ptr(H), _ptr(U), _ptr(V), _ptr(D))
+    if rc:
+        raise RuntimeError(f"oracle_solve_extended_case: info {rc}")
+    return H.T.copy(), U.T.copy(), V.T.copy(), D

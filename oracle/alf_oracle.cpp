@@ -1116,6 +1116,28 @@ int oracle_decompose(int N, char side, zc* U, zc* D, zc* V) {
   std::memcpy(D, s.D.data(), (size_t)N * sizeof(zc));
   return 0;
 }
+// The case of the reference's solve_extended_System test (testsuite/Prog.tests/
+// 17-solve-extended-system.F90): QDRP of the 2N x 2N input (in place: R above with rows
+// normalised by D3, reflectors below), U3 = Q (ZUNGQR), V3 = upper(R) with its columns moved
+// back by the pivots (ZLAPMT backward), and HLP = solve_extended_System(UCT, VINV, ...).
+int oracle_solve_extended_case(int N, zc* input, const zc* UCT, const zc* VINV, zc* HLP, zc* U3, zc* V3, zc* D3) {
+  const int N2 = 2 * N;
+  vector<int> ipvt(N2);
+  vector<zc> tau;
+  qdrp(N2, input, D3, ipvt.data(), tau);
+  std::memcpy(U3, input, (size_t)N2 * N2 * sizeof(zc));
+  int info = 0, lw = -1;
+  zc wq;
+  LA.zungqr(&N2, &N2, &N2, U3, &N2, tau.data(), &wq, &lw, &info);
+  lw = (int)std::real(wq);
+  vector<zc> work(std::max(lw, 1));
+  LA.zungqr(&N2, &N2, &N2, U3, &N2, tau.data(), work.data(), &lw, &info);
+  for (int j = 0; j < N2; ++j)  // column j of upper(R) goes to column ipvt[j] - 1
+    for (int i = 0; i < N2; ++i)
+      V3[i + (size_t)(ipvt[j] - 1) * N2] = (i <= j) ? input[i + (size_t)j * N2] : zc(0.0);
+  solve_extended(N, HLP, UCT, VINV, input, D3, tau, ipvt.data());
+  return info;
+}
 // One WRAPGRUP / WRAPGRDO on the handle's G (u: 3*M draws)
 int oracle_wrapgrup(void* h, int ntau, const double* u) { wrapgrup(*(Oracle*)h, ntau, u); return 0; }
 int oracle_wrapgrdo(void* h, int ntau, const double* u) { wrapgrdo(*(Oracle*)h, ntau, u); return 0; }

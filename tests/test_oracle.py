@@ -168,3 +168,25 @@ def test_checkerboard_families_follow_the_reference():
             w, Z = np.linalg.eigh(mdl.hopping_matrix(lat, L1, L2, chem=0.3))
             ex = (Z * np.exp(-dt * w)[None, :]) @ Z.conj().T
             assert np.max(np.abs(B - ex)) < 1.2 * dt ** 2
+
+
+def test_solve_extended_system_17():
+    # testsuite/Prog.tests/17-solve-extended-system.F90: for LQ = 1, 2, 3 the QDRP of the 2LQ Hilbert
+    # matrix, UCT = ones, VINV(i, j) = i + j (1-based); solve_extended_System must equal
+    # U3 conj(1/D3) (V3^H)^-1 blockdiag(UCT, VINV).  The reference accepts 10% per entry; the
+    # restatement agrees to rounding.
+    for LQ in (1, 2, 3):
+        n2 = 2 * LQ
+        inp = np.array([[1.0 / (i + j) for j in range(1, n2 + 1)] for i in range(1, n2 + 1)], np.complex128)
+        UCT = np.ones((LQ, LQ), np.complex128)
+        VINV = np.array([[float(i + j) for j in range(1, LQ + 1)] for i in range(1, LQ + 1)], np.complex128)
+        H, U3, V3, D3 = oracle.solve_extended_case(inp, UCT, VINV)
+        B1 = np.zeros((n2, n2), np.complex128)
+        B1[:LQ, :LQ] = UCT
+        B1[LQ:, LQ:] = VINV
+        X = np.linalg.solve(V3.conj().T, B1)
+        X = np.conj(1.0 / D3)[:, None] * X
+        Ho = U3 @ X
+        assert np.max(np.abs(H - Ho)) <= 1e-8 * np.max(np.abs(Ho)), LQ
+        # and the pieces reconstruct the input: Q diag(D3) V3 = inp
+        assert np.max(np.abs(U3 @ (D3[:, None] * V3) - inp)) < 1e-13
