@@ -81,6 +81,7 @@ def lib(build_if_missing: bool = True):
         "alfgpu_set_rng": ([vp, C.c_int32, C.c_uint64, C.c_uint64], C.c_int),
         "alfgpu_init_state": ([vp, vp], C.c_int),
         "alfgpu_sweep": ([vp, vp, OBS_CB, vp], C.c_int),
+        "alfgpu_sweep_many": ([vp, C.c_int32, vp, vp], C.c_int),
         "alfgpu_set_delay": ([vp, C.c_int32], C.c_int),
         "alfgpu_get_delay": ([vp, C.POINTER(C.c_int32)], C.c_int),
         "alfgpu_tune_delay": ([vp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),

@@ -2388,7 +2388,9 @@ static int sweep_body(alfgpu_s* h, const double* dr, alfgpu_obs_cb cb, void* ctx
   return 0;
 }
 
-int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
+// The launch part of alfgpu_sweep: everything up to the last launch of the sweep on h->st (graph
+// replay when it applies), without waiting for the GPU.
+static int sweep_launch(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
   if (!h) return ALFGPU_ERROR_ARGUMENT;
   if (!h->state_ok) return ALFGPU_ERROR_ARGUMENT;
   CK(cudaSetDevice(h->dev));
@@ -2438,9 +2440,37 @@ int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ct
   }
   if (!uniforms)
     for (int c = 0; c < h->C; ++c) h->h_ctr[c] += 6ull * M * L;
-  int rc = check_err(h);
+  return 0;
+}
+
+// The end of a sweep: wait for h->st, read the device error flags, collect the phase profile.
+static int sweep_finish(alfgpu_t* h) {
+  CK(cudaSetDevice(h->dev));
+  const int rc = check_err(h);
   prof_collect(h);
   return rc;
+}
+
+int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx) {
+  RET(sweep_launch(h, uniforms, cb, ctx));
+  return sweep_finish(h);
+}
+
+int alfgpu_sweep_many(alfgpu_t* const* hs, int32_t n, const double* const* uniforms, int32_t* status) {
+  if (!hs || n < 0 || !status) return ALFGPU_ERROR_ARGUMENT;
+  for (int k = 0; k < n; ++k)
+    if (!hs[k]) return ALFGPU_ERROR_ARGUMENT;
+  int first = 0;
+  std::vector<char> launched(n, 0);
+  for (int k = 0; k < n; ++k) {  // every handle's launches first: they run on their own streams
+    status[k] = sweep_launch(hs[k], uniforms ? uniforms[k] : nullptr, nullptr, nullptr);
+    launched[k] = status[k] == 0;
+  }
+  for (int k = 0; k < n; ++k) {
+    if (launched[k]) status[k] = sweep_finish(hs[k]);
+    if (status[k] && !first) first = status[k];
+  }
+  return first;
 }
 
 

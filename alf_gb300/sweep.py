@@ -410,3 +410,38 @@ def decompose(side: str, U, D, V):
     Dc = np.ascontiguousarray(D, np.complex128).copy()
     _lib.check(L.alfgpu_decompose(N, C.c_char(side.encode()), _p(Uc), _p(Dc), _p(Vc)), "alfgpu_decompose")
     return Uc.T.copy(), Dc, Vc.T.copy()
+
+
+def sweep_many(handles: Sequence["Chains"], uniforms: Optional[Sequence[Optional[np.ndarray]]] = None) -> None:
+    """One sweep on each of several handles through alfgpu_sweep_many: every handle's launches
+    are issued from this thread first, each on its own stream, then each handle is waited for,
+    so handles of different sizes sweep concurrently without host threads.  uniforms: None (the
+    device streams) or one host array (or None) per handle, as for Chains.sweep."""
+    n = len(handles)
+    if n == 0:
+        return
+    L = handles[0].L
+    hs = (C.c_void_p * n)(*[h.h for h in handles])
+    status = np.zeros(n, np.int32)
+    keep = []
+    if uniforms is None:
+        up = None
+    else:
+        ptrs = []
+        for h, u in zip(handles, uniforms):
+            if u is None:
+                ptrs.append(None)
+                continue
+            a = np.ascontiguousarray(u, dtype=np.float64)
+            if a.size != h.C * 6 * h.M * h.Lt:
+                raise ValueError(f"{a.size} draws, expected {h.C * 6 * h.M * h.Lt} (chains x 6 M Ltrot)")
+            keep.append(a)
+            ptrs.append(a.ctypes.data_as(C.c_void_p))
+        up = (C.c_void_p * n)(*ptrs)
+    rc = L.alfgpu_sweep_many(hs, n, up, status.ctypes.data_as(C.c_void_p))
+    for k in range(n):
+        if status[k]:
+            h = handles[k]
+            _lib.check(int(status[k]), f"alfgpu_sweep_many (handle {k})" +
+                       (f" ({h.L.alfgpu_last_error(h.h).decode()})" if status[k] == 100 else ""))
+    _lib.check(rc, "alfgpu_sweep_many")

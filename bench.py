@@ -574,15 +574,15 @@ def mixed_vs_fp64(m, seed: int, local: int, flags: int, ltau: int, wrap_bits: in
 
 def run_batch(args, ws, rank, local, precision: str, steps: int, warmup: int, e2e: bool = True):
     """Config batch128: one handle per (N_dim, Ltrot) group with per-chain U; a step is one
-    sweep of every chain.  By default the groups sweep concurrently, one host thread per
-    group (each handle launches on its own stream; the C ABI releases the GIL), and the step
-    is timed on the device from an event that every group stream waits for to an event that
-    waits for every group's end."""
+    sweep of every chain.  By default the groups sweep concurrently through alfgpu_sweep_many
+    (one host thread; each handle's launches on its own stream), and the step is timed on the
+    device from an event that every group stream waits for to an event that waits for every
+    group's end."""
     import concurrent.futures as cf
     import dataclasses
     import torch
     from alf_gb300 import model as mdl, rng, replicas
-    from alf_gb300.sweep import Chains
+    from alf_gb300.sweep import Chains, sweep_many
     torch.cuda.set_device(local)
     groups = batch128_groups(replicas.replica_seed(args.seed, rank))
     hs = []
@@ -615,8 +615,20 @@ def run_batch(args, ws, rank, local, precision: str, steps: int, warmup: int, e2
         except Exception as e:
             raise RuntimeError(f"group L={m.params.get('L1')} Ltrot={m.ltrot} chains={len(mem)}: {e}") from e
 
+    def sweep_all(us=None):
+        """One sweep of every group: alfgpu_sweep_many (one host thread, each handle's launches on
+        its own stream), or one group after another with --serial-groups."""
+        if args.serial_groups:
+            for i in range(len(hs)):
+                if us is None:
+                    sweep_group(i)
+                else:
+                    hs[i][0].sweep(us[i])
+        else:
+            sweep_many([h[0] for h in hs], us)
+
     for _ in range(warmup):
-        each(sweep_group)
+        sweep_all()
     # drift control: per group, halve Nwrap until Precision Green <= the bound (untimed sweeps)
     nwraps = each(lambda i: hs[i][0].adapt_nwrap(bound=args.drift_bound))
     for ch, _, _ in hs:
@@ -631,12 +643,11 @@ def run_batch(args, ws, rank, local, precision: str, steps: int, warmup: int, e2
             ends = [torch.cuda.Event() for _ in hs]
             e0.record(cur)
 
-            def timed(k):
+            for k in range(len(hs)):
                 streams[k].wait_event(e0)
-                sweep_group(k)
+            sweep_all()
+            for k in range(len(hs)):
                 ends[k].record(streams[k])
-
-            each(timed)
             for e in ends:
                 cur.wait_event(e)
             e1.record(cur)
@@ -661,10 +672,9 @@ def run_batch(args, ws, rank, local, precision: str, steps: int, warmup: int, e2
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(steps):
-            def host_step(k, i=i):
-                hs[k][0].sweep(us[i][k])
-                return hs[k][0].green(0)
-            each(host_step)
+            sweep_all(us[i])
+            for ch, _, _ in hs:
+                ch.green(0)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
     pool.shutdown()
@@ -767,7 +777,7 @@ def main():
             "dtype": "c128" if args.precision == "fp64" else "c128 state, digit-sliced bf16 tensor products",
             "arm": {"precision": args.precision, "chains_per_gpu": head["chains_per_gpu"], "groups": head["groups"],
                     "parallelism": f"replicas x{ws}; groups " + ("one after another" if args.serial_groups else
-                                                                  "concurrent, one host thread each"),
+                                                                  "concurrent through alfgpu_sweep_many (one host thread, a stream per handle)"),
                     "draws": "device counter stream (value); host arrays through the C ABI (e2e)"},
             "e2e": {"value": head.get("e2e"), "unit": "sweeps/s", "h2d_bytes_per_step": rb["h2d"],
                     "d2h_bytes_per_step": rb["d2h"]},

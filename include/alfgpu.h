@@ -256,6 +256,16 @@ int alfgpu_init_state(alfgpu_t* h, double* phase_out);
  * device stream.  cb may be NULL (no measurements). */
 int alfgpu_sweep(alfgpu_t* h, const double* uniforms, alfgpu_obs_cb cb, void* ctx);
 
+/* One sweep on each of n handles (no counterpart in the reference, whose walkers are MPI
+ * ranks): every handle's launches are issued first, each on its own stream (its captured
+ * graph replays where alfgpu_sweep would replay it), then each handle is waited for and
+ * checked, so handles of different N_dim / Ltrot sweep concurrently from one host thread.
+ * uniforms: NULL (every handle's device stream) or n pointers as for alfgpu_sweep (a NULL
+ * entry: that handle's device stream).  status[k] receives handle k's alfgpu_sweep code; the
+ * return value is the first non-zero one.  No measurement callbacks: use alfgpu_sweep, or the
+ * device-side observables, for measuring sweeps.  The handles may share a device or not. */
+int alfgpu_sweep_many(alfgpu_t* const* hs, int32_t n, const double* const* uniforms, int32_t* status);
+
 /* Stabilisation interval Nwrap (the reference's fixed Nwrap, main.F90:446-457): re-plans the
  * stabilisation points and grows the UDV stack as needed; G and the stack must then be
  * rebuilt from the current fields with alfgpu_init_state before the next sweep.  A driver
