@@ -1,4 +1,4 @@
-"""Host-side policies of the Python mirror (alf_gb300.sweep.Chains) on the CPU, driven by a
+"""Host-side policies of the Python mirror (alf_gb300.sweep.Chains, sweep_many) on the CPU, driven by a
 stand-in for the C library: the drift-control loop (adapt_nwrap), the sizing of the record
 buffers from the handle's current Nwrap, checkpoint / restore, the layouts of the observable
 callback and the scalar accumulators.  The library calls are the ones include/alfgpu.h
@@ -243,3 +243,34 @@ def test_callback_matrices_arrive_row_major_and_scalar_layouts(monkeypatch):
     np.testing.assert_allclose(ov, [1.0, 3.5, 4.0, 4.5])
     assert sign == (1.0 + (-1.0)) / 2 and f.log[-1] == "reset_obs"
     ch.close()
+
+
+def test_sweep_many_passes_handles_draws_and_per_handle_status(fake):
+    # alfgpu_sweep_many gets the handles, the count, one draw pointer per handle (NULL: device
+    # stream) and a status array; a non-zero status of one handle is raised for that handle
+    f = fake()
+    seen = {}
+
+    def sweep_many(hs, n, up, st):
+        hv = C.cast(hs, C.POINTER(C.c_void_p))
+        seen["handles"] = [hv[k] for k in range(n)]
+        seen["draws"] = None if up is None else [C.cast(up, C.POINTER(C.c_void_p))[k] for k in range(n)]
+        status = C.cast(st, C.POINTER(C.c_int32))
+        for k in range(n):
+            status[k] = f.many_status[k]
+        return next((s for s in f.many_status if s), 0)
+
+    f.alfgpu_sweep_many = sweep_many
+    a, b = _chains(), _chains()
+    f.many_status = [0, 0]
+    sweep.sweep_many([a, b])
+    assert seen["handles"] == [a.h.value, b.h.value] and seen["draws"] is None
+    u = np.zeros((a.C, 6 * a.M * a.Lt))
+    sweep.sweep_many([a, b], [u, None])
+    assert seen["draws"][0] == u.ctypes.data and seen["draws"][1] is None
+    with pytest.raises(ValueError):
+        sweep.sweep_many([a, b], [np.zeros(3), None])
+    f.many_status = [0, 3]
+    with pytest.raises(_lib.AlfGpuError) as e:
+        sweep.sweep_many([a, b])
+    assert e.value.code == 3 and "handle 1" in str(e.value)
