@@ -20,6 +20,9 @@ in dtau^2 by testsuite/test_vs_ed/analysis.py). Here this is pinned in three lay
 * The Kondo model's two-site vertices get the same exact Trotterized check, on one- and
   two-body observables of a 2 x 1 bilayer.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 import scipy.linalg as sl
@@ -28,8 +31,21 @@ import oracle
 from alf_gb300 import model as mdl, rng
 from alf_gb300.analysis import jackknife
 
-E_ED = -1.47261997  # testsuite/test_vs_ed/test_specs.yaml:25
-L_SITES, T_HOP, U_INT, BETA = 4, 1.0, 4.0, 2.0
+# the reference's ED test case, extracted from testsuite/test_vs_ed/test_specs.yaml by
+# tests/golden/make_golden.py
+_GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "hubbard_finT_chain.json")))
+_P = _GOLD["parameters"]
+E_ED = _GOLD["ed_energy"]
+L_SITES, T_HOP, U_INT, BETA = _P["L1"], _P["ham_T"], _P["ham_U"], _P["beta"]
+
+
+def test_golden_case_is_the_model_built_here():
+    # the fixture's lattice and ensemble are the ones the tests below build.  The reference's runs
+    # of this case use the symmetric Trotter split (Symm = true), this package the plain one: the
+    # finite-dtau energies differ, their dtau -> 0 limit (the ED energy) does not.
+    assert _P["Lattice_type"] == "N_leg_ladder" and _P["L2"] == 1 and _P["Mz"] and not _P["Checkerboard"]
+    assert _P["ham_Tperp"] == 0.0 and _P["Ltau"] == 0
+    assert abs(E_ED - (-1.47261997)) < 1e-12 and _GOLD["max_delta"] == 0.001
 
 
 def _ring(dtau, nwrap):
